@@ -1,0 +1,152 @@
+"""Synthetic hexahedral meshes in the element-descriptor form of the C-ABI.
+
+The reference builds its meshes through GMP + ``hp3gen`` + refinement; the
+element pass only sees, per element, what ``find_order``/``find_orient``/
+``nodcor``/``get_index`` return (problems/POISSON/GALERKIN/elem_opt.F90:66-74,
+constrs/celem_systemI.F90:290-350).  These generators produce exactly that
+descriptor for structured meshes of the unit cube:
+
+* ``norder``  (19)  edge orders, face orders (MODORDER=10 packed), interior
+  order (111*p style packing, set_initial_mesh.F90:56-62);
+* ``nori_edge`` (12), ``nori_face`` (6) orientation codes;
+* ``nodes`` (26)   global ids of vertex, edge and face nodes in element order
+  (vertices v1..v8, edges e1..e12, faces f1..f6 as in
+  src/modules/element_data.F90);
+* ``bcflag`` (26)  1 when the node lies on a Dirichlet boundary (all its dof
+  are known, get_index index=1);
+* ``xvert`` (8,3)  vertex coordinates: trilinear geometry, higher-order
+  geometry dof zero (EXGEOM=0, nodcor);
+* ``kappa``        per-element coefficient.
+
+Element node local numbering follows the hexahedron of the reference
+(BlendProject.F90:197-439): v1=(0,0,0) v2=(1,0,0) v3=(1,1,0) v4=(0,1,0)
+v5..v8 the same at z=1; edges e1=v1v2 e2=v2v3 e3=v4v3 e4=v1v4 e5=v5v6
+e6=v6v7 e7=v8v7 e8=v5v8 e9=v1v5 e10=v2v6 e11=v3v7 e12=v4v8; faces
+f1=z0 f2=z1 f3=y0 f4=x1 f5=y1 f6=x0.  On a lexicographically numbered grid
+every local edge/face axis is aligned with the global one, so all
+orientation codes are 0.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+HEXA = 1
+
+# vertex offsets (di,dj,dk)
+_VOFF = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
+                  [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+# edges: (axis, di, dj, dk) of the edge's start point
+_EDEF = [(0, 0, 0, 0), (1, 1, 0, 0), (0, 0, 1, 0), (1, 0, 0, 0),
+         (0, 0, 0, 1), (1, 1, 0, 1), (0, 0, 1, 1), (1, 0, 0, 1),
+         (2, 0, 0, 0), (2, 1, 0, 0), (2, 1, 1, 0), (2, 0, 1, 0)]
+# faces: (normal axis, di, dj, dk)
+_FDEF = [(2, 0, 0, 0), (2, 0, 0, 1), (1, 0, 0, 0), (0, 1, 0, 0), (1, 0, 1, 0), (0, 0, 0, 0)]
+
+
+def pack_order_hexa(p):
+    """Norder(19) of an isotropic hexa of order p (find_order form)."""
+    if np.isscalar(p):
+        px = py = pz = int(p)
+    else:
+        px, py, pz = (int(v) for v in p)
+    no = np.zeros(19, dtype=np.int32)
+    for e, (ax, *_r) in enumerate(_EDEF):
+        no[e] = (px, py, pz)[ax]
+    face_axes = [(0, 1), (0, 1), (0, 2), (1, 2), (0, 2), (1, 2)]
+    for f, (a, b) in enumerate(face_axes):
+        pa, pb = (px, py, pz)[a], (px, py, pz)[b]
+        no[12 + f] = 10 * pa + pb
+    no[18] = 100 * px + 10 * py + pz
+    return no
+
+
+def structured_hexa(n, p, perturb=0.0, kappa_logrange=None, seed=12345,
+                    dirichlet=True):
+    """n x n x n hexahedra on [0,1]^3 of order p.
+
+    perturb:  interior vertices moved by U(-perturb*h, +perturb*h) per
+              coordinate (trilinear curvilinear geometry).
+    kappa_logrange: (lo, hi) decades, kappa_e = 10**U(lo, hi); None -> 1.
+    """
+    rng = np.random.default_rng(seed)
+    nv1 = n + 1
+    h = 1.0 / n
+    idx = np.arange(nv1)
+    I, J, K = np.meshgrid(idx, idx, idx, indexing="ij")
+    coords = np.stack([I.ravel(order="F"), J.ravel(order="F"), K.ravel(order="F")], axis=1)
+    # vertex id = i + nv1*(j + nv1*k)
+    vid = lambda i, j, k: i + nv1 * (j + nv1 * k)  # noqa: E731
+    X = coords.astype(np.float64) * h
+    if perturb > 0.0:
+        interior = np.all((coords > 0) & (coords < n), axis=1)
+        d = rng.uniform(-perturb * h, perturb * h, size=X.shape)
+        X[interior] += d[interior]
+    nverts = nv1 ** 3
+    # edge ids per axis: axis a edges have n along a and nv1 along the others
+    def eid(ax, i, j, k):
+        if ax == 0:
+            return nverts + i + n * (j + nv1 * k)
+        if ax == 1:
+            return nverts + n * nv1 * nv1 + i + nv1 * (j + n * k)
+        return nverts + 2 * n * nv1 * nv1 + i + nv1 * (j + nv1 * k)
+    nedges = 3 * n * nv1 * nv1
+    def fid(ax, i, j, k):
+        base = nverts + nedges
+        if ax == 2:  # normal z: n x n x nv1
+            return base + i + n * (j + n * k)
+        if ax == 1:  # normal y: n x nv1 x n
+            return base + n * n * nv1 + i + n * (j + nv1 * k)
+        return base + 2 * n * n * nv1 + i + nv1 * (j + n * k)
+    nfaces = 3 * n * n * nv1
+    nnodes = nverts + nedges + nfaces
+    ne = n ** 3
+    nodes = np.zeros((ne, 26), dtype=np.int32)
+    bcflag = np.zeros((ne, 26), dtype=np.int32)
+    xvert = np.zeros((ne, 8, 3))
+    e = 0
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                for v in range(8):
+                    di, dj, dk = _VOFF[v]
+                    nodes[e, v] = vid(i + di, j + dj, k + dk)
+                    xvert[e, v] = X[nodes[e, v]]
+                    bcflag[e, v] = int(i + di in (0, n) or j + dj in (0, n) or k + dk in (0, n))
+                for q, (ax, di, dj, dk) in enumerate(_EDEF):
+                    nodes[e, 8 + q] = eid(ax, i + di, j + dj, k + dk)
+                    c = [i + di, j + dj, k + dk]
+                    bcflag[e, 8 + q] = int(any(c[a] in (0, n) for a in range(3) if a != ax))
+                for q, (ax, di, dj, dk) in enumerate(_FDEF):
+                    nodes[e, 20 + q] = fid(ax, i + di, j + dj, k + dk)
+                    c = [i + di, j + dj, k + dk]
+                    bcflag[e, 20 + q] = int(c[ax] in (0, n))
+                e += 1
+    if not dirichlet:
+        bcflag[:] = 0
+    if kappa_logrange is None:
+        kappa = np.ones(ne)
+    else:
+        lo, hi = kappa_logrange
+        kappa = 10.0 ** rng.uniform(lo, hi, size=ne)
+    no = pack_order_hexa(p)
+    return dict(
+        nelem=ne, n=n, h=h, p=p, nnodes=nnodes, nverts=nverts,
+        etype=np.full(ne, HEXA, dtype=np.int32),
+        norder=np.tile(no, (ne, 1)).astype(np.int32),
+        nori_edge=np.zeros((ne, 12), dtype=np.int32),
+        nori_face=np.zeros((ne, 6), dtype=np.int32),
+        nodes=nodes, bcflag=bcflag, xvert=xvert, kappa=kappa,
+        vertex_xyz=X,
+    )
+
+
+def random_orientations(mesh, seed=7):
+    """Copy of ``mesh`` with random edge (0/1) and face (0..7) orientation
+    codes: for element-level parity of orientation handling (the result is
+    not a conforming global mesh)."""
+    rng = np.random.default_rng(seed)
+    m = dict(mesh)
+    ne = mesh["nelem"]
+    m["nori_edge"] = rng.integers(0, 2, size=(ne, 12)).astype(np.int32)
+    m["nori_face"] = rng.integers(0, 8, size=(ne, 6)).astype(np.int32)
+    return m

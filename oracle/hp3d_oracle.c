@@ -1,0 +1,948 @@
+/*
+ * hp3d_oracle.c -- CPU FP64 restatement of the hp3D element pass.
+ *
+ * TEST INFRASTRUCTURE ONLY (see hp3d_oracle.h).  Compiled with
+ * -ffp-contract=off so that x86-64 and aarch64 hosts give identical bits.
+ * Citations are to Oden-EAG/hp3d, paths relative to trunk/.
+ */
+#include "hp3d_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* 1D Gauss-Legendre tables on [-1,1].  The reference tabulates them as      */
+/* 15-digit literals (src/element/quadrature/gauss_quadrature.F90:518-660,   */
+/* 25 digits for n=10); an oracle that wants the reference's element         */
+/* matrices bit for bit must use the same rounded values, so these are the   */
+/* same decimal numbers (the standard Gauss nodes/weights at that precision). */
+/* ------------------------------------------------------------------------ */
+static const double GAUSS_X[10][10] = {
+    {0.0},
+    {-.577350269189626, .577350269189626},
+    {-.774596669241483, .000000000000000, .774596669241483},
+    {-.861136311594053, -.339981043584856, .339981043584856, .861136311594053},
+    {-.906179845938664, -.538469310105683, .000000000000000, .538469310105683,
+     .906179845938664},
+    {-.932469514203152, -.661209386466265, -.238619186083197, .238619186083197,
+     .661209386466265, .932469514203152},
+    {-.949107912342759, -.741531185599394, -.405845151377397, .000000000000000,
+     .405845151377397, .741531185599394, .949107912342759},
+    {-.960289856497536, -.796666477413627, -.525532409916329, -.183434642495650,
+     .183434642495650, .525532409916329, .796666477413627, .960289856497536},
+    {-.968160239507626, -.836031107326636, -.613371432700590, -.324253423403809,
+     .000000000000000, .324253423403809, .613371432700590, .836031107326636,
+     .968160239507626},
+    {-.9739065285171717200779640, -.8650633666889845107320967,
+     -.6794095682990244062343274, -.4333953941292471907992659,
+     -.1488743389816312108848260, .1488743389816312108848260,
+     .4333953941292471907992659, .6794095682990244062343274,
+     .8650633666889845107320967, .9739065285171717200779640}};
+
+static const double GAUSS_W[10][10] = {
+    {2.000000000000000},
+    {1.000000000000000, 1.000000000000000},
+    {.555555555555556, .888888888888889, .555555555555556},
+    {.347854845137454, .652145154862546, .652145154862546, .347854845137454},
+    {.236926885056189, .478628670499366, .568888888888889, .478628670499366,
+     .236926885056189},
+    {.171324492379170, .360761573048139, .467913934572691, .467913934572691,
+     .360761573048139, .171324492379170},
+    {.129484966168870, .279705391489277, .381830050505119, .417959183673469,
+     .381830050505119, .279705391489277, .129484966168870},
+    {.101228536290376, .222381034453374, .313706645877887, .362683783378362,
+     .362683783378362, .313706645877887, .222381034453374, .101228536290376},
+    {.081274388361574, .180648160694857, .260610696402935, .312347077040003,
+     .330239355001260, .312347077040003, .260610696402935, .180648160694857,
+     .081274388361574},
+    {.0666713443086881375935688, .1494513491505805931457763,
+     .2190863625159820439955349, .2692667193099963550912269,
+     .2955242247147528701738930, .2955242247147528701738930,
+     .2692667193099963550912269, .2190863625159820439955349,
+     .1494513491505805931457763, .0666713443086881375935688}};
+
+/* rescale to [0,1]: gauss_quadrature.F90:749-750 */
+int orc_gauss1d(int n, double *x, double *w) {
+  if (n < 1 || n > 10) return -1;
+  for (int j = 0; j < n; ++j) {
+    x[j] = 0.5 * (1.0 + GAUSS_X[n - 1][j]);
+    w[j] = 0.5 * GAUSS_W[n - 1][j];
+  }
+  return 0;
+}
+
+/* decod (utility/decod.F90): split Nick into n digits base mod, most
+ * significant first. */
+static void decod(int nick, int mod, int n, int *arr) {
+  int nick1 = nick;
+  for (int i = 1; i <= n - 1; ++i) {
+    int nick2 = nick1 / mod;
+    arr[n - i] = nick1 - nick2 * mod;
+    nick1 = nick2;
+  }
+  arr[0] = nick1;
+}
+
+/* NFAXES(3,j): 1 when orientation j swaps the two face axes
+ * (modules/element_data.F90:246-249). */
+static const int NFAXES3[8] = {0, 1, 0, 1, 1, 0, 1, 0};
+
+static int imax(int a, int b) { return a > b ? a : b; }
+static int imin(int a, int b) { return a < b ? a : b; }
+
+/* set_3D_int BRICK branch (set_3D_int.F90:47-64, 155-245) with the face
+ * order swap of find_order_loc (datstrs/find_order.F90:68-108). */
+int orc_set_3D_int_hexa(const int32_t *norder, const int32_t *nori_face,
+                        int integration, double *xiloc, double *waloc) {
+  int nl[19];
+  for (int i = 0; i < 19; ++i) nl[i] = norder[i];
+  for (int j = 0; j < 6; ++j) {
+    if (NFAXES3[nori_face[j] & 7] == 1) {
+      int hv[2];
+      decod(norder[12 + j], 10, 2, hv);
+      nl[12 + j] = hv[1] * 10 + hv[0];
+    }
+  }
+  int nx = 0, ny = 0, nz = 0;
+  for (int i = 1; i <= 19; ++i) {
+    int hv[2], xyz[3];
+    switch (i) {
+      case 1: case 3: case 5: case 7: nx = imax(nx, nl[i - 1]); break;
+      case 2: case 4: case 6: case 8: ny = imax(ny, nl[i - 1]); break;
+      case 9: case 10: case 11: case 12: nz = imax(nz, nl[i - 1]); break;
+      case 13: case 14:
+        decod(nl[i - 1], 10, 2, hv); nx = imax(nx, hv[0]); ny = imax(ny, hv[1]);
+        break;
+      case 15: case 17:
+        decod(nl[i - 1], 10, 2, hv); nx = imax(nx, hv[0]); nz = imax(nz, hv[1]);
+        break;
+      case 16: case 18:
+        decod(nl[i - 1], 10, 2, hv); ny = imax(ny, hv[0]); nz = imax(nz, hv[1]);
+        break;
+      case 19:
+        decod(nl[i - 1], 10, 3, xyz);
+        nx = imax(nx, xyz[0]); ny = imax(ny, xyz[1]); nz = imax(nz, xyz[2]);
+        break;
+    }
+  }
+  nx = imin(nx + integration, ORC_MAXP);
+  ny = imin(ny + integration, ORC_MAXP);
+  nz = imin(nz + integration, ORC_MAXP);
+  int nix = nx + 1, niy = ny + 1, niz = nz + 1;
+  double gx[10], gwx[10], gy[10], gwy[10], gz[10], gwz[10];
+  orc_gauss1d(nix, gx, gwx);
+  orc_gauss1d(niy, gy, gwy);
+  orc_gauss1d(niz, gz, gwz);
+  int l = 0;
+  for (int l3 = 0; l3 < niz; ++l3)
+    for (int l2 = 0; l2 < niy; ++l2)
+      for (int l1 = 0; l1 < nix; ++l1) {
+        xiloc[3 * l + 0] = gx[l1];
+        xiloc[3 * l + 1] = gy[l2];
+        xiloc[3 * l + 2] = gz[l3];
+        waloc[l] = gwx[l1] * gwy[l2] * gwz[l3];
+        ++l;
+      }
+  return l;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Polynomials (src/element/shape_1/Polynomials.F90)                         */
+/* ------------------------------------------------------------------------ */
+
+/* PolyLegendre (Polynomials.F90:34-80): shifted scaled Legendre P(0:nord). */
+static void poly_legendre(double x, double t, int nord, double *p) {
+  p[0] = 1.0;
+  double y = 0.0;
+  if (nord >= 1) {
+    y = 2.0 * x - t;
+    p[1] = y;
+  }
+  if (nord >= 2) {
+    double tt = t * t;
+    for (int i = 2; i <= nord; ++i) {
+      p[i] = (double)(2 * i - 1) * y * p[i - 1] - (double)(i - 1) * tt * p[i - 2];
+      p[i] = p[i] / (double)i;
+    }
+  }
+}
+
+/* PolyILegendre (Polynomials.F90:113-160): integrated Legendre L(2:nord),
+ * x-derivative P(1:nord-1) and t-derivative R(1:nord-1). Arrays are indexed
+ * by the polynomial order (L[i], P[i-1] stored at index i-1). */
+static void poly_ilegendre(double x, double t, int nord, int idec, double *L,
+                           double *P, double *R) {
+  double pt[16];
+  poly_legendre(x, t, nord, pt);
+  for (int i = 1; i <= nord - 1; ++i) P[i] = pt[i];
+  double tt = t * t;
+  for (int i = 2; i <= nord; ++i) {
+    int ifact = 4 * i - 2;
+    L[i] = (pt[i] - tt * pt[i - 2]) / (double)ifact;
+    if (!idec) R[i - 1] = -(pt[i - 1] + t * pt[i - 2]) / 2.0;
+  }
+}
+
+/* HomILegendre (Polynomials.F90:494-530): homogenized integrated Legendre of
+ * the pair S=(s0,s1) with gradients DS(3,0:1); outputs HomL(i), DHomL(3,i)
+ * for i=2..nord (stored at index i). */
+static void hom_ilegendre(const double *S, const double DS[3][2], int nord,
+                          int idec, double *homL, double dhomL[][3]) {
+  double homP[16], homR[16];
+  if (idec) {
+    poly_ilegendre(S[1], 1.0, nord, 1, homL, homP, homR);
+    for (int i = 2; i <= nord; ++i)
+      for (int c = 0; c < 3; ++c) dhomL[i][c] = homP[i - 1] * DS[c][1];
+  } else {
+    poly_ilegendre(S[1], S[0] + S[1], nord, 0, homL, homP, homR);
+    double ds01[3];
+    for (int c = 0; c < 3; ++c) ds01[c] = DS[c][0] + DS[c][1];
+    for (int i = 2; i <= nord; ++i)
+      for (int c = 0; c < 3; ++c)
+        dhomL[i][c] = homP[i - 1] * DS[c][1] + homR[i - 1] * ds01[c];
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Hexahedron H1 (Hexahedron.F90:33-210; AffineHexahedron,                    */
+/* AffineCoordinates.F90:56-72; BlendHexaV / BlendProjectHexaE/F,             */
+/* BlendProject.F90:197-439; OrientE / OrientQuad, Orient.F90:9-116).         */
+/* ------------------------------------------------------------------------ */
+
+/* vertex -> (which Mu per axis) : BlendHexaV */
+static const int HEXA_V[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                 {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+/* edge -> blend1 (side, axis), blend2 (side, axis), projection axis :
+ * BlendProjectHexaE */
+static const int HEXA_E[12][5] = {
+    {0, 1, 0, 2, 0}, {1, 0, 0, 2, 1}, {1, 1, 0, 2, 0}, {0, 0, 0, 2, 1},
+    {0, 1, 1, 2, 0}, {1, 0, 1, 2, 1}, {1, 1, 1, 2, 0}, {0, 0, 1, 2, 1},
+    {0, 0, 0, 1, 2}, {1, 0, 0, 1, 2}, {1, 0, 1, 1, 2}, {0, 0, 1, 1, 2}};
+/* face -> blend (side, axis), pair-1 axis, pair-2 axis : BlendProjectHexaF */
+static const int HEXA_F[6][4] = {{0, 2, 0, 1}, {1, 2, 0, 1}, {0, 1, 0, 2},
+                                 {1, 0, 1, 2}, {1, 1, 0, 2}, {0, 0, 1, 2}};
+/* OrientQuad tables (Orient.F90:59-116): OrPa(1:2), OrGS(0:1), OrGT(0:1)
+ * with pairs 0-based. */
+static const int ORQ[8][6] = {{0, 1, 0, 1, 0, 1}, {1, 0, 0, 1, 1, 0},
+                              {0, 1, 1, 0, 1, 0}, {1, 0, 1, 0, 0, 1},
+                              {1, 0, 0, 1, 0, 1}, {0, 1, 1, 0, 0, 1},
+                              {1, 0, 1, 0, 1, 0}, {0, 1, 0, 1, 1, 0}};
+
+int orc_nrdofH_hexa(const int32_t *norder) {
+  int n = 8;
+  for (int e = 0; e < 12; ++e) n += imax(norder[e] - 1, 0);
+  for (int f = 0; f < 6; ++f) {
+    int hv[2];
+    decod(norder[12 + f], 10, 2, hv);
+    n += imax(hv[0] - 1, 0) * imax(hv[1] - 1, 0);
+  }
+  int b[3];
+  decod(norder[18], 10, 3, b);
+  n += imax(b[0] - 1, 0) * imax(b[1] - 1, 0) * imax(b[2] - 1, 0);
+  return n;
+}
+
+int orc_nrdofH_bubble(int etype, const int32_t *norder) {
+  if (etype == ORC_HEXA) {
+    int b[3];
+    decod(norder[18], 10, 3, b);
+    return imax(b[0] - 1, 0) * imax(b[1] - 1, 0) * imax(b[2] - 1, 0);
+  }
+  if (etype == ORC_TET) {
+    int p = norder[10];
+    return (p - 3) * (p - 2) * (p - 1) / 6 > 0 ? (p - 3) * (p - 2) * (p - 1) / 6 : 0;
+  }
+  return -1;
+}
+
+int orc_shape3DH_hexa(const double *xi, const int32_t *nord,
+                      const int32_t *nori_edge, const int32_t *nori_face,
+                      double *shap, double *grad) {
+  /* AffineHexahedron */
+  double Mu[2][3], DMu[3][2][3];
+  for (int d = 0; d < 3; ++d) {
+    Mu[0][d] = 1.0 - xi[d];
+    Mu[1][d] = xi[d];
+    for (int c = 0; c < 3; ++c) {
+      DMu[c][0][d] = 0.0;
+      DMu[c][1][d] = 0.0;
+    }
+    DMu[d][0][d] = -1.0;
+    DMu[d][1][d] = 1.0;
+  }
+  int m = 0;
+  /* vertices */
+  for (int v = 0; v < 8; ++v) {
+    const int *s = HEXA_V[v];
+    double b1 = Mu[s[0]][0], b2 = Mu[s[1]][1], b3 = Mu[s[2]][2];
+    shap[m] = b1 * b2 * b3;
+    for (int c = 0; c < 3; ++c)
+      grad[3 * m + c] = b1 * b2 * DMu[c][s[2]][2] + b1 * DMu[c][s[1]][1] * b3 +
+                        DMu[c][s[0]][0] * b2 * b3;
+    ++m;
+  }
+  /* edges */
+  for (int e = 0; e < 12; ++e) {
+    int ndofE = nord[e] - 1;
+    if (ndofE <= 0) continue;
+    const int *t = HEXA_E[e];
+    double mb1 = Mu[t[0]][t[1]], mb2 = Mu[t[2]][t[3]];
+    double dmb1[3], dmb2[3];
+    for (int c = 0; c < 3; ++c) {
+      dmb1[c] = DMu[c][t[0]][t[1]];
+      dmb2[c] = DMu[c][t[2]][t[3]];
+    }
+    int ax = t[4];
+    /* OrientE: Nori=1 swaps the pair */
+    int o0 = (nori_edge[e] == 1) ? 1 : 0, o1 = 1 - o0;
+    double GS[2] = {Mu[o0][ax], Mu[o1][ax]};
+    double GDS[3][2];
+    for (int c = 0; c < 3; ++c) {
+      GDS[c][0] = DMu[c][o0][ax];
+      GDS[c][1] = DMu[c][o1][ax];
+    }
+    double phi[16], dphi[16][3];
+    hom_ilegendre(GS, GDS, nord[e], 1, phi, dphi);
+    for (int i = 2; i <= nord[e]; ++i) {
+      shap[m] = mb1 * mb2 * phi[i];
+      for (int c = 0; c < 3; ++c)
+        grad[3 * m + c] = mb1 * mb2 * dphi[i][c] + mb1 * dmb2[c] * phi[i] +
+                          dmb1[c] * mb2 * phi[i];
+      ++m;
+    }
+  }
+  /* faces */
+  for (int f = 0; f < 6; ++f) {
+    int nf[2];
+    decod(nord[12 + f], 10, 2, nf);
+    int ndofF = (nf[0] - 1) * (nf[1] - 1);
+    if (nf[0] < 2 || nf[1] < 2 || ndofF <= 0) continue;
+    const int *t = HEXA_F[f];
+    double mbf = Mu[t[0]][t[1]];
+    double dmbf[3];
+    for (int c = 0; c < 3; ++c) dmbf[c] = DMu[c][t[0]][t[1]];
+    /* local pairs ST(0:1, 1:2) */
+    int axes[2] = {t[2], t[3]};
+    const int *oq = ORQ[nori_face[f] & 7];
+    /* GST(:,1) = ST(OrGS(:), OrPa(1)); GST(:,2) = ST(OrGT(:), OrPa(2)) */
+    double GS[2], GT[2], GDS[3][2], GDT[3][2];
+    int pa1 = axes[oq[0]], pa2 = axes[oq[1]];
+    GS[0] = Mu[oq[2]][pa1];
+    GS[1] = Mu[oq[3]][pa1];
+    GT[0] = Mu[oq[4]][pa2];
+    GT[1] = Mu[oq[5]][pa2];
+    for (int c = 0; c < 3; ++c) {
+      GDS[c][0] = DMu[c][oq[2]][pa1];
+      GDS[c][1] = DMu[c][oq[3]][pa1];
+      GDT[c][0] = DMu[c][oq[4]][pa2];
+      GDT[c][1] = DMu[c][oq[5]][pa2];
+    }
+    double phs[16], dphs[16][3], pht[16], dpht[16][3];
+    hom_ilegendre(GS, GDS, nf[0], 1, phs, dphs);
+    hom_ilegendre(GT, GDT, nf[1], 1, pht, dpht);
+    for (int j = 2; j <= nf[1]; ++j)
+      for (int i = 2; i <= nf[0]; ++i) {
+        double pq = phs[i] * pht[j];
+        shap[m] = mbf * pq;
+        for (int c = 0; c < 3; ++c) {
+          double dpq = phs[i] * dpht[j][c] + pht[j] * dphs[i][c];
+          grad[3 * m + c] = mbf * dpq + dmbf[c] * pq;
+        }
+        ++m;
+      }
+  }
+  /* bubbles */
+  int nb[3];
+  decod(nord[18], 10, 3, nb);
+  if (nb[0] >= 2 && nb[1] >= 2 && nb[2] >= 2) {
+    double S0[2] = {Mu[0][0], Mu[1][0]}, S1[2] = {Mu[0][1], Mu[1][1]},
+           S2[2] = {Mu[0][2], Mu[1][2]};
+    double D0[3][2], D1[3][2], D2[3][2];
+    for (int c = 0; c < 3; ++c) {
+      D0[c][0] = DMu[c][0][0]; D0[c][1] = DMu[c][1][0];
+      D1[c][0] = DMu[c][0][1]; D1[c][1] = DMu[c][1][1];
+      D2[c][0] = DMu[c][0][2]; D2[c][1] = DMu[c][1][2];
+    }
+    double px[16], dpx[16][3], py[16], dpy[16][3], pz[16], dpz[16][3];
+    hom_ilegendre(S0, D0, nb[0], 1, px, dpx);
+    hom_ilegendre(S1, D1, nb[1], 1, py, dpy);
+    hom_ilegendre(S2, D2, nb[2], 1, pz, dpz);
+    for (int k = 2; k <= nb[2]; ++k)
+      for (int j = 2; j <= nb[1]; ++j)
+        for (int i = 2; i <= nb[0]; ++i) {
+          double pq = px[i] * py[j];
+          shap[m] = pq * pz[k];
+          for (int c = 0; c < 3; ++c) {
+            double dpq = px[i] * dpy[j][c] + py[j] * dpx[i][c];
+            grad[3 * m + c] = pq * dpz[k][c] + dpq * pz[k];
+          }
+          ++m;
+        }
+  }
+  return m;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Geometry (src/element/util/geom.F90:30-138)                               */
+/* dxdxi[i + 3*j] = dx_i/dxi_j (Fortran Dxdxi(i,j)); same for dxidx.          */
+/* ------------------------------------------------------------------------ */
+#define A(i, j) dxdxi[(i - 1) + 3 * (j - 1)]
+#define B(i, j) dxidx[(i - 1) + 3 * (j - 1)]
+int orc_geom(const double *dxdxi, double *dxidx, double *rjac) {
+  int iflag = 0;
+  double r = A(1, 1) * A(2, 2) * A(3, 3) + A(2, 1) * A(3, 2) * A(1, 3) +
+             A(3, 1) * A(1, 2) * A(2, 3) - A(3, 1) * A(2, 2) * A(1, 3) -
+             A(1, 1) * A(3, 2) * A(2, 3) - A(2, 1) * A(1, 2) * A(3, 3);
+  if (r < 0.0) iflag = 1;
+  double d1, d2, d3;
+  d1 = A(2, 2) * A(3, 3) - A(3, 2) * A(2, 3);
+  d2 = -A(2, 1) * A(3, 3) + A(3, 1) * A(2, 3);
+  d3 = A(2, 1) * A(3, 2) - A(3, 1) * A(2, 2);
+  B(1, 1) = d1 / r; B(2, 1) = d2 / r; B(3, 1) = d3 / r;
+  d1 = A(3, 2) * A(1, 3) - A(1, 2) * A(3, 3);
+  d2 = A(1, 1) * A(3, 3) - A(3, 1) * A(1, 3);
+  d3 = -A(1, 1) * A(3, 2) + A(3, 1) * A(1, 2);
+  B(1, 2) = d1 / r; B(2, 2) = d2 / r; B(3, 2) = d3 / r;
+  d1 = A(1, 2) * A(2, 3) - A(2, 2) * A(1, 3);
+  d2 = -A(1, 1) * A(2, 3) + A(2, 1) * A(1, 3);
+  d3 = A(1, 1) * A(2, 2) - A(2, 1) * A(1, 2);
+  B(1, 3) = d1 / r; B(2, 3) = d2 / r; B(3, 3) = d3 / r;
+  *rjac = r;
+  return iflag;
+}
+#undef A
+#undef B
+
+/* ------------------------------------------------------------------------ */
+/* Manufactured solutions (problems/POISSON/GALERKIN/common/solution.F90,     */
+/* getf.F90: f = -(u_xx + u_yy + u_zz)).                                      */
+/* PI = 4*atan(1) (modules/common_prob_data.F90:51).                          */
+/* ------------------------------------------------------------------------ */
+static void solution(int isol, const double *X, double *u, double *gu,
+                     double *hess_trace) {
+  const double PI = 4.0 * atan(1.0);
+  double x1 = X[0], x2 = X[1], x3 = X[2];
+  *u = 0.0; gu[0] = gu[1] = gu[2] = 0.0; *hess_trace = 0.0;
+  switch (isol) {
+    case 0: {
+      double np = 6.0;
+      double fx = pow(x1, np), fy = pow(x2, np), fz = pow(x3, np);
+      double dfx = np * pow(x1, np - 1.0), dfy = np * pow(x2, np - 1.0),
+             dfz = np * pow(x3, np - 1.0);
+      double ddfx = np * (np - 1.0) * pow(x1, np - 2.0);
+      double ddfy = np * (np - 1.0) * pow(x2, np - 2.0);
+      double ddfz = np * (np - 1.0) * pow(x3, np - 2.0);
+      *u = fx * fy * fz;
+      gu[0] = dfx * fy * fz; gu[1] = fx * dfy * fz; gu[2] = fx * fy * dfz;
+      double h11 = ddfx * fy * fz, h22 = fx * ddfy * fz, h33 = fx * fy * ddfz;
+      *hess_trace = h11 + h22 + h33;
+      break;
+    }
+    case 1: {
+      *u = sin(x1 * PI) * sinh(x2 * PI);
+      gu[0] = PI * cos(x1 * PI) * sinh(x2 * PI);
+      gu[1] = PI * sin(x1 * PI) * cosh(x2 * PI);
+      double h11 = -PI * PI * sin(x1 * PI) * sinh(x2 * PI);
+      double h22 = PI * PI * sin(x1 * PI) * sinh(x2 * PI);
+      *hess_trace = h11 + h22 + 0.0;
+      break;
+    }
+    case 2: {
+      *u = sin(x1 * PI) * sinh(x2 * PI) * (x3 * x3);
+      gu[0] = PI * cos(x1 * PI) * sinh(x2 * PI) * (x3 * x3);
+      gu[1] = PI * sin(x1 * PI) * cosh(x2 * PI) * (x3 * x3);
+      gu[2] = 2. * sin(x1 * PI) * sinh(x2 * PI) * x3;
+      double h11 = -PI * PI * sin(x1 * PI) * sinh(x2 * PI) * (x3 * x3);
+      double h22 = PI * PI * sin(x1 * PI) * sinh(x2 * PI) * (x3 * x3);
+      double h33 = 2. * sin(x1 * PI) * sinh(x2 * PI);
+      *hess_trace = h11 + h22 + h33;
+      break;
+    }
+    case 10: { /* u = sin(pi x) sin(pi y) sin(pi z), f = 3 pi^2 u */
+      double s1 = sin(PI * x1), s2 = sin(PI * x2), s3 = sin(PI * x3);
+      *u = s1 * s2 * s3;
+      gu[0] = PI * cos(PI * x1) * s2 * s3;
+      gu[1] = PI * s1 * cos(PI * x2) * s3;
+      gu[2] = PI * s1 * s2 * cos(PI * x3);
+      *hess_trace = -3.0 * PI * PI * (*u);
+      break;
+    }
+    case 11: /* f == 1, no closed-form u */
+      *hess_trace = -1.0;
+      break;
+    case 12: /* u = x y z (test/poly_pois.F90:390-395) */
+      *u = x1 * x2 * x3;
+      gu[0] = x2 * x3; gu[1] = x1 * x3; gu[2] = x1 * x2;
+      *hess_trace = 0.0;
+      break;
+    default:
+      break;
+  }
+}
+
+double orc_getf(int isol, const double *x) {
+  double u, gu[3], tr;
+  solution(isol, x, &u, gu, &tr);
+  return -tr;
+}
+
+void orc_exact(int isol, const double *x, double *u, double *gradu) {
+  double tr;
+  solution(isol, x, u, gradu, &tr);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Element routine                                                           */
+/* ------------------------------------------------------------------------ */
+static int shape_dispatch(int etype, const double *xi, const int32_t *norder,
+                          const int32_t *noriE, const int32_t *noriF,
+                          double *shap, double *grad) {
+  if (etype == ORC_HEXA) return orc_shape3DH_hexa(xi, norder, noriE, noriF, shap, grad);
+  if (etype == ORC_TET) return orc_shape3DH_tet(xi, norder, noriE, noriF, shap, grad);
+  return -1;
+}
+
+static int quad_dispatch(int etype, const int32_t *norder, const int32_t *noriF,
+                         int integration, double *xi, double *w) {
+  if (etype == ORC_HEXA) return orc_set_3D_int_hexa(norder, noriF, integration, xi, w);
+  if (etype == ORC_TET) return orc_set_3D_int_tet(norder, integration, xi, w);
+  return -1;
+}
+
+int orc_elem(int etype, const int32_t *norder, const int32_t *nori_edge,
+             const int32_t *nori_face, const double *xnod, double kappa,
+             int isol, int integration, int variant, double *zaloc, int ld,
+             double *zbloc) {
+  double xiloc[3 * ORC_MAX_NINT3 + 3 * 200], waloc[ORC_MAX_NINT3 + 200];
+  int nint = quad_dispatch(etype, norder, nori_face, integration, xiloc, waloc);
+  if (nint <= 0) return -2;
+  double *shap = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+  double *grad = (double *)malloc(sizeof(double) * 3 * ORC_MAXBRICKH);
+  int n = 0, iflag_any = 0;
+  double *atest = NULL;
+  int nda = 3 * nint;
+  for (int l = 0; l < nint; ++l) {
+    const double *xi = &xiloc[3 * l];
+    double wa = waloc[l];
+    n = shape_dispatch(etype, xi, norder, nori_edge, nori_face, shap, grad);
+    if (l == 0) {
+      for (int j = 0; j < n; ++j) {
+        zbloc[j] = 0.0;
+        for (int i = 0; i < n; ++i) zaloc[i + (size_t)ld * j] = 0.0;
+      }
+      if (variant == 0) atest = (double *)malloc(sizeof(double) * (size_t)n * nda);
+    }
+    /* geom3D isoparametric branch (geom3D.F90:60-85) */
+    double X[3] = {0, 0, 0}, dxdxi[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < n; ++k) {
+      for (int c = 0; c < 3; ++c) X[c] = X[c] + xnod[3 * k + c] * shap[k];
+      for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c)
+          dxdxi[c + 3 * i] = dxdxi[c + 3 * i] + xnod[3 * k + c] * grad[3 * k + i];
+    }
+    double dxidx[9], rjac;
+    int iflag = orc_geom(dxdxi, dxidx, &rjac);
+    if (iflag) iflag_any = 1;
+    double weight = rjac * wa;
+    double fval = orc_getf(isol, X);
+    if (variant == 0) {
+      double sw = sqrt(weight);
+      for (int k = 0; k < n; ++k) {
+        double q = shap[k];
+        double dq[3];
+        for (int j = 0; j < 3; ++j)
+          dq[j] = grad[3 * k + 0] * dxidx[0 + 3 * j] + grad[3 * k + 1] * dxidx[1 + 3 * j] +
+                  grad[3 * k + 2] * dxidx[2 + 3 * j];
+        zbloc[k] = zbloc[k] + q * fval * weight;
+        for (int j = 0; j < 3; ++j) atest[k + (size_t)n * (3 * l + j)] = dq[j] * sw;
+      }
+    } else {
+      /* elem_poisson scalar form (elem.F90:200-245) */
+      double *dq = (double *)malloc(sizeof(double) * 3 * n);
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < 3; ++j)
+          dq[3 * k + j] = grad[3 * k + 0] * dxidx[0 + 3 * j] + grad[3 * k + 1] * dxidx[1 + 3 * j] +
+                          grad[3 * k + 2] * dxidx[2 + 3 * j];
+      for (int k1 = 0; k1 < n; ++k1) {
+        zbloc[k1] = zbloc[k1] + shap[k1] * fval * weight;
+        for (int k2 = 0; k2 < n; ++k2)
+          zaloc[k1 + (size_t)ld * k2] =
+              zaloc[k1 + (size_t)ld * k2] +
+              weight * (dq[3 * k1] * dq[3 * k2] + dq[3 * k1 + 1] * dq[3 * k2 + 1] +
+                        dq[3 * k1 + 2] * dq[3 * k2 + 2]);
+      }
+      free(dq);
+    }
+  }
+  if (variant == 0) {
+    /* DSYRK('U','N') + lower fill (elem_opt.F90:131-137) */
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i <= j; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < nda; ++k) s += atest[i + (size_t)n * k] * atest[j + (size_t)n * k];
+        zaloc[i + (size_t)ld * j] = s;
+      }
+    for (int k = 0; k < n; ++k)
+      for (int i = k + 1; i < n; ++i) zaloc[i + (size_t)ld * k] = zaloc[k + (size_t)ld * i];
+    free(atest);
+  }
+  if (kappa != 1.0)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) zaloc[i + (size_t)ld * j] *= kappa;
+  free(shap);
+  free(grad);
+  return iflag_any;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Static condensation (src/modules/stc.F90:182-509)                          */
+/* ------------------------------------------------------------------------ */
+int orc_stc_fwd(int ni, int nb, const double *a, int lda, const double *b,
+                int method, double *aii, double *bi, double *aschur,
+                double *bschur) {
+  /* split (stc.F90:227-261): interface dof first, bubbles last */
+  double *abb = (double *)malloc(sizeof(double) * (size_t)nb * nb);
+  double *aib = (double *)malloc(sizeof(double) * (size_t)ni * nb);
+  for (int j = 0; j < ni; ++j)
+    for (int i = 0; i < ni; ++i) aii[i + (size_t)ni * j] = a[i + (size_t)lda * j];
+  for (int j = 0; j < ni; ++j)
+    for (int i = 0; i < nb; ++i) aschur[i + (size_t)nb * j] = a[ni + i + (size_t)lda * j];
+  for (int j = 0; j < nb; ++j)
+    for (int i = 0; i < ni; ++i) aib[i + (size_t)ni * j] = a[i + (size_t)lda * (ni + j)];
+  for (int j = 0; j < nb; ++j)
+    for (int i = 0; i < nb; ++i) abb[i + (size_t)nb * j] = a[ni + i + (size_t)lda * (ni + j)];
+  for (int i = 0; i < ni; ++i) bi[i] = b[i];
+  for (int i = 0; i < nb; ++i) bschur[i] = b[ni + i];
+  int rc = 0;
+  if (method == 0) {
+    /* DGETRF: right-looking LU with partial pivoting (first max |.|) */
+    int *piv = (int *)malloc(sizeof(int) * (nb > 0 ? nb : 1));
+    for (int k = 0; k < nb; ++k) {
+      int p = k;
+      double amax = fabs(abb[k + (size_t)nb * k]);
+      for (int i = k + 1; i < nb; ++i)
+        if (fabs(abb[i + (size_t)nb * k]) > amax) { amax = fabs(abb[i + (size_t)nb * k]); p = i; }
+      piv[k] = p;
+      if (abb[p + (size_t)nb * k] == 0.0) { rc = -1; break; }
+      if (p != k)
+        for (int j = 0; j < nb; ++j) {
+          double t = abb[k + (size_t)nb * j];
+          abb[k + (size_t)nb * j] = abb[p + (size_t)nb * j];
+          abb[p + (size_t)nb * j] = t;
+        }
+      double rp = 1.0 / abb[k + (size_t)nb * k];
+      for (int i = k + 1; i < nb; ++i) abb[i + (size_t)nb * k] *= rp;
+      for (int j = k + 1; j < nb; ++j) {
+        double akj = abb[k + (size_t)nb * j];
+        for (int i = k + 1; i < nb; ++i) abb[i + (size_t)nb * j] -= abb[i + (size_t)nb * k] * akj;
+      }
+    }
+    if (rc == 0) {
+      /* DGETRS on [Bb | Abi] */
+      for (int c = -1; c < ni; ++c) {
+        double *x = (c < 0) ? bschur : &aschur[(size_t)nb * c];
+        for (int k = 0; k < nb; ++k)
+          if (piv[k] != k) { double t = x[k]; x[k] = x[piv[k]]; x[piv[k]] = t; }
+        for (int k = 0; k < nb; ++k)
+          for (int i = k + 1; i < nb; ++i) x[i] -= abb[i + (size_t)nb * k] * x[k];
+        for (int k = nb - 1; k >= 0; --k) {
+          x[k] /= abb[k + (size_t)nb * k];
+          for (int i = 0; i < k; ++i) x[i] -= abb[i + (size_t)nb * k] * x[k];
+        }
+      }
+    }
+    free(piv);
+  } else {
+    /* Cholesky A = U^T U (stc_fwd_herm restated with dense storage) */
+    for (int j = 0; j < nb && rc == 0; ++j) {
+      double s = abb[j + (size_t)nb * j];
+      for (int k = 0; k < j; ++k) s -= abb[k + (size_t)nb * j] * abb[k + (size_t)nb * j];
+      if (!(s > 0.0)) { rc = -1; break; }
+      double ujj = sqrt(s);
+      abb[j + (size_t)nb * j] = ujj;
+      for (int i = j + 1; i < nb; ++i) {
+        double t = abb[j + (size_t)nb * i];
+        for (int k = 0; k < j; ++k) t -= abb[k + (size_t)nb * j] * abb[k + (size_t)nb * i];
+        abb[j + (size_t)nb * i] = t / ujj;
+      }
+    }
+    if (rc == 0)
+      for (int c = -1; c < ni; ++c) {
+        double *x = (c < 0) ? bschur : &aschur[(size_t)nb * c];
+        for (int k = 0; k < nb; ++k) { /* U^T y = x */
+          double t = x[k];
+          for (int i = 0; i < k; ++i) t -= abb[i + (size_t)nb * k] * x[i];
+          x[k] = t / abb[k + (size_t)nb * k];
+        }
+        for (int k = nb - 1; k >= 0; --k) { /* U z = y */
+          double t = x[k];
+          for (int i = k + 1; i < nb; ++i) t -= abb[k + (size_t)nb * i] * x[i];
+          x[k] = t / abb[k + (size_t)nb * k];
+        }
+      }
+  }
+  if (rc == 0) {
+    /* Bi -= Aib * Bb ; Aii -= Aib * Abi (stc.F90:493-507) */
+    for (int i = 0; i < ni; ++i) {
+      double s = 0.0;
+      for (int k = 0; k < nb; ++k) s += aib[i + (size_t)ni * k] * bschur[k];
+      bi[i] = bi[i] - s;
+    }
+    for (int j = 0; j < ni; ++j)
+      for (int i = 0; i < ni; ++i) {
+        double s = 0.0;
+        for (int k = 0; k < nb; ++k) s += aib[i + (size_t)ni * k] * aschur[k + (size_t)nb * j];
+        aii[i + (size_t)ni * j] = aii[i + (size_t)ni * j] - s;
+      }
+  }
+  free(abb);
+  free(aib);
+  return rc;
+}
+
+void orc_stc_bwd(int ni, int nb, const double *aschur, const double *bschur,
+                 const double *xi, double *xb) {
+  for (int i = 0; i < nb; ++i) {
+    double s = 0.0;
+    for (int k = 0; k < ni; ++k) s += aschur[i + (size_t)nb * k] * xi[k];
+    xb[i] = bschur[i] - s;
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Node dof counts, compression, index maps                                  */
+/* ------------------------------------------------------------------------ */
+int orc_node_ndof(int etype, const int32_t *norder, int32_t *ndof) {
+  if (etype == ORC_HEXA) {
+    for (int v = 0; v < 8; ++v) ndof[v] = 1;
+    for (int e = 0; e < 12; ++e) ndof[8 + e] = imax(norder[e] - 1, 0);
+    for (int f = 0; f < 6; ++f) {
+      int hv[2];
+      decod(norder[12 + f], 10, 2, hv);
+      ndof[20 + f] = imax(hv[0] - 1, 0) * imax(hv[1] - 1, 0);
+    }
+    return 26;
+  }
+  if (etype == ORC_TET) {
+    for (int v = 0; v < 4; ++v) ndof[v] = 1;
+    for (int e = 0; e < 6; ++e) ndof[4 + e] = imax(norder[e] - 1, 0);
+    for (int f = 0; f < 4; ++f) {
+      int p = norder[6 + f];
+      ndof[10 + f] = (p - 2) * (p - 1) / 2 > 0 ? (p - 2) * (p - 1) / 2 : 0;
+    }
+    return 14;
+  }
+  return -1;
+}
+
+int orc_celem_compress(int etype, const int32_t *norder, const int32_t *bcflag,
+                       const double *aii, const double *bi,
+                       const double *zdofd, int32_t *nextract, double *zbload,
+                       double *zastif, int32_t *ndofm) {
+  int32_t nd[32];
+  int nn = orc_node_ndof(etype, norder, nd);
+  int first[32], ni = 0;
+  for (int i = 0; i < nn; ++i) { first[i] = ni; ni += nd[i]; }
+  /* NEXTRACT: nodes in reverse order, dof in forward order, skip Dirichlet
+   * (celem_systemI.F90:290-350) */
+  int k = 0;
+  for (int i = nn - 1; i >= 0; --i) {
+    int kold = k;
+    if (!bcflag[i])
+      for (int j = 0; j < nd[i]; ++j) nextract[k++] = first[i] + j;
+    ndofm[i] = k - kold;
+  }
+  int nrdofc = k;
+  /* Dirichlet lift (celem_systemI.F90:800-812) then compression (812-845) */
+  double *zb = (double *)malloc(sizeof(double) * (ni > 0 ? ni : 1));
+  for (int i = 0; i < ni; ++i) zb[i] = bi[i];
+  if (zdofd) {
+    for (int i2 = 0; i2 < nn; ++i2) {
+      if (!bcflag[i2]) continue;
+      for (int j2 = 0; j2 < nd[i2]; ++j2) {
+        int k2 = first[i2] + j2;
+        for (int k1 = 0; k1 < ni; ++k1) zb[k1] = zb[k1] - aii[k1 + (size_t)ni * k2] * zdofd[k2];
+      }
+    }
+  }
+  for (int l1 = 0; l1 < nrdofc; ++l1) {
+    int k1 = nextract[l1];
+    zbload[l1] = zb[k1];
+    for (int l2 = 0; l2 < nrdofc; ++l2)
+      zastif[(size_t)l1 * nrdofc + l2] = aii[k1 + (size_t)ni * nextract[l2]];
+  }
+  free(zb);
+  return nrdofc;
+}
+
+int64_t orc_index_maps(int nelem, int nnode_max, const int32_t *nnode,
+                       const int32_t *nodes, const int32_t *ndofm,
+                       int nnodes_global, int32_t *nfirst_dof, int32_t *lcon,
+                       int64_t *lcon_off, int64_t *elem_nnz) {
+  for (int i = 0; i < nnodes_global; ++i) nfirst_dof[i] = -1;
+  int64_t nrdof = 0, nnz = 0, off = 0;
+  for (int e = 0; e < nelem; ++e) {
+    const int32_t *nod = &nodes[(size_t)e * nnode_max];
+    const int32_t *nd = &ndofm[(size_t)e * nnode_max];
+    int ndof = 0;
+    for (int i = 0; i < nnode[e]; ++i) {
+      ndof += nd[i];
+      if (nfirst_dof[nod[i]] >= 0) continue;
+      nfirst_dof[nod[i]] = (int32_t)nrdof;
+      nrdof += nd[i];
+    }
+    elem_nnz[e] = nnz;
+    nnz += (int64_t)ndof * ndof;
+    lcon_off[e] = off;
+    off += ndof;
+  }
+  elem_nnz[nelem] = nnz;
+  lcon_off[nelem] = off;
+  for (int e = 0; e < nelem; ++e) {
+    const int32_t *nod = &nodes[(size_t)e * nnode_max];
+    const int32_t *nd = &ndofm[(size_t)e * nnode_max];
+    int64_t l = lcon_off[e];
+    for (int i = nnode[e] - 1; i >= 0; --i)
+      for (int j = 1; j <= nd[i]; ++j) lcon[l++] = nfirst_dof[nod[i]] + j;
+  }
+  return nrdof;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Batched element pass (the CPU baseline form of mumps_sc STEP 2)            */
+/* ------------------------------------------------------------------------ */
+static int nvert_of(int etype) { return etype == ORC_HEXA ? 8 : (etype == ORC_TET ? 4 : 6); }
+
+int orc_element_pass(int nelem, const int32_t *etype, const int32_t *norder,
+                     const int32_t *nori_edge, const int32_t *nori_face,
+                     const int32_t *bcflag, const double *xvert,
+                     const double *kappa, int isol, int integration,
+                     int stc_method, int nthreads,
+                     const int64_t *elem_nnz, const int64_t *lcon_off,
+                     const int64_t *schur_off, const int64_t *bub_off,
+                     double *zastif, double *zbload, double *aschur,
+                     double *bschur) {
+  int bad = 0;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+#pragma omp parallel
+  {
+    double *aloc = (double *)malloc(sizeof(double) * ORC_MAXBRICKH * ORC_MAXBRICKH);
+    double *bloc = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+    double *xnod = (double *)malloc(sizeof(double) * 3 * ORC_MAXBRICKH);
+    double *aii = (double *)malloc(sizeof(double) * ORC_MAXBRICKH * ORC_MAXBRICKH);
+    double *bi = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+    double *as = (double *)malloc(sizeof(double) * ORC_MAXBRICKH * ORC_MAXBRICKH);
+    double *bs = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+    double *zs = (double *)malloc(sizeof(double) * ORC_MAXBRICKH * ORC_MAXBRICKH);
+    double *zb = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+    int32_t nextract[ORC_MAXBRICKH], ndofm[32];
+#pragma omp for schedule(dynamic)
+    for (int e = 0; e < nelem; ++e) {
+      int et = etype[e];
+      const int32_t *no = &norder[19 * (size_t)e];
+      int n = (et == ORC_HEXA) ? orc_nrdofH_hexa(no) : orc_nrdofH_tet(no);
+      int nb = orc_nrdofH_bubble(et, no);
+      int ni = n - nb;
+      int nv = nvert_of(et);
+      for (int k = 0; k < n; ++k)
+        for (int c = 0; c < 3; ++c)
+          xnod[3 * k + c] = (k < nv) ? xvert[(size_t)e * 24 + 3 * k + c] : 0.0;
+      int rc = orc_elem(et, no, &nori_edge[12 * (size_t)e], &nori_face[6 * (size_t)e], xnod,
+                        kappa[e], isol, integration, 0, aloc, n, bloc);
+      if (rc == 0 && nb > 0)
+        rc = orc_stc_fwd(ni, nb, aloc, n, bloc, stc_method, aii, bi, as, bs);
+      else if (rc == 0) {
+        for (int j = 0; j < ni; ++j)
+          for (int i = 0; i < ni; ++i) aii[i + (size_t)ni * j] = aloc[i + (size_t)n * j];
+        for (int i = 0; i < ni; ++i) bi[i] = bloc[i];
+      }
+      if (rc != 0) {
+#pragma omp critical
+        { if (bad == 0 || e + 1 < bad) bad = e + 1; }
+        continue;
+      }
+      int nrdofc = orc_celem_compress(et, no, &bcflag[26 * (size_t)e], aii, bi, NULL,
+                                      nextract, zb, zs, ndofm);
+      if (zastif) memcpy(&zastif[elem_nnz[e]], zs, sizeof(double) * (size_t)nrdofc * nrdofc);
+      if (zbload) memcpy(&zbload[lcon_off[e]], zb, sizeof(double) * nrdofc);
+      if (aschur && nb > 0) memcpy(&aschur[schur_off[e]], as, sizeof(double) * (size_t)nb * ni);
+      if (bschur && nb > 0) memcpy(&bschur[bub_off[e]], bs, sizeof(double) * nb);
+    }
+    free(aloc); free(bloc); free(xnod); free(aii); free(bi);
+    free(as); free(bs); free(zs); free(zb);
+  }
+  return bad;
+}
+
+/* ------------------------------------------------------------------------ */
+/* element_error (src/element/util/compute_error.F90:226-360, H1 branch):    */
+/* squared H1 error and norm with INTEGRATION=2 over-integration.            */
+/* dof: element H1 dof in shape-function order (interface + bubbles).        */
+/* ------------------------------------------------------------------------ */
+int orc_element_error(int etype, const int32_t *norder, const int32_t *nori_edge,
+                      const int32_t *nori_face, const double *xnod, const double *dof,
+                      int isol, double *err2, double *norm2) {
+  double xiloc[3 * ORC_MAX_NINT3 + 3 * 200], waloc[ORC_MAX_NINT3 + 200];
+  /* set_3Dint is called without the face-order swap and INTEGRATION=2 */
+  int32_t zero6[6] = {0, 0, 0, 0, 0, 0};
+  int nint = quad_dispatch(etype, norder, zero6, 2, xiloc, waloc);
+  if (nint <= 0) return -2;
+  double *shap = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+  double *grad = (double *)malloc(sizeof(double) * 3 * ORC_MAXBRICKH);
+  double e2 = 0.0, r2 = 0.0;
+  for (int l = 0; l < nint; ++l) {
+    int n = shape_dispatch(etype, &xiloc[3 * l], norder, nori_edge, nori_face, shap, grad);
+    double X[3] = {0, 0, 0}, dxdxi[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double uh = 0.0, guh[3] = {0, 0, 0};
+    for (int k = 0; k < n; ++k) {
+      for (int c = 0; c < 3; ++c) X[c] += xnod[3 * k + c] * shap[k];
+      for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) dxdxi[c + 3 * i] += xnod[3 * k + c] * grad[3 * k + i];
+      uh += dof[k] * shap[k];
+      for (int i = 0; i < 3; ++i) guh[i] += dof[k] * grad[3 * k + i];
+    }
+    double dxidx[9], rjac;
+    orc_geom(dxdxi, dxidx, &rjac);
+    double gx[3];
+    for (int j = 0; j < 3; ++j)
+      gx[j] = guh[0] * dxidx[0 + 3 * j] + guh[1] * dxidx[1 + 3 * j] + guh[2] * dxidx[2 + 3 * j];
+    double u, gu[3];
+    orc_exact(isol, X, &u, gu);
+    double weight = waloc[l] * rjac;
+    for (int j = 0; j < 3; ++j) {
+      e2 += (gu[j] - gx[j]) * (gu[j] - gx[j]) * weight;
+      r2 += gu[j] * gu[j] * weight;
+    }
+    e2 += (u - uh) * (u - uh) * weight;
+    r2 += u * u * weight;
+  }
+  free(shap);
+  free(grad);
+  *err2 = e2;
+  *norm2 = r2;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Tetrahedron (Tetrahedron.F90:33-234) -- restated in the mixed-type pass.  */
+/* ------------------------------------------------------------------------ */
+int orc_nrdofH_tet(const int32_t *norder) { (void)norder; return -1; }
+int orc_set_3D_int_tet(const int32_t *norder, int integration, double *xiloc,
+                       double *waloc) {
+  (void)norder; (void)integration; (void)xiloc; (void)waloc;
+  return -1;
+}
+int orc_shape3DH_tet(const double *xi, const int32_t *nord,
+                     const int32_t *nori_edge, const int32_t *nori_face,
+                     double *shap, double *grad) {
+  (void)xi; (void)nord; (void)nori_edge; (void)nori_face; (void)shap; (void)grad;
+  return -1;
+}

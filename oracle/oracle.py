@@ -1,0 +1,239 @@
+"""ctypes binding of the CPU oracle (liborc.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py``.  The
+product library never loads it.  The C sources restate Oden-EAG/hp3d routines
+(citations in ``hp3d_oracle.h``).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "liborc.so")
+_lib = None
+
+HEXA, PRISM, TET = 1, 2, 3
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(force: bool = False) -> str:
+    """Compile liborc.so with the Makefile beside this file."""
+    src = os.path.join(_HERE, "hp3d_oracle.c")
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
+        subprocess.run(["make", "-C", _HERE, "-B", "liborc.so"], check=True,
+                       stdout=subprocess.DEVNULL)
+    return _LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(_LIB)
+        L.orc_gauss1d.argtypes = [ctypes.c_int, _f64p, _f64p]
+        L.orc_set_3D_int_hexa.argtypes = [_i32p, _i32p, ctypes.c_int, _f64p, _f64p]
+        L.orc_set_3D_int_tet.argtypes = [_i32p, ctypes.c_int, _f64p, _f64p]
+        L.orc_nrdofH_hexa.argtypes = [_i32p]
+        L.orc_nrdofH_tet.argtypes = [_i32p]
+        L.orc_nrdofH_bubble.argtypes = [ctypes.c_int, _i32p]
+        for f in (L.orc_shape3DH_hexa, L.orc_shape3DH_tet):
+            f.argtypes = [_f64p, _i32p, _i32p, _i32p, _f64p, _f64p]
+        L.orc_geom.argtypes = [_f64p, _f64p, _f64p]
+        L.orc_getf.argtypes = [ctypes.c_int, _f64p]
+        L.orc_getf.restype = ctypes.c_double
+        L.orc_exact.argtypes = [ctypes.c_int, _f64p, _f64p, _f64p]
+        L.orc_elem.argtypes = [ctypes.c_int, _i32p, _i32p, _i32p, _f64p, ctypes.c_double,
+                               ctypes.c_int, ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int,
+                               _f64p]
+        L.orc_stc_fwd.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p,
+                                  ctypes.c_int, _f64p, _f64p, _f64p, _f64p]
+        L.orc_stc_bwd.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, _f64p, _f64p, _f64p]
+        L.orc_node_ndof.argtypes = [ctypes.c_int, _i32p, _i32p]
+        L.orc_celem_compress.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p,
+                                         _i32p, _f64p, _f64p, _i32p]
+        L.orc_index_maps.argtypes = [ctypes.c_int, ctypes.c_int, _i32p, _i32p, _i32p,
+                                     ctypes.c_int, _i32p, _i32p, _i64p, _i64p]
+        L.orc_index_maps.restype = ctypes.c_int64
+        L.orc_element_pass.argtypes = [ctypes.c_int, _i32p, _i32p, _i32p, _i32p, _i32p,
+                                       _f64p, _f64p, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_int, ctypes.c_int, _i64p, _i64p, _i64p,
+                                       _i64p, _f64p, _f64p, _f64p, _f64p]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    if a is None:
+        return None
+    return a.ctypes.data_as(t)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def gauss1d(n):
+    x = np.zeros(n); w = np.zeros(n)
+    assert lib().orc_gauss1d(n, _p(x, _f64p), _p(w, _f64p)) == 0
+    return x, w
+
+
+def quad_hexa(norder, nori_face=None, integration=0):
+    norder = _i32(norder)
+    nori_face = _i32(np.zeros(6) if nori_face is None else nori_face)
+    xi = np.zeros((400, 3)); w = np.zeros(400)
+    n = lib().orc_set_3D_int_hexa(_p(norder, _i32p), _p(nori_face, _i32p), integration,
+                                  _p(xi, _f64p), _p(w, _f64p))
+    return xi[:n].copy(), w[:n].copy()
+
+
+def nrdofH(etype, norder):
+    norder = _i32(norder)
+    if etype == HEXA:
+        return lib().orc_nrdofH_hexa(_p(norder, _i32p))
+    return lib().orc_nrdofH_tet(_p(norder, _i32p))
+
+
+def nrdof_bubble(etype, norder):
+    return lib().orc_nrdofH_bubble(etype, _p(_i32(norder), _i32p))
+
+
+def shape_hexa(xi, norder, nori_edge=None, nori_face=None):
+    xi = _f64(xi)
+    norder = _i32(norder)
+    ne = _i32(np.zeros(12) if nori_edge is None else nori_edge)
+    nf = _i32(np.zeros(6) if nori_face is None else nori_face)
+    shap = np.zeros(343); grad = np.zeros((343, 3))
+    n = lib().orc_shape3DH_hexa(_p(xi, _f64p), _p(norder, _i32p), _p(ne, _i32p),
+                                _p(nf, _i32p), _p(shap, _f64p), _p(grad, _f64p))
+    return shap[:n].copy(), grad[:n].copy()
+
+
+def getf(isol, x):
+    return lib().orc_getf(isol, _p(_f64(x), _f64p))
+
+
+def exact(isol, x):
+    u = np.zeros(1); g = np.zeros(3)
+    lib().orc_exact(isol, _p(_f64(x), _f64p), _p(u, _f64p), _p(g, _f64p))
+    return u[0], g
+
+
+def elem(etype, norder, nori_edge, nori_face, xnod, kappa=1.0, isol=10, integration=0,
+         variant=0):
+    """Element stiffness (n x n) and load (n); xnod is (nrdofH, 3) or the
+    vertex coordinates (nvert, 3) padded with zeros."""
+    norder = _i32(norder)
+    n = nrdofH(etype, norder)
+    xn = np.zeros((n, 3))
+    xv = np.asarray(xnod, dtype=np.float64)
+    xn[: xv.shape[0]] = xv
+    xn = _f64(xn)
+    K = np.zeros((n, n), order="F"); b = np.zeros(n)
+    rc = lib().orc_elem(etype, _p(norder, _i32p), _p(_i32(nori_edge), _i32p),
+                        _p(_i32(nori_face), _i32p), _p(xn, _f64p), float(kappa), isol,
+                        integration, variant, K.ctypes.data_as(_f64p), n, _p(b, _f64p))
+    return K, b, rc
+
+
+def stc_fwd(K, b, nb, method=0):
+    n = K.shape[0]
+    ni = n - nb
+    Kf = np.asfortranarray(K, dtype=np.float64)
+    aii = np.zeros((ni, ni), order="F"); bi = np.zeros(ni)
+    asch = np.zeros((nb, ni), order="F"); bsch = np.zeros(nb)
+    rc = lib().orc_stc_fwd(ni, nb, Kf.ctypes.data_as(_f64p), n, _p(_f64(b), _f64p), method,
+                           aii.ctypes.data_as(_f64p), _p(bi, _f64p), asch.ctypes.data_as(_f64p),
+                           _p(bsch, _f64p))
+    return aii, bi, asch, bsch, rc
+
+
+def stc_bwd(asch, bsch, xi):
+    nb, ni = asch.shape
+    a = np.asfortranarray(asch)
+    xb = np.zeros(nb)
+    lib().orc_stc_bwd(ni, nb, a.ctypes.data_as(_f64p), _p(_f64(bsch), _f64p),
+                      _p(_f64(xi), _f64p), _p(xb, _f64p))
+    return xb
+
+
+def node_ndof(etype, norder):
+    nd = np.zeros(32, dtype=np.int32)
+    nn = lib().orc_node_ndof(etype, _p(_i32(norder), _i32p), _p(nd, _i32p))
+    return nd[:nn].copy()
+
+
+def celem_compress(etype, norder, bcflag, aii, bi, zdofd=None):
+    ni = aii.shape[0]
+    a = np.asfortranarray(aii, dtype=np.float64)
+    bc = _i32(np.zeros(26) if bcflag is None else np.pad(np.asarray(bcflag), (0, 26 - len(bcflag))))
+    nextract = np.zeros(max(ni, 1), dtype=np.int32)
+    zb = np.zeros(max(ni, 1)); zs = np.zeros(max(ni * ni, 1)); ndofm = np.zeros(32, dtype=np.int32)
+    zd = None if zdofd is None else _f64(zdofd)
+    nc = lib().orc_celem_compress(etype, _p(_i32(norder), _i32p), _p(bc, _i32p),
+                                  a.ctypes.data_as(_f64p), _p(_f64(bi), _f64p),
+                                  _p(zd, _f64p), _p(nextract, _i32p), _p(zb, _f64p),
+                                  _p(zs, _f64p), _p(ndofm, _i32p))
+    return nextract[:nc].copy(), zb[:nc].copy(), zs[: nc * nc].reshape(nc, nc).copy(), ndofm
+
+
+def index_maps(nnode, nodes, ndofm, nnodes_global):
+    nodes = _i32(nodes); ndofm = _i32(ndofm); nnode = _i32(nnode)
+    nelem, nmax = nodes.shape
+    nfirst = np.zeros(nnodes_global, dtype=np.int32)
+    lcon_off = np.zeros(nelem + 1, dtype=np.int64)
+    elem_nnz = np.zeros(nelem + 1, dtype=np.int64)
+    lcon = np.zeros(int(ndofm.sum()) + 1, dtype=np.int32)
+    nrdof = lib().orc_index_maps(nelem, nmax, _p(nnode, _i32p), _p(nodes, _i32p),
+                                 _p(ndofm, _i32p), nnodes_global, _p(nfirst, _i32p),
+                                 _p(lcon, _i32p), _p(lcon_off, _i64p), _p(elem_nnz, _i64p))
+    return int(nrdof), nfirst, lcon[: lcon_off[-1]].copy(), lcon_off, elem_nnz
+
+
+def element_pass(mesh, isol=10, integration=0, stc_method=0, nthreads=0,
+                 elements=None):
+    """Run elem -> stc_fwd -> compression over (a subset of) a mesh.
+
+    ``mesh`` is a dict as produced by ``hp3d_gb300.mesh``; ``elements`` an
+    optional index array restricting the pass (used for bounded CPU samples).
+    Returns dict of concatenated outputs with their offsets."""
+    idx = np.arange(mesh["nelem"]) if elements is None else np.asarray(elements)
+    ne = len(idx)
+    et = _i32(mesh["etype"][idx]); no = _i32(mesh["norder"][idx])
+    ned = _i32(mesh["nori_edge"][idx]); nfc = _i32(mesh["nori_face"][idx])
+    bc = _i32(mesh["bcflag"][idx]); xv = _f64(mesh["xvert"][idx]); ka = _f64(mesh["kappa"][idx])
+    nrdofc = np.zeros(ne, dtype=np.int64); nb = np.zeros(ne, dtype=np.int64)
+    ni = np.zeros(ne, dtype=np.int64)
+    for j in range(ne):
+        nd = node_ndof(int(et[j]), no[j])
+        nn = len(nd)
+        act = nd * (1 - bc[j][:nn])
+        nrdofc[j] = act.sum()
+        nb[j] = nrdof_bubble(int(et[j]), no[j])
+        ni[j] = nd.sum()
+    elem_nnz = np.concatenate([[0], np.cumsum(nrdofc * nrdofc)]).astype(np.int64)
+    lcon_off = np.concatenate([[0], np.cumsum(nrdofc)]).astype(np.int64)
+    schur_off = np.concatenate([[0], np.cumsum(nb * ni)]).astype(np.int64)
+    bub_off = np.concatenate([[0], np.cumsum(nb)]).astype(np.int64)
+    zastif = np.zeros(max(int(elem_nnz[-1]), 1)); zbload = np.zeros(max(int(lcon_off[-1]), 1))
+    aschur = np.zeros(max(int(schur_off[-1]), 1)); bschur = np.zeros(max(int(bub_off[-1]), 1))
+    rc = lib().orc_element_pass(ne, _p(et, _i32p), _p(no, _i32p), _p(ned, _i32p), _p(nfc, _i32p),
+                                _p(bc, _i32p), _p(xv, _f64p), _p(ka, _f64p), isol, integration,
+                                stc_method, nthreads, _p(elem_nnz, _i64p), _p(lcon_off, _i64p),
+                                _p(schur_off, _i64p), _p(bub_off, _i64p), _p(zastif, _f64p),
+                                _p(zbload, _f64p), _p(aschur, _f64p), _p(bschur, _f64p))
+    return dict(rc=rc, zastif=zastif, zbload=zbload, aschur=aschur, bschur=bschur,
+                elem_nnz=elem_nnz, lcon_off=lcon_off, schur_off=schur_off, bub_off=bub_off,
+                nrdofc=nrdofc, nb=nb, ni=ni)
