@@ -1,0 +1,322 @@
+#!/usr/bin/env python
+"""Benchmark of the hp3D element pass on GB300 (one JSON line on rank 0).
+
+Workload (the metric's configuration): Galerkin Poisson on 24^3 = 13,824
+hexahedra of the unit cube, isotropic p = 5 (216 H1 dof per element,
+64 bubbles, 152 interface dof), INTEGRATION = 1 (7^3 Gauss points),
+interior vertices perturbed by U(-0.15h, 0.15h) (trilinear geometry),
+kappa_e = 10**U(-2, 2), f = 3 pi^2 sin(pi x) sin(pi y) sin(pi z),
+homogeneous Dirichlet BC on the whole boundary.  Seeded synthetic mesh.
+
+A step = one element pass over the whole mesh: geometry + load, B^T D B
+contraction, static condensation, compression and index maps (everything the
+reference's mumps_sc STEP 2 element loop computes before MUMPS).
+``value`` times ``hp3dg_batch_run`` with the inputs already in HBM;
+``e2e`` times submit (host -> device) + run + download (device -> host of
+the condensed matrices, loads, Schur blocks and LCON) through the C ABI.
+
+--impl reference times the CPU oracle (a restatement of the reference's
+Fortran element loop; the Fortran reference cannot be compiled here) with
+OpenMP over the host cores on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "condensed elements/s at p=5: mixed-precision vs plain FP64 GPU at 1e-10 rel err"
+
+
+def make_mesh(n, p, seed=12345):
+    from hp3d_gb300 import mesh as M
+    return M.structured_hexa(n, p, perturb=0.15, kappa_logrange=(-2, 2), seed=seed)
+
+
+def per_element_work(n, nint):
+    """Algorithmic work per element (roofline)."""
+    nb = (round(n ** (1 / 3)) - 1) ** 3
+    ni = n - nb
+    ncols = n * (n + 1) // 2
+    f_syrk = n * (n + 1) * 3 * nint
+    f_dm = 2 * 6 * nint * ncols          # one D.M product (FLOP)
+    f_stc = (2 / 3) * nb ** 3 + 2 * nb * nb * (ni + 1) + 2 * ni * ni * nb + 2 * ni * nb
+    bytes_out = 8 * (ni * ni + ni + nb * ni + nb) + 4 * ni
+    bytes_in = 8 * (24 + 1) + 364
+    return dict(nb=nb, ni=ni, ncols=ncols, f_syrk=f_syrk, f_dm=f_dm, f_stc=f_stc,
+                bytes=bytes_out + bytes_in)
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def cpu_baseline(mesh, isol, integration, seconds=15.0, nthreads=0):
+    """Time the oracle (OpenMP, all host cores) on a bounded sample."""
+    from oracle import oracle as O
+    cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
+    # size the sample: one probe round of `cores` elements
+    probe = np.arange(min(cores, mesh["nelem"]))
+    t0 = time.perf_counter()
+    O.element_pass(mesh, isol=isol, integration=integration, stc_method=0, nthreads=cores,
+                   elements=probe)
+    dt = time.perf_counter() - t0
+    per_round = max(dt, 1e-3)
+    rounds = max(1, int(seconds / per_round))
+    ns = min(mesh["nelem"], rounds * len(probe))
+    sample = np.arange(ns)
+    t0 = time.perf_counter()
+    r = O.element_pass(mesh, isol=isol, integration=integration, stc_method=0, nthreads=cores,
+                       elements=sample)
+    dt = time.perf_counter() - t0
+    assert r["rc"] == 0
+    return {"value": ns / dt, "unit": "elements/s", "cores": cores, "kind": "port",
+            "sample": f"{ns} of {mesh['nelem']} elements (first in ELEM_ORDER), one pass, "
+                      f"{dt:.1f} s, oracle C restatement (elem_opt DSYRK form + LU condensation "
+                      f"+ compression), OpenMP"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    mesh = make_mesh(args.n, args.p)
+    vals = []
+    cb = None
+    for i in range(args.warmup + args.steps):
+        c = cpu_baseline(mesh, args.isol, args.integration, seconds=args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(c["value"])
+            cb = c
+    v = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * mesh["nelem"] / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_dict(args, world),
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args, world):
+    return {"workload": f"galerkin_poisson_hexa_{args.n}^3_p{args.p}_integration{args.integration}",
+            "elements_per_gpu": args.n ** 3, "p": args.p, "quadrature_points": (min(args.p + args.integration, 6) + 1) ** 3,
+            "perturbation": "U(-0.15h,0.15h) interior vertices", "kappa": "10**U(-2,2)",
+            "precision": args.precision, "parallelism": f"replicas{world}" if world > 1 else "single",
+            "l2": "working set per step > L2 (condensed outputs 3.7 GB), no flush needed"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--n", type=int, default=24)
+    ap.add_argument("--p", type=int, default=5)
+    ap.add_argument("--integration", type=int, default=1)
+    ap.add_argument("--isol", type=int, default=10)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    from hp3d_gb300 import build as B
+    B.build()
+    from hp3d_gb300 import hp3dg as H
+
+    mesh = make_mesh(args.n, args.p, seed=12345 + rank)
+    prec = H.MIXED if args.precision == "mixed" else H.FP64
+    stream = torch.cuda.current_stream()
+
+    def timed(precision, steps, warmup):
+        ep = H.ElementPass(precision, integration=args.integration, isol=args.isol, timing=True,
+                           device=local)
+        ep.set_stream(stream.cuda_stream)
+        ep.submit(mesh)
+        for _ in range(warmup):
+            ep.run()
+        ep.sync()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        phases = []
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            ep.run()
+            ep.sync()
+            phases.append(ep.phase_times())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        if world > 1:
+            t = torch.tensor([ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ep, ms, phases
+
+    clk = ClockSampler(local)
+    clk.start()
+    ep, ms, phases = timed(prec, args.steps, args.warmup)
+    clocks = clk.stop()
+    ms_step = ms / args.steps
+    nel = mesh["nelem"]
+    value = world * nel / (ms_step / 1000.0)
+
+    # end to end through the C ABI with host buffers (submit + run + download)
+    nnz, nl, ns, nbub = ep.sizes()
+    h2d = int(ep.desc.nbytes + ep.xvert.nbytes + ep.kappa.nbytes)
+    d2h = int(8 * (nnz + nl + ns + nbub) + 4 * nl)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        ep.submit(mesh)
+        ep.run()
+        ep.download()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * nel / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * e2e_s}
+
+    # the plain FP64 GPU form on the same mesh (the comparison the metric names)
+    fp64 = None
+    if prec == H.MIXED and not args.no_fp64_compare:
+        ep64, ms64, ph64 = timed(H.FP64, max(2, min(3, args.steps)), 1)
+        fp64 = {"value": world * nel / (ms64 / max(2, min(3, args.steps)) / 1000.0),
+                "unit": "elements/s", "phase_ms": [round(x, 3) for x in ph64[-1]]}
+        ep64.close()
+
+    nint = (min(args.p + args.integration, 6) + 1) ** 3
+    n = (args.p + 1) ** 3
+    w = per_element_work(n, nint)
+    ph = np.median(np.array(phases), axis=0)
+    hbm, bf16, peak_kind = measured_peaks()
+    # dominant kernel = contraction phase (one launch per bin; one bin here)
+    t_con = ph[2] / 1000.0
+    if prec == H.MIXED:
+        pairs = ep.ozaki_pairs() if hasattr(ep, "ozaki_pairs") else None
+        flops = nel * w["f_dm"] * (pairs or 0)
+        roof = {"bound": "tensor", "achieved": flops / t_con / 1e12 if t_con > 0 else None,
+                "peak": bf16, "unit": "TFLOP/s", "kernel": "k_ozaki_gemm",
+                "note": f"{pairs} digit-pair products of the D.M contraction; peak {peak_kind}"}
+    else:
+        flops = nel * w["f_syrk"]
+        roof = {"bound": "tensor", "achieved": flops / t_con / 1e12 if t_con > 0 else None,
+                "peak": bf16, "unit": "TFLOP/s", "kernel": "k_contract_fp64",
+                "note": "FP64 CUDA-core contraction measured against the bf16 peak"}
+    if roof["achieved"] is not None:
+        roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["traffic"] = None
+
+    cb = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cb = cpu_baseline(mesh, args.isol, args.integration, seconds=args.cpu_seconds)
+
+    launches_per_step = 10 if prec == H.FP64 else 11
+    line = {"metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if prec == H.FP64 else "bf16-digits->f64", "data": "synthetic",
+            "config": config_dict(args, world), "e2e": e2e, "roofline": roof,
+            "cpu_baseline": cb, "clocks": clocks,
+            "gpu_launches": launches_per_step * args.steps,
+            "phase_ms": {"tables": float(ph[0]), "geometry_load": float(ph[1]),
+                         "contraction": float(ph[2]), "condensation": float(ph[3]),
+                         "index_maps": float(ph[4]), "pass": float(ph[5])},
+            "fp64_gpu": fp64,
+            "speedup_vs_fp64_gpu": (value / fp64["value"]) if fp64 else None}
+    ep.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,663 @@
+// api.cu -- host runtime behind the C ABI (include/hp3dg.h).
+//
+// Owns the device buffers of one batch, groups elements into bins (type +
+// local order tuple, find_order_loc), builds the per-bin reference tables
+// once, and launches the pass on one stream.  The descriptor bookkeeping of
+// mumps_sc STEP 1 (solver/omp_mumps/mumps_sc.F90:102-188: dof counts,
+// elem_nnz offsets) and of celem_systemI's extraction vector
+// (constrs/celem_systemI.F90:290-350: NEXTRACT, nodes in reverse order,
+// Dirichlet dof skipped) happens here at submit time; everything numerical
+// happens on the GPU.
+#include "../../include/hp3dg.h"
+#include "hp3dg_internal.cuh"
+#include "hp3dg_kernels.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+using namespace hp3dg;
+
+namespace {
+
+// 1D Gauss-Legendre tables of the reference (gauss_quadrature.F90:518-660,
+// rescaled to [0,1] as at 749-750); the same rounded decimal values.
+const double GX[10][10] = {
+    {0.0},
+    {-.577350269189626, .577350269189626},
+    {-.774596669241483, .000000000000000, .774596669241483},
+    {-.861136311594053, -.339981043584856, .339981043584856, .861136311594053},
+    {-.906179845938664, -.538469310105683, .000000000000000, .538469310105683, .906179845938664},
+    {-.932469514203152, -.661209386466265, -.238619186083197, .238619186083197, .661209386466265,
+     .932469514203152},
+    {-.949107912342759, -.741531185599394, -.405845151377397, .000000000000000, .405845151377397,
+     .741531185599394, .949107912342759},
+    {-.960289856497536, -.796666477413627, -.525532409916329, -.183434642495650, .183434642495650,
+     .525532409916329, .796666477413627, .960289856497536},
+    {-.968160239507626, -.836031107326636, -.613371432700590, -.324253423403809, .000000000000000,
+     .324253423403809, .613371432700590, .836031107326636, .968160239507626},
+    {-.9739065285171717200779640, -.8650633666889845107320967, -.6794095682990244062343274,
+     -.4333953941292471907992659, -.1488743389816312108848260, .1488743389816312108848260,
+     .4333953941292471907992659, .6794095682990244062343274, .8650633666889845107320967,
+     .9739065285171717200779640}};
+const double GW[10][10] = {
+    {2.000000000000000},
+    {1.000000000000000, 1.000000000000000},
+    {.555555555555556, .888888888888889, .555555555555556},
+    {.347854845137454, .652145154862546, .652145154862546, .347854845137454},
+    {.236926885056189, .478628670499366, .568888888888889, .478628670499366, .236926885056189},
+    {.171324492379170, .360761573048139, .467913934572691, .467913934572691, .360761573048139,
+     .171324492379170},
+    {.129484966168870, .279705391489277, .381830050505119, .417959183673469, .381830050505119,
+     .279705391489277, .129484966168870},
+    {.101228536290376, .222381034453374, .313706645877887, .362683783378362, .362683783378362,
+     .313706645877887, .222381034453374, .101228536290376},
+    {.081274388361574, .180648160694857, .260610696402935, .312347077040003, .330239355001260,
+     .312347077040003, .260610696402935, .180648160694857, .081274388361574},
+    {.0666713443086881375935688, .1494513491505805931457763, .2190863625159820439955349,
+     .2692667193099963550912269, .2955242247147528701738930, .2955242247147528701738930,
+     .2692667193099963550912269, .2190863625159820439955349, .1494513491505805931457763,
+     .0666713443086881375935688}};
+
+// set_3Dint_aux BRICK branch (set_3D_int.F90:155-245) on local orders.
+int hexa_quadrature(const int* nl, int integration, std::vector<double>& xi,
+                    std::vector<double>& w) {
+  int nx = 0, ny = 0, nz = 0;
+  auto mx = [](int& a, int b) { a = std::max(a, b); };
+  for (int i = 1; i <= 19; ++i) {
+    int h, v, x, y, z;
+    switch (i) {
+      case 1: case 3: case 5: case 7: mx(nx, nl[i - 1]); break;
+      case 2: case 4: case 6: case 8: mx(ny, nl[i - 1]); break;
+      case 9: case 10: case 11: case 12: mx(nz, nl[i - 1]); break;
+      case 13: case 14: decod2(nl[i - 1], h, v); mx(nx, h); mx(ny, v); break;
+      case 15: case 17: decod2(nl[i - 1], h, v); mx(nx, h); mx(nz, v); break;
+      case 16: case 18: decod2(nl[i - 1], h, v); mx(ny, h); mx(nz, v); break;
+      case 19: decod3(nl[i - 1], x, y, z); mx(nx, x); mx(ny, y); mx(nz, z); break;
+    }
+  }
+  nx = std::min(nx + integration, MAXP) + 1;
+  ny = std::min(ny + integration, MAXP) + 1;
+  nz = std::min(nz + integration, MAXP) + 1;
+  xi.clear(); w.clear();
+  for (int l3 = 0; l3 < nz; ++l3)
+    for (int l2 = 0; l2 < ny; ++l2)
+      for (int l1 = 0; l1 < nx; ++l1) {
+        xi.push_back(0.5 * (1.0 + GX[nx - 1][l1]));
+        xi.push_back(0.5 * (1.0 + GX[ny - 1][l2]));
+        xi.push_back(0.5 * (1.0 + GX[nz - 1][l3]));
+        w.push_back((0.5 * GW[nx - 1][l1]) * (0.5 * GW[ny - 1][l2]) * (0.5 * GW[nz - 1][l3]));
+      }
+  return (int)w.size();
+}
+
+template <class T>
+T* dalloc(size_t count, int* err) {
+  if (count == 0) count = 1;
+  void* p = nullptr;
+  if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) { *err = HP3DG_ERR_ALLOC; return nullptr; }
+  return (T*)p;
+}
+
+struct Bin {
+  int nord_loc[19];
+  int n = 0, nb = 0, ni = 0, nint = 0;
+  std::vector<int> elems;
+  std::vector<double> xi, wq;
+  bool tables = false;
+  int* d_elist = nullptr;
+  double *d_xi = nullptr, *d_wq = nullptr, *d_shap = nullptr, *d_grad = nullptr;
+  double *d_D = nullptr, *d_F = nullptr, *d_b0 = nullptr, *d_PK = nullptr, *d_S = nullptr;
+  uint32_t* d_perm = nullptr;
+  uint8_t* d_dmask = nullptr;
+  // mixed precision
+  bool mtable = false;
+  OzakiPlan plan{};
+  uint16_t *d_mdig = nullptr, *d_ddig = nullptr;
+  double *d_mscale = nullptr, *d_dscale = nullptr;
+};
+
+}  // namespace
+
+struct hp3dg_ctx {
+  hp3dg_opts opts{};
+  int device = 0;
+  cudaStream_t own = nullptr, stream = nullptr;
+  int nel = 0, nnodes = 0;
+  bool submitted = false, ran = false, downloaded = false;
+  int last_bad = -1;
+  std::vector<int> n_e, nb_e, ni_e, bin_of, pos_in_bin;
+  std::vector<int64_t> elem_nnz, lcon_off, schur_off, bub_off, zd_off;
+  std::vector<int> nextract;
+  std::vector<Bin> bins;
+  bool have_zdofd = false;
+  // device inputs
+  int *d_norder = nullptr, *d_nori_e = nullptr, *d_nori_f = nullptr, *d_nodes = nullptr,
+      *d_ndofm = nullptr, *d_nextract = nullptr;
+  double *d_xvert = nullptr, *d_kappa = nullptr, *d_zdofd = nullptr;
+  int64_t *d_elem_nnz = nullptr, *d_lcon_off = nullptr, *d_schur_off = nullptr,
+          *d_bub_off = nullptr, *d_zd_off = nullptr;
+  // outputs
+  double *d_zastif = nullptr, *d_zbload = nullptr, *d_aschur = nullptr, *d_bschur = nullptr;
+  int *d_lcon = nullptr, *d_nfirst = nullptr;
+  // index-map scratch
+  int *d_first = nullptr, *d_cnt = nullptr;
+  int64_t *d_scan = nullptr, *d_blk = nullptr, *d_total = nullptr;
+  int* d_flags = nullptr;  // [0] bad Jacobian element, [1] non-SPD element, [2] mixed flag
+  // host results
+  double *h_zastif = nullptr, *h_zbload = nullptr, *h_aschur = nullptr, *h_bschur = nullptr,
+         *h_PK = nullptr, *h_b0 = nullptr;
+  int *h_lcon = nullptr, *h_nfirst = nullptr;
+  int64_t h_nrdof = 0;
+  size_t pk_total = 0, b0_total = 0;
+  std::vector<int64_t> pk_off, b0_off;  // per element, into h_PK / h_b0 when keep_elem
+  cudaEvent_t ev[8] = {};
+  float times[6] = {0, 0, 0, 0, 0, 0};
+};
+
+namespace {
+
+void free_bin(Bin& b) {
+  cudaFree(b.d_elist); cudaFree(b.d_xi); cudaFree(b.d_wq); cudaFree(b.d_shap); cudaFree(b.d_grad);
+  cudaFree(b.d_D); cudaFree(b.d_F); cudaFree(b.d_b0); cudaFree(b.d_PK); cudaFree(b.d_S);
+  cudaFree(b.d_perm); cudaFree(b.d_dmask); cudaFree(b.d_mdig); cudaFree(b.d_ddig);
+  cudaFree(b.d_mscale); cudaFree(b.d_dscale);
+  b = Bin();
+}
+
+void free_batch(hp3dg_ctx* c) {
+  for (auto& b : c->bins) free_bin(b);
+  c->bins.clear();
+  void* dev[] = {c->d_norder, c->d_nori_e, c->d_nori_f, c->d_nodes, c->d_ndofm, c->d_nextract,
+                 c->d_xvert, c->d_kappa, c->d_zdofd, c->d_elem_nnz, c->d_lcon_off,
+                 c->d_schur_off, c->d_bub_off, c->d_zd_off, c->d_zastif, c->d_zbload,
+                 c->d_aschur, c->d_bschur, c->d_lcon, c->d_nfirst, c->d_first, c->d_cnt,
+                 c->d_scan, c->d_blk, c->d_total};
+  for (void* p : dev) cudaFree(p);
+  void* host[] = {c->h_zastif, c->h_zbload, c->h_aschur, c->h_bschur, c->h_lcon, c->h_nfirst,
+                  c->h_PK, c->h_b0};
+  for (void* p : host) cudaFreeHost(p);
+  c->d_norder = c->d_nori_e = c->d_nori_f = c->d_nodes = c->d_ndofm = c->d_nextract = nullptr;
+  c->d_xvert = c->d_kappa = c->d_zdofd = nullptr;
+  c->d_elem_nnz = c->d_lcon_off = c->d_schur_off = c->d_bub_off = c->d_zd_off = nullptr;
+  c->d_zastif = c->d_zbload = c->d_aschur = c->d_bschur = nullptr;
+  c->d_lcon = c->d_nfirst = c->d_first = c->d_cnt = nullptr;
+  c->d_scan = c->d_blk = c->d_total = nullptr;
+  c->h_zastif = c->h_zbload = c->h_aschur = c->h_bschur = c->h_PK = c->h_b0 = nullptr;
+  c->h_lcon = c->h_nfirst = nullptr;
+  c->submitted = c->ran = c->downloaded = false;
+}
+
+#define CK(x)                                  \
+  do {                                         \
+    if ((x) != cudaSuccess) return HP3DG_ERR_CUDA; \
+  } while (0)
+
+}  // namespace
+
+extern "C" {
+
+const char* hp3dg_strerror(int s) {
+  switch (s) {
+    case HP3DG_OK: return "ok";
+    case HP3DG_ERR_NEG_JACOBIAN: return "negative Jacobian at a quadrature point";
+    case HP3DG_ERR_NOT_SPD: return "bubble block is not positive definite";
+    case HP3DG_ERR_BAD_ORDER: return "order outside 1..MAXP or unsupported element type";
+    case HP3DG_ERR_ALLOC: return "allocation failed";
+    case HP3DG_ERR_CUDA: return "CUDA call failed";
+    case HP3DG_ERR_TIMEOUT: return "bounded device wait gave up";
+    case HP3DG_ERR_ARG: return "invalid argument";
+    case HP3DG_ERR_STATE: return "call out of order";
+    case HP3DG_ERR_UNSUPPORTED: return "unsupported on this device or configuration";
+    default: return "unknown status";
+  }
+}
+
+int hp3dg_batch_begin(const hp3dg_opts* opts, hp3dg_ctx** out) {
+  if (!out) return HP3DG_ERR_ARG;
+  *out = nullptr;
+  hp3dg_ctx* c = new hp3dg_ctx();
+  if (opts) c->opts = *opts;
+  else c->opts.isol = 10;
+  if (c->opts.precision != HP3DG_FP64 && c->opts.precision != HP3DG_MIXED) { delete c; return HP3DG_ERR_ARG; }
+  if (c->opts.integration < 0 || c->opts.integration > MAXP) { delete c; return HP3DG_ERR_ARG; }
+  c->device = c->opts.device;
+  if (cudaSetDevice(c->device) != cudaSuccess) { delete c; return HP3DG_ERR_CUDA; }
+  if (c->opts.precision == HP3DG_MIXED) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, c->device) != cudaSuccess) { delete c; return HP3DG_ERR_CUDA; }
+    if (p.major != 10) { delete c; return HP3DG_ERR_UNSUPPORTED; }  // tcgen05 needs sm_10x
+  }
+  if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) { delete c; return HP3DG_ERR_CUDA; }
+  c->stream = c->own;
+  for (auto& e : c->ev) cudaEventCreate(&e);
+  if (cudaMalloc(&c->d_flags, 4 * sizeof(int)) != cudaSuccess) { delete c; return HP3DG_ERR_ALLOC; }
+  *out = c;
+  return HP3DG_OK;
+}
+
+int hp3dg_set_stream(hp3dg_ctx* c, void* stream) {
+  if (!c) return HP3DG_ERR_ARG;
+  c->stream = stream ? (cudaStream_t)stream : c->own;
+  return HP3DG_OK;
+}
+
+int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
+                       const double* xvert, const double* kappa, const double* zdofd,
+                       int32_t nnodes) {
+  if (!c || nel < 0 || (nel > 0 && (!desc || !xvert)) || nnodes < 0) return HP3DG_ERR_ARG;
+  cudaSetDevice(c->device);
+  free_batch(c);
+  c->nel = nel;
+  c->nnodes = nnodes;
+  c->n_e.assign(nel, 0); c->nb_e.assign(nel, 0); c->ni_e.assign(nel, 0);
+  c->bin_of.assign(nel, 0); c->pos_in_bin.assign(nel, 0);
+  c->elem_nnz.assign(nel + 1, 0); c->lcon_off.assign(nel + 1, 0);
+  c->schur_off.assign(nel + 1, 0); c->bub_off.assign(nel + 1, 0); c->zd_off.assign(nel + 1, 0);
+  c->nextract.clear();
+  std::vector<int> norder((size_t)nel * 19), nori_e((size_t)nel * 12), nori_f((size_t)nel * 6),
+      nodes((size_t)nel * 26), ndofm((size_t)nel * 26);
+  std::map<std::vector<int>, int> binmap;
+  c->last_bad = -1;
+  for (int e = 0; e < nel; ++e) {
+    const hp3dg_elem_desc& d = desc[e];
+    if (d.etype != HP3DG_HEXA) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
+    for (int i = 0; i < 12; ++i)
+      if (d.norder[i] < 1 || d.norder[i] > MAXP || (d.nori_edge[i] & ~1)) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
+    for (int f = 0; f < 6; ++f) {
+      int h, v; decod2(d.norder[12 + f], h, v);
+      if (h < 1 || h > MAXP || v < 1 || v > MAXP || d.nori_face[f] < 0 || d.nori_face[f] > 7) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
+    }
+    {
+      int x, y, z; decod3(d.norder[18], x, y, z);
+      if (x < 1 || x > MAXP || y < 1 || y > MAXP || z < 1 || z > MAXP || d.norder[18] > 999) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
+    }
+    for (int i = 0; i < 26; ++i)
+      if (d.nodes[i] < 0 || d.nodes[i] >= nnodes) { c->last_bad = e; return HP3DG_ERR_ARG; }
+    std::copy(d.norder, d.norder + 19, &norder[19 * (size_t)e]);
+    std::copy(d.nori_edge, d.nori_edge + 12, &nori_e[12 * (size_t)e]);
+    std::copy(d.nori_face, d.nori_face + 6, &nori_f[6 * (size_t)e]);
+    std::copy(d.nodes, d.nodes + 26, &nodes[26 * (size_t)e]);
+    int loc[19];
+    hexa_order_loc(d.norder, d.nori_face, loc);
+    std::vector<int> key(loc, loc + 19);
+    auto it = binmap.find(key);
+    int b;
+    if (it == binmap.end()) {
+      b = (int)c->bins.size();
+      binmap[key] = b;
+      c->bins.emplace_back();
+      Bin& B = c->bins.back();
+      std::copy(loc, loc + 19, B.nord_loc);
+      B.n = hexa_ndof(loc);
+      B.nb = hexa_nbub(loc);
+      B.ni = B.n - B.nb;
+      B.nint = hexa_quadrature(loc, c->opts.integration, B.xi, B.wq);
+      if (condense_smem(B.ni, B.nb) > 227 * 1024) { c->last_bad = e; free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
+    } else {
+      b = it->second;
+    }
+    c->bin_of[e] = b;
+    c->pos_in_bin[e] = (int)c->bins[b].elems.size();
+    c->bins[b].elems.push_back(e);
+    // per-node dof counts (ndof_nod) in element node order, Dirichlet skipped
+    int nd[26];
+    for (int v = 0; v < 8; ++v) nd[v] = 1;
+    for (int q = 0; q < 12; ++q) nd[8 + q] = d.norder[q] - 1;
+    for (int f = 0; f < 6; ++f) { int h, v; decod2(d.norder[12 + f], h, v); nd[20 + f] = (h - 1) * (v - 1); }
+    int first[26], ni = 0;
+    for (int i = 0; i < 26; ++i) { first[i] = ni; ni += nd[i]; }
+    int nrdofc = 0;
+    for (int i = 25; i >= 0; --i) {
+      int act = d.bcflag[i] ? 0 : nd[i];
+      ndofm[26 * (size_t)e + i] = act;
+      for (int q = 0; q < act; ++q) c->nextract.push_back(first[i] + q);
+      nrdofc += act;
+    }
+    c->n_e[e] = c->bins[b].n; c->nb_e[e] = c->bins[b].nb; c->ni_e[e] = ni;
+    c->elem_nnz[e + 1] = c->elem_nnz[e] + (int64_t)nrdofc * nrdofc;
+    c->lcon_off[e + 1] = c->lcon_off[e] + nrdofc;
+    c->schur_off[e + 1] = c->schur_off[e] + (int64_t)c->nb_e[e] * ni;
+    c->bub_off[e + 1] = c->bub_off[e] + c->nb_e[e];
+    c->zd_off[e + 1] = c->zd_off[e] + ni;
+  }
+  int err = 0;
+  // ---- device inputs ----
+  c->d_norder = dalloc<int>(norder.size(), &err);
+  c->d_nori_e = dalloc<int>(nori_e.size(), &err);
+  c->d_nori_f = dalloc<int>(nori_f.size(), &err);
+  c->d_nodes = dalloc<int>(nodes.size(), &err);
+  c->d_ndofm = dalloc<int>(ndofm.size(), &err);
+  c->d_nextract = dalloc<int>(c->nextract.size(), &err);
+  c->d_xvert = dalloc<double>((size_t)nel * 24, &err);
+  c->d_kappa = dalloc<double>(nel, &err);
+  c->d_elem_nnz = dalloc<int64_t>(nel + 1, &err);
+  c->d_lcon_off = dalloc<int64_t>(nel + 1, &err);
+  c->d_schur_off = dalloc<int64_t>(nel + 1, &err);
+  c->d_bub_off = dalloc<int64_t>(nel + 1, &err);
+  c->d_zd_off = dalloc<int64_t>(nel + 1, &err);
+  c->have_zdofd = zdofd != nullptr;
+  if (zdofd) c->d_zdofd = dalloc<double>(c->zd_off[nel], &err);
+  // ---- outputs ----
+  c->d_zastif = dalloc<double>(c->elem_nnz[nel], &err);
+  c->d_zbload = dalloc<double>(c->lcon_off[nel], &err);
+  c->d_aschur = dalloc<double>(c->schur_off[nel], &err);
+  c->d_bschur = dalloc<double>(c->bub_off[nel], &err);
+  c->d_lcon = dalloc<int>(c->lcon_off[nel], &err);
+  c->d_nfirst = dalloc<int>(nnodes, &err);
+  int64_t ns = (int64_t)nel * 26;
+  c->d_first = dalloc<int>(nnodes, &err);
+  c->d_cnt = dalloc<int>(ns, &err);
+  c->d_scan = dalloc<int64_t>(ns, &err);
+  c->d_blk = dalloc<int64_t>((ns + 1023) / 1024 + 1, &err);
+  c->d_total = dalloc<int64_t>(1, &err);
+  if (err) { free_batch(c); return err; }
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->d_norder, norder.data(), norder.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_nori_e, nori_e.data(), nori_e.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_nori_f, nori_f.data(), nori_f.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_nodes, nodes.data(), nodes.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_ndofm, ndofm.data(), ndofm.size() * 4, cudaMemcpyHostToDevice, st));
+  if (!c->nextract.empty())
+    CK(cudaMemcpyAsync(c->d_nextract, c->nextract.data(), c->nextract.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_xvert, xvert, (size_t)nel * 24 * 8, cudaMemcpyHostToDevice, st));
+  if (kappa) {
+    CK(cudaMemcpyAsync(c->d_kappa, kappa, (size_t)nel * 8, cudaMemcpyHostToDevice, st));
+  } else {
+    std::vector<double> one(nel, 1.0);
+    CK(cudaMemcpyAsync(c->d_kappa, one.data(), (size_t)nel * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  }
+  CK(cudaMemcpyAsync(c->d_elem_nnz, c->elem_nnz.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_lcon_off, c->lcon_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_schur_off, c->schur_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_bub_off, c->bub_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_zd_off, c->zd_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
+  if (zdofd)
+    CK(cudaMemcpyAsync(c->d_zdofd, zdofd, c->zd_off[nel] * 8, cudaMemcpyHostToDevice, st));
+  // ---- per-bin buffers ----
+  for (auto& B : c->bins) {
+    size_t ne = B.elems.size();
+    B.d_elist = dalloc<int>(ne, &err);
+    B.d_xi = dalloc<double>(B.xi.size(), &err);
+    B.d_wq = dalloc<double>(B.wq.size(), &err);
+    B.d_shap = dalloc<double>((size_t)B.nint * B.n, &err);
+    B.d_grad = dalloc<double>((size_t)B.nint * 3 * B.n, &err);
+    B.d_D = dalloc<double>(ne * B.nint * 6, &err);
+    B.d_F = dalloc<double>(ne * B.nint, &err);
+    B.d_b0 = dalloc<double>(ne * B.n, &err);
+    B.d_PK = dalloc<double>(ne * ((size_t)B.n * (B.n + 1) / 2), &err);
+    B.d_S = dalloc<double>(ne * ((size_t)B.ni * (B.ni + 1) / 2), &err);
+    B.d_perm = dalloc<uint32_t>(ne * B.n, &err);
+    B.d_dmask = dalloc<uint8_t>(ne * B.ni, &err);
+    if (err) { free_batch(c); return err; }
+    CK(cudaMemcpyAsync(B.d_elist, B.elems.data(), ne * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B.d_xi, B.xi.data(), B.xi.size() * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B.d_wq, B.wq.data(), B.wq.size() * 8, cudaMemcpyHostToDevice, st));
+    if (zdofd) {
+      std::vector<uint8_t> dm(ne * B.ni, 0);
+      for (size_t j = 0; j < ne; ++j) {
+        const hp3dg_elem_desc& d = desc[B.elems[j]];
+        int k = 0;
+        for (int i = 0; i < 26; ++i) {
+          int ndi = i < 8 ? 1 : (i < 20 ? d.norder[i - 8] - 1 : 0);
+          if (i >= 20) { int h, v; decod2(d.norder[12 + i - 20], h, v); ndi = (h - 1) * (v - 1); }
+          for (int q = 0; q < ndi; ++q) dm[j * B.ni + k++] = d.bcflag[i] ? 1 : 0;
+        }
+      }
+      CK(cudaMemcpyAsync(B.d_dmask, dm.data(), dm.size(), cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+    }
+    if (c->opts.precision == HP3DG_MIXED) {
+      int rc = ozaki_plan(B.nint, B.n, c->opts.ozaki_radix, c->opts.ozaki_digits, &B.plan);
+      if (rc) { free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
+      B.d_ddig = (uint16_t*)dalloc<uint8_t>(ozaki_d_bytes(B.plan, (int)ne), &err);
+      B.d_dscale = dalloc<double>(ne + 128, &err);
+      if (err) { free_batch(c); return err; }
+    }
+  }
+  CK(cudaStreamSynchronize(st));
+  c->submitted = true;
+  return HP3DG_OK;
+}
+
+int hp3dg_batch_run(hp3dg_ctx* c) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  int err = 0;
+  CK(cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st));
+  bool tm = c->opts.timing != 0;
+  if (tm) cudaEventRecord(c->ev[0], st);
+  // tables (once per bin)
+  for (auto& B : c->bins) {
+    if (!B.tables) {
+      launch_tables_hexa(B.nord_loc, B.nint, B.n, B.d_xi, B.d_shap, B.d_grad, st);
+      B.tables = true;
+    }
+    if (c->opts.precision == HP3DG_MIXED && !B.mtable) {
+      B.d_mdig = (uint16_t*)dalloc<uint8_t>(ozaki_m_bytes(B.plan), &err);
+      B.d_mscale = dalloc<double>(B.plan.ncols, &err);
+      double* work = dalloc<double>((size_t)B.plan.kdim * 64, &err);
+      if (err) { cudaFree(work); return err; }
+      int rc = launch_ozaki_build_m(B.plan, B.nint, B.n, B.ni, B.nb, B.d_grad, B.d_mdig,
+                                    B.d_mscale, work, st);
+      cudaStreamSynchronize(st);
+      cudaFree(work);
+      if (rc) return HP3DG_ERR_CUDA;
+      B.mtable = true;
+    }
+  }
+  if (tm) cudaEventRecord(c->ev[1], st);
+  for (auto& B : c->bins) {
+    int ne = (int)B.elems.size();
+    launch_orient_hexa(ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.n, B.d_perm, st);
+    launch_geom_hexa(ne, B.d_elist, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert,
+                     c->d_kappa, c->opts.isol, B.d_D, B.d_F, c->d_flags, st);
+    launch_load_hexa(ne, B.nint, B.n, B.d_shap, B.d_F, B.d_b0, st);
+    if (c->opts.precision == HP3DG_MIXED)
+      launch_ozaki_slice_d(B.plan, ne, B.nint, B.d_D, B.d_ddig, B.d_dscale, st);
+  }
+  if (tm) cudaEventRecord(c->ev[2], st);
+  for (auto& B : c->bins) {
+    int ne = (int)B.elems.size();
+    if (c->opts.precision == HP3DG_MIXED) {
+      if (launch_ozaki_gemm(B.plan, ne, B.n, B.d_ddig, B.d_dscale, B.d_mdig, B.d_mscale, B.d_PK,
+                            c->d_flags + 2, st))
+        return HP3DG_ERR_CUDA;
+    } else {
+      launch_contract_fp64(ne, B.nint, B.n, B.ni, B.nb, B.d_grad, B.d_D, B.d_PK, st);
+    }
+  }
+  if (tm) cudaEventRecord(c->ev[3], st);
+  for (auto& B : c->bins) {
+    int ne = (int)B.elems.size();
+    if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, B.d_PK, B.d_b0, B.d_perm, c->d_nextract,
+                        c->d_lcon_off, c->d_elem_nnz, c->d_schur_off, c->d_bub_off, c->d_zd_off,
+                        c->have_zdofd ? c->d_zdofd : nullptr, B.d_dmask, B.d_S, c->d_zastif,
+                        c->d_zbload, c->d_aschur, c->d_bschur, c->d_flags + 1, st))
+      return HP3DG_ERR_CUDA;
+  }
+  if (tm) cudaEventRecord(c->ev[4], st);
+  launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,
+                    c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon, st);
+  if (tm) cudaEventRecord(c->ev[5], st);
+  if (cudaPeekAtLastError() != cudaSuccess) return HP3DG_ERR_CUDA;
+  c->ran = true;
+  c->downloaded = false;
+  return HP3DG_OK;
+}
+
+int hp3dg_batch_sync(hp3dg_ctx* c) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->ran) return HP3DG_ERR_STATE;
+  cudaSetDevice(c->device);
+  CK(cudaStreamSynchronize(c->stream));
+  int fl[4];
+  CK(cudaMemcpy(fl, c->d_flags, sizeof(fl), cudaMemcpyDeviceToHost));
+  if (c->opts.timing) {
+    for (int i = 0; i < 5; ++i) cudaEventElapsedTime(&c->times[i], c->ev[i], c->ev[i + 1]);
+    cudaEventElapsedTime(&c->times[5], c->ev[0], c->ev[5]);
+  }
+  const int NONE = 0x7f7f7f7f;
+  c->last_bad = -1;
+  if (fl[0] != NONE) { c->last_bad = fl[0]; return HP3DG_ERR_NEG_JACOBIAN; }
+  if (fl[1] != NONE) { c->last_bad = fl[1]; return HP3DG_ERR_NOT_SPD; }
+  return HP3DG_OK;
+}
+
+int hp3dg_batch_download(hp3dg_ctx* c) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->ran) return HP3DG_ERR_STATE;
+  cudaSetDevice(c->device);
+  int rc = hp3dg_batch_sync(c);
+  if (rc != HP3DG_OK) return rc;
+  int nel = c->nel;
+  auto hal = [](void** p, size_t bytes) {
+    if (*p) return true;
+    return cudaMallocHost(p, bytes ? bytes : 8) == cudaSuccess;
+  };
+  if (!hal((void**)&c->h_zastif, c->elem_nnz[nel] * 8) || !hal((void**)&c->h_zbload, c->lcon_off[nel] * 8) ||
+      !hal((void**)&c->h_aschur, c->schur_off[nel] * 8) || !hal((void**)&c->h_bschur, c->bub_off[nel] * 8) ||
+      !hal((void**)&c->h_lcon, c->lcon_off[nel] * 4) || !hal((void**)&c->h_nfirst, (size_t)c->nnodes * 4))
+    return HP3DG_ERR_ALLOC;
+  cudaStream_t st = c->stream;
+  CK(cudaMemcpyAsync(c->h_zastif, c->d_zastif, c->elem_nnz[nel] * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(c->h_zbload, c->d_zbload, c->lcon_off[nel] * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(c->h_aschur, c->d_aschur, c->schur_off[nel] * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(c->h_bschur, c->d_bschur, c->bub_off[nel] * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(c->h_lcon, c->d_lcon, c->lcon_off[nel] * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(c->h_nfirst, c->d_nfirst, (size_t)c->nnodes * 4, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(&c->h_nrdof, c->d_total, 8, cudaMemcpyDeviceToHost, st));
+  if (c->opts.keep_elem) {
+    c->pk_off.assign(nel, 0); c->b0_off.assign(nel, 0);
+    size_t pk = 0, b0 = 0;
+    for (auto& B : c->bins) { pk += B.elems.size() * ((size_t)B.n * (B.n + 1) / 2); b0 += B.elems.size() * B.n; }
+    if (!hal((void**)&c->h_PK, pk * 8) || !hal((void**)&c->h_b0, b0 * 8)) return HP3DG_ERR_ALLOC;
+    size_t po = 0, bo = 0;
+    for (auto& B : c->bins) {
+      size_t ne = B.elems.size(), pe = (size_t)B.n * (B.n + 1) / 2;
+      CK(cudaMemcpyAsync(c->h_PK + po, B.d_PK, ne * pe * 8, cudaMemcpyDeviceToHost, st));
+      CK(cudaMemcpyAsync(c->h_b0 + bo, B.d_b0, ne * B.n * 8, cudaMemcpyDeviceToHost, st));
+      for (size_t j = 0; j < ne; ++j) { c->pk_off[B.elems[j]] = po + j * pe; c->b0_off[B.elems[j]] = bo + j * B.n; }
+      po += ne * pe; bo += ne * B.n;
+    }
+  }
+  CK(cudaStreamSynchronize(st));
+  c->downloaded = true;
+  return HP3DG_OK;
+}
+
+int hp3dg_get_elem(const hp3dg_ctx* c, int32_t iel, double* aloc, int32_t ld, double* bloc) {
+  if (!c || !aloc || !bloc) return HP3DG_ERR_ARG;
+  if (!c->downloaded || !c->opts.keep_elem) return HP3DG_ERR_STATE;
+  if (iel < 0 || iel >= c->nel) return HP3DG_ERR_ARG;
+  int n = c->n_e[iel], ni = n - c->nb_e[iel], nb = c->nb_e[iel];
+  if (ld < n) return HP3DG_ERR_ARG;
+  const Bin& B = c->bins[c->bin_of[iel]];
+  // oriented dof map of this element (same map the device uses)
+  int no[19], oe[12], of[6];
+  (void)B;
+  // descriptors are not kept on the host; recompute the map from device copies
+  cudaMemcpy(no, c->d_norder + 19 * (size_t)iel, sizeof(no), cudaMemcpyDeviceToHost);
+  cudaMemcpy(oe, c->d_nori_e + 12 * (size_t)iel, sizeof(oe), cudaMemcpyDeviceToHost);
+  cudaMemcpy(of, c->d_nori_f + 6 * (size_t)iel, sizeof(of), cudaMemcpyDeviceToHost);
+  const double* PK = c->h_PK + c->pk_off[iel];
+  const double* b0 = c->h_b0 + c->b0_off[iel];
+  for (int a = 0; a < n; ++a) {
+    uint32_t ma = hexa_orient_map(a, no, oe, of);
+    int ra = (int)(ma & 0x7fffffffu);
+    bloc[a] = (ma & 0x80000000u) ? -b0[ra] : b0[ra];
+    for (int b = 0; b < n; ++b) {
+      uint32_t mb = hexa_orient_map(b, no, oe, of);
+      int rb = (int)(mb & 0x7fffffffu);
+      double v = PK[pk_index(ra, rb, ni, nb)];
+      aloc[(size_t)b * ld + a] = ((ma ^ mb) & 0x80000000u) ? -v : v;
+    }
+  }
+  return HP3DG_OK;
+}
+
+int hp3dg_get_condensed(const hp3dg_ctx* c, int32_t iel, double* zbload, double* zastif,
+                        int32_t* nrdofc) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->downloaded) return HP3DG_ERR_STATE;
+  if (iel < 0 || iel >= c->nel) return HP3DG_ERR_ARG;
+  int64_t nc = c->lcon_off[iel + 1] - c->lcon_off[iel];
+  if (nrdofc) *nrdofc = (int32_t)nc;
+  if (zbload) std::memcpy(zbload, c->h_zbload + c->lcon_off[iel], nc * 8);
+  if (zastif) std::memcpy(zastif, c->h_zastif + c->elem_nnz[iel], nc * nc * 8);
+  return HP3DG_OK;
+}
+
+int hp3dg_get_schur(const hp3dg_ctx* c, int32_t iel, double* aschur, double* bschur,
+                    int32_t* nb, int32_t* ni) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->downloaded) return HP3DG_ERR_STATE;
+  if (iel < 0 || iel >= c->nel) return HP3DG_ERR_ARG;
+  if (nb) *nb = c->nb_e[iel];
+  if (ni) *ni = c->ni_e[iel];
+  if (aschur) std::memcpy(aschur, c->h_aschur + c->schur_off[iel], (c->schur_off[iel + 1] - c->schur_off[iel]) * 8);
+  if (bschur) std::memcpy(bschur, c->h_bschur + c->bub_off[iel], (c->bub_off[iel + 1] - c->bub_off[iel]) * 8);
+  return HP3DG_OK;
+}
+
+int hp3dg_index_map(const hp3dg_ctx* c, int32_t* nfirst_dof, int64_t* elem_nnz,
+                    int64_t* lcon_off, int32_t* lcon, int64_t* nrdof) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->downloaded) return HP3DG_ERR_STATE;
+  if (nfirst_dof) std::memcpy(nfirst_dof, c->h_nfirst, (size_t)c->nnodes * 4);
+  if (elem_nnz) std::memcpy(elem_nnz, c->elem_nnz.data(), (c->nel + 1) * 8);
+  if (lcon_off) std::memcpy(lcon_off, c->lcon_off.data(), (c->nel + 1) * 8);
+  if (lcon) std::memcpy(lcon, c->h_lcon, c->lcon_off[c->nel] * 4);
+  if (nrdof) *nrdof = c->h_nrdof;
+  return HP3DG_OK;
+}
+
+int hp3dg_output_sizes(const hp3dg_ctx* c, int64_t* nnz, int64_t* lcon, int64_t* schur,
+                       int64_t* bub) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  if (nnz) *nnz = c->elem_nnz[c->nel];
+  if (lcon) *lcon = c->lcon_off[c->nel];
+  if (schur) *schur = c->schur_off[c->nel];
+  if (bub) *bub = c->bub_off[c->nel];
+  return HP3DG_OK;
+}
+
+int hp3dg_device_outputs(const hp3dg_ctx* c, const double** zastif, const double** zbload,
+                         const double** aschur, const double** bschur, const int32_t** lcon) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  if (zastif) *zastif = c->d_zastif;
+  if (zbload) *zbload = c->d_zbload;
+  if (aschur) *aschur = c->d_aschur;
+  if (bschur) *bschur = c->d_bschur;
+  if (lcon) *lcon = c->d_lcon;
+  return HP3DG_OK;
+}
+
+int hp3dg_phase_times(const hp3dg_ctx* c, float* ms, int32_t n) {
+  if (!c || !ms || n < 0) return HP3DG_ERR_ARG;
+  for (int i = 0; i < n && i < 6; ++i) ms[i] = c->times[i];
+  return HP3DG_OK;
+}
+
+int32_t hp3dg_last_bad_element(const hp3dg_ctx* c) { return c ? c->last_bad : -1; }
+
+void hp3dg_batch_end(hp3dg_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  free_batch(c);
+  cudaFree(c->d_flags);
+  for (auto& e : c->ev) cudaEventDestroy(e);
+  cudaStreamDestroy(c->own);
+  delete c;
+}
+
+}  // extern "C"

@@ -1,0 +1,56 @@
+// hp3dg_kernels.h -- host launchers of the device kernels (internal).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hp3dg {
+
+void launch_tables_hexa(const int* nord_loc, int nint, int n, const double* d_xi,
+                        double* d_shap, double* d_grad, cudaStream_t st);
+void launch_orient_hexa(int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
+                        const int* d_nori_f, int n, uint32_t* d_perm, cudaStream_t st);
+void launch_geom_hexa(int nel, const int* d_elist, int nint, int n, const double* d_wq,
+                      const double* d_shap, const double* d_grad, const double* d_xvert,
+                      const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
+                      cudaStream_t st);
+void launch_load_hexa(int nel, int nint, int n, const double* d_shap, const double* d_F,
+                      double* d_b0, cudaStream_t st);
+void launch_contract_fp64(int nel, int nint, int n, int ni, int nb, const double* d_grad,
+                          const double* d_D, double* d_PK, cudaStream_t st);
+size_t condense_smem(int ni, int nb);
+int launch_condense(int nel, int n, int ni, int nb, const int* d_elist, const double* d_PK,
+                    const double* d_b0, const uint32_t* d_perm, const int* d_nextract,
+                    const int64_t* d_lcon_off, const int64_t* d_elem_nnz,
+                    const int64_t* d_schur_off, const int64_t* d_bub_off,
+                    const int64_t* d_zd_off, const double* d_zdofd, const uint8_t* d_dmask,
+                    double* d_S, double* d_zastif, double* d_zbload, double* d_aschur,
+                    double* d_bschur, int* d_bad_spd, cudaStream_t st);
+int launch_index_maps(int nel, int nnode, int nnodes_global, const int* d_nodes, const int* d_ndofm,
+                      const int64_t* d_lcon_off, int* d_first, int* d_cnt, int64_t* d_scan,
+                      int64_t* d_blk, int64_t* d_total, int* d_nfirst, int* d_lcon,
+                      cudaStream_t st);
+
+// mixed precision (split-BF16 digits on tcgen05) -- k_ozaki.cu
+struct OzakiPlan {
+  int radix;      // bits per digit
+  int digits;     // digits per operand
+  int levels;     // number of exact FP32 level accumulators
+  int kdim;       // 6*nint rounded up to the K tile
+  int ncols;      // n(n+1)/2 rounded up to the N tile
+};
+int ozaki_plan(int nint, int n, int radix, int digits, OzakiPlan* plan);
+// build the M digit table of a bin (once): B operand, column scales
+int launch_ozaki_build_m(const OzakiPlan& plan, int nint, int n, int ni, int nb,
+                         const double* d_grad, uint16_t* d_mdig, double* d_mscale,
+                         double* d_work, cudaStream_t st);
+size_t ozaki_m_bytes(const OzakiPlan& plan);
+// slice the per-element D rows into digits (A operand) with row scales
+int launch_ozaki_slice_d(const OzakiPlan& plan, int nel, int nint, const double* d_D,
+                         uint16_t* d_ddig, double* d_dscale, cudaStream_t st);
+size_t ozaki_d_bytes(const OzakiPlan& plan, int nel);
+// the tensor-core contraction: PK = dscale*mscale*sum_s 2^-radix*s acc_s
+int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_ddig,
+                      const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                      double* d_PK, int* d_flag, cudaStream_t st);
+
+}  // namespace hp3dg

@@ -1,0 +1,208 @@
+"""Python mirror of the C ABI (include/hp3dg.h) over ctypes.
+
+This is the host-side interface a Python caller (tests, benchmark, the torch
+autograd harness) uses; the Fortran host binds the same entry points through
+ISO_C_BINDING.  Loading fails loudly when libhp3dg.so is
+missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIBPATH = os.path.join(HERE, "libhp3dg.so")
+
+HEXA, PRISM, TET = 1, 2, 3
+FP64, MIXED = 0, 1
+
+ERRORS = {0: "OK", -1: "NEG_JACOBIAN", -2: "NOT_SPD", -3: "BAD_ORDER", -4: "ALLOC", -5: "CUDA",
+          -6: "TIMEOUT", -7: "ARG", -8: "STATE", -9: "UNSUPPORTED"}
+
+
+class HP3DGError(RuntimeError):
+    def __init__(self, code, msg, bad=-1):
+        super().__init__(f"hp3dg error {code} ({ERRORS.get(code, '?')}): {msg}"
+                         + (f" [element {bad}]" if bad >= 0 else ""))
+        self.code = code
+        self.bad = bad
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int32), ("integration", ctypes.c_int32),
+                ("isol", ctypes.c_int32), ("keep_elem", ctypes.c_int32),
+                ("timing", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("ozaki_radix", ctypes.c_int32), ("ozaki_digits", ctypes.c_int32),
+                ("stc_method", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+
+
+DESC_DTYPE = np.dtype([("etype", np.int32), ("mdle", np.int32), ("norder", np.int32, 19),
+                       ("nori_edge", np.int32, 12), ("nori_face", np.int32, 6),
+                       ("nodes", np.int32, 26), ("bcflag", np.int32, 26)])
+
+_lib = None
+_vp = ctypes.c_void_p
+_i32p = ctypes.POINTER(ctypes.c_int32)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_f64p = ctypes.POINTER(ctypes.c_double)
+_f32p = ctypes.POINTER(ctypes.c_float)
+
+EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit", "hp3dg_batch_run",
+           "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
+           "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_output_sizes", "hp3dg_device_outputs",
+           "hp3dg_phase_times", "hp3dg_last_bad_element", "hp3dg_batch_end", "hp3dg_strerror"]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIBPATH):
+            raise RuntimeError(f"{LIBPATH} is missing: build it with hp3d_gb300.build.build()")
+        L = ctypes.CDLL(LIBPATH)
+        L.hp3dg_batch_begin.argtypes = [ctypes.POINTER(Opts), ctypes.POINTER(_vp)]
+        L.hp3dg_set_stream.argtypes = [_vp, _vp]
+        L.hp3dg_batch_submit.argtypes = [_vp, ctypes.c_int32, _vp, _f64p, _f64p, _f64p,
+                                         ctypes.c_int32]
+        L.hp3dg_batch_run.argtypes = [_vp]
+        L.hp3dg_batch_sync.argtypes = [_vp]
+        L.hp3dg_batch_download.argtypes = [_vp]
+        L.hp3dg_get_elem.argtypes = [_vp, ctypes.c_int32, _f64p, ctypes.c_int32, _f64p]
+        L.hp3dg_get_condensed.argtypes = [_vp, ctypes.c_int32, _f64p, _f64p, _i32p]
+        L.hp3dg_get_schur.argtypes = [_vp, ctypes.c_int32, _f64p, _f64p, _i32p, _i32p]
+        L.hp3dg_index_map.argtypes = [_vp, _i32p, _i64p, _i64p, _i32p, _i64p]
+        L.hp3dg_output_sizes.argtypes = [_vp, _i64p, _i64p, _i64p, _i64p]
+        L.hp3dg_device_outputs.argtypes = [_vp] + [ctypes.POINTER(_vp)] * 5
+        L.hp3dg_phase_times.argtypes = [_vp, _f32p, ctypes.c_int32]
+        L.hp3dg_last_bad_element.argtypes = [_vp]
+        L.hp3dg_last_bad_element.restype = ctypes.c_int32
+        L.hp3dg_batch_end.argtypes = [_vp]
+        L.hp3dg_batch_end.restype = None
+        L.hp3dg_strerror.argtypes = [ctypes.c_int]
+        L.hp3dg_strerror.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def mesh_descriptors(mesh):
+    """Element descriptors (hp3dg_elem_desc array) of a mesh dict."""
+    ne = mesh["nelem"]
+    d = np.zeros(ne, dtype=DESC_DTYPE)
+    d["etype"] = mesh["etype"]
+    d["mdle"] = np.arange(ne, dtype=np.int32)
+    d["norder"] = mesh["norder"]
+    d["nori_edge"] = mesh["nori_edge"]
+    d["nori_face"] = mesh["nori_face"]
+    d["nodes"] = mesh["nodes"]
+    d["bcflag"] = mesh["bcflag"]
+    return d
+
+
+def _p(a, t):
+    return None if a is None else a.ctypes.data_as(t)
+
+
+class ElementPass:
+    """One batched element pass (a context of the C ABI)."""
+
+    def __init__(self, precision=FP64, integration=0, isol=10, keep_elem=False, timing=False,
+                 device=0, ozaki_radix=0, ozaki_digits=0):
+        self.L = lib()
+        o = Opts()
+        o.precision = precision
+        o.integration = integration
+        o.isol = isol
+        o.keep_elem = int(keep_elem)
+        o.timing = int(timing)
+        o.device = device
+        o.ozaki_radix = ozaki_radix
+        o.ozaki_digits = ozaki_digits
+        self.ctx = _vp()
+        self._check(self.L.hp3dg_batch_begin(ctypes.byref(o), ctypes.byref(self.ctx)), "begin")
+        self.nel = 0
+
+    def _check(self, rc, what):
+        if rc != 0:
+            bad = self.L.hp3dg_last_bad_element(self.ctx) if self.ctx else -1
+            raise HP3DGError(rc, f"{what}: {self.L.hp3dg_strerror(rc).decode()}", bad)
+
+    def set_stream(self, stream_ptr):
+        self._check(self.L.hp3dg_set_stream(self.ctx, _vp(stream_ptr)), "set_stream")
+
+    def submit(self, mesh, zdofd=None, desc=None):
+        self.mesh = mesh
+        self.desc = mesh_descriptors(mesh) if desc is None else desc
+        self.xvert = np.ascontiguousarray(mesh["xvert"], dtype=np.float64)
+        self.kappa = np.ascontiguousarray(mesh["kappa"], dtype=np.float64)
+        self.zd = None if zdofd is None else np.ascontiguousarray(np.concatenate(zdofd), np.float64)
+        self.nel = mesh["nelem"]
+        self._check(self.L.hp3dg_batch_submit(self.ctx, self.nel, self.desc.ctypes.data_as(_vp),
+                                              _p(self.xvert, _f64p), _p(self.kappa, _f64p),
+                                              _p(self.zd, _f64p), int(mesh["nnodes"])), "submit")
+
+    def run(self):
+        self._check(self.L.hp3dg_batch_run(self.ctx), "run")
+
+    def sync(self):
+        self._check(self.L.hp3dg_batch_sync(self.ctx), "sync")
+
+    def download(self):
+        self._check(self.L.hp3dg_batch_download(self.ctx), "download")
+
+    def sizes(self):
+        v = [ctypes.c_int64() for _ in range(4)]
+        self._check(self.L.hp3dg_output_sizes(self.ctx, *[ctypes.byref(x) for x in v]), "sizes")
+        return [x.value for x in v]
+
+    def condensed(self, e):
+        nnz, nl, _, _ = self.sizes()
+        nc = ctypes.c_int32()
+        self._check(self.L.hp3dg_get_condensed(self.ctx, e, None, None, ctypes.byref(nc)), "cond")
+        zb = np.zeros(max(nc.value, 1)); zs = np.zeros(max(nc.value ** 2, 1))
+        self._check(self.L.hp3dg_get_condensed(self.ctx, e, _p(zb, _f64p), _p(zs, _f64p),
+                                               ctypes.byref(nc)), "cond")
+        n = nc.value
+        return zb[:n], zs[: n * n].reshape(n, n)
+
+    def schur(self, e):
+        nb = ctypes.c_int32(); ni = ctypes.c_int32()
+        self._check(self.L.hp3dg_get_schur(self.ctx, e, None, None, ctypes.byref(nb),
+                                           ctypes.byref(ni)), "schur")
+        a = np.zeros(max(nb.value * ni.value, 1)); b = np.zeros(max(nb.value, 1))
+        self._check(self.L.hp3dg_get_schur(self.ctx, e, _p(a, _f64p), _p(b, _f64p),
+                                           ctypes.byref(nb), ctypes.byref(ni)), "schur")
+        return (a[: nb.value * ni.value].reshape(ni.value, nb.value).T.copy(), b[: nb.value])
+
+    def elem(self, e, n):
+        a = np.zeros((n, n), order="F"); b = np.zeros(n)
+        self._check(self.L.hp3dg_get_elem(self.ctx, e, a.ctypes.data_as(_f64p), n,
+                                          _p(b, _f64p)), "elem")
+        return a, b
+
+    def index_map(self):
+        nnz, nl, _, _ = self.sizes()
+        nf = np.zeros(self.mesh["nnodes"], dtype=np.int32)
+        en = np.zeros(self.nel + 1, dtype=np.int64)
+        lo = np.zeros(self.nel + 1, dtype=np.int64)
+        lc = np.zeros(max(nl, 1), dtype=np.int32)
+        nr = ctypes.c_int64()
+        self._check(self.L.hp3dg_index_map(self.ctx, _p(nf, _i32p), _p(en, _i64p), _p(lo, _i64p),
+                                           _p(lc, _i32p), ctypes.byref(nr)), "index_map")
+        return nr.value, nf, lc[:nl], lo, en
+
+    def phase_times(self):
+        t = (ctypes.c_float * 6)()
+        self._check(self.L.hp3dg_phase_times(self.ctx, t, 6), "times")
+        return list(t)
+
+    def close(self):
+        if self.ctx:
+            self.L.hp3dg_batch_end(self.ctx)
+            self.ctx = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

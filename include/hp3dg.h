@@ -1,0 +1,178 @@
+/*
+ * hp3dg.h -- C ABI of the GB300 element pass for hp3D.
+ *
+ * One batched, device-resident pass replaces hp3D's per-element work inside
+ * the assembly loop of the MUMPS driver (Oden-EAG/hp3d, paths relative to
+ * trunk/):
+ *
+ *   solver/omp_mumps/mumps_sc.F90:253-330   element loop (OpenMP)
+ *     -> constrs/celem_systemI.F90:54-951   modified element, compression
+ *        -> problems/POISSON/GALERKIN/elem.F90:20-55 / elem_opt.F90:22-141
+ *           (set_3D_int, shape3DH, geom3D, getf, A_TEST, DSYRK)
+ *        -> modules/stc.F90:182-509         static condensation
+ *     -> mumps_sc.F90:266-321               LCON / triplets
+ *
+ * The caller describes each element as find_order/find_orient/nodcor/
+ * get_index would (hp3dg_elem_desc), submits the batch once before the
+ * element loop, runs it, and then reads per element exactly what the
+ * reference routines return.  All entry points are plain C: pointers and
+ * sizes, no C++ or torch types.  Every result is computed on the GPU; there
+ * is no CPU fallback.  A call returns HP3DG_OK (0) or a negative error code.
+ *
+ * Thread safety: submit/run/download are called by one thread (the
+ * reference's STEP 1.5, before its parallel region).  The hp3dg_get_* calls
+ * only read host buffers filled by hp3dg_batch_download and may be called
+ * concurrently from the OpenMP threads of the element loop.
+ */
+#ifndef HP3DG_H
+#define HP3DG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes (the reference stops on these conditions: geom.F90:70-71
+ * negative Jacobian, stc.F90:464-488 LAPACK info /= 0) */
+#define HP3DG_OK 0
+#define HP3DG_ERR_NEG_JACOBIAN -1 /* det J < 0 at a quadrature point */
+#define HP3DG_ERR_NOT_SPD -2      /* bubble block not positive definite */
+#define HP3DG_ERR_BAD_ORDER -3    /* order outside 1..MAXP or unsupported type */
+#define HP3DG_ERR_ALLOC -4        /* device or pinned allocation failed */
+#define HP3DG_ERR_CUDA -5         /* a CUDA call failed */
+#define HP3DG_ERR_TIMEOUT -6      /* a bounded device wait gave up */
+#define HP3DG_ERR_ARG -7          /* invalid argument */
+#define HP3DG_ERR_STATE -8        /* call out of order (e.g. get before run) */
+#define HP3DG_ERR_UNSUPPORTED -9  /* feature not available on this device */
+
+/* element types: node types MDLB / MDLP / MDLN of data_structure3D */
+#define HP3DG_HEXA 1
+#define HP3DG_PRISM 2
+#define HP3DG_TET 3
+
+/* precision of the B^T D B contraction */
+#define HP3DG_FP64 0  /* FP64 on CUDA cores (the plain GPU form) */
+#define HP3DG_MIXED 1 /* split-BF16 digits on tcgen05 tensor cores, exact
+                         FP32 accumulation per digit level, FP64 recombination */
+
+#define HP3DG_MAXP 6 /* parameters.F90:17 */
+
+typedef struct hp3dg_ctx hp3dg_ctx;
+
+typedef struct hp3dg_opts {
+  int32_t precision;   /* HP3DG_FP64 or HP3DG_MIXED */
+  int32_t integration; /* control INTEGRATION: quadrature order p+INTEGRATION
+                          (set_3D_int.F90:236-244), capped at MAXP */
+  int32_t isol;        /* source selector of getf (common/getf.F90:63):
+                          0,1,2 as common/solution.F90; 10 = sin sin sin;
+                          11 = f == 1; 12 = u = xyz (f = 0) */
+  int32_t keep_elem;   /* 1: keep the unconstrained element matrices so that
+                          hp3dg_get_elem can serve the elem() contract */
+  int32_t timing;      /* 1: record per-phase CUDA-event timings */
+  int32_t device;      /* CUDA device ordinal */
+  int32_t ozaki_radix; /* mixed: bits per BF16 digit (0 = default 7) */
+  int32_t ozaki_digits;/* mixed: digits per operand (0 = default 7) */
+  int32_t stc_method;  /* condensation: 0 = Cholesky (the Poisson bubble block
+                          is SPD); reserved for an LU variant */
+  int32_t reserved[7];
+} hp3dg_opts;
+
+/* Element descriptor: what find_order (datstrs/find_order.F90:5),
+ * find_orient (datstrs/find_orient.F90:8), elem_nodes and get_index
+ * (datstrs/get_index.F90:27) return for element Mdle. */
+typedef struct hp3dg_elem_desc {
+  int32_t etype;         /* HP3DG_HEXA (only hexahedra in this release) */
+  int32_t mdle;          /* middle node id, returned back for bookkeeping */
+  int32_t norder[19];    /* Norder: edges, faces (MODORDER=10 packed), interior */
+  int32_t nori_edge[12]; /* NoriE: 0/1 */
+  int32_t nori_face[6];  /* NoriF: 0..7 */
+  int32_t nodes[26];     /* global ids of vertex, edge, face nodes, element order */
+  int32_t bcflag[26];    /* 1: every dof of this node is Dirichlet (index=1) */
+} hp3dg_elem_desc;
+
+/* Create a context on opts->device (NULL opts = defaults: FP64,
+ * INTEGRATION=0, isol=10). */
+int hp3dg_batch_begin(const hp3dg_opts *opts, hp3dg_ctx **ctx);
+
+/* Bind the context to an existing CUDA stream (cudaStream_t passed as
+ * void*; NULL = the context's own stream). */
+int hp3dg_set_stream(hp3dg_ctx *ctx, void *stream);
+
+/* Submit a batch: n_elem descriptors in ELEM_ORDER, vertex coordinates
+ * xvert (n_elem x 8 x 3, the nodcor geometry dof of a trilinear map;
+ * higher-order geometry dof are zero), per-element coefficient kappa
+ * (NULL = 1), Dirichlet data zdofd (NULL = homogeneous; else for each
+ * element its interface dof values in element dof order, concatenated),
+ * and the number of global nodes (size of NFIRST_DOF).
+ * Validates orders and copies the batch to the device.
+ * Replaces: mumps_sc.F90 STEP 1 (102-188). */
+int hp3dg_batch_submit(hp3dg_ctx *ctx, int32_t n_elem, const hp3dg_elem_desc *desc,
+                       const double *xvert, const double *kappa, const double *zdofd,
+                       int32_t n_nodes_global);
+
+/* Run the whole element pass on the device (asynchronous on the context's
+ * stream; errors of the pass are reported by hp3dg_batch_sync).
+ * Replaces: the STEP 2 element loop (mumps_sc.F90:253-330). */
+int hp3dg_batch_run(hp3dg_ctx *ctx);
+
+/* Wait for the pass and return its status (first bad element via
+ * hp3dg_last_bad_element). */
+int hp3dg_batch_sync(hp3dg_ctx *ctx);
+
+/* Copy all outputs into pinned host buffers owned by the context. */
+int hp3dg_batch_download(hp3dg_ctx *ctx);
+
+/* elem() contract (problems/POISSON/GALERKIN/elem.F90:20-55): unconstrained
+ * stiffness ALOC(1,1) written with leading dimension ld (= ALOC(1,1)%nrow)
+ * and load BLOC(1).  Needs opts.keep_elem = 1. */
+int hp3dg_get_elem(const hp3dg_ctx *ctx, int32_t iel, double *aloc, int32_t ld,
+                   double *bloc);
+
+/* celem_systemI contract (constrs/celem_systemI.F90:812-845, ISYM_FLAG=2):
+ * compressed condensed load Zbload(nrdofc) and row-major stiffness
+ * Zastif(nrdofc**2); nrdofc returned. */
+int hp3dg_get_condensed(const hp3dg_ctx *ctx, int32_t iel, double *zbload,
+                        double *zastif, int32_t *nrdofc);
+
+/* Schur blocks kept for back-substitution (stc.F90:273-277): ASchur =
+ * inv(Abb) Abi (nb x ni column-major), BSchur = inv(Abb) Bb (nb). */
+int hp3dg_get_schur(const hp3dg_ctx *ctx, int32_t iel, double *aschur, double *bschur,
+                    int32_t *nb, int32_t *ni);
+
+/* Index maps of mumps_sc (STEP 1 NFIRST_DOF, STEP 2 LCON): nfirst_dof
+ * (n_nodes_global, -1 for unvisited), elem_nnz (n_elem+1 prefix of
+ * nrdofc**2), lcon_off (n_elem+1 prefix of nrdofc), lcon (1-based global
+ * dof, nodes in reverse order), nrdof (number of interface dof).  Any
+ * pointer may be NULL. */
+int hp3dg_index_map(const hp3dg_ctx *ctx, int32_t *nfirst_dof, int64_t *elem_nnz,
+                    int64_t *lcon_off, int32_t *lcon, int64_t *nrdof);
+
+/* Sizes of the batch outputs (for the caller's allocation). */
+int hp3dg_output_sizes(const hp3dg_ctx *ctx, int64_t *nnz_total, int64_t *lcon_total,
+                       int64_t *schur_total, int64_t *bubble_total);
+
+/* Device pointers of the outputs (for consumers that stay on the GPU). */
+int hp3dg_device_outputs(const hp3dg_ctx *ctx, const double **zastif,
+                         const double **zbload, const double **aschur,
+                         const double **bschur, const int32_t **lcon);
+
+/* Per-phase device times (ms) of the last run when opts.timing = 1:
+ * [0] tables, [1] geometry+load, [2] contraction, [3] condensation,
+ * [4] index maps, [5] whole pass.  n = number of entries wanted. */
+int hp3dg_phase_times(const hp3dg_ctx *ctx, float *ms, int32_t n);
+
+/* First element (0-based) that failed in the last run, or -1. */
+int32_t hp3dg_last_bad_element(const hp3dg_ctx *ctx);
+
+/* Release everything. */
+void hp3dg_batch_end(hp3dg_ctx *ctx);
+
+/* Message for a status code. */
+const char *hp3dg_strerror(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HP3DG_H */
