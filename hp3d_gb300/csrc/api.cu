@@ -507,6 +507,7 @@ int hp3dg_batch_sync(hp3dg_ctx* c) {
   c->last_bad = -1;
   if (fl[0] != NONE) { c->last_bad = fl[0]; return HP3DG_ERR_NEG_JACOBIAN; }
   if (fl[1] != NONE) { c->last_bad = fl[1]; return HP3DG_ERR_NOT_SPD; }
+  if (fl[2] != NONE) return HP3DG_ERR_TIMEOUT;  // a bounded wait of the tensor-core kernel gave up
   return HP3DG_OK;
 }
 
@@ -644,6 +645,16 @@ int hp3dg_device_outputs(const hp3dg_ctx* c, const double** zastif, const double
 int hp3dg_phase_times(const hp3dg_ctx* c, float* ms, int32_t n) {
   if (!c || !ms || n < 0) return HP3DG_ERR_ARG;
   for (int i = 0; i < n && i < 6; ++i) ms[i] = c->times[i];
+  return HP3DG_OK;
+}
+
+int hp3dg_mixed_config(const hp3dg_ctx* c, int32_t* radix, int32_t* digits, int32_t* pairs) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted || c->opts.precision != HP3DG_MIXED || c->bins.empty()) return HP3DG_ERR_STATE;
+  const OzakiPlan& p = c->bins[0].plan;
+  if (radix) *radix = p.radix;
+  if (digits) *digits = p.digits;
+  if (pairs) *pairs = ozaki_pairs(p);
   return HP3DG_OK;
 }
 

@@ -48,6 +48,7 @@ size_t ozaki_m_bytes(const OzakiPlan& plan);
 int launch_ozaki_slice_d(const OzakiPlan& plan, int nel, int nint, const double* d_D,
                          uint16_t* d_ddig, double* d_dscale, cudaStream_t st);
 size_t ozaki_d_bytes(const OzakiPlan& plan, int nel);
+int ozaki_pairs(const OzakiPlan& plan);
 // the tensor-core contraction: PK = dscale*mscale*sum_s 2^-radix*s acc_s
 int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,

@@ -1,13 +1,651 @@
-// k_ozaki.cu -- mixed-precision contraction (placeholder until the tcgen05 kernel lands).
+// k_ozaki.cu -- mixed-precision B^T D B contraction on tcgen05 tensor cores.
+//
+// The stiffness of every element of a bin is one row of a GEMM with a shared
+// operand (elem_opt.F90:86-137 computes it per element as A_TEST*A_TEST^T):
+//
+//   PK[e, c] = sum_q D[e, q] M[q, c],   q = (point l, component pair ij),
+//   c = packed (a <= b) entry,  M[(l,ij), (a,b)] = G_i[l,a] G_j[l,b] (+ sym).
+//
+// Both operands are FP64.  They are split into balanced integer digits of
+// `radix` bits (scaled per element row / per column by powers of two):
+//   D = s_e * sum_i d_i 2^(-radix*i),   M = t_c * sum_j m_j 2^(-radix*j),
+// every digit an integer |d| <= 2^radix, exact in BF16.  The digit products
+// d_i * m_j are exact and, grouped by level s = i + j, their sums over q stay
+// below 2^24 and are therefore exact in the FP32 TMEM accumulators.  The
+// levels s = 2 .. digits+1 are recombined exactly as 64-bit integers and
+// scaled to FP64 in the epilogue (the FP64 residual correction of the
+// split): the result carries ~radix*digits bits.
+//
+// Kernel structure (one CTA per SM, persistent over 128 x 128 output tiles):
+//   warp 0   TMA producer: digit tiles of A = M (128 packed columns x 16 q)
+//            and B = D (128 elements x 16 q), SWIZZLE_32B, 3-stage ring
+//   warp 1   TMEM allocation (512 columns) and the single MMA-issuing thread
+//   warps 2-5 epilogue: tcgen05.ld of up to 4 level accumulators, exact
+//            integer recombination, FP64 scaling, coalesced stores of PK
+// Levels are processed in passes of <= 4 accumulators (4 x 128 TMEM
+// columns); pass > 1 adds into the FP64 tile written by pass 1.
+#include "hp3dg_internal.cuh"
 #include "hp3dg_kernels.h"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <dlfcn.h>
+#include <math.h>
+#include <string.h>
+
 namespace hp3dg {
-int ozaki_plan(int, int, int, int, OzakiPlan*) { return -1; }
-int launch_ozaki_build_m(const OzakiPlan&, int, int, int, int, const double*, uint16_t*, double*,
-                         double*, cudaStream_t) { return -1; }
-size_t ozaki_m_bytes(const OzakiPlan&) { return 0; }
-int launch_ozaki_slice_d(const OzakiPlan&, int, int, const double*, uint16_t*, double*,
-                         cudaStream_t) { return -1; }
-size_t ozaki_d_bytes(const OzakiPlan&, int) { return 0; }
-int launch_ozaki_gemm(const OzakiPlan&, int, int, const uint16_t*, const double*, const uint16_t*,
-                      const double*, double*, int*, cudaStream_t) { return -1; }
+
+namespace {
+constexpr int BM = 128;       // packed columns per tile (MMA M, TMEM lanes)
+constexpr int BN = 128;       // elements per tile (MMA N, TMEM columns per level)
+constexpr int BK = 16;        // q per k-block (one MMA K step), 32-byte rows
+constexpr int MAXDIG = 7;
+constexpr int MAXPASS = 4;
+constexpr int MAXPAIR = 40;
+constexpr int NSTAGE = 4;
+constexpr int TILE_BYTES = BM * BK * 2;  // 4096, A and B tiles have the same size
+constexpr int STAGE_BYTES = 2 * MAXDIG * TILE_BYTES;  // room for all digits
+constexpr int NTHREADS = 192;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr long WAIT_LIMIT = 1L << 24;  // bounded mbarrier waits
+
+struct PassDesc {
+  int first_level;  // level of accumulator slot 0
+  int nlev;         // accumulator slots used (<= 4)
+  int nA, nB;       // digits of A (M) and B (D) needed: 1..nA, 1..nB
+  int pair0, npair; // range in the pair table
+};
+struct GemmParams {
+  int npass;
+  PassDesc pass[MAXPASS];
+  int npairs;
+  int8_t pi[MAXPAIR], pj[MAXPAIR], pslot[MAXPAIR], pfirst[MAXPAIR];
+  int radix;
+  int s1;           // two-pass recombination shift (see epi_chunk)
+  int scale_shift;  // radix*last level of pass 0 (+ s1) : final power-of-two shift
+  int nk;        // k-blocks
+  int ncb, neb;  // column / element blocks
+  int nel, ncols;
+};
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// PTX helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(a) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false if the limit was hit or another role aborted
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile int* abort_) {
+  for (long it = 0; it < WAIT_LIMIT; ++it) {
+    if (mbar_try(a, parity)) return true;
+    if ((it & 255) == 255 && *abort_) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t mbar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(mbar), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+// shared-memory matrix descriptor: K-major, SWIZZLE_32B, 32-byte rows,
+// 8-row groups 256 bytes apart (SBO), LBO unused (1), version 1.
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;                 // LBO (ignored for swizzled K-major)
+  d |= (uint64_t)(256 >> 4) << 32;        // SBO
+  d |= (uint64_t)1 << 46;                 // descriptor version
+  d |= (uint64_t)6 << 61;                 // SWIZZLE_32B
+  return d;
+}
+__device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
+                                          uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void umma_commit(uint32_t mbar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar)
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// tile t -> (column block, element block): groups of 8 column blocks sweep
+// all element blocks, so the digit tiles of a group stay resident in L2.
+__device__ __forceinline__ void tile_coords(int t, const GemmParams& P, int& cb, int& eb) {
+  const int grp = 8;
+  int g = t / (grp * P.neb);
+  int r = t - g * grp * P.neb;
+  int gw = P.ncb - g * grp;
+  if (gw > grp) gw = grp;
+  cb = g * grp + r % gw;
+  eb = r / gw;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// instruction descriptor: kind::f16, A = B = BF16, D = F32, K-major, M=128, N=128
+__host__ __device__ constexpr uint32_t idesc_bf16_m128_n128() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
+
+// exponent k of an exact power of two 2^k (the digit scales)
+__device__ __forceinline__ int pow2_exponent(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
+}
+// x * 2^k for normal results (k within the normal range), exact
+__device__ __forceinline__ double times_pow2(double x, int k) {
+  if (k >= -1022 && k <= 1023) return x * __longlong_as_double((long long)(k + 1023) << 52);
+  return ldexp(x, k);
+}
+
+// Epilogue of one 16-element chunk of one pass.  The level accumulators are
+// exact integers (< 2^24) in FP32; they are recombined exactly as 64-bit
+// integers.  With two passes, pass 0 stores its integer V1 in the output
+// slot and the last pass forms W = V1 * 2^S1 + V2 * 2^(S1 - radix*nlev2)
+// (|W| < 2^63) before the single conversion to FP64 and the power-of-two
+// scaling by the element and column scales.
+template <int NLEV>
+__device__ __forceinline__ void epi_chunk(const GemmParams& P, int ps, uint32_t tlane, int ch,
+                                          int e0, int c, bool cok, int kc,
+                                          const double* __restrict__ dscale,
+                                          double* __restrict__ PK, int lane) {
+  uint32_t v[NLEV][16];
+#pragma unroll
+  for (int k = 0; k < NLEV; ++k) tmem_ld16(tlane + (uint32_t)(k * BN + ch * 16), v[k]);
+  const int el = e0 + (lane & 15);
+  const int ke_lane = (el < P.nel) ? pow2_exponent(dscale[el]) : 0;
+  long long* out = (long long*)PK;
+  const bool two = P.npass == 2;
+  const bool last = ps == P.npass - 1;
+  long long prev[16];
+  if (two && last) {
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      const int e = e0 + q;
+      prev[q] = (cok && e < P.nel) ? out[(size_t)e * P.ncols + c] : 0;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    long long s = 0;
+#pragma unroll
+    for (int k = 0; k < NLEV; ++k)
+      s = s * (1LL << P.radix) + (long long)__float2int_rn(__uint_as_float(v[k][q]));
+    const int e = e0 + q;
+    const int ke = __shfl_sync(0xffffffffu, ke_lane, q);
+    if (!(cok && e < P.nel)) continue;
+    const size_t idx = (size_t)e * P.ncols + c;
+    if (two && !last) {
+      out[idx] = s;  // exact partial sum V1
+    } else if (two) {
+      const int sh = P.radix * P.pass[1].nlev - P.s1;
+      long long w = prev[q] * (1LL << P.s1) + (sh >= 0 ? (s >> sh) : s * (1LL << (-sh)));
+      PK[idx] = times_pow2((double)w, ke + kc - P.scale_shift);
+    } else {
+      PK[idx] = times_pow2((double)s, ke + kc - P.scale_shift);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the GEMM
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_ozaki_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                 const GemmParams P, const double* __restrict__ dscale,
+                 const double* __restrict__ mscale, double* __restrict__ PK,
+                 int* __restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smraw[];
+  // align the ring to 1024 bytes (swizzle repeat)
+  uint8_t* ring = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  __shared__ __align__(8) uint64_t full_bar[NSTAGE], empty_bar[NSTAGE], acc_full, acc_empty;
+  __shared__ uint32_t tmem_base;
+  __shared__ volatile int abort_;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = P.ncb * P.neb;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NSTAGE; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), 1);
+    }
+    mbar_init(smem_u32(&acc_full), 1);
+    mbar_init(smem_u32(&acc_empty), 128);
+    abort_ = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tbase = tmem_base;
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
+      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
+      int stage = 0;
+      uint32_t phase = 0;
+      for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
+        int cb, eb;
+        tile_coords(t, P, cb, eb);
+        for (int ps = 0; ps < P.npass && !abort_; ++ps) {
+          const PassDesc& pd = P.pass[ps];
+          for (int kb = 0; kb < P.nk; ++kb) {
+            if (!mbar_wait(smem_u32(&empty_bar[stage]), phase ^ 1, &abort_)) {
+              abort_ = 1; atomicExch(err, 1); break;
+            }
+            uint32_t fb = smem_u32(&full_bar[stage]);
+            mbar_expect_tx(fb, (uint32_t)(pd.nA + pd.nB) * TILE_BYTES);
+            uint8_t* st = ring + (size_t)stage * STAGE_BYTES;
+            for (int i = 0; i < pd.nA; ++i)
+              tma_load_3d(smem_u32(st + i * TILE_BYTES), &tmA, fb, kb * BK, cb * BM, i);
+            for (int j = 0; j < pd.nB; ++j)
+              tma_load_3d(smem_u32(st + (MAXDIG + j) * TILE_BYTES), &tmB, fb, kb * BK, eb * BN, j);
+            if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_m128_n128();
+      int stage = 0;
+      uint32_t phase = 0, accph = 0;
+      for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
+        for (int ps = 0; ps < P.npass && !abort_; ++ps) {
+          const PassDesc& pd = P.pass[ps];
+          // the epilogue must have drained the accumulators
+          if (!mbar_wait(smem_u32(&acc_empty), accph ^ 1, &abort_)) {
+            abort_ = 1; atomicExch(err, 2); break;
+          }
+          accph ^= 1;
+          tc_fence_after();
+          for (int kb = 0; kb < P.nk; ++kb) {
+            if (!mbar_wait(smem_u32(&full_bar[stage]), phase, &abort_)) {
+              abort_ = 1; atomicExch(err, 3); break;
+            }
+            tc_fence_after();
+            uint8_t* st = ring + (size_t)stage * STAGE_BYTES;
+            for (int p = pd.pair0; p < pd.pair0 + pd.npair; ++p) {
+              uint64_t ad = sdesc_sw32(smem_u32(st + (P.pi[p] - 1) * TILE_BYTES));
+              uint64_t bd = sdesc_sw32(smem_u32(st + (MAXDIG + P.pj[p] - 1) * TILE_BYTES));
+              uint32_t acc = (kb > 0 || !P.pfirst[p]) ? 1u : 0u;
+              umma_bf16(tbase + (uint32_t)P.pslot[p] * BN, ad, bd, idesc, acc);
+            }
+            umma_commit(smem_u32(&empty_bar[stage]));  // frees the stage when done
+            if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+          }
+          umma_commit(smem_u32(&acc_full));  // accumulators complete
+        }
+      }
+    }
+  } else {
+    // ---------------- epilogue (warps 2..5, one TMEM lane quarter each) ----------------
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;  // TMEM lane = packed column within the tile
+    const uint32_t tlane = tbase + ((uint32_t)(quarter * 32) << 16);
+    uint32_t accph = 0;
+    for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
+      int cb, eb;
+      tile_coords(t, P, cb, eb);
+      const int c = cb * BM + row;
+      const bool cok = c < P.ncols;
+      const int kc = cok ? pow2_exponent(mscale[c]) : 0;
+      for (int ps = 0; ps < P.npass; ++ps) {
+        const PassDesc& pd = P.pass[ps];
+        if (!mbar_wait(smem_u32(&acc_full), accph, &abort_)) {
+          abort_ = 1; atomicExch(err, 4); break;
+        }
+        accph ^= 1;
+        tc_fence_after();
+        for (int ch = 0; ch < BN / 16; ++ch) {
+          const int e0 = eb * BN + ch * 16;
+          switch (pd.nlev) {
+            case 1: epi_chunk<1>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
+            case 2: epi_chunk<2>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
+            case 3: epi_chunk<3>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
+            default: epi_chunk<4>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
+          }
+        }
+        tc_fence_before();
+        mbar_arrive(smem_u32(&acc_empty));
+      }
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase),
+                 "r"(TMEM_COLS));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// digit builders
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double pow2_ceil_scale(double mx) {
+  if (!(mx > 0.0)) return 1.0;
+  int ex;
+  frexp(mx, &ex);  // mx = m 2^ex, m in [0.5, 1)
+  return ldexp(1.0, ex);
+}
+
+__device__ __forceinline__ uint16_t bf16_bits(double d) {
+  __nv_bfloat16 h = __float2bfloat16_rn((float)d);
+  return *(uint16_t*)&h;
+}
+
+// M[q, c] for q = (l, comp), c = packed index (pk_index order)
+__device__ __forceinline__ double m_entry(const double* __restrict__ grad, int n, int l, int comp,
+                                          int a, int b) {
+  const double* g = grad + (size_t)l * 3 * n;
+  const int I[6] = {0, 1, 2, 0, 0, 1}, J[6] = {0, 1, 2, 1, 2, 2};
+  int i = I[comp], j = J[comp];
+  double v = g[i * n + a] * g[j * n + b];
+  if (i != j) v += g[j * n + a] * g[i * n + b];
+  return v;
+}
+
+__device__ inline void pk_decode(int64_t c, int ni, int nb, int& a, int& b) {
+  int64_t nbb = (int64_t)nb * (nb + 1) / 2, nbi = (int64_t)nb * ni;
+  if (c < nbb) {
+    int cc = (int)((sqrt(8.0 * (double)c + 1.0) - 1.0) * 0.5);
+    while ((int64_t)(cc + 1) * (cc + 2) / 2 <= c) ++cc;
+    while ((int64_t)cc * (cc + 1) / 2 > c) --cc;
+    a = ni + (int)(c - (int64_t)cc * (cc + 1) / 2);
+    b = ni + cc;
+  } else if (c < nbb + nbi) {
+    int64_t r = c - nbb;
+    a = (int)(r / nb);           // interface
+    b = ni + (int)(r % nb);      // bubble
+  } else {
+    int64_t r = c - nbb - nbi;
+    int bb = (int)((sqrt(8.0 * (double)r + 1.0) - 1.0) * 0.5);
+    while ((int64_t)(bb + 1) * (bb + 2) / 2 <= r) ++bb;
+    while ((int64_t)bb * (bb + 1) / 2 > r) --bb;
+    a = (int)(r - (int64_t)bb * (bb + 1) / 2);
+    b = bb;
+  }
+}
+
+// one block of 128 threads per 128 packed columns; q loop inside
+__global__ void k_build_m(int nint, int n, int ni, int nb, int ncols, int ncols_pad, int kpad,
+                          int radix, int digits, const double* __restrict__ grad,
+                          uint16_t* __restrict__ mdig, double* __restrict__ mscale) {
+  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols_pad) return;
+  const int K = 6 * nint;
+  if (c >= ncols) {
+    for (int s = 0; s < digits; ++s)
+      for (int q = 0; q < kpad; ++q) mdig[((size_t)s * ncols_pad + c) * kpad + q] = 0;
+    mscale[c] = 0.0;
+    return;
+  }
+  int a, b;
+  pk_decode(c, ni, nb, a, b);
+  double mx = 0.0;
+  for (int q = 0; q < K; ++q) mx = fmax(mx, fabs(m_entry(grad, n, q / 6, q % 6, a, b)));
+  double sc = pow2_ceil_scale(mx);
+  mscale[c] = sc;
+  double rs = 1.0 / sc, up = ldexp(1.0, radix);
+  for (int q = 0; q < kpad; ++q) {
+    double r = (q < K) ? m_entry(grad, n, q / 6, q % 6, a, b) * rs : 0.0;
+    for (int s = 0; s < digits; ++s) {
+      r *= up;
+      double d = rint(r);
+      r -= d;
+      mdig[((size_t)s * ncols_pad + c) * kpad + q] = bf16_bits(d);
+    }
+  }
+}
+
+// one block per element row: scale = 2^ceil(log2 max|D|), digits
+__global__ void k_slice_d(int nint, int kpad, int nel_pad, int radix, int digits,
+                          const double* __restrict__ D, uint16_t* __restrict__ ddig,
+                          double* __restrict__ dscale, int nel) {
+  int e = blockIdx.x;
+  const int K = 6 * nint;
+  __shared__ double red[256];
+  double mx = 0.0;
+  if (e < nel)
+    for (int q = threadIdx.x; q < K; q += blockDim.x) mx = fmax(mx, fabs(D[(size_t)e * K + q]));
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
+    __syncthreads();
+  }
+  double sc = pow2_ceil_scale(red[0]);
+  if (threadIdx.x == 0) dscale[e] = (e < nel) ? sc : 0.0;
+  double rs = 1.0 / sc, up = ldexp(1.0, radix);
+  for (int q = threadIdx.x; q < kpad; q += blockDim.x) {
+    double r = (e < nel && q < K) ? D[(size_t)e * K + q] * rs : 0.0;
+    for (int s = 0; s < digits; ++s) {
+      r *= up;
+      double d = rint(r);
+      r -= d;
+      ddig[((size_t)s * nel_pad + e) * kpad + q] = bf16_bits(d);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn get_encode() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+int make_map(CUtensorMap* m, const void* base, int kpad, int rows_pad, int digits) {
+  EncodeTiledFn enc = get_encode();
+  if (!enc) return -1;
+  cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)digits};
+  cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)rows_pad * kpad * 2};
+  cuuint32_t box[3] = {BK, 128, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides,
+                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : -2;
+}
+
+int round_up(int v, int m) { return (v + m - 1) / m * m; }
+}  // namespace
+
+int ozaki_plan(int nint, int n, int radix, int digits, OzakiPlan* plan) {
+  if (radix <= 0) radix = 7;
+  if (digits <= 0) digits = 7;
+  if (radix < 4 || radix > 8 || digits < 2 || digits > MAXDIG) return -1;
+  plan->radix = radix;
+  plan->digits = digits;
+  plan->levels = digits;  // levels 2 .. digits+1
+  plan->kdim = round_up(6 * nint, BK);
+  plan->ncols = round_up(n * (n + 1) / 2, BM);
+  return 0;
+}
+
+size_t ozaki_m_bytes(const OzakiPlan& p) { return (size_t)p.digits * p.ncols * p.kdim * 2; }
+size_t ozaki_d_bytes(const OzakiPlan& p, int nel) {
+  return (size_t)p.digits * round_up(nel, BN) * p.kdim * 2;
+}
+
+int launch_ozaki_build_m(const OzakiPlan& p, int nint, int n, int ni, int nb, const double* d_grad,
+                         uint16_t* d_mdig, double* d_mscale, double* d_work, cudaStream_t st) {
+  (void)d_work;
+  int ncols = n * (n + 1) / 2;
+  k_build_m<<<p.ncols / 128, 128, 0, st>>>(nint, n, ni, nb, ncols, p.ncols, p.kdim, p.radix,
+                                           p.digits, d_grad, d_mdig, d_mscale);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_ozaki_slice_d(const OzakiPlan& p, int nel, int nint, const double* d_D,
+                         uint16_t* d_ddig, double* d_dscale, cudaStream_t st) {
+  int nel_pad = round_up(nel, BN);
+  if (nel_pad == 0) return 0;
+  k_slice_d<<<nel_pad, 256, 0, st>>>(nint, p.kdim, nel_pad, p.radix, p.digits, d_D, d_ddig,
+                                     d_dscale, nel);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+// pass / pair table: levels 2..digits+1 in passes of <= 4 accumulators
+static void build_params(const OzakiPlan& p, GemmParams* G) {
+  memset(G, 0, sizeof(*G));
+  G->radix = p.radix;
+  int lev_lo = 2, lev_hi = p.digits + 1;
+  int np = 0, npair = 0;
+  for (int L0 = lev_lo; L0 <= lev_hi; L0 += 4) {
+    PassDesc& pd = G->pass[np++];
+    pd.first_level = L0;
+    pd.nlev = (lev_hi - L0 + 1) < 4 ? (lev_hi - L0 + 1) : 4;
+    pd.pair0 = npair;
+    pd.nA = pd.nB = 0;
+    for (int s = L0; s < L0 + pd.nlev; ++s) {
+      bool first = true;
+      for (int i = 1; i <= p.digits; ++i) {
+        int j = s - i;
+        if (j < 1 || j > p.digits) continue;
+        G->pi[npair] = (int8_t)i;
+        G->pj[npair] = (int8_t)j;
+        G->pslot[npair] = (int8_t)(s - L0);
+        G->pfirst[npair] = first ? 1 : 0;
+        first = false;
+        pd.nA = pd.nA > i ? pd.nA : i;
+        pd.nB = pd.nB > j ? pd.nB : j;
+        ++npair;
+      }
+    }
+    pd.npair = npair - pd.pair0;
+  }
+  G->npass = np;
+  G->npairs = npair;
+  const PassDesc& p0 = G->pass[0];
+  int last0 = p0.first_level + p0.nlev - 1;
+  if (np == 2) {
+    G->s1 = 62 - (24 + p.radix * (p0.nlev - 1));
+    G->scale_shift = p.radix * last0 + G->s1;
+  } else {
+    G->s1 = 0;
+    G->scale_shift = p.radix * last0;
+  }
+}
+
+int ozaki_pairs(const OzakiPlan& p) {
+  GemmParams G;
+  build_params(p, &G);
+  return G.npairs;
+}
+
+int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig,
+                      const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                      double* d_PK, int* d_flag, cudaStream_t st) {
+  if (nel <= 0) return 0;
+  static int num_sms = 0;
+  if (!num_sms) {
+    int dev;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  GemmParams G;
+  build_params(p, &G);
+  int nel_pad = round_up(nel, BN);
+  G.nk = p.kdim / BK;
+  G.ncb = p.ncols / BM;
+  G.neb = nel_pad / BN;
+  G.nel = nel;
+  G.ncols = n * (n + 1) / 2;
+  CUtensorMap ta, tb;
+  if (make_map(&ta, d_mdig, p.kdim, p.ncols, p.digits)) return -1;
+  if (make_map(&tb, d_ddig, p.kdim, nel_pad, p.digits)) return -1;
+  size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024;
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem) != cudaSuccess)
+      return -1;
+    attr = true;
+  }
+  int ntiles = G.ncb * G.neb;
+  int grid = ntiles < num_sms ? ntiles : num_sms;
+  k_ozaki_gemm<<<grid, NTHREADS, smem, st>>>(ta, tb, G, d_dscale, d_mscale, d_PK, d_flag);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
 }  // namespace hp3dg

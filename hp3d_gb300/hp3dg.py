@@ -52,7 +52,7 @@ _f32p = ctypes.POINTER(ctypes.c_float)
 EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit", "hp3dg_batch_run",
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_output_sizes", "hp3dg_device_outputs",
-           "hp3dg_phase_times", "hp3dg_last_bad_element", "hp3dg_batch_end", "hp3dg_strerror"]
+           "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_last_bad_element", "hp3dg_batch_end", "hp3dg_strerror"]
 
 
 def lib():
@@ -75,6 +75,7 @@ def lib():
         L.hp3dg_output_sizes.argtypes = [_vp, _i64p, _i64p, _i64p, _i64p]
         L.hp3dg_device_outputs.argtypes = [_vp] + [ctypes.POINTER(_vp)] * 5
         L.hp3dg_phase_times.argtypes = [_vp, _f32p, ctypes.c_int32]
+        L.hp3dg_mixed_config.argtypes = [_vp, _i32p, _i32p, _i32p]
         L.hp3dg_last_bad_element.argtypes = [_vp]
         L.hp3dg_last_bad_element.restype = ctypes.c_int32
         L.hp3dg_batch_end.argtypes = [_vp]
@@ -195,6 +196,15 @@ class ElementPass:
         t = (ctypes.c_float * 6)()
         self._check(self.L.hp3dg_phase_times(self.ctx, t, 6), "times")
         return list(t)
+
+    def mixed_config(self):
+        r, d, p = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        self._check(self.L.hp3dg_mixed_config(self.ctx, ctypes.byref(r), ctypes.byref(d),
+                                              ctypes.byref(p)), "mixed_config")
+        return r.value, d.value, p.value
+
+    def ozaki_pairs(self):
+        return self.mixed_config()[2]
 
     def close(self):
         if self.ctx:

@@ -162,6 +162,11 @@ int hp3dg_device_outputs(const hp3dg_ctx *ctx, const double **zastif,
  * [4] index maps, [5] whole pass.  n = number of entries wanted. */
 int hp3dg_phase_times(const hp3dg_ctx *ctx, float *ms, int32_t n);
 
+/* Mixed-precision configuration of the context's first bin: bits per digit,
+ * digits per operand, number of digit-pair products (tensor-core passes).
+ * Returns HP3DG_ERR_STATE before a mixed-precision submit. */
+int hp3dg_mixed_config(const hp3dg_ctx *ctx, int32_t *radix, int32_t *digits, int32_t *pairs);
+
 /* First element (0-based) that failed in the last run, or -1. */
 int32_t hp3dg_last_bad_element(const hp3dg_ctx *ctx);
 
