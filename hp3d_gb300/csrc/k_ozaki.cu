@@ -17,8 +17,11 @@
 // split): the result carries ~radix*digits bits.
 //
 // Kernel structure (one CTA per SM, persistent over 128 x 128 output tiles):
-//   warp 0   TMA producer: digit tiles of A = M (128 packed columns x 16 q)
-//            and B = D (128 elements x 16 q), SWIZZLE_32B, 3-stage ring
+//   warp 0   producer: per k-block one contiguous bulk copy (cp.async.bulk)
+//            of the A = M digit tiles (128 packed columns x 16 q each) and one
+//            of the B = D digit tiles (128 elements x 16 q); the digits are
+//            stored in HBM already in the UMMA canonical K-major layout
+//            (8-row x 16-byte core matrices), 4-stage ring
 //   warp 1   TMEM allocation (512 columns) and the single MMA-issuing thread
 //   warps 2-5 epilogue: tcgen05.ld of up to 4 level accumulators, exact
 //            integer recombination, FP64 scaling, coalesced stores of PK
@@ -27,9 +30,7 @@
 #include "hp3dg_internal.cuh"
 #include "hp3dg_kernels.h"
 
-#include <cuda.h>
 #include <cuda_bf16.h>
-#include <dlfcn.h>
 #include <math.h>
 #include <string.h>
 
@@ -63,6 +64,7 @@ struct GemmParams {
   int radix;
   int s1;           // two-pass recombination shift (see epi_chunk)
   int scale_shift;  // radix*last level of pass 0 (+ s1) : final power-of-two shift
+  int digits;
   int nk;        // k-blocks
   int ncb, neb;  // column / element blocks
   int nel, ncols;
@@ -103,12 +105,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile 
   }
   return false;
 }
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, uint32_t mbar,
-                                            int c0, int c1, int c2) {
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
+                                          uint32_t mbar) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
-      "l"((uint64_t)map), "r"(mbar), "r"(c0), "r"(c1), "r"(c2)
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(dst), "l"((uint64_t)src), "r"(bytes), "r"(mbar)
       : "memory");
 }
 __device__ __forceinline__ void tc_fence_before() {
@@ -117,16 +118,16 @@ __device__ __forceinline__ void tc_fence_before() {
 __device__ __forceinline__ void tc_fence_after() {
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-// shared-memory matrix descriptor: K-major, SWIZZLE_32B, 32-byte rows,
-// 8-row groups 256 bytes apart (SBO), LBO unused (1), version 1.
-__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t saddr) {
+// shared-memory matrix descriptor: K-major, no swizzle (canonical interleaved
+// layout): 8-row x 16-byte core matrices, K-direction core matrices 128 bytes
+// apart (LBO), 8-row groups 256 bytes apart (SBO), descriptor version 1.
+__device__ __forceinline__ uint64_t sdesc_kmajor(uint32_t saddr) {
   uint64_t d = 0;
   d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-  d |= (uint64_t)1 << 16;                 // LBO (ignored for swizzled K-major)
+  d |= (uint64_t)(128 >> 4) << 16;        // LBO
   d |= (uint64_t)(256 >> 4) << 32;        // SBO
   d |= (uint64_t)1 << 46;                 // descriptor version
-  d |= (uint64_t)6 << 61;                 // SWIZZLE_32B
-  return d;
+  return d;                               // layout type 0 = no swizzle
 }
 __device__ __forceinline__ void umma_bf16(uint32_t dtmem, uint64_t adesc, uint64_t bdesc,
                                           uint32_t idesc, uint32_t accumulate) {
@@ -246,7 +247,7 @@ __device__ __forceinline__ void epi_chunk(const GemmParams& P, int ps, uint32_t 
 // the GEMM
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_ozaki_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+    k_ozaki_gemm(const uint8_t* __restrict__ Atiles, const uint8_t* __restrict__ Btiles,
                  const GemmParams P, const double* __restrict__ dscale,
                  const double* __restrict__ mscale, double* __restrict__ PK,
                  int* __restrict__ err) {
@@ -283,8 +284,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmA) : "memory");
-      asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&tmB) : "memory");
       int stage = 0;
       uint32_t phase = 0;
       for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
@@ -299,10 +298,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             uint32_t fb = smem_u32(&full_bar[stage]);
             mbar_expect_tx(fb, (uint32_t)(pd.nA + pd.nB) * TILE_BYTES);
             uint8_t* st = ring + (size_t)stage * STAGE_BYTES;
-            for (int i = 0; i < pd.nA; ++i)
-              tma_load_3d(smem_u32(st + i * TILE_BYTES), &tmA, fb, kb * BK, cb * BM, i);
-            for (int j = 0; j < pd.nB; ++j)
-              tma_load_3d(smem_u32(st + (MAXDIG + j) * TILE_BYTES), &tmB, fb, kb * BK, eb * BN, j);
+            // digits 0..nA-1 of (column block, k-block) are contiguous, likewise for B
+            const size_t ablk = ((size_t)cb * P.nk + kb) * P.digits;
+            const size_t bblk = ((size_t)eb * P.nk + kb) * P.digits;
+            bulk_load(smem_u32(st), Atiles + ablk * TILE_BYTES, (uint32_t)pd.nA * TILE_BYTES, fb);
+            bulk_load(smem_u32(st + MAXDIG * TILE_BYTES), Btiles + bblk * TILE_BYTES,
+                      (uint32_t)pd.nB * TILE_BYTES, fb);
             if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
           }
         }
@@ -330,8 +331,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             tc_fence_after();
             uint8_t* st = ring + (size_t)stage * STAGE_BYTES;
             for (int p = pd.pair0; p < pd.pair0 + pd.npair; ++p) {
-              uint64_t ad = sdesc_sw32(smem_u32(st + (P.pi[p] - 1) * TILE_BYTES));
-              uint64_t bd = sdesc_sw32(smem_u32(st + (MAXDIG + P.pj[p] - 1) * TILE_BYTES));
+              uint64_t ad = sdesc_kmajor(smem_u32(st + (P.pi[p] - 1) * TILE_BYTES));
+              uint64_t bd = sdesc_kmajor(smem_u32(st + (MAXDIG + P.pj[p] - 1) * TILE_BYTES));
               uint32_t acc = (kb > 0 || !P.pfirst[p]) ? 1u : 0u;
               umma_bf16(tbase + (uint32_t)P.pslot[p] * BN, ad, bd, idesc, acc);
             }
@@ -386,6 +387,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // ---------------------------------------------------------------------------
 // digit builders
 // ---------------------------------------------------------------------------
+// Digit tiles in HBM: tile (block, k-block, digit) = 128 rows x 16 q in the
+// UMMA canonical K-major layout; byte offset of (row r, q-in-block k):
+//   (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2
+// Tiles of one (block, k-block) are consecutive over the digits.
+__host__ __device__ __forceinline__ size_t tile_base(int blk, int kb, int dig, int nk, int ndig) {
+  return (((size_t)blk * nk + kb) * ndig + dig) * (size_t)TILE_BYTES;
+}
+
 __device__ __forceinline__ double pow2_ceil_scale(double mx) {
   if (!(mx > 0.0)) return 1.0;
   int ex;
@@ -393,17 +402,17 @@ __device__ __forceinline__ double pow2_ceil_scale(double mx) {
   return ldexp(1.0, ex);
 }
 
-__device__ __forceinline__ uint16_t bf16_bits(double d) {
-  __nv_bfloat16 h = __float2bfloat16_rn((float)d);
-  return *(uint16_t*)&h;
+__device__ __forceinline__ uint32_t bf16pair(double lo, double hi) {
+  __nv_bfloat16 a = __float2bfloat16_rn((float)lo), b = __float2bfloat16_rn((float)hi);
+  return (uint32_t)(*(uint16_t*)&a) | ((uint32_t)(*(uint16_t*)&b) << 16);
 }
 
 // M[q, c] for q = (l, comp), c = packed index (pk_index order)
 __device__ __forceinline__ double m_entry(const double* __restrict__ grad, int n, int l, int comp,
                                           int a, int b) {
   const double* g = grad + (size_t)l * 3 * n;
-  const int I[6] = {0, 1, 2, 0, 0, 1}, J[6] = {0, 1, 2, 1, 2, 2};
-  int i = I[comp], j = J[comp];
+  int i = comp < 3 ? comp : (comp == 5 ? 1 : 0);
+  int j = comp < 3 ? comp : (comp == 3 ? 1 : 2);
   double v = g[i * n + a] * g[j * n + b];
   if (i != j) v += g[j * n + a] * g[i * n + b];
   return v;
@@ -431,43 +440,22 @@ __device__ inline void pk_decode(int64_t c, int ni, int nb, int& a, int& b) {
   }
 }
 
-// one block of 128 threads per 128 packed columns; q loop inside
-__global__ void k_build_m(int nint, int n, int ni, int nb, int ncols, int ncols_pad, int kpad,
-                          int radix, int digits, const double* __restrict__ grad,
-                          uint16_t* __restrict__ mdig, double* __restrict__ mscale) {
-  int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// column scales of M: 2^ceil(log2 max_q |M[q,c]|)
+__global__ void k_m_scale(int nint, int n, int ni, int nb, int ncols, int ncols_pad,
+                          const double* __restrict__ grad, double* __restrict__ mscale) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncols_pad) return;
-  const int K = 6 * nint;
-  if (c >= ncols) {
-    for (int s = 0; s < digits; ++s)
-      for (int q = 0; q < kpad; ++q) mdig[((size_t)s * ncols_pad + c) * kpad + q] = 0;
-    mscale[c] = 0.0;
-    return;
-  }
+  if (c >= ncols) { mscale[c] = 1.0; return; }
   int a, b;
   pk_decode(c, ni, nb, a, b);
   double mx = 0.0;
-  for (int q = 0; q < K; ++q) mx = fmax(mx, fabs(m_entry(grad, n, q / 6, q % 6, a, b)));
-  double sc = pow2_ceil_scale(mx);
-  mscale[c] = sc;
-  double rs = 1.0 / sc, up = ldexp(1.0, radix);
-  for (int q = 0; q < kpad; ++q) {
-    double r = (q < K) ? m_entry(grad, n, q / 6, q % 6, a, b) * rs : 0.0;
-    for (int s = 0; s < digits; ++s) {
-      r *= up;
-      double d = rint(r);
-      r -= d;
-      mdig[((size_t)s * ncols_pad + c) * kpad + q] = bf16_bits(d);
-    }
-  }
+  for (int q = 0; q < 6 * nint; ++q) mx = fmax(mx, fabs(m_entry(grad, n, q / 6, q % 6, a, b)));
+  mscale[c] = pow2_ceil_scale(mx);
 }
 
-// one block per element row: scale = 2^ceil(log2 max|D|), digits
-__global__ void k_slice_d(int nint, int kpad, int nel_pad, int radix, int digits,
-                          const double* __restrict__ D, uint16_t* __restrict__ ddig,
-                          double* __restrict__ dscale, int nel) {
+// row scales of D: 2^ceil(log2 max_q |D[e,q]|); one block per element row
+__global__ void k_d_scale(int K, int nel, const double* __restrict__ D, double* __restrict__ dscale) {
   int e = blockIdx.x;
-  const int K = 6 * nint;
   __shared__ double red[256];
   double mx = 0.0;
   if (e < nel)
@@ -478,55 +466,76 @@ __global__ void k_slice_d(int nint, int kpad, int nel_pad, int radix, int digits
     if (threadIdx.x < o) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + o]);
     __syncthreads();
   }
-  double sc = pow2_ceil_scale(red[0]);
-  if (threadIdx.x == 0) dscale[e] = (e < nel) ? sc : 0.0;
-  double rs = 1.0 / sc, up = ldexp(1.0, radix);
-  for (int q = threadIdx.x; q < kpad; q += blockDim.x) {
-    double r = (e < nel && q < K) ? D[(size_t)e * K + q] * rs : 0.0;
-    for (int s = 0; s < digits; ++s) {
-      r *= up;
-      double d = rint(r);
-      r -= d;
-      ddig[((size_t)s * nel_pad + e) * kpad + q] = bf16_bits(d);
+  if (threadIdx.x == 0) dscale[e] = (e < nel) ? pow2_ceil_scale(red[0]) : 1.0;
+}
+
+// digits of 8 consecutive values -> one 16-byte core-matrix row per digit
+__device__ __forceinline__ void write_digits8(const double* vals, double rs, int radix, int digits,
+                                              uint8_t* __restrict__ base, int nk, int blk, int kb,
+                                              int r, int kg) {
+  double up = ldexp(1.0, radix);
+  double rr[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) rr[t] = vals[t] * rs;
+  const size_t off = (size_t)(r >> 3) * 256 + (size_t)kg * 128 + (size_t)(r & 7) * 16;
+  for (int s = 0; s < digits; ++s) {
+    double d[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      rr[t] *= up;
+      d[t] = rint(rr[t]);
+      rr[t] -= d[t];
     }
+    uint4 w;
+    w.x = bf16pair(d[0], d[1]);
+    w.y = bf16pair(d[2], d[3]);
+    w.z = bf16pair(d[4], d[5]);
+    w.w = bf16pair(d[6], d[7]);
+    *(uint4*)(base + tile_base(blk, kb, s, nk, digits) + off) = w;
   }
+}
+
+// M digit tiles: grid (k-blocks, column blocks), 256 threads = 128 rows x 2 q-groups
+__global__ void k_build_m(int nint, int n, int ni, int nb, int ncols, int nk, int radix,
+                          int digits, const double* __restrict__ grad,
+                          const double* __restrict__ mscale, uint8_t* __restrict__ mdig) {
+  const int kb = blockIdx.x, cb = blockIdx.y;
+  const int r = threadIdx.x >> 1, kg = threadIdx.x & 1;
+  const int c = cb * 128 + r;
+  const int K = 6 * nint;
+  double vals[8];
+  int a = 0, b = 0;
+  if (c < ncols) pk_decode(c, ni, nb, a, b);
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    int q = kb * 16 + kg * 8 + t;
+    vals[t] = (c < ncols && q < K) ? m_entry(grad, n, q / 6, q % 6, a, b) : 0.0;
+  }
+  double rs = (c < ncols) ? 1.0 / mscale[c] : 0.0;
+  write_digits8(vals, rs, radix, digits, mdig, nk, cb, kb, r, kg);
+}
+
+// D digit tiles: grid (k-blocks, element blocks), 256 threads
+__global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
+                          const double* __restrict__ D, const double* __restrict__ dscale,
+                          uint8_t* __restrict__ ddig) {
+  const int kb = blockIdx.x, eb = blockIdx.y;
+  const int r = threadIdx.x >> 1, kg = threadIdx.x & 1;
+  const int e = eb * 128 + r;
+  double vals[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    int q = kb * 16 + kg * 8 + t;
+    vals[t] = (e < nel && q < K) ? D[(size_t)e * K + q] : 0.0;
+  }
+  double rs = (e < nel) ? 1.0 / dscale[e] : 0.0;
+  write_digits8(vals, rs, radix, digits, ddig, nk, eb, kb, r, kg);
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 namespace {
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
-                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
-                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn get_encode() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = (EncodeTiledFn)p;
-  }
-  return fn;
-}
-
-int make_map(CUtensorMap* m, const void* base, int kpad, int rows_pad, int digits) {
-  EncodeTiledFn enc = get_encode();
-  if (!enc) return -1;
-  cuuint64_t dims[3] = {(cuuint64_t)kpad, (cuuint64_t)rows_pad, (cuuint64_t)digits};
-  cuuint64_t strides[2] = {(cuuint64_t)kpad * 2, (cuuint64_t)rows_pad * kpad * 2};
-  cuuint32_t box[3] = {BK, 128, 1};
-  cuuint32_t es[3] = {1, 1, 1};
-  CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides,
-                   box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
-                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? 0 : -2;
-}
-
 int round_up(int v, int m) { return (v + m - 1) / m * m; }
 }  // namespace
 
@@ -551,8 +560,10 @@ int launch_ozaki_build_m(const OzakiPlan& p, int nint, int n, int ni, int nb, co
                          uint16_t* d_mdig, double* d_mscale, double* d_work, cudaStream_t st) {
   (void)d_work;
   int ncols = n * (n + 1) / 2;
-  k_build_m<<<p.ncols / 128, 128, 0, st>>>(nint, n, ni, nb, ncols, p.ncols, p.kdim, p.radix,
-                                           p.digits, d_grad, d_mdig, d_mscale);
+  k_m_scale<<<p.ncols / 128, 128, 0, st>>>(nint, n, ni, nb, ncols, p.ncols, d_grad, d_mscale);
+  dim3 g(p.kdim / BK, p.ncols / BM);
+  k_build_m<<<g, 256, 0, st>>>(nint, n, ni, nb, ncols, p.kdim / BK, p.radix, p.digits, d_grad,
+                               d_mscale, (uint8_t*)d_mdig);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -560,8 +571,10 @@ int launch_ozaki_slice_d(const OzakiPlan& p, int nel, int nint, const double* d_
                          uint16_t* d_ddig, double* d_dscale, cudaStream_t st) {
   int nel_pad = round_up(nel, BN);
   if (nel_pad == 0) return 0;
-  k_slice_d<<<nel_pad, 256, 0, st>>>(nint, p.kdim, nel_pad, p.radix, p.digits, d_D, d_ddig,
-                                     d_dscale, nel);
+  k_d_scale<<<nel_pad, 256, 0, st>>>(6 * nint, nel, d_D, d_dscale);
+  dim3 g(p.kdim / BK, nel_pad / BN);
+  k_slice_d<<<g, 256, 0, st>>>(6 * nint, p.kdim / BK, nel, p.radix, p.digits, d_D, d_dscale,
+                               (uint8_t*)d_ddig);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -627,13 +640,11 @@ int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig
   build_params(p, &G);
   int nel_pad = round_up(nel, BN);
   G.nk = p.kdim / BK;
+  G.digits = p.digits;
   G.ncb = p.ncols / BM;
   G.neb = nel_pad / BN;
   G.nel = nel;
   G.ncols = n * (n + 1) / 2;
-  CUtensorMap ta, tb;
-  if (make_map(&ta, d_mdig, p.kdim, p.ncols, p.digits)) return -1;
-  if (make_map(&tb, d_ddig, p.kdim, nel_pad, p.digits)) return -1;
   size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024;
   static bool attr = false;
   if (!attr) {
@@ -644,7 +655,8 @@ int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig
   }
   int ntiles = G.ncb * G.neb;
   int grid = ntiles < num_sms ? ntiles : num_sms;
-  k_ozaki_gemm<<<grid, NTHREADS, smem, st>>>(ta, tb, G, d_dscale, d_mscale, d_PK, d_flag);
+  k_ozaki_gemm<<<grid, NTHREADS, smem, st>>>((const uint8_t*)d_mdig, (const uint8_t*)d_ddig, G,
+                                              d_dscale, d_mscale, d_PK, d_flag);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
