@@ -167,6 +167,37 @@ int hp3dg_phase_times(const hp3dg_ctx *ctx, float *ms, int32_t n);
  * Returns HP3DG_ERR_STATE before a mixed-precision submit. */
 int hp3dg_mixed_config(const hp3dg_ctx *ctx, int32_t *radix, int32_t *digits, int32_t *pairs);
 
+/* Size of the fixed device scratch array used by hp3dg_condense_noalloc:
+ * 2^20 doubles (8 MiB), resident on every GPU that loads the library. */
+#define HP3DG_NOALLOC_SCRATCH_DOUBLES (1 << 20)
+
+/* Static condensation of caller-supplied dense element matrices, with no
+ * allocation of any kind.  This entry point has no counterpart in the
+ * reference: it exists for callers that cannot allocate device memory (an
+ * element loop inside an OpenMP region of a host solver, where cudaMalloc
+ * would serialise the threads and synchronise the device; applications
+ * whose device memory belongs to their own pool or to a solver sharing the
+ * GPU).  All pointers are device pointers supplied by the caller:
+ *   K      n_elem x (n x n) column-major element matrices, interface dof
+ *          first and the nb bubble dof last (the order of stc_fwd_wrapper)
+ *   b      n_elem x n loads
+ *   aii    n_elem x (ni x ni) column-major condensed matrices, ni = n - nb
+ *   bi     n_elem x ni condensed loads
+ *   aschur n_elem x (nb x ni) column-major inv(Abb) Abi
+ *   bschur n_elem x nb inv(Abb) Bb
+ * Scratch: the packed Schur triangles, n_elem * ni*(ni+1)/2 doubles, live in
+ * a fixed device array of HP3DG_NOALLOC_SCRATCH_DOUBLES - 1 usable doubles;
+ * larger batches are rejected with HP3DG_ERR_ARG (split them).  Calls share
+ * that array: calls whose kernels overlap on the GPU race and must be
+ * ordered by the caller.  The first call on a device looks up the array's
+ * device address; make it before any stream capture begins.  The call waits
+ * for its kernel on `stream` (NULL = legacy default stream) and returns
+ * HP3DG_ERR_NOT_SPD with *bad_element set when a bubble block is not
+ * positive definite. */
+int hp3dg_condense_noalloc(int32_t n_elem, int32_t n, int32_t nb, const double *K,
+                           const double *b, double *aii, double *bi, double *aschur,
+                           double *bschur, int32_t *bad_element, void *stream);
+
 /* First element (0-based) that failed in the last run, or -1. */
 int32_t hp3dg_last_bad_element(const hp3dg_ctx *ctx);
 
