@@ -44,6 +44,9 @@ constexpr int MAXDIG = 7;
 constexpr int MAXPASS = 4;
 constexpr int MAXPAIR = 40;
 constexpr int NSTAGE = 4;
+#ifndef KGROUP
+#define KGROUP 2  // k-blocks per accumulator run (NSTAGE / KGROUP groups in flight)
+#endif
 constexpr int TILE_BYTES = BM * BK * 2;  // 4096, A and B tiles have the same size
 constexpr int STAGE_BYTES = 2 * MAXDIG * TILE_BYTES;  // room for all digits
 constexpr int NTHREADS = 192;
@@ -324,20 +327,40 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           accph ^= 1;
           tc_fence_after();
-          for (int kb = 0; kb < P.nk; ++kb) {
-            if (!mbar_wait(smem_u32(&full_bar[stage]), phase, &abort_)) {
-              abort_ = 1; atomicExch(err, 3); break;
+          // k-blocks are consumed in groups of KGROUP stages so that each level
+          // accumulator receives a run of (pairs of the level) x KGROUP MMAs:
+          // switching the accumulator between MMAs stalls the tensor pipe.
+          for (int kb0 = 0; kb0 < P.nk && !abort_; kb0 += KGROUP) {
+            const int ng = (P.nk - kb0) < KGROUP ? (P.nk - kb0) : KGROUP;
+            uint32_t sbase[KGROUP];
+            for (int g = 0; g < ng; ++g) {
+              int sg = stage + g;
+              uint32_t pg = phase;
+              if (sg >= NSTAGE) { sg -= NSTAGE; pg ^= 1; }
+              if (!mbar_wait(smem_u32(&full_bar[sg]), pg, &abort_)) {
+                abort_ = 1; atomicExch(err, 3); break;
+              }
+              sbase[g] = smem_u32(ring + (size_t)sg * STAGE_BYTES);
             }
+            if (abort_) break;
             tc_fence_after();
-            uint8_t* st = ring + (size_t)stage * STAGE_BYTES;
             for (int p = pd.pair0; p < pd.pair0 + pd.npair; ++p) {
-              uint64_t ad = sdesc_kmajor(smem_u32(st + (P.pi[p] - 1) * TILE_BYTES));
-              uint64_t bd = sdesc_kmajor(smem_u32(st + (MAXDIG + P.pj[p] - 1) * TILE_BYTES));
-              uint32_t acc = (kb > 0 || !P.pfirst[p]) ? 1u : 0u;
-              umma_bf16(tbase + (uint32_t)P.pslot[p] * BN, ad, bd, idesc, acc);
+              const uint32_t aoff = (uint32_t)(P.pi[p] - 1) * TILE_BYTES;
+              const uint32_t boff = (uint32_t)(MAXDIG + P.pj[p] - 1) * TILE_BYTES;
+              const uint32_t dt = tbase + (uint32_t)P.pslot[p] * BN;
+              for (int g = 0; g < ng; ++g) {
+                uint32_t acc = (kb0 + g > 0 || !P.pfirst[p]) ? 1u : 0u;
+                umma_bf16(dt, sdesc_kmajor(sbase[g] + aoff), sdesc_kmajor(sbase[g] + boff), idesc,
+                          acc);
+              }
             }
-            umma_commit(smem_u32(&empty_bar[stage]));  // frees the stage when done
-            if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+            for (int g = 0; g < ng; ++g) {
+              int sg = stage + g;
+              if (sg >= NSTAGE) sg -= NSTAGE;
+              umma_commit(smem_u32(&empty_bar[sg]));  // frees the stage when done
+            }
+            stage += ng;
+            if (stage >= NSTAGE) { stage -= NSTAGE; phase ^= 1; }
           }
           umma_commit(smem_u32(&acc_full));  // accumulators complete
         }
