@@ -298,7 +298,9 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(mesh, args.isol, args.integration, seconds=args.cpu_seconds)
 
-    launches_per_step = 10 if prec == H.FP64 else 11
+    # kernels per pass: orient, geom, load, contraction (+ d_scale, slice_d when mixed),
+    # condense, and 7 index-map kernels
+    launches_per_step = 12 if prec == H.FP64 else 14
     line = {"metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
