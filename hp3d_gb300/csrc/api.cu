@@ -113,6 +113,11 @@ struct Bin {
   double *d_D = nullptr, *d_F = nullptr, *d_b0 = nullptr, *d_PK = nullptr, *d_S = nullptr;
   uint32_t* d_perm = nullptr;
   uint8_t* d_dmask = nullptr;
+  // error-evaluation tables (INTEGRATION = 2 rule)
+  bool etable = false;
+  int nint_err = 0;
+  std::vector<double> xi_err, wq_err;
+  double *d_xi_err = nullptr, *d_wq_err = nullptr, *d_shap_err = nullptr, *d_grad_err = nullptr;
   // mixed precision
   bool mtable = false;
   OzakiPlan plan{};
@@ -154,6 +159,12 @@ struct hp3dg_ctx {
   int64_t h_nrdof = 0;
   size_t pk_total = 0, b0_total = 0;
   std::vector<int64_t> pk_off, b0_off;  // per element, into h_PK / h_b0 when keep_elem
+  // after the solve
+  std::vector<int64_t> dof_off;
+  int64_t *d_dof_off = nullptr;
+  double *d_dofs = nullptr, *d_xglob = nullptr, *h_dofs = nullptr;
+  double *d_err2 = nullptr, *d_nrm2 = nullptr, *d_djdk = nullptr, *d_djdx = nullptr;
+  bool have_dofs = false;
   cudaEvent_t ev[8] = {};
   float times[6] = {0, 0, 0, 0, 0, 0};
 };
@@ -165,6 +176,7 @@ void free_bin(Bin& b) {
   cudaFree(b.d_D); cudaFree(b.d_F); cudaFree(b.d_b0); cudaFree(b.d_PK); cudaFree(b.d_S);
   cudaFree(b.d_perm); cudaFree(b.d_dmask); cudaFree(b.d_mdig); cudaFree(b.d_ddig);
   cudaFree(b.d_mscale); cudaFree(b.d_dscale);
+  cudaFree(b.d_xi_err); cudaFree(b.d_wq_err); cudaFree(b.d_shap_err); cudaFree(b.d_grad_err);
   b = Bin();
 }
 
@@ -175,8 +187,14 @@ void free_batch(hp3dg_ctx* c) {
                  c->d_xvert, c->d_kappa, c->d_zdofd, c->d_elem_nnz, c->d_lcon_off,
                  c->d_schur_off, c->d_bub_off, c->d_zd_off, c->d_zastif, c->d_zbload,
                  c->d_aschur, c->d_bschur, c->d_lcon, c->d_nfirst, c->d_first, c->d_cnt,
-                 c->d_scan, c->d_blk, c->d_total};
+                 c->d_scan, c->d_blk, c->d_total, c->d_dof_off, c->d_dofs, c->d_xglob,
+                 c->d_err2, c->d_nrm2, c->d_djdk, c->d_djdx};
   for (void* p : dev) cudaFree(p);
+  cudaFreeHost(c->h_dofs);
+  c->h_dofs = nullptr;
+  c->d_dof_off = nullptr; c->d_dofs = c->d_xglob = nullptr;
+  c->d_err2 = c->d_nrm2 = c->d_djdk = c->d_djdx = nullptr;
+  c->have_dofs = false;
   void* host[] = {c->h_zastif, c->h_zbload, c->h_aschur, c->h_bschur, c->h_lcon, c->h_nfirst,
                   c->h_PK, c->h_b0};
   for (void* p : host) cudaFreeHost(p);
@@ -324,6 +342,8 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
     c->bub_off[e + 1] = c->bub_off[e] + c->nb_e[e];
     c->zd_off[e + 1] = c->zd_off[e] + ni;
   }
+  c->dof_off.assign(nel + 1, 0);
+  for (int e = 0; e < nel; ++e) c->dof_off[e + 1] = c->dof_off[e] + c->n_e[e];
   int err = 0;
   // ---- device inputs ----
   c->d_norder = dalloc<int>(norder.size(), &err);
@@ -339,6 +359,7 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   c->d_schur_off = dalloc<int64_t>(nel + 1, &err);
   c->d_bub_off = dalloc<int64_t>(nel + 1, &err);
   c->d_zd_off = dalloc<int64_t>(nel + 1, &err);
+  c->d_dof_off = dalloc<int64_t>(nel + 1, &err);
   c->have_zdofd = zdofd != nullptr;
   if (zdofd) c->d_zdofd = dalloc<double>(c->zd_off[nel], &err);
   // ---- outputs ----
@@ -376,6 +397,7 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   CK(cudaMemcpyAsync(c->d_schur_off, c->schur_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->d_bub_off, c->bub_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->d_zd_off, c->zd_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(c->d_dof_off, c->dof_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
   if (zdofd)
     CK(cudaMemcpyAsync(c->d_zdofd, zdofd, c->zd_off[nel] * 8, cudaMemcpyHostToDevice, st));
   // ---- per-bin buffers ----
@@ -617,6 +639,99 @@ int hp3dg_index_map(const hp3dg_ctx* c, int32_t* nfirst_dof, int64_t* elem_nnz,
   if (lcon) std::memcpy(lcon, c->h_lcon, c->lcon_off[c->nel] * 4);
   if (nrdof) *nrdof = c->h_nrdof;
   return HP3DG_OK;
+}
+
+int hp3dg_backsub(hp3dg_ctx* c, const double* x_global) {
+  if (!c || !x_global) return HP3DG_ERR_ARG;
+  if (!c->ran) return HP3DG_ERR_STATE;
+  cudaSetDevice(c->device);
+  int rc = hp3dg_batch_sync(c);
+  if (rc != HP3DG_OK) return rc;
+  cudaStream_t st = c->stream;
+  int err = 0;
+  // nrdof is known after the index maps ran
+  int64_t nrdof = 0;
+  CK(cudaMemcpy(&nrdof, c->d_total, 8, cudaMemcpyDeviceToHost));
+  if (!c->d_xglob) c->d_xglob = dalloc<double>(nrdof > 0 ? nrdof : 1, &err);
+  if (!c->d_dofs) c->d_dofs = dalloc<double>(c->dof_off[c->nel], &err);
+  if (err) return err;
+  if (!c->h_dofs && cudaMallocHost((void**)&c->h_dofs, c->dof_off[c->nel] * 8 + 8) != cudaSuccess)
+    return HP3DG_ERR_ALLOC;
+  CK(cudaMemcpyAsync(c->d_xglob, x_global, nrdof * 8, cudaMemcpyHostToDevice, st));
+  for (auto& B : c->bins)
+    launch_backsub((int)B.elems.size(), B.ni, B.nb, B.d_elist, c->d_nextract, c->d_lcon_off,
+                   c->d_lcon, c->d_xglob, c->d_zd_off, c->have_zdofd ? c->d_zdofd : nullptr,
+                   c->d_schur_off, c->d_bub_off, c->d_aschur, c->d_bschur, c->d_dof_off,
+                   c->d_dofs, st);
+  CK(cudaMemcpyAsync(c->h_dofs, c->d_dofs, c->dof_off[c->nel] * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  if (cudaPeekAtLastError() != cudaSuccess) return HP3DG_ERR_CUDA;
+  c->have_dofs = true;
+  return HP3DG_OK;
+}
+
+int hp3dg_get_dofs(const hp3dg_ctx* c, int32_t iel, double* dof, int32_t* n) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->have_dofs) return HP3DG_ERR_STATE;
+  if (iel < 0 || iel >= c->nel) return HP3DG_ERR_ARG;
+  if (n) *n = c->n_e[iel];
+  if (dof) std::memcpy(dof, c->h_dofs + c->dof_off[iel], c->n_e[iel] * 8);
+  return HP3DG_OK;
+}
+
+int hp3dg_element_error(hp3dg_ctx* c, int32_t isol, double* err2, double* nrm2) {
+  if (!c || !err2 || !nrm2) return HP3DG_ERR_ARG;
+  if (!c->have_dofs) return HP3DG_ERR_STATE;
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  int err = 0;
+  if (!c->d_err2) c->d_err2 = dalloc<double>(c->nel, &err);
+  if (!c->d_nrm2) c->d_nrm2 = dalloc<double>(c->nel, &err);
+  if (err) return err;
+  for (auto& B : c->bins) {
+    if (!B.etable) {
+      B.nint_err = hexa_quadrature(B.nord_loc, 2, B.xi_err, B.wq_err);
+      B.d_xi_err = dalloc<double>(B.xi_err.size(), &err);
+      B.d_wq_err = dalloc<double>(B.wq_err.size(), &err);
+      B.d_shap_err = dalloc<double>((size_t)B.nint_err * B.n, &err);
+      B.d_grad_err = dalloc<double>((size_t)B.nint_err * 3 * B.n, &err);
+      if (err) return err;
+      CK(cudaMemcpyAsync(B.d_xi_err, B.xi_err.data(), B.xi_err.size() * 8, cudaMemcpyHostToDevice, st));
+      CK(cudaMemcpyAsync(B.d_wq_err, B.wq_err.data(), B.wq_err.size() * 8, cudaMemcpyHostToDevice, st));
+      launch_tables_hexa(B.nord_loc, B.nint_err, B.n, B.d_xi_err, B.d_shap_err, B.d_grad_err, st);
+      CK(cudaStreamSynchronize(st));
+      B.etable = true;
+    }
+    launch_element_error((int)B.elems.size(), B.nint_err, B.n, isol, B.d_elist, B.d_wq_err,
+                         B.d_shap_err, B.d_grad_err, c->d_xvert, B.d_perm, c->d_dof_off, c->d_dofs,
+                         c->d_err2, c->d_nrm2, st);
+  }
+  CK(cudaMemcpyAsync(err2, c->d_err2, (size_t)c->nel * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(nrm2, c->d_nrm2, (size_t)c->nel * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return cudaPeekAtLastError() == cudaSuccess ? HP3DG_OK : HP3DG_ERR_CUDA;
+}
+
+int hp3dg_adjoint(hp3dg_ctx* c, const double* dofs, double* djdkappa, double* djdx) {
+  if (!c || !djdkappa || !djdx) return HP3DG_ERR_ARG;
+  if (!c->ran) return HP3DG_ERR_STATE;
+  if (!dofs && !c->have_dofs) return HP3DG_ERR_STATE;
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  int err = 0;
+  if (!c->d_dofs) c->d_dofs = dalloc<double>(c->dof_off[c->nel], &err);
+  if (!c->d_djdk) c->d_djdk = dalloc<double>(c->nel, &err);
+  if (!c->d_djdx) c->d_djdx = dalloc<double>((size_t)c->nel * 24, &err);
+  if (err) return err;
+  if (dofs) CK(cudaMemcpyAsync(c->d_dofs, dofs, c->dof_off[c->nel] * 8, cudaMemcpyHostToDevice, st));
+  for (auto& B : c->bins)
+    launch_adjoint((int)B.elems.size(), B.nint, B.n, c->opts.isol, B.d_elist, B.d_wq, B.d_shap,
+                   B.d_grad, c->d_xvert, c->d_kappa, B.d_perm, c->d_dof_off, c->d_dofs, c->d_djdk,
+                   c->d_djdx, st);
+  CK(cudaMemcpyAsync(djdkappa, c->d_djdk, (size_t)c->nel * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(djdx, c->d_djdx, (size_t)c->nel * 24 * 8, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return cudaPeekAtLastError() == cudaSuccess ? HP3DG_OK : HP3DG_ERR_CUDA;
 }
 
 int hp3dg_output_sizes(const hp3dg_ctx* c, int64_t* nnz, int64_t* lcon, int64_t* schur,

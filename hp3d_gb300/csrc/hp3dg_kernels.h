@@ -30,6 +30,21 @@ int launch_index_maps(int nel, int nnode, int nnodes_global, const int* d_nodes,
                       int64_t* d_blk, int64_t* d_total, int* d_nfirst, int* d_lcon,
                       cudaStream_t st);
 
+// after the solve -- k_post.cu
+void launch_backsub(int nel, int ni, int nb, const int* d_elist, const int* d_nextract,
+                    const int64_t* d_lcon_off, const int* d_lcon, const double* d_x,
+                    const int64_t* d_zd_off, const double* d_zdofd, const int64_t* d_schur_off,
+                    const int64_t* d_bub_off, const double* d_aschur, const double* d_bschur,
+                    const int64_t* d_dof_off, double* d_dofs, cudaStream_t st);
+void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+                          const double* d_shap, const double* d_grad, const double* d_xvert,
+                          const uint32_t* d_perm, const int64_t* d_dof_off, const double* d_dofs,
+                          double* d_err2, double* d_nrm2, cudaStream_t st);
+void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+                    const double* d_shap, const double* d_grad, const double* d_xvert,
+                    const double* d_kappa, const uint32_t* d_perm, const int64_t* d_dof_off,
+                    const double* d_dofs, double* d_djdk, double* d_djdx, cudaStream_t st);
+
 // mixed precision (split-BF16 digits on tcgen05) -- k_ozaki.cu
 struct OzakiPlan {
   int radix;      // bits per digit

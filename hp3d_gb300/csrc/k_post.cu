@@ -1,0 +1,302 @@
+// k_post.cu -- kernels that run after the global solve (sm_103a).
+//
+//   k_backsub        interface solution -> element dof: xi from the global
+//                    vector through LCON/NEXTRACT (Dirichlet dof from the
+//                    submitted data), bubbles xb = BSchur - ASchur xi
+//                    (modules/stc.F90:529-679 stc_bwd_wrapper / stc_bwd,
+//                    solver/frontal/interf/solout.F90:457)
+//   k_element_error  squared H1 error and norm per element against the
+//                    manufactured solution (element/util/compute_error.F90:
+//                    226-360, H1 branch, INTEGRATION = 2 rule)
+//   k_adjoint        compliance sensitivities: dJ/dkappa_e and dJ/dx of the
+//                    element's vertices (differentiation)
+#include "hp3dg_internal.cuh"
+#include "hp3dg_kernels.h"
+
+#include <math.h>
+
+namespace hp3dg {
+
+// one block per element
+__global__ void k_backsub(int ni, int nb, const int* __restrict__ elist,
+                          const int* __restrict__ nextract, const int64_t* __restrict__ lcon_off,
+                          const int* __restrict__ lcon, const double* __restrict__ xglob,
+                          const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
+                          const int64_t* __restrict__ schur_off, const int64_t* __restrict__ bub_off,
+                          const double* __restrict__ aschur, const double* __restrict__ bschur,
+                          const int64_t* __restrict__ dof_off, double* __restrict__ dofs) {
+  extern __shared__ double xi[];
+  const int j = blockIdx.x, e = elist[j];
+  const int n = ni + nb;
+  double* out = dofs + dof_off[e];
+  // Dirichlet (or zero) values first, then the active dof from the solution
+  for (int k = threadIdx.x; k < ni; k += blockDim.x) xi[k] = zdofd ? zdofd[zd_off[e] + k] : 0.0;
+  __syncthreads();
+  const int64_t lo = lcon_off[e];
+  const int nc = (int)(lcon_off[e + 1] - lo);
+  for (int l = threadIdx.x; l < nc; l += blockDim.x) xi[nextract[lo + l]] = xglob[lcon[lo + l] - 1];
+  __syncthreads();
+  for (int k = threadIdx.x; k < ni; k += blockDim.x) out[k] = xi[k];
+  const double* A = aschur + schur_off[e];  // nb x ni column-major
+  const double* B = bschur + bub_off[e];
+  for (int r = threadIdx.x; r < nb; r += blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < ni; ++k) s += A[(size_t)k * nb + r] * xi[k];
+    out[ni + r] = B[r] - s;
+  }
+  (void)n;
+}
+
+void launch_backsub(int nel, int ni, int nb, const int* d_elist, const int* d_nextract,
+                    const int64_t* d_lcon_off, const int* d_lcon, const double* d_x,
+                    const int64_t* d_zd_off, const double* d_zdofd, const int64_t* d_schur_off,
+                    const int64_t* d_bub_off, const double* d_aschur, const double* d_bschur,
+                    const int64_t* d_dof_off, double* d_dofs, cudaStream_t st) {
+  if (nel <= 0) return;
+  k_backsub<<<nel, 128, ni * sizeof(double), st>>>(ni, nb, d_elist, d_nextract, d_lcon_off, d_lcon,
+                                                   d_x, d_zd_off, d_zdofd, d_schur_off, d_bub_off,
+                                                   d_aschur, d_bschur, d_dof_off, d_dofs);
+}
+
+// manufactured solutions (common/solution.F90:45-134, plus 10 and 12)
+__device__ inline void exact_dev(int isol, const double* X, double& u, double* g) {
+  const double PI = 3.141592653589793238462643383279502884;
+  double x1 = X[0], x2 = X[1], x3 = X[2];
+  u = 0.0; g[0] = g[1] = g[2] = 0.0;
+  switch (isol) {
+    case 0: {
+      double fx = pow(x1, 6.0), fy = pow(x2, 6.0), fz = pow(x3, 6.0);
+      u = fx * fy * fz;
+      g[0] = 6.0 * pow(x1, 5.0) * fy * fz; g[1] = fx * 6.0 * pow(x2, 5.0) * fz;
+      g[2] = fx * fy * 6.0 * pow(x3, 5.0);
+      break;
+    }
+    case 1:
+      u = sin(x1 * PI) * sinh(x2 * PI);
+      g[0] = PI * cos(x1 * PI) * sinh(x2 * PI); g[1] = PI * sin(x1 * PI) * cosh(x2 * PI);
+      break;
+    case 2:
+      u = sin(x1 * PI) * sinh(x2 * PI) * (x3 * x3);
+      g[0] = PI * cos(x1 * PI) * sinh(x2 * PI) * (x3 * x3);
+      g[1] = PI * sin(x1 * PI) * cosh(x2 * PI) * (x3 * x3);
+      g[2] = 2.0 * sin(x1 * PI) * sinh(x2 * PI) * x3;
+      break;
+    case 10: {
+      double s1 = sin(PI * x1), s2 = sin(PI * x2), s3 = sin(PI * x3);
+      u = s1 * s2 * s3;
+      g[0] = PI * cos(PI * x1) * s2 * s3; g[1] = PI * s1 * cos(PI * x2) * s3;
+      g[2] = PI * s1 * s2 * cos(PI * x3);
+      break;
+    }
+    case 12:
+      u = x1 * x2 * x3; g[0] = x2 * x3; g[1] = x1 * x3; g[2] = x1 * x2;
+      break;
+    default: break;
+  }
+}
+
+// geometry at point l from the 8 vertex functions of the bin's tables
+__device__ inline double geom_point(const double* xv, const double* ts, const double* tg, int n,
+                                    double* X, double a[3][3]) {
+  double dx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  X[0] = X[1] = X[2] = 0.0;
+  for (int v = 0; v < 8; ++v) {
+    double s = ts[v], g0 = tg[v], g1 = tg[n + v], g2 = tg[2 * n + v];
+    for (int i = 0; i < 3; ++i) {
+      double xi_ = xv[3 * v + i];
+      X[i] += xi_ * s; dx[i][0] += xi_ * g0; dx[i][1] += xi_ * g1; dx[i][2] += xi_ * g2;
+    }
+  }
+  double r = dx[0][0] * dx[1][1] * dx[2][2] + dx[1][0] * dx[2][1] * dx[0][2] +
+             dx[2][0] * dx[0][1] * dx[1][2] - dx[2][0] * dx[1][1] * dx[0][2] -
+             dx[0][0] * dx[2][1] * dx[1][2] - dx[1][0] * dx[0][1] * dx[2][2];
+  double ir = 1.0 / r;
+  a[0][0] = (dx[1][1] * dx[2][2] - dx[2][1] * dx[1][2]) * ir;
+  a[1][0] = (-dx[1][0] * dx[2][2] + dx[2][0] * dx[1][2]) * ir;
+  a[2][0] = (dx[1][0] * dx[2][1] - dx[2][0] * dx[1][1]) * ir;
+  a[0][1] = (dx[2][1] * dx[0][2] - dx[0][1] * dx[2][2]) * ir;
+  a[1][1] = (dx[0][0] * dx[2][2] - dx[2][0] * dx[0][2]) * ir;
+  a[2][1] = (-dx[0][0] * dx[2][1] + dx[2][0] * dx[0][1]) * ir;
+  a[0][2] = (dx[0][1] * dx[1][2] - dx[1][1] * dx[0][2]) * ir;
+  a[1][2] = (-dx[0][0] * dx[1][2] + dx[1][0] * dx[0][2]) * ir;
+  a[2][2] = (dx[0][0] * dx[1][1] - dx[1][0] * dx[0][1]) * ir;
+  return r;
+}
+
+// Element dof in the bin's reference enumeration: dref[pi(a)] = sign_a dof_a
+__device__ inline void to_reference(const double* dof, const uint32_t* pm, int n, double* dref) {
+  for (int a = threadIdx.x; a < n; a += blockDim.x) {
+    uint32_t m = pm[a];
+    double v = dof[a];
+    dref[m & 0x7fffffffu] = (m & 0x80000000u) ? -v : v;
+  }
+}
+
+// one block per element, one warp per point (lanes split the dof sum)
+__global__ void k_element_error(int nint, int n, int isol, const int* __restrict__ elist,
+                                const double* __restrict__ wq, const double* __restrict__ ts,
+                                const double* __restrict__ tg, const double* __restrict__ xvert,
+                                const uint32_t* __restrict__ perm, const int64_t* __restrict__ dof_off,
+                                const double* __restrict__ dofs, double* __restrict__ err2,
+                                double* __restrict__ nrm2) {
+  extern __shared__ double dref[];
+  __shared__ double xv[24];
+  __shared__ double red[2][32];
+  const int j = blockIdx.x, e = elist[j];
+  if (threadIdx.x < 24) xv[threadIdx.x] = xvert[(size_t)e * 24 + threadIdx.x];
+  to_reference(dofs + dof_off[e], perm + (size_t)j * n, n, dref);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  double e2 = 0.0, r2 = 0.0;
+  for (int l = warp; l < nint; l += nw) {
+    const double* s = ts + (size_t)l * n;
+    const double* g = tg + (size_t)l * 3 * n;
+    double u = 0.0, gu[3] = {0, 0, 0};
+    for (int r = lane; r < n; r += 32) {
+      double d = dref[r];
+      u += d * s[r]; gu[0] += d * g[r]; gu[1] += d * g[n + r]; gu[2] += d * g[2 * n + r];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      u += __shfl_xor_sync(0xffffffffu, u, o);
+      for (int c = 0; c < 3; ++c) gu[c] += __shfl_xor_sync(0xffffffffu, gu[c], o);
+    }
+    if (lane == 0) {
+      double X[3], a[3][3];
+      double rjac = geom_point(xv, s, g, n, X, a);
+      double gx[3];
+      for (int c = 0; c < 3; ++c) gx[c] = gu[0] * a[0][c] + gu[1] * a[1][c] + gu[2] * a[2][c];
+      double ue, ge[3];
+      exact_dev(isol, X, ue, ge);
+      double w = wq[l] * rjac;
+      for (int c = 0; c < 3; ++c) { e2 += (ge[c] - gx[c]) * (ge[c] - gx[c]) * w; r2 += ge[c] * ge[c] * w; }
+      e2 += (ue - u) * (ue - u) * w;
+      r2 += ue * ue * w;
+    }
+  }
+  if (lane == 0) { red[0][warp] = e2; red[1][warp] = r2; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < nw; ++w) { a += red[0][w]; b += red[1][w]; }
+    err2[e] = a;
+    nrm2[e] = b;
+  }
+}
+
+void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+                          const double* d_shap, const double* d_grad, const double* d_xvert,
+                          const uint32_t* d_perm, const int64_t* d_dof_off, const double* d_dofs,
+                          double* d_err2, double* d_nrm2, cudaStream_t st) {
+  if (nel <= 0) return;
+  k_element_error<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_wq, d_shap, d_grad,
+                                                        d_xvert, d_perm, d_dof_off, d_dofs, d_err2,
+                                                        d_nrm2);
+}
+
+// ---------------------------------------------------------------------------
+// adjoint: compliance J = b^T u (K u = b, lambda = u)
+//   dJ/dkappa_e = -u_e^T (K_e / kappa_e) u_e
+//   dJ/dX_{v,k} = -u_e^T (dK_e/dX_{v,k}) u_e + 2 u_e^T (db_e/dX_{v,k})
+// per point: e = kappa w detJ |J^-T g|^2 with g = G_l u_e (reference
+// gradient), v = J^-T g, q = J^-1 v:
+//   de/dJ_{ij} = kappa w detJ ( (J^-1)_{ji} |v|^2 - 2 v_i q_j )
+// load: b = sum_l phi f(x_l) w detJ; with u_h(l) = phi_l . u_e:
+//   d(u_h f w detJ)/dJ_{ij} = u_h w ( f detJ (J^-1)_{ji} ) + u_h w detJ (df/dx_i) phi_v-part
+// J_{ij} = sum_v X_{v,i} dphi_v/dxi_j, x_i = sum_v X_{v,i} phi_v.
+// ---------------------------------------------------------------------------
+__device__ inline void source_grad(int isol, const double* X, double& f, double* df) {
+  const double PI = 3.141592653589793238462643383279502884;
+  df[0] = df[1] = df[2] = 0.0;
+  switch (isol) {
+    case 10: {
+      double s1 = sin(PI * X[0]), s2 = sin(PI * X[1]), s3 = sin(PI * X[2]);
+      double c = 3.0 * PI * PI;
+      f = c * s1 * s2 * s3;
+      df[0] = c * PI * cos(PI * X[0]) * s2 * s3;
+      df[1] = c * PI * s1 * cos(PI * X[1]) * s3;
+      df[2] = c * PI * s1 * s2 * cos(PI * X[2]);
+      break;
+    }
+    case 11: f = 1.0; break;
+    default: f = 0.0; break;
+  }
+}
+
+__global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ elist,
+                          const double* __restrict__ wq, const double* __restrict__ ts,
+                          const double* __restrict__ tg, const double* __restrict__ xvert,
+                          const double* __restrict__ kappa, const uint32_t* __restrict__ perm,
+                          const int64_t* __restrict__ dof_off, const double* __restrict__ dofs,
+                          double* __restrict__ djdk, double* __restrict__ djdx) {
+  extern __shared__ double dref[];
+  __shared__ double xv[24];
+  __shared__ double red[8][25];
+  const int j = blockIdx.x, e = elist[j];
+  if (threadIdx.x < 24) xv[threadIdx.x] = xvert[(size_t)e * 24 + threadIdx.x];
+  to_reference(dofs + dof_off[e], perm + (size_t)j * n, n, dref);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const double kap = kappa[e];
+  double acc[25];  // [0] energy/kappa, [1..24] dJ/dX
+  for (int i = 0; i < 25; ++i) acc[i] = 0.0;
+  for (int l = warp; l < nint; l += nw) {
+    const double* s = ts + (size_t)l * n;
+    const double* g = tg + (size_t)l * 3 * n;
+    double u = 0.0, gu[3] = {0, 0, 0};
+    for (int r = lane; r < n; r += 32) {
+      double d = dref[r];
+      u += d * s[r]; gu[0] += d * g[r]; gu[1] += d * g[n + r]; gu[2] += d * g[2 * n + r];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      u += __shfl_xor_sync(0xffffffffu, u, o);
+      for (int c = 0; c < 3; ++c) gu[c] += __shfl_xor_sync(0xffffffffu, gu[c], o);
+    }
+    if (lane == 0) {
+      double X[3], a[3][3];  // a = J^-1: a[i][k] = dxi_i/dx_k
+      double det = geom_point(xv, s, g, n, X, a);
+      double w = wq[l];
+      double v[3], q[3];
+      for (int c = 0; c < 3; ++c) v[c] = gu[0] * a[0][c] + gu[1] * a[1][c] + gu[2] * a[2][c];
+      for (int c = 0; c < 3; ++c) q[c] = a[c][0] * v[0] + a[c][1] * v[1] + a[c][2] * v[2];
+      double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+      acc[0] += w * det * vv;  // energy density without kappa
+      double f, df[3];
+      source_grad(isol, X, f, df);
+      // dJ/dJ_{ik} (matrix T): stiffness part (with the minus sign) + load part
+      double T[3][3];
+      for (int i = 0; i < 3; ++i)
+        for (int k = 0; k < 3; ++k)
+          T[i][k] = -kap * w * det * (a[k][i] * vv - 2.0 * v[i] * q[k]) +
+                    2.0 * u * w * f * det * a[k][i];
+      for (int vtx = 0; vtx < 8; ++vtx) {
+        double gv[3] = {g[vtx], g[n + vtx], g[2 * n + vtx]};
+        for (int i = 0; i < 3; ++i) {
+          double t = T[i][0] * gv[0] + T[i][1] * gv[1] + T[i][2] * gv[2];
+          t += 2.0 * u * w * det * df[i] * s[vtx];  // d f(x_l) / d X_{vtx,i}
+          acc[1 + 3 * vtx + i] += t;
+        }
+      }
+    }
+  }
+  if (lane == 0)
+    for (int i = 0; i < 25; ++i) red[warp][i] = acc[i];
+  __syncthreads();
+  if (threadIdx.x < 25) {
+    double sum = 0.0;
+    for (int w = 0; w < nw; ++w) sum += red[w][threadIdx.x];
+    if (threadIdx.x == 0) djdk[e] = -sum;  // -u^T (K/kappa) u
+    else djdx[(size_t)e * 24 + threadIdx.x - 1] = sum;
+  }
+}
+
+void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+                    const double* d_shap, const double* d_grad, const double* d_xvert,
+                    const double* d_kappa, const uint32_t* d_perm, const int64_t* d_dof_off,
+                    const double* d_dofs, double* d_djdk, double* d_djdx, cudaStream_t st) {
+  if (nel <= 0) return;
+  k_adjoint<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_wq, d_shap, d_grad,
+                                                  d_xvert, d_kappa, d_perm, d_dof_off, d_dofs, d_djdk,
+                                                  d_djdx);
+}
+
+}  // namespace hp3dg

@@ -51,7 +51,8 @@ _f32p = ctypes.POINTER(ctypes.c_float)
 
 EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit", "hp3dg_batch_run",
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
-           "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_output_sizes", "hp3dg_device_outputs",
+           "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
+           "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_output_sizes", "hp3dg_device_outputs",
            "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_last_bad_element", "hp3dg_batch_end", "hp3dg_strerror"]
 
 
@@ -73,6 +74,10 @@ def lib():
         L.hp3dg_get_schur.argtypes = [_vp, ctypes.c_int32, _f64p, _f64p, _i32p, _i32p]
         L.hp3dg_index_map.argtypes = [_vp, _i32p, _i64p, _i64p, _i32p, _i64p]
         L.hp3dg_output_sizes.argtypes = [_vp, _i64p, _i64p, _i64p, _i64p]
+        L.hp3dg_backsub.argtypes = [_vp, _f64p]
+        L.hp3dg_get_dofs.argtypes = [_vp, ctypes.c_int32, _f64p, _i32p]
+        L.hp3dg_element_error.argtypes = [_vp, ctypes.c_int32, _f64p, _f64p]
+        L.hp3dg_adjoint.argtypes = [_vp, _f64p, _f64p, _f64p]
         L.hp3dg_device_outputs.argtypes = [_vp] + [ctypes.POINTER(_vp)] * 5
         L.hp3dg_phase_times.argtypes = [_vp, _f32p, ctypes.c_int32]
         L.hp3dg_mixed_config.argtypes = [_vp, _i32p, _i32p, _i32p]
@@ -191,6 +196,33 @@ class ElementPass:
         self._check(self.L.hp3dg_index_map(self.ctx, _p(nf, _i32p), _p(en, _i64p), _p(lo, _i64p),
                                            _p(lc, _i32p), ctypes.byref(nr)), "index_map")
         return nr.value, nf, lc[:nl], lo, en
+
+    def backsub(self, x_global):
+        self._xg = np.ascontiguousarray(x_global, dtype=np.float64)
+        self._check(self.L.hp3dg_backsub(self.ctx, _p(self._xg, _f64p)), "backsub")
+
+    def dofs(self, e):
+        n = ctypes.c_int32()
+        self._check(self.L.hp3dg_get_dofs(self.ctx, e, None, ctypes.byref(n)), "dofs")
+        d = np.zeros(n.value)
+        self._check(self.L.hp3dg_get_dofs(self.ctx, e, _p(d, _f64p), ctypes.byref(n)), "dofs")
+        return d
+
+    def element_error(self, isol):
+        e2 = np.zeros(self.nel); n2 = np.zeros(self.nel)
+        self._check(self.L.hp3dg_element_error(self.ctx, isol, _p(e2, _f64p), _p(n2, _f64p)),
+                    "element_error")
+        return e2, n2
+
+    def adjoint(self, dofs=None):
+        """dJ/dkappa (n_elem) and per-element vertex contributions (n_elem, 8, 3)
+        of the compliance J = f^T u; dofs: list of full element dof vectors or
+        None (those of backsub)."""
+        d = None if dofs is None else np.ascontiguousarray(np.concatenate(dofs), np.float64)
+        dk = np.zeros(self.nel); dx = np.zeros((self.nel, 8, 3))
+        self._check(self.L.hp3dg_adjoint(self.ctx, _p(d, _f64p), _p(dk, _f64p), _p(dx, _f64p)),
+                    "adjoint")
+        return dk, dx
 
     def phase_times(self):
         t = (ctypes.c_float * 6)()

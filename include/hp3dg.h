@@ -148,6 +148,35 @@ int hp3dg_get_schur(const hp3dg_ctx *ctx, int32_t iel, double *aschur, double *b
 int hp3dg_index_map(const hp3dg_ctx *ctx, int32_t *nfirst_dof, int64_t *elem_nnz,
                     int64_t *lcon_off, int32_t *lcon, int64_t *nrdof);
 
+/* Back-substitution after the global solve (stc_bwd_wrapper / stc_bwd /
+ * stc_solout, modules/stc.F90:529-991; called from solout,
+ * solver/frontal/interf/solout.F90:457): x_global holds the nrdof interface
+ * unknowns (host memory, 1-based LCON numbering).  Builds every element's
+ * full dof vector (interface dof from x_global or the submitted Dirichlet
+ * data, bubbles = BSchur - ASchur xi) on the device and copies it to the
+ * host; read it with hp3dg_get_dofs. */
+int hp3dg_backsub(hp3dg_ctx *ctx, const double *x_global);
+
+/* Full dof vector of element iel (interface dof then bubbles, element dof
+ * order) after hp3dg_backsub; n returned. */
+int hp3dg_get_dofs(const hp3dg_ctx *ctx, int32_t iel, double *dof, int32_t *n);
+
+/* Squared H1 error and squared H1 norm of every element against the
+ * manufactured solution isol (element_error, element/util/compute_error.F90:
+ * 226-360, H1 branch with the INTEGRATION = 2 rule), using the dof of the
+ * last hp3dg_backsub.  err2, nrm2: host arrays of n_elem. */
+int hp3dg_element_error(hp3dg_ctx *ctx, int32_t isol, double *err2, double *nrm2);
+
+/* Compliance sensitivities (J = f^T u with K u = f, adjoint lambda = u):
+ * dJ/dkappa_e = -u_e^T (dK_e/dkappa_e) u_e for every element, and the
+ * element contributions to dJ/dx of its 8 vertices (n_elem x 8 x 3; sum
+ * them over elements sharing a vertex), including the dependence of the
+ * load on the geometry.  dofs: host array of the full element dof vectors
+ * concatenated in element order, or NULL to use those of hp3dg_backsub.
+ * No counterpart in the reference solver (used for design optimisation on
+ * top of its element pass). */
+int hp3dg_adjoint(hp3dg_ctx *ctx, const double *dofs, double *djdkappa, double *djdx);
+
 /* Sizes of the batch outputs (for the caller's allocation). */
 int hp3dg_output_sizes(const hp3dg_ctx *ctx, int64_t *nnz_total, int64_t *lcon_total,
                        int64_t *schur_total, int64_t *bubble_total);

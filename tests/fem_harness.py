@@ -119,6 +119,31 @@ def oracle_element_outputs(mesh, isol, integration=0, zdofd=None, stc_method=0):
     return res
 
 
+def assemble_solve(mesh, elems):
+    """Assemble the condensed interface system from per-element outputs
+    (mumps_sc.F90:300-321 triplets) and solve it; returns the global interface
+    solution x and the index maps."""
+    ne = mesh["nelem"]
+    nnode = np.full(ne, 26, dtype=np.int32)
+    ndofm = np.stack([el["ndofm"] for el in elems]).astype(np.int32)
+    nrdof, nfirst, lcon, lcon_off, elem_nnz = O.index_maps(nnode, mesh["nodes"], ndofm,
+                                                           mesh["nnodes"])
+    rows, cols, vals = [], [], []
+    rhs = np.zeros(nrdof)
+    for e in range(ne):
+        lc = lcon[lcon_off[e]:lcon_off[e + 1]] - 1
+        nc = len(lc)
+        if nc == 0:
+            continue
+        rows.append(np.repeat(lc, nc)); cols.append(np.tile(lc, nc))
+        vals.append(elems[e]["zastif"].ravel())
+        np.add.at(rhs, lc, elems[e]["zbload"])
+    A = sp.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(nrdof, nrdof)).tocsc()
+    x = spla.spsolve(A, rhs) if nrdof > 0 else np.zeros(0)
+    return x, lcon, lcon_off
+
+
 def solve_and_error(mesh, elems, isol, zdofd=None):
     """Assemble the condensed interface system from per-element outputs
     (dicts with nextract/zbload/zastif/ndofm/aschur/bschur), solve it,
