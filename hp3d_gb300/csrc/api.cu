@@ -103,7 +103,7 @@ T* dalloc(size_t count, int* err) {
 }
 
 struct Bin {
-  int nord_loc[19];
+  int nord_loc[19];  // full (bin) orders: per-axis maxima of the member elements' local orders
   int n = 0, nb = 0, ni = 0, nint = 0;
   std::vector<int> elems;
   std::vector<double> xi, wq;
@@ -111,6 +111,7 @@ struct Bin {
   int* d_elist = nullptr;
   double *d_xi = nullptr, *d_wq = nullptr, *d_shap = nullptr, *d_grad = nullptr;
   double *d_D = nullptr, *d_F = nullptr, *d_b0 = nullptr, *d_PK = nullptr, *d_S = nullptr;
+  double* d_Yg = nullptr;  // global Y slab for bins whose Y does not fit in shared memory
   uint32_t* d_perm = nullptr;
   uint8_t* d_dmask = nullptr;
   // error-evaluation tables (INTEGRATION = 2 rule)
@@ -141,7 +142,8 @@ struct hp3dg_ctx {
   bool have_zdofd = false;
   // device inputs
   int *d_norder = nullptr, *d_nori_e = nullptr, *d_nori_f = nullptr, *d_nodes = nullptr,
-      *d_ndofm = nullptr, *d_nextract = nullptr;
+      *d_ndofm = nullptr, *d_nextract = nullptr, *d_n_e = nullptr, *d_ni_e = nullptr,
+      *d_nb_e = nullptr;
   double *d_xvert = nullptr, *d_kappa = nullptr, *d_zdofd = nullptr;
   int64_t *d_elem_nnz = nullptr, *d_lcon_off = nullptr, *d_schur_off = nullptr,
           *d_bub_off = nullptr, *d_zd_off = nullptr;
@@ -174,6 +176,7 @@ namespace {
 void free_bin(Bin& b) {
   cudaFree(b.d_elist); cudaFree(b.d_xi); cudaFree(b.d_wq); cudaFree(b.d_shap); cudaFree(b.d_grad);
   cudaFree(b.d_D); cudaFree(b.d_F); cudaFree(b.d_b0); cudaFree(b.d_PK); cudaFree(b.d_S);
+  cudaFree(b.d_Yg);
   cudaFree(b.d_perm); cudaFree(b.d_dmask); cudaFree(b.d_mdig); cudaFree(b.d_ddig);
   cudaFree(b.d_mscale); cudaFree(b.d_dscale);
   cudaFree(b.d_xi_err); cudaFree(b.d_wq_err); cudaFree(b.d_shap_err); cudaFree(b.d_grad_err);
@@ -184,6 +187,7 @@ void free_batch(hp3dg_ctx* c) {
   for (auto& b : c->bins) free_bin(b);
   c->bins.clear();
   void* dev[] = {c->d_norder, c->d_nori_e, c->d_nori_f, c->d_nodes, c->d_ndofm, c->d_nextract,
+                 c->d_n_e, c->d_ni_e, c->d_nb_e,
                  c->d_xvert, c->d_kappa, c->d_zdofd, c->d_elem_nnz, c->d_lcon_off,
                  c->d_schur_off, c->d_bub_off, c->d_zd_off, c->d_zastif, c->d_zbload,
                  c->d_aschur, c->d_bschur, c->d_lcon, c->d_nfirst, c->d_first, c->d_cnt,
@@ -199,6 +203,7 @@ void free_batch(hp3dg_ctx* c) {
                   c->h_PK, c->h_b0};
   for (void* p : host) cudaFreeHost(p);
   c->d_norder = c->d_nori_e = c->d_nori_f = c->d_nodes = c->d_ndofm = c->d_nextract = nullptr;
+  c->d_n_e = c->d_ni_e = c->d_nb_e = nullptr;
   c->d_xvert = c->d_kappa = c->d_zdofd = nullptr;
   c->d_elem_nnz = c->d_lcon_off = c->d_schur_off = c->d_bub_off = c->d_zd_off = nullptr;
   c->d_zastif = c->d_zbload = c->d_aschur = c->d_bschur = nullptr;
@@ -299,9 +304,10 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
     std::copy(d.nori_edge, d.nori_edge + 12, &nori_e[12 * (size_t)e]);
     std::copy(d.nori_face, d.nori_face + 6, &nori_f[6 * (size_t)e]);
     std::copy(d.nodes, d.nodes + 26, &nodes[26 * (size_t)e]);
-    int loc[19];
+    int loc[19], full[19];
     hexa_order_loc(d.norder, d.nori_face, loc);
-    std::vector<int> key(loc, loc + 19);
+    hexa_bin_orders(loc, full);
+    std::vector<int> key(full, full + 19);
     auto it = binmap.find(key);
     int b;
     if (it == binmap.end()) {
@@ -309,12 +315,12 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
       binmap[key] = b;
       c->bins.emplace_back();
       Bin& B = c->bins.back();
-      std::copy(loc, loc + 19, B.nord_loc);
-      B.n = hexa_ndof(loc);
-      B.nb = hexa_nbub(loc);
+      std::copy(full, full + 19, B.nord_loc);
+      B.n = hexa_ndof(full);
+      B.nb = hexa_nbub(full);
       B.ni = B.n - B.nb;
-      B.nint = hexa_quadrature(loc, c->opts.integration, B.xi, B.wq);
-      if (condense_smem(B.ni, B.nb) > 227 * 1024) { c->last_bad = e; free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
+      B.nint = hexa_quadrature(full, c->opts.integration, B.xi, B.wq);
+      if (condense_smem_small(B.ni, B.nb) > 227 * 1024) { c->last_bad = e; free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
     } else {
       b = it->second;
     }
@@ -335,7 +341,7 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
       for (int q = 0; q < act; ++q) c->nextract.push_back(first[i] + q);
       nrdofc += act;
     }
-    c->n_e[e] = c->bins[b].n; c->nb_e[e] = c->bins[b].nb; c->ni_e[e] = ni;
+    c->nb_e[e] = hexa_nbub(d.norder); c->ni_e[e] = ni; c->n_e[e] = ni + c->nb_e[e];
     c->elem_nnz[e + 1] = c->elem_nnz[e] + (int64_t)nrdofc * nrdofc;
     c->lcon_off[e + 1] = c->lcon_off[e] + nrdofc;
     c->schur_off[e + 1] = c->schur_off[e] + (int64_t)c->nb_e[e] * ni;
@@ -360,6 +366,9 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   c->d_bub_off = dalloc<int64_t>(nel + 1, &err);
   c->d_zd_off = dalloc<int64_t>(nel + 1, &err);
   c->d_dof_off = dalloc<int64_t>(nel + 1, &err);
+  c->d_n_e = dalloc<int>(nel, &err);
+  c->d_ni_e = dalloc<int>(nel, &err);
+  c->d_nb_e = dalloc<int>(nel, &err);
   c->have_zdofd = zdofd != nullptr;
   if (zdofd) c->d_zdofd = dalloc<double>(c->zd_off[nel], &err);
   // ---- outputs ----
@@ -398,6 +407,11 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   CK(cudaMemcpyAsync(c->d_bub_off, c->bub_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->d_zd_off, c->zd_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(c->d_dof_off, c->dof_off.data(), (nel + 1) * 8, cudaMemcpyHostToDevice, st));
+  if (nel > 0) {
+    CK(cudaMemcpyAsync(c->d_n_e, c->n_e.data(), (size_t)nel * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_ni_e, c->ni_e.data(), (size_t)nel * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(c->d_nb_e, c->nb_e.data(), (size_t)nel * 4, cudaMemcpyHostToDevice, st));
+  }
   if (zdofd)
     CK(cudaMemcpyAsync(c->d_zdofd, zdofd, c->zd_off[nel] * 8, cudaMemcpyHostToDevice, st));
   // ---- per-bin buffers ----
@@ -415,12 +429,14 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
     B.d_S = dalloc<double>(ne * ((size_t)B.ni * (B.ni + 1) / 2), &err);
     B.d_perm = dalloc<uint32_t>(ne * B.n, &err);
     B.d_dmask = dalloc<uint8_t>(ne * B.ni, &err);
+    if (condense_smem(B.ni, B.nb) > 227 * 1024)
+      B.d_Yg = dalloc<double>(ne * (size_t)B.nb * (B.ni + 1), &err);
     if (err) { free_batch(c); return err; }
     CK(cudaMemcpyAsync(B.d_elist, B.elems.data(), ne * 4, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(B.d_xi, B.xi.data(), B.xi.size() * 8, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(B.d_wq, B.wq.data(), B.wq.size() * 8, cudaMemcpyHostToDevice, st));
     if (zdofd) {
-      std::vector<uint8_t> dm(ne * B.ni, 0);
+      std::vector<uint8_t> dm(ne * B.ni, 0);  // element ni <= bin ni
       for (size_t j = 0; j < ne; ++j) {
         const hp3dg_elem_desc& d = desc[B.elems[j]];
         int k = 0;
@@ -477,7 +493,8 @@ int hp3dg_batch_run(hp3dg_ctx* c) {
   if (tm) cudaEventRecord(c->ev[1], st);
   for (auto& B : c->bins) {
     int ne = (int)B.elems.size();
-    launch_orient_hexa(ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.n, B.d_perm, st);
+    launch_orient_hexa(ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n,
+                       B.d_perm, st);
     launch_geom_hexa(ne, B.d_elist, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert,
                      c->d_kappa, c->opts.isol, B.d_D, B.d_F, c->d_flags, st);
     launch_load_hexa(ne, B.nint, B.n, B.d_shap, B.d_F, B.d_b0, st);
@@ -498,10 +515,11 @@ int hp3dg_batch_run(hp3dg_ctx* c) {
   if (tm) cudaEventRecord(c->ev[3], st);
   for (auto& B : c->bins) {
     int ne = (int)B.elems.size();
-    if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, B.d_PK, B.d_b0, B.d_perm, c->d_nextract,
-                        c->d_lcon_off, c->d_elem_nnz, c->d_schur_off, c->d_bub_off, c->d_zd_off,
-                        c->have_zdofd ? c->d_zdofd : nullptr, B.d_dmask, B.d_S, c->d_zastif,
-                        c->d_zbload, c->d_aschur, c->d_bschur, c->d_flags + 1, st))
+    if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
+                        B.d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
+                        c->d_bub_off, c->d_zd_off, c->have_zdofd ? c->d_zdofd : nullptr, B.d_dmask,
+                        B.d_S, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur, B.d_Yg,
+                        c->d_flags + 1, st))
       return HP3DG_ERR_CUDA;
   }
   if (tm) cudaEventRecord(c->ev[4], st);
@@ -579,12 +597,12 @@ int hp3dg_get_elem(const hp3dg_ctx* c, int32_t iel, double* aloc, int32_t ld, do
   if (!c || !aloc || !bloc) return HP3DG_ERR_ARG;
   if (!c->downloaded || !c->opts.keep_elem) return HP3DG_ERR_STATE;
   if (iel < 0 || iel >= c->nel) return HP3DG_ERR_ARG;
-  int n = c->n_e[iel], ni = n - c->nb_e[iel], nb = c->nb_e[iel];
+  int n = c->n_e[iel];
   if (ld < n) return HP3DG_ERR_ARG;
   const Bin& B = c->bins[c->bin_of[iel]];
-  // oriented dof map of this element (same map the device uses)
+  const int ni = B.ni, nb = B.nb;  // the packed matrix is the bin element's
+  // dof map of this element (same map the device uses)
   int no[19], oe[12], of[6];
-  (void)B;
   // descriptors are not kept on the host; recompute the map from device copies
   cudaMemcpy(no, c->d_norder + 19 * (size_t)iel, sizeof(no), cudaMemcpyDeviceToHost);
   cudaMemcpy(oe, c->d_nori_e + 12 * (size_t)iel, sizeof(oe), cudaMemcpyDeviceToHost);
@@ -592,11 +610,11 @@ int hp3dg_get_elem(const hp3dg_ctx* c, int32_t iel, double* aloc, int32_t ld, do
   const double* PK = c->h_PK + c->pk_off[iel];
   const double* b0 = c->h_b0 + c->b0_off[iel];
   for (int a = 0; a < n; ++a) {
-    uint32_t ma = hexa_orient_map(a, no, oe, of);
+    uint32_t ma = hexa_dof_map(a, no, oe, of, B.nord_loc);
     int ra = (int)(ma & 0x7fffffffu);
     bloc[a] = (ma & 0x80000000u) ? -b0[ra] : b0[ra];
     for (int b = 0; b < n; ++b) {
-      uint32_t mb = hexa_orient_map(b, no, oe, of);
+      uint32_t mb = hexa_dof_map(b, no, oe, of, B.nord_loc);
       int rb = (int)(mb & 0x7fffffffu);
       double v = PK[pk_index(ra, rb, ni, nb)];
       aloc[(size_t)b * ld + a] = ((ma ^ mb) & 0x80000000u) ? -v : v;
@@ -659,10 +677,10 @@ int hp3dg_backsub(hp3dg_ctx* c, const double* x_global) {
     return HP3DG_ERR_ALLOC;
   CK(cudaMemcpyAsync(c->d_xglob, x_global, nrdof * 8, cudaMemcpyHostToDevice, st));
   for (auto& B : c->bins)
-    launch_backsub((int)B.elems.size(), B.ni, B.nb, B.d_elist, c->d_nextract, c->d_lcon_off,
-                   c->d_lcon, c->d_xglob, c->d_zd_off, c->have_zdofd ? c->d_zdofd : nullptr,
-                   c->d_schur_off, c->d_bub_off, c->d_aschur, c->d_bschur, c->d_dof_off,
-                   c->d_dofs, st);
+    launch_backsub((int)B.elems.size(), B.ni, B.d_elist, c->d_ni_e, c->d_nb_e, c->d_nextract,
+                   c->d_lcon_off, c->d_lcon, c->d_xglob, c->d_zd_off,
+                   c->have_zdofd ? c->d_zdofd : nullptr, c->d_schur_off, c->d_bub_off,
+                   c->d_aschur, c->d_bschur, c->d_dof_off, c->d_dofs, st);
   CK(cudaMemcpyAsync(c->h_dofs, c->d_dofs, c->dof_off[c->nel] * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   if (cudaPeekAtLastError() != cudaSuccess) return HP3DG_ERR_CUDA;
@@ -702,7 +720,7 @@ int hp3dg_element_error(hp3dg_ctx* c, int32_t isol, double* err2, double* nrm2) 
       CK(cudaStreamSynchronize(st));
       B.etable = true;
     }
-    launch_element_error((int)B.elems.size(), B.nint_err, B.n, isol, B.d_elist, B.d_wq_err,
+    launch_element_error((int)B.elems.size(), B.nint_err, B.n, isol, B.d_elist, c->d_n_e, B.d_wq_err,
                          B.d_shap_err, B.d_grad_err, c->d_xvert, B.d_perm, c->d_dof_off, c->d_dofs,
                          c->d_err2, c->d_nrm2, st);
   }
@@ -725,7 +743,7 @@ int hp3dg_adjoint(hp3dg_ctx* c, const double* dofs, double* djdkappa, double* dj
   if (err) return err;
   if (dofs) CK(cudaMemcpyAsync(c->d_dofs, dofs, c->dof_off[c->nel] * 8, cudaMemcpyHostToDevice, st));
   for (auto& B : c->bins)
-    launch_adjoint((int)B.elems.size(), B.nint, B.n, c->opts.isol, B.d_elist, B.d_wq, B.d_shap,
+    launch_adjoint((int)B.elems.size(), B.nint, B.n, c->opts.isol, B.d_elist, c->d_n_e, B.d_wq, B.d_shap,
                    B.d_grad, c->d_xvert, c->d_kappa, B.d_perm, c->d_dof_off, c->d_dofs, c->d_djdk,
                    c->d_djdx, st);
   CK(cudaMemcpyAsync(djdkappa, c->d_djdk, (size_t)c->nel * 8, cudaMemcpyDeviceToHost, st));

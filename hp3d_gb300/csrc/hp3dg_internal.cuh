@@ -169,26 +169,64 @@ __host__ __device__ inline int hexa_shape0(const double* xi, const int* nord, do
   return m;
 }
 
+// Full (bin) orders of a hexa from its local orders: per axis the maximum
+// over edges, faces and interior -- the orders set_3Dint_aux integrates
+// exactly (quadrature/set_3D_int.F90:193-230).  Every element of the bin
+// uses the bin's quadrature, and its dof are a subset of the bin element's
+// (the H1 basis is hierarchical: an edge of order p carries the first p-1
+// edge functions of any higher order, a face the leading sub-rectangle).
+__host__ __device__ inline void hexa_bin_orders(const int* loc, int* full) {
+  int nx = 0, ny = 0, nz = 0;
+  for (int e = 0; e < 12; ++e) {
+    int ax = hexa_e(e, 4);
+    if (ax == 0) nx = loc[e] > nx ? loc[e] : nx;
+    else if (ax == 1) ny = loc[e] > ny ? loc[e] : ny;
+    else nz = loc[e] > nz ? loc[e] : nz;
+  }
+  for (int f = 0; f < 6; ++f) {
+    int h, v; decod2(loc[12 + f], h, v);
+    int a1 = hexa_f(f, 2), a2 = hexa_f(f, 3);
+    int* m1 = a1 == 0 ? &nx : (a1 == 1 ? &ny : &nz);
+    int* m2 = a2 == 0 ? &nx : (a2 == 1 ? &ny : &nz);
+    if (h > *m1) *m1 = h;
+    if (v > *m2) *m2 = v;
+  }
+  int x, y, z; decod3(loc[18], x, y, z);
+  nx = x > nx ? x : nx; ny = y > ny ? y : ny; nz = z > nz ? z : nz;
+  for (int e = 0; e < 12; ++e) {
+    int ax = hexa_e(e, 4);
+    full[e] = ax == 0 ? nx : (ax == 1 ? ny : nz);
+  }
+  for (int f = 0; f < 6; ++f) {
+    int a1 = hexa_f(f, 2), a2 = hexa_f(f, 3);
+    int o1 = a1 == 0 ? nx : (a1 == 1 ? ny : nz), o2 = a2 == 0 ? nx : (a2 == 1 ? ny : nz);
+    full[12 + f] = 10 * o1 + o2;
+  }
+  full[18] = 100 * nx + 10 * ny + nz;
+}
+
 // Oriented dof a of an element with (global-frame) orders nord and
-// orientations -> reference dof in the bin's local-order enumeration, with
-// sign.  Edge reversal multiplies L_i by (-1)^i; a face orientation swaps
-// and/or reverses the face axes (OrientE / OrientQuad, Orient.F90:9-116).
-// Returns (ref index) | (sign < 0 ? 0x80000000 : 0).
-__host__ __device__ inline uint32_t hexa_orient_map(int a, const int* nord, const int* nori_e,
-                                                    const int* nori_f) {
+// orientations -> dof of the bin element (orders `full`, orientation 0),
+// with sign.  Edge reversal multiplies L_i by (-1)^i; a face orientation
+// swaps and/or reverses the two face axes (OrientE / OrientQuad,
+// shape_1/Orient.F90:9-116).  Returns (bin dof) | (sign < 0 ? 0x80000000 : 0).
+__host__ __device__ inline uint32_t hexa_dof_map(int a, const int* nord, const int* nori_e,
+                                                 const int* nori_f, const int* full) {
   if (a < 8) return (uint32_t)a;
-  int off = 8;      // oriented offset
+  int off = 8, boff = 8;  // element / bin offsets
   for (int e = 0; e < 12; ++e) {
     int nd = nord[e] > 1 ? nord[e] - 1 : 0;
     if (a < off + nd) {
       int i = a - off + 2;
       bool neg = (nori_e[e] == 1) && (i & 1);
-      return (uint32_t)a | (neg ? 0x80000000u : 0u);
+      return (uint32_t)(boff + i - 2) | (neg ? 0x80000000u : 0u);
     }
     off += nd;
+    boff += full[e] > 1 ? full[e] - 1 : 0;
   }
   for (int f = 0; f < 6; ++f) {
     int n1, n2; decod2(nord[12 + f], n1, n2);
+    int b1, b2; decod2(full[12 + f], b1, b2);
     int nd = (n1 > 1 && n2 > 1) ? (n1 - 1) * (n2 - 1) : 0;
     if (a < off + nd) {
       int r = a - off;
@@ -198,14 +236,19 @@ __host__ __device__ inline uint32_t hexa_orient_map(int a, const int* nord, cons
       // GS1 = Mu[OrGS(1)] of pair OrPa(1): reversed when OrGS(1)==0
       bool negs = (orq(o, 3) == 0) && (i & 1);
       bool negt = (orq(o, 5) == 0) && (j & 1);
-      int ref;
-      if (!swap) ref = off + (j - 2) * (n1 - 1) + (i - 2);
-      else ref = off + (i - 2) * (n2 - 1) + (j - 2);  // local orders (n2, n1)
+      int il = swap ? j : i, jl = swap ? i : j;  // local face indices
+      int ref = boff + (jl - 2) * (b1 - 1) + (il - 2);
       return (uint32_t)ref | ((negs != negt) ? 0x80000000u : 0u);
     }
     off += nd;
+    boff += (b1 > 1 && b2 > 1) ? (b1 - 1) * (b2 - 1) : 0;
   }
-  return (uint32_t)a;  // bubbles: no orientation
+  int px, py, pz; decod3(nord[18], px, py, pz);
+  int bx, by, bz; decod3(full[18], bx, by, bz);
+  int r = a - off;
+  int i = r % (px - 1) + 2, t = r / (px - 1), j = t % (py - 1) + 2, k = t / (py - 1) + 2;
+  (void)bz;
+  return (uint32_t)(boff + ((k - 2) * (by - 1) + (j - 2)) * (bx - 1) + (i - 2));
 }
 
 // Local (bin) orders of a hexa: find_order_loc (datstrs/find_order.F90:68-108).

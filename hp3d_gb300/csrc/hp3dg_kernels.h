@@ -8,7 +8,8 @@ namespace hp3dg {
 void launch_tables_hexa(const int* nord_loc, int nint, int n, const double* d_xi,
                         double* d_shap, double* d_grad, cudaStream_t st);
 void launch_orient_hexa(int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
-                        const int* d_nori_f, int n, uint32_t* d_perm, cudaStream_t st);
+                        const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
+                        cudaStream_t st);
 void launch_geom_hexa(int nel, const int* d_elist, int nint, int n, const double* d_wq,
                       const double* d_shap, const double* d_grad, const double* d_xvert,
                       const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
@@ -18,29 +19,34 @@ void launch_load_hexa(int nel, int nint, int n, const double* d_shap, const doub
 void launch_contract_fp64(int nel, int nint, int n, int ni, int nb, const double* d_grad,
                           const double* d_D, double* d_PK, cudaStream_t st);
 size_t condense_smem(int ni, int nb);
-int launch_condense(int nel, int n, int ni, int nb, const int* d_elist, const double* d_PK,
-                    const double* d_b0, const uint32_t* d_perm, const int* d_nextract,
-                    const int64_t* d_lcon_off, const int64_t* d_elem_nnz,
-                    const int64_t* d_schur_off, const int64_t* d_bub_off,
-                    const int64_t* d_zd_off, const double* d_zdofd, const uint8_t* d_dmask,
-                    double* d_S, double* d_zastif, double* d_zbload, double* d_aschur,
-                    double* d_bschur, int* d_bad_spd, cudaStream_t st);
+size_t condense_smem_small(int ni, int nb);
+int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
+                    const int* d_nb_e, const double* d_PK, const double* d_b0,
+                    const uint32_t* d_perm, const int* d_nextract, const int64_t* d_lcon_off,
+                    const int64_t* d_elem_nnz, const int64_t* d_schur_off,
+                    const int64_t* d_bub_off, const int64_t* d_zd_off, const double* d_zdofd,
+                    const uint8_t* d_dmask, double* d_S, double* d_zastif, double* d_zbload,
+                    double* d_aschur, double* d_bschur, double* d_Yg, int* d_bad_spd,
+                    cudaStream_t st);
 int launch_index_maps(int nel, int nnode, int nnodes_global, const int* d_nodes, const int* d_ndofm,
                       const int64_t* d_lcon_off, int* d_first, int* d_cnt, int64_t* d_scan,
                       int64_t* d_blk, int64_t* d_total, int* d_nfirst, int* d_lcon,
                       cudaStream_t st);
 
 // after the solve -- k_post.cu
-void launch_backsub(int nel, int ni, int nb, const int* d_elist, const int* d_nextract,
+void launch_backsub(int nel, int nif, const int* d_elist, const int* d_ni_e, const int* d_nb_e,
+                    const int* d_nextract,
                     const int64_t* d_lcon_off, const int* d_lcon, const double* d_x,
                     const int64_t* d_zd_off, const double* d_zdofd, const int64_t* d_schur_off,
                     const int64_t* d_bub_off, const double* d_aschur, const double* d_bschur,
                     const int64_t* d_dof_off, double* d_dofs, cudaStream_t st);
-void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+                          const double* d_wq,
                           const double* d_shap, const double* d_grad, const double* d_xvert,
                           const uint32_t* d_perm, const int64_t* d_dof_off, const double* d_dofs,
                           double* d_err2, double* d_nrm2, cudaStream_t st);
-void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+                    const double* d_wq,
                     const double* d_shap, const double* d_grad, const double* d_xvert,
                     const double* d_kappa, const uint32_t* d_perm, const int64_t* d_dof_off,
                     const double* d_dofs, double* d_djdk, double* d_djdx, cudaStream_t st);

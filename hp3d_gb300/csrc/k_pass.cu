@@ -42,11 +42,11 @@ void launch_tables_hexa(const int* nord_loc, int nint, int n, const double* d_xi
 }
 
 // ---------------------------------------------------------------------------
-// orientation maps: perm[e][a] = reference dof of oriented dof a (bit31 sign)
+// dof maps: perm[j][a] = bin dof of the element's oriented dof a (bit31 sign)
 // ---------------------------------------------------------------------------
 __global__ void k_orient_hexa(int nel, const int* __restrict__ elist, const int* __restrict__ norder,
                               const int* __restrict__ nori_e, const int* __restrict__ nori_f,
-                              int n, uint32_t* __restrict__ perm) {
+                              Ord19 full, int nfull, uint32_t* __restrict__ perm) {
   int j = blockIdx.x;
   if (j >= nel) return;
   int e = elist[j];
@@ -55,13 +55,18 @@ __global__ void k_orient_hexa(int nel, const int* __restrict__ elist, const int*
   if (threadIdx.x < 12) oe[threadIdx.x] = nori_e[12 * e + threadIdx.x];
   if (threadIdx.x < 6) of[threadIdx.x] = nori_f[6 * e + threadIdx.x];
   __syncthreads();
-  for (int a = threadIdx.x; a < n; a += blockDim.x)
-    perm[(size_t)j * n + a] = hexa_orient_map(a, no, oe, of);
+  const int n = hexa_ndof(no);
+  for (int a = threadIdx.x; a < nfull; a += blockDim.x)
+    perm[(size_t)j * nfull + a] = a < n ? hexa_dof_map(a, no, oe, of, full.v) : 0u;
 }
 
 void launch_orient_hexa(int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
-                        const int* d_nori_f, int n, uint32_t* d_perm, cudaStream_t st) {
-  if (nel > 0) k_orient_hexa<<<nel, 128, 0, st>>>(nel, d_elist, d_norder, d_nori_e, d_nori_f, n, d_perm);
+                        const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
+                        cudaStream_t st) {
+  Ord19 o;
+  for (int i = 0; i < 19; ++i) o.v[i] = full[i];
+  if (nel > 0)
+    k_orient_hexa<<<nel, 128, 0, st>>>(nel, d_elist, d_norder, d_nori_e, d_nori_f, o, nfull, d_perm);
 }
 
 // ---------------------------------------------------------------------------
@@ -284,42 +289,46 @@ __device__ inline void upper_decode(int64_t idx, int& a, int& b) {
 }
 
 __global__ void __launch_bounds__(CND_THREADS) k_condense(
-    int n, int ni, int nb, const int* __restrict__ elist, const double* __restrict__ PK,
-    const double* __restrict__ b0, const uint32_t* __restrict__ perm,
-    const int* __restrict__ nextract, const int64_t* __restrict__ lcon_off,
-    const int64_t* __restrict__ elem_nnz, const int64_t* __restrict__ schur_off,
-    const int64_t* __restrict__ bub_off, const int64_t* __restrict__ zd_off,
-    const double* __restrict__ zdofd, const uint8_t* __restrict__ dmask, double* __restrict__ Sbuf,
-    double* __restrict__ zastif, double* __restrict__ zbload, double* __restrict__ aschur,
-    double* __restrict__ bschur, int* __restrict__ bad_spd) {
+    int nfull, int nif, int nbf, const int* __restrict__ elist, const int* __restrict__ ni_e,
+    const int* __restrict__ nb_e, const double* __restrict__ PK, const double* __restrict__ b0,
+    const uint32_t* __restrict__ perm, const int* __restrict__ nextract,
+    const int64_t* __restrict__ lcon_off, const int64_t* __restrict__ elem_nnz,
+    const int64_t* __restrict__ schur_off, const int64_t* __restrict__ bub_off,
+    const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
+    const uint8_t* __restrict__ dmask, double* __restrict__ Sbuf, double* __restrict__ zastif,
+    double* __restrict__ zbload, double* __restrict__ aschur, double* __restrict__ bschur,
+    double* __restrict__ Yg, int* __restrict__ bad_spd) {
   extern __shared__ double sm[];
   const int j = blockIdx.x;
   const int e = elist[j];
-  const double* PKj = PK + (size_t)j * ((size_t)n * (n + 1) / 2);
-  const uint32_t* pm = perm + (size_t)j * n;
-  const double* bj = b0 + (size_t)j * n;
+  const int ni = ni_e[e], nb = nb_e[e];  // this element's dof (a subset of the bin's)
+  const double* PKj = PK + (size_t)j * ((size_t)nfull * (nfull + 1) / 2);
+  const uint32_t* pm = perm + (size_t)j * nfull;
+  const double* bj = b0 + (size_t)j * nfull;
   const int ld = ni + 1;
+  // L and the condensed load live in shared memory; Y = L^-1 [K_bi | b_b]
+  // too, unless the bin is too large, then in a global scratch slab (Yg)
   double* L = sm;
-  double* Ys = sm + (size_t)nb * nb;
-  double* bi = Ys + (size_t)nb * ld;
+  double* Ys = Yg ? Yg + (size_t)j * nbf * (nif + 1) : sm + (size_t)nb * nb;
+  double* bi = Yg ? sm + (size_t)nb * nb : Ys + (size_t)nb * ld;
   __shared__ int fail;
   const int tid = threadIdx.x;
   if (tid == 0) fail = 0;
-  double* S = Sbuf + (size_t)j * ((size_t)ni * (ni + 1) / 2);
-  // ---- load K_bb (bubbles are never permuted) and [K_bi | b_b] ----
+  double* S = Sbuf + (size_t)j * ((size_t)nif * (nif + 1) / 2);
+  // ---- gather K_bb and [K_bi | b_b] through the dof map ----
   for (int idx = tid; idx < nb * nb; idx += CND_THREADS) {
     int r = idx / nb, c = idx % nb;
-    int lo = r < c ? r : c, hi = r < c ? c : r;
-    L[idx] = PKj[(size_t)hi * (hi + 1) / 2 + lo];
+    L[idx] = pk_get(PKj, pm, ni + r, ni + c, nif, nbf);
   }
-  const double* BI = PKj + (size_t)nb * (nb + 1) / 2;
   for (int idx = tid; idx < nb * ni; idx += CND_THREADS) {
     int c = idx / nb, r = idx % nb;
-    uint32_t mc = pm[c];
-    double v = BI[(size_t)(mc & 0x7fffffffu) * nb + r];
-    Ys[r * ld + c] = (mc & 0x80000000u) ? -v : v;
+    Ys[r * ld + c] = pk_get(PKj, pm, ni + r, c, nif, nbf);
   }
-  for (int r = tid; r < nb; r += CND_THREADS) Ys[r * ld + ni] = bj[ni + r];
+  for (int r = tid; r < nb; r += CND_THREADS) {
+    uint32_t m = pm[ni + r];
+    double v = bj[m & 0x7fffffffu];
+    Ys[r * ld + ni] = (m & 0x80000000u) ? -v : v;
+  }
   __syncthreads();
   // ---- Cholesky K_bb = L L^T ----
   for (int k = 0; k < nb; ++k) {
@@ -362,7 +371,7 @@ __global__ void __launch_bounds__(CND_THREADS) k_condense(
   for (int64_t idx = tid; idx < nup; idx += CND_THREADS) {
     int a, b;
     upper_decode(idx, a, b);
-    double v = pk_get(PKj, pm, a, b, ni, nb);
+    double v = pk_get(PKj, pm, a, b, nif, nbf);
     double s = 0.0;
     for (int r = 0; r < nb; ++r) s += Ys[r * ld + a] * Ys[r * ld + b];
     S[idx] = v - s;
@@ -381,7 +390,7 @@ __global__ void __launch_bounds__(CND_THREADS) k_condense(
       Z[idx] = S[(int64_t)b * (b + 1) / 2 + a];
     }
     const double* zd = zdofd ? zdofd + zd_off[e] : nullptr;
-    const uint8_t* dm = dmask + (size_t)j * ni;
+    const uint8_t* dm = dmask + (size_t)j * nif;
     for (int l1 = tid; l1 < nc; l1 += CND_THREADS) {
       int k1 = nx[l1];
       double v = bi[k1];
@@ -417,24 +426,30 @@ __global__ void __launch_bounds__(CND_THREADS) k_condense(
 size_t condense_smem(int ni, int nb) {
   return ((size_t)nb * nb + (size_t)nb * (ni + 1) + ni + nb) * sizeof(double);
 }
+// shared memory when Y is kept in global memory (large bubble blocks)
+size_t condense_smem_small(int ni, int nb) {
+  return ((size_t)nb * nb + ni + nb) * sizeof(double);
+}
 
-int launch_condense(int nel, int n, int ni, int nb, const int* d_elist, const double* d_PK,
-                    const double* d_b0, const uint32_t* d_perm, const int* d_nextract,
-                    const int64_t* d_lcon_off, const int64_t* d_elem_nnz,
-                    const int64_t* d_schur_off, const int64_t* d_bub_off,
-                    const int64_t* d_zd_off, const double* d_zdofd, const uint8_t* d_dmask,
-                    double* d_S, double* d_zastif, double* d_zbload, double* d_aschur,
-                    double* d_bschur, int* d_bad_spd, cudaStream_t st) {
+int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
+                    const int* d_nb_e, const double* d_PK, const double* d_b0,
+                    const uint32_t* d_perm, const int* d_nextract, const int64_t* d_lcon_off,
+                    const int64_t* d_elem_nnz, const int64_t* d_schur_off,
+                    const int64_t* d_bub_off, const int64_t* d_zd_off, const double* d_zdofd,
+                    const uint8_t* d_dmask, double* d_S, double* d_zastif, double* d_zbload,
+                    double* d_aschur, double* d_bschur, double* d_Yg, int* d_bad_spd,
+                    cudaStream_t st) {
   if (nel <= 0) return 0;
-  size_t smem = condense_smem(ni, nb);
+  size_t smem = d_Yg ? condense_smem_small(nif, nbf) : condense_smem(nif, nbf);
   if (smem > 227 * 1024) return -2;
   if (cudaFuncSetAttribute(k_condense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
-  k_condense<<<nel, CND_THREADS, smem, st>>>(n, ni, nb, d_elist, d_PK, d_b0, d_perm, d_nextract,
-                                              d_lcon_off, d_elem_nnz, d_schur_off, d_bub_off,
-                                              d_zd_off, d_zdofd, d_dmask, d_S, d_zastif, d_zbload,
-                                              d_aschur, d_bschur, d_bad_spd);
+  k_condense<<<nel, CND_THREADS, smem, st>>>(nfull, nif, nbf, d_elist, d_ni_e, d_nb_e, d_PK, d_b0,
+                                              d_perm, d_nextract, d_lcon_off, d_elem_nnz,
+                                              d_schur_off, d_bub_off, d_zd_off, d_zdofd, d_dmask,
+                                              d_S, d_zastif, d_zbload, d_aschur, d_bschur,
+                                              d_Yg, d_bad_spd);
   return 0;
 }
 

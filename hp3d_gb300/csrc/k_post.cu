@@ -18,8 +18,8 @@
 namespace hp3dg {
 
 // one block per element
-__global__ void k_backsub(int ni, int nb, const int* __restrict__ elist,
-                          const int* __restrict__ nextract, const int64_t* __restrict__ lcon_off,
+__global__ void k_backsub(const int* __restrict__ elist, const int* __restrict__ ni_e,
+                          const int* __restrict__ nb_e, const int* __restrict__ nextract, const int64_t* __restrict__ lcon_off,
                           const int* __restrict__ lcon, const double* __restrict__ xglob,
                           const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
                           const int64_t* __restrict__ schur_off, const int64_t* __restrict__ bub_off,
@@ -27,7 +27,7 @@ __global__ void k_backsub(int ni, int nb, const int* __restrict__ elist,
                           const int64_t* __restrict__ dof_off, double* __restrict__ dofs) {
   extern __shared__ double xi[];
   const int j = blockIdx.x, e = elist[j];
-  const int n = ni + nb;
+  const int ni = ni_e[e], nb = nb_e[e];
   double* out = dofs + dof_off[e];
   // Dirichlet (or zero) values first, then the active dof from the solution
   for (int k = threadIdx.x; k < ni; k += blockDim.x) xi[k] = zdofd ? zdofd[zd_off[e] + k] : 0.0;
@@ -44,18 +44,18 @@ __global__ void k_backsub(int ni, int nb, const int* __restrict__ elist,
     for (int k = 0; k < ni; ++k) s += A[(size_t)k * nb + r] * xi[k];
     out[ni + r] = B[r] - s;
   }
-  (void)n;
 }
 
-void launch_backsub(int nel, int ni, int nb, const int* d_elist, const int* d_nextract,
-                    const int64_t* d_lcon_off, const int* d_lcon, const double* d_x,
-                    const int64_t* d_zd_off, const double* d_zdofd, const int64_t* d_schur_off,
-                    const int64_t* d_bub_off, const double* d_aschur, const double* d_bschur,
-                    const int64_t* d_dof_off, double* d_dofs, cudaStream_t st) {
+void launch_backsub(int nel, int nif, const int* d_elist, const int* d_ni_e, const int* d_nb_e,
+                    const int* d_nextract, const int64_t* d_lcon_off, const int* d_lcon,
+                    const double* d_x, const int64_t* d_zd_off, const double* d_zdofd,
+                    const int64_t* d_schur_off, const int64_t* d_bub_off, const double* d_aschur,
+                    const double* d_bschur, const int64_t* d_dof_off, double* d_dofs,
+                    cudaStream_t st) {
   if (nel <= 0) return;
-  k_backsub<<<nel, 128, ni * sizeof(double), st>>>(ni, nb, d_elist, d_nextract, d_lcon_off, d_lcon,
-                                                   d_x, d_zd_off, d_zdofd, d_schur_off, d_bub_off,
-                                                   d_aschur, d_bschur, d_dof_off, d_dofs);
+  k_backsub<<<nel, 128, nif * sizeof(double), st>>>(d_elist, d_ni_e, d_nb_e, d_nextract, d_lcon_off,
+                                                    d_lcon, d_x, d_zd_off, d_zdofd, d_schur_off,
+                                                    d_bub_off, d_aschur, d_bschur, d_dof_off, d_dofs);
 }
 
 // manufactured solutions (common/solution.F90:45-134, plus 10 and 12)
@@ -123,8 +123,12 @@ __device__ inline double geom_point(const double* xv, const double* ts, const do
   return r;
 }
 
-// Element dof in the bin's reference enumeration: dref[pi(a)] = sign_a dof_a
-__device__ inline void to_reference(const double* dof, const uint32_t* pm, int n, double* dref) {
+// Element dof in the bin's enumeration: dref[pi(a)] = sign_a dof_a, zero for
+// bin dof the element does not have.  Ends with a block barrier.
+__device__ inline void to_reference(const double* dof, const uint32_t* pm, int n, int nfull,
+                                    double* dref) {
+  for (int r = threadIdx.x; r < nfull; r += blockDim.x) dref[r] = 0.0;
+  __syncthreads();
   for (int a = threadIdx.x; a < n; a += blockDim.x) {
     uint32_t m = pm[a];
     double v = dof[a];
@@ -134,6 +138,7 @@ __device__ inline void to_reference(const double* dof, const uint32_t* pm, int n
 
 // one block per element, one warp per point (lanes split the dof sum)
 __global__ void k_element_error(int nint, int n, int isol, const int* __restrict__ elist,
+                                const int* __restrict__ n_e,
                                 const double* __restrict__ wq, const double* __restrict__ ts,
                                 const double* __restrict__ tg, const double* __restrict__ xvert,
                                 const uint32_t* __restrict__ perm, const int64_t* __restrict__ dof_off,
@@ -144,7 +149,7 @@ __global__ void k_element_error(int nint, int n, int isol, const int* __restrict
   __shared__ double red[2][32];
   const int j = blockIdx.x, e = elist[j];
   if (threadIdx.x < 24) xv[threadIdx.x] = xvert[(size_t)e * 24 + threadIdx.x];
-  to_reference(dofs + dof_off[e], perm + (size_t)j * n, n, dref);
+  to_reference(dofs + dof_off[e], perm + (size_t)j * n, n_e[e], n, dref);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double e2 = 0.0, r2 = 0.0;
@@ -183,12 +188,13 @@ __global__ void k_element_error(int nint, int n, int isol, const int* __restrict
   }
 }
 
-void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+                          const double* d_wq,
                           const double* d_shap, const double* d_grad, const double* d_xvert,
                           const uint32_t* d_perm, const int64_t* d_dof_off, const double* d_dofs,
                           double* d_err2, double* d_nrm2, cudaStream_t st) {
   if (nel <= 0) return;
-  k_element_error<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_wq, d_shap, d_grad,
+  k_element_error<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_n_e, d_wq, d_shap, d_grad,
                                                         d_xvert, d_perm, d_dof_off, d_dofs, d_err2,
                                                         d_nrm2);
 }
@@ -223,6 +229,7 @@ __device__ inline void source_grad(int isol, const double* X, double& f, double*
 }
 
 __global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ elist,
+                          const int* __restrict__ n_e,
                           const double* __restrict__ wq, const double* __restrict__ ts,
                           const double* __restrict__ tg, const double* __restrict__ xvert,
                           const double* __restrict__ kappa, const uint32_t* __restrict__ perm,
@@ -233,7 +240,7 @@ __global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ eli
   __shared__ double red[8][25];
   const int j = blockIdx.x, e = elist[j];
   if (threadIdx.x < 24) xv[threadIdx.x] = xvert[(size_t)e * 24 + threadIdx.x];
-  to_reference(dofs + dof_off[e], perm + (size_t)j * n, n, dref);
+  to_reference(dofs + dof_off[e], perm + (size_t)j * n, n_e[e], n, dref);
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   const double kap = kappa[e];
@@ -289,12 +296,13 @@ __global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ eli
   }
 }
 
-void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const double* d_wq,
+void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+                    const double* d_wq,
                     const double* d_shap, const double* d_grad, const double* d_xvert,
                     const double* d_kappa, const uint32_t* d_perm, const int64_t* d_dof_off,
                     const double* d_dofs, double* d_djdk, double* d_djdx, cudaStream_t st) {
   if (nel <= 0) return;
-  k_adjoint<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_wq, d_shap, d_grad,
+  k_adjoint<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_n_e, d_wq, d_shap, d_grad,
                                                   d_xvert, d_kappa, d_perm, d_dof_off, d_dofs, d_djdk,
                                                   d_djdx);
 }

@@ -150,3 +150,59 @@ def random_orientations(mesh, seed=7):
     m["nori_edge"] = rng.integers(0, 2, size=(ne, 12)).astype(np.int32)
     m["nori_face"] = rng.integers(0, 8, size=(ne, 6)).astype(np.int32)
     return m
+
+
+def hp_hexa(n, seed=2024, perturb=0.0, kappa_logrange=(-1, 1), pmax=6, dirichlet=True):
+    """n^3 hexahedra of the unit cube with per-element anisotropic orders.
+
+    Each (px, py, pz) is drawn in 1..pmax from a seeded geometric
+    distribution whose mean grows with the distance of the element centre
+    from the corner (0,0,0), so orders fall toward that corner.  Edge and face
+    orders follow the minimum rule of the reference's adaptivity
+    (adapt/enforce_min_rule.F90): an edge takes the minimum order of the
+    elements sharing it along its direction, a face the minimum of its two
+    elements along each of its axes.  Orientations are 0 (lexicographic
+    grid), so local and global face frames coincide.
+    """
+    m = structured_hexa(n, 1, perturb=perturb, kappa_logrange=kappa_logrange, seed=seed,
+                        dirichlet=dirichlet)
+    rng = np.random.default_rng(seed + 1)
+    ne = m["nelem"]
+    orders = np.zeros((ne, 3), dtype=np.int32)
+    e = 0
+    centres = np.zeros((ne, 3))
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                centres[e] = (np.array([i, j, k]) + 0.5) / n
+                e += 1
+    r = np.linalg.norm(centres, axis=1) / np.sqrt(3.0)
+    mean = 1.0 + (pmax - 1) * r  # mean order 1 at the corner, pmax far away
+    for a in range(3):
+        q = 1.0 / np.maximum(mean, 1.0)  # geometric with mean 1/q on {1,2,...}
+        orders[:, a] = np.minimum(rng.geometric(q), pmax)
+    # min rule over shared edges / faces
+    edge_min = {}
+    face_min = {}
+    for e in range(ne):
+        for q in range(12):
+            g = int(m["nodes"][e, 8 + q])
+            ax = _EDEF[q][0]
+            edge_min[g] = min(edge_min.get(g, 99), int(orders[e, ax]))
+        for q in range(6):
+            g = int(m["nodes"][e, 20 + q])
+            a1, a2 = [(0, 1), (0, 1), (0, 2), (1, 2), (0, 2), (1, 2)][q]
+            cur = face_min.get(g, (99, 99))
+            face_min[g] = (min(cur[0], int(orders[e, a1])), min(cur[1], int(orders[e, a2])))
+    norder = np.zeros((ne, 19), dtype=np.int32)
+    for e in range(ne):
+        for q in range(12):
+            norder[e, q] = edge_min[int(m["nodes"][e, 8 + q])]
+        for q in range(6):
+            o1, o2 = face_min[int(m["nodes"][e, 20 + q])]
+            norder[e, 12 + q] = 10 * o1 + o2
+        norder[e, 18] = 100 * orders[e, 0] + 10 * orders[e, 1] + orders[e, 2]
+    m["norder"] = norder
+    m["p"] = None
+    m["orders"] = orders
+    return m
