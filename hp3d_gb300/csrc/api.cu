@@ -169,6 +169,7 @@ struct hp3dg_ctx {
   bool have_dofs = false;
   cudaEvent_t ev[8] = {};
   float times[6] = {0, 0, 0, 0, 0, 0};
+  cudaGraphExec_t graph = nullptr;  // the captured pass; rebuilt after every submit
 };
 
 namespace {
@@ -184,6 +185,8 @@ void free_bin(Bin& b) {
 }
 
 void free_batch(hp3dg_ctx* c) {
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->graph = nullptr;
   for (auto& b : c->bins) free_bin(b);
   c->bins.clear();
   void* dev[] = {c->d_norder, c->d_nori_e, c->d_nori_f, c->d_nodes, c->d_ndofm, c->d_nextract,
@@ -462,16 +465,73 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   return HP3DG_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Marks a phase boundary for hp3dg_phase_times.  Inside a stream capture the
+// record must be an external event node so that the replayed graph records it.
+void mark(hp3dg_ctx* c, int i, cudaStream_t st, bool capturing) {
+  if (!c->opts.timing) return;
+  if (capturing) cudaEventRecordWithFlags(c->ev[i], st, cudaEventRecordExternal);
+  else cudaEventRecord(c->ev[i], st);
+}
+
+// The per-run work of the pass, enqueued on st: flags reset, per bin the
+// orientation map, geometry, load, (mixed) digit slicing, contraction and
+// condensation, then the global index maps.  Bin tables are built beforehand.
+int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
+  if (cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st) != cudaSuccess) return HP3DG_ERR_CUDA;
+  for (auto& B : c->bins) {
+    int ne = (int)B.elems.size();
+    launch_orient_hexa(ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n,
+                       B.d_perm, st);
+    launch_geom_hexa(ne, B.d_elist, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert,
+                     c->d_kappa, c->opts.isol, B.d_D, B.d_F, c->d_flags, st);
+    launch_load_hexa(ne, B.nint, B.n, B.d_shap, B.d_F, B.d_b0, st);
+    if (c->opts.precision == HP3DG_MIXED)
+      launch_ozaki_slice_d(B.plan, ne, B.nint, B.d_D, B.d_ddig, B.d_dscale, st);
+  }
+  mark(c, 2, st, capturing);
+  for (auto& B : c->bins) {
+    int ne = (int)B.elems.size();
+    if (c->opts.precision == HP3DG_MIXED) {
+      if (launch_ozaki_gemm(B.plan, ne, B.n, B.d_ddig, B.d_dscale, B.d_mdig, B.d_mscale, B.d_PK,
+                            c->d_flags + 2, st))
+        return HP3DG_ERR_CUDA;
+    } else {
+      launch_contract_fp64(ne, B.nint, B.n, B.ni, B.nb, B.d_grad, B.d_D, B.d_PK, st);
+    }
+  }
+  mark(c, 3, st, capturing);
+  for (auto& B : c->bins) {
+    int ne = (int)B.elems.size();
+    if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
+                        B.d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
+                        c->d_bub_off, c->d_zd_off, c->have_zdofd ? c->d_zdofd : nullptr, B.d_dmask,
+                        B.d_S, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur, B.d_Yg,
+                        c->d_flags + 1, st))
+      return HP3DG_ERR_CUDA;
+  }
+  mark(c, 4, st, capturing);
+  launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,
+                    c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon, st);
+  mark(c, 5, st, capturing);
+  return cudaPeekAtLastError() == cudaSuccess ? HP3DG_OK : HP3DG_ERR_CUDA;
+}
+
+}  // namespace
+
+extern "C" {
+
 int hp3dg_batch_run(hp3dg_ctx* c) {
   if (!c) return HP3DG_ERR_ARG;
   if (!c->submitted) return HP3DG_ERR_STATE;
   cudaSetDevice(c->device);
   cudaStream_t st = c->stream;
   int err = 0;
-  CK(cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st));
-  bool tm = c->opts.timing != 0;
-  if (tm) cudaEventRecord(c->ev[0], st);
-  // tables (once per bin)
+  mark(c, 0, st, false);
+  // tables (once per bin; they stay resident across runs)
   for (auto& B : c->bins) {
     if (!B.tables) {
       launch_tables_hexa(B.nord_loc, B.nint, B.n, B.d_xi, B.d_shap, B.d_grad, st);
@@ -490,43 +550,27 @@ int hp3dg_batch_run(hp3dg_ctx* c) {
       B.mtable = true;
     }
   }
-  if (tm) cudaEventRecord(c->ev[1], st);
-  for (auto& B : c->bins) {
-    int ne = (int)B.elems.size();
-    launch_orient_hexa(ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n,
-                       B.d_perm, st);
-    launch_geom_hexa(ne, B.d_elist, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert,
-                     c->d_kappa, c->opts.isol, B.d_D, B.d_F, c->d_flags, st);
-    launch_load_hexa(ne, B.nint, B.n, B.d_shap, B.d_F, B.d_b0, st);
-    if (c->opts.precision == HP3DG_MIXED)
-      launch_ozaki_slice_d(B.plan, ne, B.nint, B.d_D, B.d_ddig, B.d_dscale, st);
-  }
-  if (tm) cudaEventRecord(c->ev[2], st);
-  for (auto& B : c->bins) {
-    int ne = (int)B.elems.size();
-    if (c->opts.precision == HP3DG_MIXED) {
-      if (launch_ozaki_gemm(B.plan, ne, B.n, B.d_ddig, B.d_dscale, B.d_mdig, B.d_mscale, B.d_PK,
-                            c->d_flags + 2, st))
-        return HP3DG_ERR_CUDA;
-    } else {
-      launch_contract_fp64(ne, B.nint, B.n, B.ni, B.nb, B.d_grad, B.d_D, B.d_PK, st);
+  mark(c, 1, st, false);
+  if (c->opts.launch_mode == 1) {
+    int rc = enqueue_pass(c, st, false);
+    if (rc) return rc;
+  } else {
+    if (!c->graph) {
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+      int rc = enqueue_pass(c, st, true);
+      cudaError_t ce = cudaStreamEndCapture(st, &g);
+      if (rc || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : HP3DG_ERR_CUDA;
+      }
+      ce = cudaGraphInstantiate(&c->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (ce != cudaSuccess) { c->graph = nullptr; return HP3DG_ERR_CUDA; }
     }
+    CK(cudaGraphLaunch(c->graph, st));
   }
-  if (tm) cudaEventRecord(c->ev[3], st);
-  for (auto& B : c->bins) {
-    int ne = (int)B.elems.size();
-    if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
-                        B.d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
-                        c->d_bub_off, c->d_zd_off, c->have_zdofd ? c->d_zdofd : nullptr, B.d_dmask,
-                        B.d_S, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur, B.d_Yg,
-                        c->d_flags + 1, st))
-      return HP3DG_ERR_CUDA;
-  }
-  if (tm) cudaEventRecord(c->ev[4], st);
-  launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,
-                    c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon, st);
-  if (tm) cudaEventRecord(c->ev[5], st);
-  if (cudaPeekAtLastError() != cudaSuccess) return HP3DG_ERR_CUDA;
   c->ran = true;
   c->downloaded = false;
   return HP3DG_OK;

@@ -35,7 +35,8 @@ class Opts(ctypes.Structure):
                 ("isol", ctypes.c_int32), ("keep_elem", ctypes.c_int32),
                 ("timing", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("ozaki_radix", ctypes.c_int32), ("ozaki_digits", ctypes.c_int32),
-                ("stc_method", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("stc_method", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 DESC_DTYPE = np.dtype([("etype", np.int32), ("mdle", np.int32), ("norder", np.int32, 19),
@@ -113,7 +114,7 @@ class ElementPass:
     """One batched element pass (a context of the C ABI)."""
 
     def __init__(self, precision=FP64, integration=0, isol=10, keep_elem=False, timing=False,
-                 device=0, ozaki_radix=0, ozaki_digits=0):
+                 device=0, ozaki_radix=0, ozaki_digits=0, graph=True):
         self.L = lib()
         o = Opts()
         o.precision = precision
@@ -124,6 +125,7 @@ class ElementPass:
         o.device = device
         o.ozaki_radix = ozaki_radix
         o.ozaki_digits = ozaki_digits
+        o.launch_mode = 0 if graph else 1
         self.ctx = _vp()
         self._check(self.L.hp3dg_batch_begin(ctypes.byref(o), ctypes.byref(self.ctx)), "begin")
         self.nel = 0

@@ -75,7 +75,10 @@ typedef struct hp3dg_opts {
   int32_t ozaki_digits;/* mixed: digits per operand (0 = default 7) */
   int32_t stc_method;  /* condensation: 0 = Cholesky (the Poisson bubble block
                           is SPD); reserved for an LU variant */
-  int32_t reserved[7];
+  int32_t launch_mode; /* 0 = hp3dg_batch_run replays one CUDA graph of the pass
+                          (captured on the first run after a submit);
+                          1 = direct stream launches */
+  int32_t reserved[6];
 } hp3dg_opts;
 
 /* Element descriptor: what find_order (datstrs/find_order.F90:5),
