@@ -11,6 +11,7 @@
 #include "../../include/hp3dg.h"
 #include "hp3dg_internal.cuh"
 #include "hp3dg_kernels.h"
+#include "hp3dg_simplex.cuh"
 
 #include <cuda_runtime.h>
 
@@ -94,6 +95,104 @@ int hexa_quadrature(const int* nl, int integration, std::vector<double>& xi,
   return (int)w.size();
 }
 
+// set_3Dint_aux TETRA branch (set_3D_int.F90:305-323): order p = max order
+// + INTEGRATION (capped at MAXP), Duffy-collapsed Gauss rule of
+// init_gauss_quadrature (gauss_quadrature.F90:757-787): p+1 points in x and
+// y, p+2 in z, xi = (x(1-y)(1-z), y(1-z), z), w = wx wy wz (1-z)^2 (1-y).
+int tet_quadrature(int pm, int integration, std::vector<double>& xi, std::vector<double>& w) {
+  int np = std::min(pm + integration, MAXP);
+  xi.clear(); w.clear();
+  for (int k = 0; k < np + 2; ++k) {
+    double z = 0.5 * (1.0 + GX[np + 1][k]), wz = 0.5 * GW[np + 1][k];
+    for (int j = 0; j < np + 1; ++j) {
+      double y = 0.5 * (1.0 + GX[np][j]), wy = 0.5 * GW[np][j];
+      for (int i = 0; i < np + 1; ++i) {
+        double x = 0.5 * (1.0 + GX[np][i]), wx = 0.5 * GW[np][i];
+        xi.push_back(x * (1.0 - y) * (1.0 - z));
+        xi.push_back(y * (1.0 - z));
+        xi.push_back(z);
+        w.push_back(wx * wy * wz * ((1.0 - z) * (1.0 - z)) * (1.0 - y));
+      }
+    }
+  }
+  return (int)w.size();
+}
+
+// ---- per element type (element_data.F90 node tables, ndof_nod 808-884) ----
+int type_nvert(int t) { return t == HP3DG_HEXA ? 8 : (t == HP3DG_PRISM ? 6 : 4); }
+int type_nnode(int t) { return t == HP3DG_HEXA ? 26 : (t == HP3DG_PRISM ? 20 : 14); }
+
+// dof per vertex / edge / face node in element node order; returns node count
+int node_ndof(int t, const int* no, int* nd) {
+  if (t == HP3DG_TET) {
+    for (int v = 0; v < 4; ++v) nd[v] = 1;
+    for (int e = 0; e < 6; ++e) nd[4 + e] = no[e] > 1 ? no[e] - 1 : 0;
+    for (int f = 0; f < 4; ++f) nd[10 + f] = tri_ndof(no[6 + f]);
+    return 14;
+  }
+  for (int v = 0; v < 8; ++v) nd[v] = 1;
+  for (int q = 0; q < 12; ++q) nd[8 + q] = no[q] - 1;
+  for (int f = 0; f < 6; ++f) { int h, v; decod2(no[12 + f], h, v); nd[20 + f] = (h - 1) * (v - 1); }
+  return 26;
+}
+int elem_nbub(int t, const int* no) { return t == HP3DG_TET ? tet_nbub(no[10]) : hexa_nbub(no); }
+int elem_ndof(int t, const int* no) { return t == HP3DG_TET ? tet_ndof(no) : hexa_ndof(no); }
+
+// descriptor checks (CheckOrder / the reference's order and orientation ranges)
+int validate_desc(const hp3dg_elem_desc& d, int nnodes) {
+  if (d.etype == HP3DG_HEXA) {
+    for (int i = 0; i < 12; ++i)
+      if (d.norder[i] < 1 || d.norder[i] > MAXP || (d.nori_edge[i] & ~1)) return HP3DG_ERR_BAD_ORDER;
+    for (int f = 0; f < 6; ++f) {
+      int h, v; decod2(d.norder[12 + f], h, v);
+      if (h < 1 || h > MAXP || v < 1 || v > MAXP || d.nori_face[f] < 0 || d.nori_face[f] > 7)
+        return HP3DG_ERR_BAD_ORDER;
+    }
+    int x, y, z; decod3(d.norder[18], x, y, z);
+    if (x < 1 || x > MAXP || y < 1 || y > MAXP || z < 1 || z > MAXP || d.norder[18] > 999)
+      return HP3DG_ERR_BAD_ORDER;
+  } else if (d.etype == HP3DG_TET) {
+    for (int i = 0; i < 11; ++i)
+      if (d.norder[i] < 1 || d.norder[i] > MAXP) return HP3DG_ERR_BAD_ORDER;
+    for (int e = 0; e < 6; ++e)
+      if (d.nori_edge[e] & ~1) return HP3DG_ERR_BAD_ORDER;
+    for (int f = 0; f < 4; ++f)
+      if (d.nori_face[f] < 0 || d.nori_face[f] > 5) return HP3DG_ERR_BAD_ORDER;
+  } else {
+    return HP3DG_ERR_BAD_ORDER;
+  }
+  for (int i = 0; i < type_nnode(d.etype); ++i)
+    if (d.nodes[i] < 0 || d.nodes[i] >= nnodes) return HP3DG_ERR_ARG;
+  return HP3DG_OK;
+}
+
+// Bin of an element: hexa by its per-axis maximum local orders; tet by its
+// maximum order and the orientation class of each triangle face.  full =
+// the bin element's orders, fo = the face orientations of the bin tables.
+void bin_key(const hp3dg_elem_desc& d, std::vector<int>& key, int* full, int* fo) {
+  for (int i = 0; i < 19; ++i) full[i] = 0;
+  for (int f = 0; f < 6; ++f) fo[f] = 0;
+  if (d.etype == HP3DG_TET) {
+    int pm = 0;
+    for (int i = 0; i < 11; ++i) pm = std::max(pm, (int)d.norder[i]);
+    for (int i = 0; i < 11; ++i) full[i] = pm;
+    for (int f = 0; f < 4; ++f) fo[f] = tri_class(d.nori_face[f]);
+    key = {HP3DG_TET, pm, fo[0], fo[1], fo[2], fo[3]};
+    return;
+  }
+  int loc[19];
+  hexa_order_loc(d.norder, d.nori_face, loc);
+  hexa_bin_orders(loc, full);
+  key.assign(full, full + 19);
+  key.insert(key.begin(), HP3DG_HEXA);
+}
+
+int bin_quadrature(int t, const int* full, int integration, std::vector<double>& xi,
+                   std::vector<double>& w) {
+  if (t == HP3DG_TET) return tet_quadrature(full[0], integration, xi, w);
+  return hexa_quadrature(full, integration, xi, w);
+}
+
 template <class T>
 T* dalloc(size_t count, int* err) {
   if (count == 0) count = 1;
@@ -103,7 +202,9 @@ T* dalloc(size_t count, int* err) {
 }
 
 struct Bin {
+  int etype = HP3DG_HEXA, nvert = 8;
   int nord_loc[19];  // full (bin) orders: per-axis maxima of the member elements' local orders
+  int face_nori[6] = {0, 0, 0, 0, 0, 0};  // face orientations of the tables (tet: class)
   int n = 0, nb = 0, ni = 0, nint = 0;
   std::vector<int> elems;
   std::vector<double> xi, wq;
@@ -135,7 +236,7 @@ struct hp3dg_ctx {
   int nel = 0, nnodes = 0;
   bool submitted = false, ran = false, downloaded = false;
   int last_bad = -1;
-  std::vector<int> n_e, nb_e, ni_e, bin_of, pos_in_bin;
+  std::vector<int> n_e, nb_e, ni_e, bin_of, pos_in_bin, etype_e;
   std::vector<int64_t> elem_nnz, lcon_off, schur_off, bub_off, zd_off;
   std::vector<int> nextract;
   std::vector<Bin> bins;
@@ -280,7 +381,7 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   c->nel = nel;
   c->nnodes = nnodes;
   c->n_e.assign(nel, 0); c->nb_e.assign(nel, 0); c->ni_e.assign(nel, 0);
-  c->bin_of.assign(nel, 0); c->pos_in_bin.assign(nel, 0);
+  c->bin_of.assign(nel, 0); c->pos_in_bin.assign(nel, 0); c->etype_e.assign(nel, 0);
   c->elem_nnz.assign(nel + 1, 0); c->lcon_off.assign(nel + 1, 0);
   c->schur_off.assign(nel + 1, 0); c->bub_off.assign(nel + 1, 0); c->zd_off.assign(nel + 1, 0);
   c->nextract.clear();
@@ -290,27 +391,19 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   c->last_bad = -1;
   for (int e = 0; e < nel; ++e) {
     const hp3dg_elem_desc& d = desc[e];
-    if (d.etype != HP3DG_HEXA) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
-    for (int i = 0; i < 12; ++i)
-      if (d.norder[i] < 1 || d.norder[i] > MAXP || (d.nori_edge[i] & ~1)) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
-    for (int f = 0; f < 6; ++f) {
-      int h, v; decod2(d.norder[12 + f], h, v);
-      if (h < 1 || h > MAXP || v < 1 || v > MAXP || d.nori_face[f] < 0 || d.nori_face[f] > 7) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
-    }
-    {
-      int x, y, z; decod3(d.norder[18], x, y, z);
-      if (x < 1 || x > MAXP || y < 1 || y > MAXP || z < 1 || z > MAXP || d.norder[18] > 999) { c->last_bad = e; return HP3DG_ERR_BAD_ORDER; }
-    }
-    for (int i = 0; i < 26; ++i)
-      if (d.nodes[i] < 0 || d.nodes[i] >= nnodes) { c->last_bad = e; return HP3DG_ERR_ARG; }
+    int vr = validate_desc(d, nnodes);
+    if (vr != HP3DG_OK) { c->last_bad = e; return vr; }
+    const int t = d.etype;
+    c->etype_e[e] = t;
     std::copy(d.norder, d.norder + 19, &norder[19 * (size_t)e]);
     std::copy(d.nori_edge, d.nori_edge + 12, &nori_e[12 * (size_t)e]);
     std::copy(d.nori_face, d.nori_face + 6, &nori_f[6 * (size_t)e]);
-    std::copy(d.nodes, d.nodes + 26, &nodes[26 * (size_t)e]);
-    int loc[19], full[19];
-    hexa_order_loc(d.norder, d.nori_face, loc);
-    hexa_bin_orders(loc, full);
-    std::vector<int> key(full, full + 19);
+    const int nn = type_nnode(t);
+    // slots beyond the type's node count are padding (-1: skipped by the index maps)
+    for (int i = 0; i < 26; ++i) nodes[26 * (size_t)e + i] = i < nn ? d.nodes[i] : -1;
+    std::vector<int> key;
+    int full[19], fo[6];
+    bin_key(d, key, full, fo);
     auto it = binmap.find(key);
     int b;
     if (it == binmap.end()) {
@@ -318,11 +411,14 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
       binmap[key] = b;
       c->bins.emplace_back();
       Bin& B = c->bins.back();
+      B.etype = t;
+      B.nvert = type_nvert(t);
       std::copy(full, full + 19, B.nord_loc);
-      B.n = hexa_ndof(full);
-      B.nb = hexa_nbub(full);
+      std::copy(fo, fo + 6, B.face_nori);
+      B.n = elem_ndof(t, full);
+      B.nb = elem_nbub(t, full);
       B.ni = B.n - B.nb;
-      B.nint = hexa_quadrature(full, c->opts.integration, B.xi, B.wq);
+      B.nint = bin_quadrature(t, full, c->opts.integration, B.xi, B.wq);
       if (condense_smem_small(B.ni, B.nb) > 227 * 1024) { c->last_bad = e; free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
     } else {
       b = it->second;
@@ -332,19 +428,17 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
     c->bins[b].elems.push_back(e);
     // per-node dof counts (ndof_nod) in element node order, Dirichlet skipped
     int nd[26];
-    for (int v = 0; v < 8; ++v) nd[v] = 1;
-    for (int q = 0; q < 12; ++q) nd[8 + q] = d.norder[q] - 1;
-    for (int f = 0; f < 6; ++f) { int h, v; decod2(d.norder[12 + f], h, v); nd[20 + f] = (h - 1) * (v - 1); }
+    node_ndof(t, d.norder, nd);
     int first[26], ni = 0;
-    for (int i = 0; i < 26; ++i) { first[i] = ni; ni += nd[i]; }
+    for (int i = 0; i < nn; ++i) { first[i] = ni; ni += nd[i]; }
     int nrdofc = 0;
     for (int i = 25; i >= 0; --i) {
-      int act = d.bcflag[i] ? 0 : nd[i];
+      int act = (i >= nn || d.bcflag[i]) ? 0 : nd[i];
       ndofm[26 * (size_t)e + i] = act;
       for (int q = 0; q < act; ++q) c->nextract.push_back(first[i] + q);
       nrdofc += act;
     }
-    c->nb_e[e] = hexa_nbub(d.norder); c->ni_e[e] = ni; c->n_e[e] = ni + c->nb_e[e];
+    c->nb_e[e] = elem_nbub(t, d.norder); c->ni_e[e] = ni; c->n_e[e] = ni + c->nb_e[e];
     c->elem_nnz[e + 1] = c->elem_nnz[e] + (int64_t)nrdofc * nrdofc;
     c->lcon_off[e + 1] = c->lcon_off[e] + nrdofc;
     c->schur_off[e + 1] = c->schur_off[e] + (int64_t)c->nb_e[e] * ni;
@@ -442,12 +536,10 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
       std::vector<uint8_t> dm(ne * B.ni, 0);  // element ni <= bin ni
       for (size_t j = 0; j < ne; ++j) {
         const hp3dg_elem_desc& d = desc[B.elems[j]];
-        int k = 0;
-        for (int i = 0; i < 26; ++i) {
-          int ndi = i < 8 ? 1 : (i < 20 ? d.norder[i - 8] - 1 : 0);
-          if (i >= 20) { int h, v; decod2(d.norder[12 + i - 20], h, v); ndi = (h - 1) * (v - 1); }
-          for (int q = 0; q < ndi; ++q) dm[j * B.ni + k++] = d.bcflag[i] ? 1 : 0;
-        }
+        int nd[26];
+        int nn = node_ndof(d.etype, d.norder, nd), k = 0;
+        for (int i = 0; i < nn; ++i)
+          for (int q = 0; q < nd[i]; ++q) dm[j * B.ni + k++] = d.bcflag[i] ? 1 : 0;
       }
       CK(cudaMemcpyAsync(B.d_dmask, dm.data(), dm.size(), cudaMemcpyHostToDevice, st));
       CK(cudaStreamSynchronize(st));
@@ -484,10 +576,10 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
   if (cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st) != cudaSuccess) return HP3DG_ERR_CUDA;
   for (auto& B : c->bins) {
     int ne = (int)B.elems.size();
-    launch_orient_hexa(ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n,
-                       B.d_perm, st);
-    launch_geom_hexa(ne, B.d_elist, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert,
-                     c->d_kappa, c->opts.isol, B.d_D, B.d_F, c->d_flags, st);
+    launch_orient(B.etype, ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n,
+                  B.d_perm, st);
+    launch_geom(ne, B.nvert, B.d_elist, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert,
+                c->d_kappa, c->opts.isol, B.d_D, B.d_F, c->d_flags, st);
     launch_load_hexa(ne, B.nint, B.n, B.d_shap, B.d_F, B.d_b0, st);
     if (c->opts.precision == HP3DG_MIXED)
       launch_ozaki_slice_d(B.plan, ne, B.nint, B.d_D, B.d_ddig, B.d_dscale, st);
@@ -534,7 +626,7 @@ int hp3dg_batch_run(hp3dg_ctx* c) {
   // tables (once per bin; they stay resident across runs)
   for (auto& B : c->bins) {
     if (!B.tables) {
-      launch_tables_hexa(B.nord_loc, B.nint, B.n, B.d_xi, B.d_shap, B.d_grad, st);
+      launch_tables(B.etype, B.nord_loc, B.face_nori, B.nint, B.n, B.d_xi, B.d_shap, B.d_grad, st);
       B.tables = true;
     }
     if (c->opts.precision == HP3DG_MIXED && !B.mtable) {
@@ -653,12 +745,16 @@ int hp3dg_get_elem(const hp3dg_ctx* c, int32_t iel, double* aloc, int32_t ld, do
   cudaMemcpy(of, c->d_nori_f + 6 * (size_t)iel, sizeof(of), cudaMemcpyDeviceToHost);
   const double* PK = c->h_PK + c->pk_off[iel];
   const double* b0 = c->h_b0 + c->b0_off[iel];
+  const bool tet = B.etype == HP3DG_TET;
+  auto dmap = [&](int a) {
+    return tet ? tet_dof_map(a, no, oe, of, B.nord_loc[0]) : hexa_dof_map(a, no, oe, of, B.nord_loc);
+  };
   for (int a = 0; a < n; ++a) {
-    uint32_t ma = hexa_dof_map(a, no, oe, of, B.nord_loc);
+    uint32_t ma = dmap(a);
     int ra = (int)(ma & 0x7fffffffu);
     bloc[a] = (ma & 0x80000000u) ? -b0[ra] : b0[ra];
     for (int b = 0; b < n; ++b) {
-      uint32_t mb = hexa_dof_map(b, no, oe, of, B.nord_loc);
+      uint32_t mb = dmap(b);
       int rb = (int)(mb & 0x7fffffffu);
       double v = PK[pk_index(ra, rb, ni, nb)];
       aloc[(size_t)b * ld + a] = ((ma ^ mb) & 0x80000000u) ? -v : v;
@@ -752,7 +848,7 @@ int hp3dg_element_error(hp3dg_ctx* c, int32_t isol, double* err2, double* nrm2) 
   if (err) return err;
   for (auto& B : c->bins) {
     if (!B.etable) {
-      B.nint_err = hexa_quadrature(B.nord_loc, 2, B.xi_err, B.wq_err);
+      B.nint_err = bin_quadrature(B.etype, B.nord_loc, 2, B.xi_err, B.wq_err);
       B.d_xi_err = dalloc<double>(B.xi_err.size(), &err);
       B.d_wq_err = dalloc<double>(B.wq_err.size(), &err);
       B.d_shap_err = dalloc<double>((size_t)B.nint_err * B.n, &err);
@@ -760,11 +856,12 @@ int hp3dg_element_error(hp3dg_ctx* c, int32_t isol, double* err2, double* nrm2) 
       if (err) return err;
       CK(cudaMemcpyAsync(B.d_xi_err, B.xi_err.data(), B.xi_err.size() * 8, cudaMemcpyHostToDevice, st));
       CK(cudaMemcpyAsync(B.d_wq_err, B.wq_err.data(), B.wq_err.size() * 8, cudaMemcpyHostToDevice, st));
-      launch_tables_hexa(B.nord_loc, B.nint_err, B.n, B.d_xi_err, B.d_shap_err, B.d_grad_err, st);
+      launch_tables(B.etype, B.nord_loc, B.face_nori, B.nint_err, B.n, B.d_xi_err, B.d_shap_err,
+                    B.d_grad_err, st);
       CK(cudaStreamSynchronize(st));
       B.etable = true;
     }
-    launch_element_error((int)B.elems.size(), B.nint_err, B.n, isol, B.d_elist, c->d_n_e, B.d_wq_err,
+    launch_element_error((int)B.elems.size(), B.nvert, B.nint_err, B.n, isol, B.d_elist, c->d_n_e, B.d_wq_err,
                          B.d_shap_err, B.d_grad_err, c->d_xvert, B.d_perm, c->d_dof_off, c->d_dofs,
                          c->d_err2, c->d_nrm2, st);
   }
@@ -787,7 +884,7 @@ int hp3dg_adjoint(hp3dg_ctx* c, const double* dofs, double* djdkappa, double* dj
   if (err) return err;
   if (dofs) CK(cudaMemcpyAsync(c->d_dofs, dofs, c->dof_off[c->nel] * 8, cudaMemcpyHostToDevice, st));
   for (auto& B : c->bins)
-    launch_adjoint((int)B.elems.size(), B.nint, B.n, c->opts.isol, B.d_elist, c->d_n_e, B.d_wq, B.d_shap,
+    launch_adjoint((int)B.elems.size(), B.nvert, B.nint, B.n, c->opts.isol, B.d_elist, c->d_n_e, B.d_wq, B.d_shap,
                    B.d_grad, c->d_xvert, c->d_kappa, B.d_perm, c->d_dof_off, c->d_dofs, c->d_djdk,
                    c->d_djdx, st);
   CK(cudaMemcpyAsync(djdkappa, c->d_djdk, (size_t)c->nel * 8, cudaMemcpyDeviceToHost, st));

@@ -5,15 +5,21 @@
 
 namespace hp3dg {
 
-void launch_tables_hexa(const int* nord_loc, int nint, int n, const double* d_xi,
-                        double* d_shap, double* d_grad, cudaStream_t st);
-void launch_orient_hexa(int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
-                        const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
-                        cudaStream_t st);
-void launch_geom_hexa(int nel, const int* d_elist, int nint, int n, const double* d_wq,
-                      const double* d_shap, const double* d_grad, const double* d_xvert,
-                      const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
-                      cudaStream_t st);
+// element types as in the C ABI (HP3DG_HEXA / HP3DG_PRISM / HP3DG_TET)
+constexpr int ETYPE_HEXA = 1, ETYPE_PRISM = 2, ETYPE_TET = 3;
+
+// bin tables: nord_loc = the bin's full orders (hexa: 19 local orders; tet:
+// every entry the bin order), face_nori = orientation of each face in the
+// tables (tets: the orientation class of each triangle face)
+void launch_tables(int etype, const int* nord_loc, const int* face_nori, int nint, int n,
+                   const double* d_xi, double* d_shap, double* d_grad, cudaStream_t st);
+void launch_orient(int etype, int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
+                   const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
+                   cudaStream_t st);
+void launch_geom(int nel, int nvert, const int* d_elist, int nint, int n, const double* d_wq,
+                 const double* d_shap, const double* d_grad, const double* d_xvert,
+                 const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
+                 cudaStream_t st);
 void launch_load_hexa(int nel, int nint, int n, const double* d_shap, const double* d_F,
                       double* d_b0, cudaStream_t st);
 void launch_contract_fp64(int nel, int nint, int n, int ni, int nb, const double* d_grad,
@@ -40,12 +46,14 @@ void launch_backsub(int nel, int nif, const int* d_elist, const int* d_ni_e, con
                     const int64_t* d_zd_off, const double* d_zdofd, const int64_t* d_schur_off,
                     const int64_t* d_bub_off, const double* d_aschur, const double* d_bschur,
                     const int64_t* d_dof_off, double* d_dofs, cudaStream_t st);
-void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+void launch_element_error(int nel, int nvert, int nint, int n, int isol, const int* d_elist,
+                          const int* d_n_e,
                           const double* d_wq,
                           const double* d_shap, const double* d_grad, const double* d_xvert,
                           const uint32_t* d_perm, const int64_t* d_dof_off, const double* d_dofs,
                           double* d_err2, double* d_nrm2, cudaStream_t st);
-void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+void launch_adjoint(int nel, int nvert, int nint, int n, int isol, const int* d_elist,
+                    const int* d_n_e,
                     const double* d_wq,
                     const double* d_shap, const double* d_grad, const double* d_xvert,
                     const double* d_kappa, const uint32_t* d_perm, const int64_t* d_dof_off,

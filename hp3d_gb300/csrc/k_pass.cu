@@ -2,11 +2,12 @@
 //
 // Each kernel restates one stage of hp3D's per-element work as a batched
 // device pass over one bin (elements with the same type and local orders):
-//   k_tables_hexa   shape3DHHexa at the set_3D_int points, once per bin
-//                   (shape_1/Hexahedron.F90:33-210, quadrature/set_3D_int.F90)
-//   k_orient_hexa   signed permutation of the element's oriented dof onto the
-//                   bin's reference enumeration (shape_1/Orient.F90:9-116)
-//   k_geom_hexa     geom3D + geom + getf per point (util/geom3D.F90:30-112,
+//   k_tables_*      shape3DHHexa / shape3DHTet at the set_3D_int points, once
+//                   per bin (shape_1/Hexahedron.F90:33-210,
+//                   shape_1/Tetrahedron.F90:33-234, quadrature/set_3D_int.F90)
+//   k_orient_*      signed permutation of the element's oriented dof onto the
+//                   bin's reference enumeration (shape_1/Orient.F90:9-162)
+//   k_geom          geom3D + geom + getf per point (util/geom3D.F90:30-112,
 //                   util/geom.F90:30-138, common/getf.F90:63)
 //   k_load_hexa     load vector (elem_opt.F90:118)
 //   k_contract_fp64 B^T D B in FP64 (elem_opt.F90:86-137 DSYRK)
@@ -15,6 +16,7 @@
 //   k_index_*       NFIRST_DOF / LCON (solver/omp_mumps/mumps_sc.F90:149-157, 266-299)
 #include "hp3dg_internal.cuh"
 #include "hp3dg_kernels.h"
+#include "hp3dg_simplex.cuh"
 
 #include <math.h>
 
@@ -34,11 +36,26 @@ __global__ void k_tables_hexa(Ord19 ord, int nint, int n, const double* __restri
   hexa_shape0(x, ord.v, tab_shap + (size_t)l * n, tab_grad + (size_t)l * 3 * n, n);
 }
 
-void launch_tables_hexa(const int* nord_loc, int nint, int n, const double* d_xi,
-                        double* d_shap, double* d_grad, cudaStream_t st) {
-  Ord19 o;
+// tetrahedron tables: edge orientation 0, face orientations = the bin's
+// orientation classes (fo)
+__global__ void k_tables_tet(Ord19 ord, Ord19 fo, int nint, int n, const double* __restrict__ xi,
+                             double* __restrict__ tab_shap, double* __restrict__ tab_grad) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nint) return;
+  double x[3] = {xi[3 * l], xi[3 * l + 1], xi[3 * l + 2]};
+  const int oe[6] = {0, 0, 0, 0, 0, 0};
+  tet_shape(x, ord.v, oe, fo.v, tab_shap + (size_t)l * n, tab_grad + (size_t)l * 3 * n, n);
+}
+
+void launch_tables(int etype, const int* nord_loc, const int* face_nori, int nint, int n,
+                   const double* d_xi, double* d_shap, double* d_grad, cudaStream_t st) {
+  Ord19 o, f;
   for (int i = 0; i < 19; ++i) o.v[i] = nord_loc[i];
-  k_tables_hexa<<<(nint + 63) / 64, 64, 0, st>>>(o, nint, n, d_xi, d_shap, d_grad);
+  for (int i = 0; i < 19; ++i) f.v[i] = i < 6 ? face_nori[i] : 0;
+  if (etype == ETYPE_TET)
+    k_tables_tet<<<(nint + 63) / 64, 64, 0, st>>>(o, f, nint, n, d_xi, d_shap, d_grad);
+  else
+    k_tables_hexa<<<(nint + 63) / 64, 64, 0, st>>>(o, nint, n, d_xi, d_shap, d_grad);
 }
 
 // ---------------------------------------------------------------------------
@@ -60,13 +77,34 @@ __global__ void k_orient_hexa(int nel, const int* __restrict__ elist, const int*
     perm[(size_t)j * nfull + a] = a < n ? hexa_dof_map(a, no, oe, of, full.v) : 0u;
 }
 
-void launch_orient_hexa(int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
-                        const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
-                        cudaStream_t st) {
+__global__ void k_orient_tet(int nel, const int* __restrict__ elist, const int* __restrict__ norder,
+                             const int* __restrict__ nori_e, const int* __restrict__ nori_f, int pm,
+                             int nfull, uint32_t* __restrict__ perm) {
+  int j = blockIdx.x;
+  if (j >= nel) return;
+  int e = elist[j];
+  __shared__ int no[19], oe[12], of[6];
+  if (threadIdx.x < 19) no[threadIdx.x] = norder[19 * e + threadIdx.x];
+  if (threadIdx.x < 12) oe[threadIdx.x] = nori_e[12 * e + threadIdx.x];
+  if (threadIdx.x < 6) of[threadIdx.x] = nori_f[6 * e + threadIdx.x];
+  __syncthreads();
+  const int n = tet_ndof(no);
+  for (int a = threadIdx.x; a < nfull; a += blockDim.x)
+    perm[(size_t)j * nfull + a] = a < n ? tet_dof_map(a, no, oe, of, pm) : 0u;
+}
+
+void launch_orient(int etype, int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
+                   const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
+                   cudaStream_t st) {
+  if (nel <= 0) return;
+  if (etype == ETYPE_TET) {
+    k_orient_tet<<<nel, 128, 0, st>>>(nel, d_elist, d_norder, d_nori_e, d_nori_f, full[0], nfull,
+                                      d_perm);
+    return;
+  }
   Ord19 o;
   for (int i = 0; i < 19; ++i) o.v[i] = full[i];
-  if (nel > 0)
-    k_orient_hexa<<<nel, 128, 0, st>>>(nel, d_elist, d_norder, d_nori_e, d_nori_f, o, nfull, d_perm);
+  k_orient_hexa<<<nel, 128, 0, st>>>(nel, d_elist, d_norder, d_nori_e, d_nori_f, o, nfull, d_perm);
 }
 
 // ---------------------------------------------------------------------------
@@ -91,7 +129,8 @@ __device__ inline double getf_dev(int isol, double x1, double x2, double x3) {
   }
 }
 
-__global__ void k_geom_hexa(int nel, const int* __restrict__ elist, int nint, int n,
+template <int NV>
+__global__ void k_geom(int nel, const int* __restrict__ elist, int nint, int n,
                             const double* __restrict__ wq, const double* __restrict__ tab_shap,
                             const double* __restrict__ tab_grad, const double* __restrict__ xvert,
                             const double* __restrict__ kappa, int isol, double* __restrict__ D,
@@ -108,7 +147,7 @@ __global__ void k_geom_hexa(int nel, const int* __restrict__ elist, int nint, in
   const double* gs = tab_shap + (size_t)l * n;
   const double* gg = tab_grad + (size_t)l * 3 * n;
 #pragma unroll
-  for (int v = 0; v < 8; ++v) {
+  for (int v = 0; v < NV; ++v) {
     double s = gs[v];
     double g0 = gg[v], g1 = gg[n + v], g2 = gg[2 * n + v];
 #pragma unroll
@@ -148,13 +187,20 @@ __global__ void k_geom_hexa(int nel, const int* __restrict__ elist, int nint, in
   F[(size_t)j * nint + l] = getf_dev(isol, X[0], X[1], X[2]) * weight;
 }
 
-void launch_geom_hexa(int nel, const int* d_elist, int nint, int n, const double* d_wq,
-                      const double* d_shap, const double* d_grad, const double* d_xvert,
-                      const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
-                      cudaStream_t st) {
+void launch_geom(int nel, int nvert, const int* d_elist, int nint, int n, const double* d_wq,
+                 const double* d_shap, const double* d_grad, const double* d_xvert,
+                 const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
+                 cudaStream_t st) {
   if (nel <= 0) return;
   dim3 g((nint + 127) / 128, nel);
-  k_geom_hexa<<<g, 128, 0, st>>>(nel, d_elist, nint, n, d_wq, d_shap, d_grad, d_xvert, d_kappa,
+  if (nvert == 4)
+    k_geom<4><<<g, 128, 0, st>>>(nel, d_elist, nint, n, d_wq, d_shap, d_grad, d_xvert, d_kappa,
+                                 isol, d_D, d_F, d_bad);
+  else if (nvert == 6)
+    k_geom<6><<<g, 128, 0, st>>>(nel, d_elist, nint, n, d_wq, d_shap, d_grad, d_xvert, d_kappa,
+                                 isol, d_D, d_F, d_bad);
+  else
+    k_geom<8><<<g, 128, 0, st>>>(nel, d_elist, nint, n, d_wq, d_shap, d_grad, d_xvert, d_kappa,
                                  isol, d_D, d_F, d_bad);
 }
 
@@ -458,14 +504,14 @@ int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, co
 // ---------------------------------------------------------------------------
 __global__ void k_first_visit(int64_t nslots, const int* __restrict__ nodes, int* __restrict__ first) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s < nslots) atomicMin(&first[nodes[s]], (int)s);
+  if (s < nslots && nodes[s] >= 0) atomicMin(&first[nodes[s]], (int)s);
 }
 
 __global__ void k_slot_counts(int64_t nslots, const int* __restrict__ nodes,
                               const int* __restrict__ first, const int* __restrict__ ndofm,
                               int* __restrict__ cnt) {
   int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (s < nslots) cnt[s] = (first[nodes[s]] == (int)s) ? ndofm[s] : 0;
+  if (s < nslots) cnt[s] = (nodes[s] >= 0 && first[nodes[s]] == (int)s) ? ndofm[s] : 0;
 }
 
 // block-local exclusive scan (1024 per block) + block totals
@@ -516,6 +562,7 @@ __global__ void k_lcon(int nel, int nnode, const int* __restrict__ nodes, const 
   int64_t l = lcon_off[e];
   for (int i = nnode - 1; i >= 0; --i) {
     int g = nodes[(size_t)e * nnode + i];
+    if (g < 0) continue;  // padding slot of an element with fewer nodes
     int nd = ndofm[(size_t)e * nnode + i];
     int base = nfirst[g];
     for (int q = 1; q <= nd; ++q) lcon[l++] = base + q;

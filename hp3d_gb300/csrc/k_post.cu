@@ -9,7 +9,8 @@
 //                    manufactured solution (element/util/compute_error.F90:
 //                    226-360, H1 branch, INTEGRATION = 2 rule)
 //   k_adjoint        compliance sensitivities: dJ/dkappa_e and dJ/dx of the
-//                    element's vertices (differentiation)
+//                    element's vertices (vertex slots beyond the element
+//                    type's vertex count are written as zero)
 #include "hp3dg_internal.cuh"
 #include "hp3dg_kernels.h"
 
@@ -95,12 +96,12 @@ __device__ inline void exact_dev(int isol, const double* X, double& u, double* g
   }
 }
 
-// geometry at point l from the 8 vertex functions of the bin's tables
-__device__ inline double geom_point(const double* xv, const double* ts, const double* tg, int n,
-                                    double* X, double a[3][3]) {
+// geometry at point l from the nvert vertex functions of the bin's tables
+__device__ inline double geom_point(const double* xv, int nvert, const double* ts, const double* tg,
+                                    int n, double* X, double a[3][3]) {
   double dx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
   X[0] = X[1] = X[2] = 0.0;
-  for (int v = 0; v < 8; ++v) {
+  for (int v = 0; v < nvert; ++v) {
     double s = ts[v], g0 = tg[v], g1 = tg[n + v], g2 = tg[2 * n + v];
     for (int i = 0; i < 3; ++i) {
       double xi_ = xv[3 * v + i];
@@ -137,7 +138,7 @@ __device__ inline void to_reference(const double* dof, const uint32_t* pm, int n
 }
 
 // one block per element, one warp per point (lanes split the dof sum)
-__global__ void k_element_error(int nint, int n, int isol, const int* __restrict__ elist,
+__global__ void k_element_error(int nvert, int nint, int n, int isol, const int* __restrict__ elist,
                                 const int* __restrict__ n_e,
                                 const double* __restrict__ wq, const double* __restrict__ ts,
                                 const double* __restrict__ tg, const double* __restrict__ xvert,
@@ -167,7 +168,7 @@ __global__ void k_element_error(int nint, int n, int isol, const int* __restrict
     }
     if (lane == 0) {
       double X[3], a[3][3];
-      double rjac = geom_point(xv, s, g, n, X, a);
+      double rjac = geom_point(xv, nvert, s, g, n, X, a);
       double gx[3];
       for (int c = 0; c < 3; ++c) gx[c] = gu[0] * a[0][c] + gu[1] * a[1][c] + gu[2] * a[2][c];
       double ue, ge[3];
@@ -188,13 +189,14 @@ __global__ void k_element_error(int nint, int n, int isol, const int* __restrict
   }
 }
 
-void launch_element_error(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+void launch_element_error(int nel, int nvert, int nint, int n, int isol, const int* d_elist,
+                          const int* d_n_e,
                           const double* d_wq,
                           const double* d_shap, const double* d_grad, const double* d_xvert,
                           const uint32_t* d_perm, const int64_t* d_dof_off, const double* d_dofs,
                           double* d_err2, double* d_nrm2, cudaStream_t st) {
   if (nel <= 0) return;
-  k_element_error<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_n_e, d_wq, d_shap, d_grad,
+  k_element_error<<<nel, 256, n * sizeof(double), st>>>(nvert, nint, n, isol, d_elist, d_n_e, d_wq, d_shap, d_grad,
                                                         d_xvert, d_perm, d_dof_off, d_dofs, d_err2,
                                                         d_nrm2);
 }
@@ -228,7 +230,7 @@ __device__ inline void source_grad(int isol, const double* X, double& f, double*
   }
 }
 
-__global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ elist,
+__global__ void k_adjoint(int nvert, int nint, int n, int isol, const int* __restrict__ elist,
                           const int* __restrict__ n_e,
                           const double* __restrict__ wq, const double* __restrict__ ts,
                           const double* __restrict__ tg, const double* __restrict__ xvert,
@@ -260,7 +262,7 @@ __global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ eli
     }
     if (lane == 0) {
       double X[3], a[3][3];  // a = J^-1: a[i][k] = dxi_i/dx_k
-      double det = geom_point(xv, s, g, n, X, a);
+      double det = geom_point(xv, nvert, s, g, n, X, a);
       double w = wq[l];
       double v[3], q[3];
       for (int c = 0; c < 3; ++c) v[c] = gu[0] * a[0][c] + gu[1] * a[1][c] + gu[2] * a[2][c];
@@ -275,7 +277,7 @@ __global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ eli
         for (int k = 0; k < 3; ++k)
           T[i][k] = -kap * w * det * (a[k][i] * vv - 2.0 * v[i] * q[k]) +
                     2.0 * u * w * f * det * a[k][i];
-      for (int vtx = 0; vtx < 8; ++vtx) {
+      for (int vtx = 0; vtx < nvert; ++vtx) {
         double gv[3] = {g[vtx], g[n + vtx], g[2 * n + vtx]};
         for (int i = 0; i < 3; ++i) {
           double t = T[i][0] * gv[0] + T[i][1] * gv[1] + T[i][2] * gv[2];
@@ -296,13 +298,14 @@ __global__ void k_adjoint(int nint, int n, int isol, const int* __restrict__ eli
   }
 }
 
-void launch_adjoint(int nel, int nint, int n, int isol, const int* d_elist, const int* d_n_e,
+void launch_adjoint(int nel, int nvert, int nint, int n, int isol, const int* d_elist,
+                    const int* d_n_e,
                     const double* d_wq,
                     const double* d_shap, const double* d_grad, const double* d_xvert,
                     const double* d_kappa, const uint32_t* d_perm, const int64_t* d_dof_off,
                     const double* d_dofs, double* d_djdk, double* d_djdx, cudaStream_t st) {
   if (nel <= 0) return;
-  k_adjoint<<<nel, 256, n * sizeof(double), st>>>(nint, n, isol, d_elist, d_n_e, d_wq, d_shap, d_grad,
+  k_adjoint<<<nel, 256, n * sizeof(double), st>>>(nvert, nint, n, isol, d_elist, d_n_e, d_wq, d_shap, d_grad,
                                                   d_xvert, d_kappa, d_perm, d_dof_off, d_dofs, d_djdk,
                                                   d_djdx);
 }

@@ -206,3 +206,153 @@ def hp_hexa(n, seed=2024, perturb=0.0, kappa_logrange=(-1, 1), pmax=6, dirichlet
     m["p"] = None
     m["orders"] = orders
     return m
+
+
+TET = 3
+# tetrahedron local edges / faces (shape_1/BlendProject.F90 ProjectTetE/F)
+TET_EDGES = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
+TET_FACES = [(0, 1, 2), (0, 1, 3), (1, 2, 3), (0, 2, 3)]
+# OrientTri: GS(k) = S(Or(nori, k)) (shape_1/Orient.F90:119-162)
+ORIENT_TRI = [(0, 1, 2), (1, 2, 0), (2, 0, 1), (0, 2, 1), (1, 0, 2), (2, 1, 0)]
+
+
+def tri_orientation(local, glob):
+    """Orientation code o with local[ORIENT_TRI[o][k]] == glob[k]: the
+    element's face functions then use the face node's own vertex order, so
+    neighbours share their traces."""
+    for o, perm in enumerate(ORIENT_TRI):
+        if all(local[perm[k]] == glob[k] for k in range(3)):
+            return o
+    raise ValueError("face vertices do not match")
+
+
+def _on_boundary(pts, n):
+    """A straight edge or flat face lies on a face of the cube [0,n]^3 of
+    grid indices when all its vertices share a coordinate equal to 0 or n."""
+    pts = np.asarray(pts)
+    for c in range(3):
+        if np.all(pts[:, c] == 0) or np.all(pts[:, c] == n):
+            return True
+    return False
+
+
+def _kappa(rng, ne, kappa_logrange):
+    if kappa_logrange is None:
+        return np.ones(ne)
+    lo, hi = kappa_logrange
+    return 10.0 ** rng.uniform(lo, hi, size=ne)
+
+
+def structured_tet(n, p, perturb=0.0, kappa_logrange=None, seed=12345, dirichlet=True,
+                   orders=None):
+    """n^3 cubes of [0,1]^3, each split into the 6 tetrahedra of the Kuhn
+    (Freudenthal) subdivision along its main diagonal, so neighbouring cubes
+    share their face diagonals and the mesh is conforming.
+
+    Element vertices follow the Kuhn path c, c+e_a, c+e_a+e_b, c+(1,1,1),
+    with the last two swapped where that makes the Jacobian positive.  Edge
+    nodes are oriented from the lower to the higher vertex id and face nodes
+    list their vertices in increasing id; each element's codes follow from
+    its local order (tri_orientation).  orders: optional per-element tet
+    order (interior), edges and faces then take the minimum of their
+    elements (min rule); otherwise all orders are p.
+    """
+    rng = np.random.default_rng(seed)
+    nv1 = n + 1
+    h = 1.0 / n
+    idx = np.arange(nv1)
+    I, J, K = np.meshgrid(idx, idx, idx, indexing="ij")
+    coords = np.stack([I.ravel(order="F"), J.ravel(order="F"), K.ravel(order="F")], axis=1)
+    X = coords.astype(np.float64) * h
+    if perturb > 0.0:
+        interior = np.all((coords > 0) & (coords < n), axis=1)
+        d = rng.uniform(-perturb * h, perturb * h, size=X.shape)
+        X[interior] += d[interior]
+    vid = lambda i, j, k: i + nv1 * (j + nv1 * k)  # noqa: E731
+    unit = np.eye(3, dtype=int)
+    perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    tets = []
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                c = np.array([i, j, k])
+                for pa in perms:
+                    path = [c, c + unit[pa[0]], c + unit[pa[0]] + unit[pa[1]], c + 1]
+                    v = [vid(*q) for q in path]
+                    x = X[v]
+                    vol = np.linalg.det(np.stack([x[1] - x[0], x[2] - x[0], x[3] - x[0]]))
+                    if vol < 0:
+                        v[2], v[3] = v[3], v[2]
+                    tets.append(v)
+    ne = len(tets)
+    nverts = nv1 ** 3
+    edge_id, face_id = {}, {}
+    for v in tets:
+        for a, b in TET_EDGES:
+            key = tuple(sorted((v[a], v[b])))
+            if key not in edge_id:
+                edge_id[key] = nverts + len(edge_id)
+    for v in tets:
+        for f in TET_FACES:
+            key = tuple(sorted(v[q] for q in f))
+            if key not in face_id:
+                face_id[key] = nverts + len(edge_id) + len(face_id)
+    nnodes = nverts + len(edge_id) + len(face_id)
+    if orders is None:
+        orders = np.full(ne, p, dtype=np.int32)
+    orders = np.asarray(orders, dtype=np.int32)
+    emin, fmin = {}, {}
+    for e, v in enumerate(tets):
+        for a, b in TET_EDGES:
+            key = tuple(sorted((v[a], v[b])))
+            emin[key] = min(emin.get(key, 99), int(orders[e]))
+        for f in TET_FACES:
+            key = tuple(sorted(v[q] for q in f))
+            fmin[key] = min(fmin.get(key, 99), int(orders[e]))
+    nodes = np.zeros((ne, 26), dtype=np.int32)
+    bcflag = np.zeros((ne, 26), dtype=np.int32)
+    xvert = np.zeros((ne, 8, 3))
+    norder = np.zeros((ne, 19), dtype=np.int32)
+    nori_e = np.zeros((ne, 12), dtype=np.int32)
+    nori_f = np.zeros((ne, 6), dtype=np.int32)
+    for e, v in enumerate(tets):
+        xvert[e, :4] = X[v]
+        for q in range(4):
+            nodes[e, q] = v[q]
+            bcflag[e, q] = int(_on_boundary(coords[[v[q]]], n))
+        for q, (a, b) in enumerate(TET_EDGES):
+            key = tuple(sorted((v[a], v[b])))
+            nodes[e, 4 + q] = edge_id[key]
+            nori_e[e, q] = 0 if v[a] < v[b] else 1
+            norder[e, q] = emin[key]
+            bcflag[e, 4 + q] = int(_on_boundary(coords[list(key)], n))
+        for q, f in enumerate(TET_FACES):
+            loc = [v[r] for r in f]
+            key = tuple(sorted(loc))
+            nodes[e, 10 + q] = face_id[key]
+            nori_f[e, q] = tri_orientation(loc, key)
+            norder[e, 6 + q] = fmin[key]
+            bcflag[e, 10 + q] = int(_on_boundary(coords[list(key)], n))
+        norder[e, 10] = orders[e]
+    if not dirichlet:
+        bcflag[:] = 0
+    return dict(
+        nelem=ne, n=n, h=h, p=p, nnodes=nnodes, nverts=nverts,
+        etype=np.full(ne, TET, dtype=np.int32), norder=norder, nori_edge=nori_e,
+        nori_face=nori_f, nodes=nodes, bcflag=bcflag, xvert=xvert,
+        kappa=_kappa(rng, ne, kappa_logrange), vertex_xyz=X, orders=orders,
+    )
+
+
+def hp_tet(n, seed=2024, perturb=0.0, kappa_logrange=(-1, 1), pmax=6, dirichlet=True):
+    """Kuhn tetrahedral mesh with per-element orders drawn in 1..pmax from a
+    seeded geometric distribution whose mean grows away from the corner
+    (0,0,0), edge and face orders by the minimum rule."""
+    base = structured_tet(n, 1, seed=seed)
+    rng = np.random.default_rng(seed + 1)
+    cen = base["xvert"][:, :4].mean(axis=1)
+    r = np.linalg.norm(cen, axis=1) / np.sqrt(3.0)
+    mean = 1.0 + (pmax - 1) * r
+    orders = np.minimum(rng.geometric(1.0 / np.maximum(mean, 1.0)), pmax).astype(np.int32)
+    return structured_tet(n, None, perturb=perturb, kappa_logrange=kappa_logrange, seed=seed,
+                          dirichlet=dirichlet, orders=orders)

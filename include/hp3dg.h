@@ -85,12 +85,16 @@ typedef struct hp3dg_opts {
  * find_orient (datstrs/find_orient.F90:8), elem_nodes and get_index
  * (datstrs/get_index.F90:27) return for element Mdle. */
 typedef struct hp3dg_elem_desc {
-  int32_t etype;         /* HP3DG_HEXA (only hexahedra in this release) */
+  int32_t etype;         /* HP3DG_HEXA or HP3DG_TET */
   int32_t mdle;          /* middle node id, returned back for bookkeeping */
-  int32_t norder[19];    /* Norder: edges, faces (MODORDER=10 packed), interior */
-  int32_t nori_edge[12]; /* NoriE: 0/1 */
-  int32_t nori_face[6];  /* NoriF: 0..7 */
-  int32_t nodes[26];     /* global ids of vertex, edge, face nodes, element order */
+  int32_t norder[19];    /* Norder.  hexa: 12 edges, 6 faces (MODORDER=10
+                            packed), interior (3 digits); tet: 6 edges,
+                            4 faces, interior (one order each, 11 used) */
+  int32_t nori_edge[12]; /* NoriE: 0/1 (tet: 6 used) */
+  int32_t nori_face[6];  /* NoriF: hexa 0..7 (OrientQuad); tet 0..5
+                            (OrientTri, 4 used) */
+  int32_t nodes[26];     /* global ids of vertex, edge, face nodes in element
+                            order (hexa 26, tet 14 used; the rest ignored) */
   int32_t bcflag[26];    /* 1: every dof of this node is Dirichlet (index=1) */
 } hp3dg_elem_desc;
 
@@ -103,8 +107,9 @@ int hp3dg_batch_begin(const hp3dg_opts *opts, hp3dg_ctx **ctx);
 int hp3dg_set_stream(hp3dg_ctx *ctx, void *stream);
 
 /* Submit a batch: n_elem descriptors in ELEM_ORDER, vertex coordinates
- * xvert (n_elem x 8 x 3, the nodcor geometry dof of a trilinear map;
- * higher-order geometry dof are zero), per-element coefficient kappa
+ * xvert (n_elem x 8 x 3, the nodcor geometry dof of a trilinear map, a
+ * tetrahedron using the first 4 vertex slots; higher-order geometry dof are
+ * zero), per-element coefficient kappa
  * (NULL = 1), Dirichlet data zdofd (NULL = homogeneous; else for each
  * element its interface dof values in element dof order, concatenated),
  * and the number of global nodes (size of NFIRST_DOF).

@@ -932,17 +932,233 @@ int orc_element_error(int etype, const int32_t *norder, const int32_t *nori_edge
 }
 
 /* ------------------------------------------------------------------------ */
-/* Tetrahedron (Tetrahedron.F90:33-234) -- restated in the mixed-type pass.  */
+/* Jacobi families (Polynomials.F90:197-431, 553-646)                         */
 /* ------------------------------------------------------------------------ */
-int orc_nrdofH_tet(const int32_t *norder) { (void)norder; return -1; }
+#define JMAX 9
+
+/* PolyJacobi (Polynomials.F90:197-268): shifted scaled Jacobi polynomials
+ * P[a][i], rows a = 0..nord with alpha = minalpha + 2a, orders i = 0..nord-a
+ * (the first subdiagonal is filled too, as in the reference). */
+static void poly_jacobi(double x, double t, int nord, int minalpha, double P[JMAX][JMAX]) {
+  for (int a = 0; a <= nord; ++a) P[a][0] = 1.0;
+  double y = 0.0;
+  if (nord >= 1) {
+    y = 2.0 * x - t;
+    for (int a = 0; a <= nord - 1; ++a) P[a][1] = y + (double)(minalpha + 2 * a) * x;
+  }
+  if (nord >= 2) {
+    double tt = t * t;
+    for (int a = 0; a <= nord - 2; ++a) {
+      int al = minalpha + 2 * a;
+      int aa = al * al;
+      for (int i = 2; i <= nord - a; ++i) {
+        int ai = 2 * i * (i + al) * (2 * i + al - 2);
+        int bi = 2 * i + al - 1;
+        int ci = (2 * i + al) * (2 * i + al - 2);
+        int di = 2 * (i + al - 1) * (i - 1) * (2 * i + al);
+        double v = (double)bi * ((double)ci * y + (double)aa * t) * P[a][i - 1] -
+                   (double)di * tt * P[a][i - 2];
+        P[a][i] = v / (double)ai;
+      }
+    }
+  }
+}
+
+/* PolyIJacobi (Polynomials.F90:303-431): integrated Jacobi L[a][i], rows
+ * a = 1..nord (alpha = minalpha + 2(a-1)), orders i = 1..nord-a+1; P[a][i-1]
+ * the x-derivative (Jacobi), R[a][i-1] the t-derivative (idec == 0 only). */
+static void poly_ijacobi(double x, double t, int nord, int minalpha, int idec,
+                         double L[JMAX][JMAX], double P[JMAX][JMAX], double R[JMAX][JMAX]) {
+  double pj[JMAX][JMAX];
+  poly_jacobi(x, t, nord, minalpha, pj);
+  /* ptemp(a, i) of the reference is row a-1 of PolyJacobi */
+  for (int a = 1; a <= nord; ++a) {
+    for (int i = 0; i <= nord - 1; ++i) P[a][i] = pj[a - 1][i];
+    L[a][1] = x;
+    if (!idec) R[a][0] = 0.0;
+  }
+  if (nord >= 2) {
+    double tt = t * t;
+    for (int a = 1; a <= nord - 1; ++a) {
+      int al = minalpha + 2 * (a - 1);
+      for (int i = 2; i <= nord - (a - 1); ++i) {
+        int tia = i + i + al, tiam1 = tia - 1, tiam2 = tia - 2;
+        double ai = (double)(i + al) / (double)(tiam1 * tia);
+        double bi = (double)al / (double)(tiam2 * tia);
+        double ci = ((double)i - 1.0) / (double)(tiam2 * tiam1);
+        L[a][i] = ai * pj[a - 1][i] + bi * t * pj[a - 1][i - 1] - ci * tt * pj[a - 1][i - 2];
+        if (!idec) {
+          double r = -((double)(i - 1) * (pj[a - 1][i - 1] + t * pj[a - 1][i - 2]));
+          R[a][i - 1] = r / (double)tiam2;
+        }
+      }
+    }
+  }
+}
+
+/* HomIJacobi (Polynomials.F90:604-646): homogenized integrated Jacobi of the
+ * pair S = (s0, s1) with gradients DS[c][k]; HomL[a][i], DHomL[a][i][c]. */
+static void hom_ijacobi(const double *S, const double DS[3][2], int nord, int minalpha,
+                        int idec, double HomL[JMAX][JMAX], double DHomL[JMAX][JMAX][3]) {
+  double hP[JMAX][JMAX], hR[JMAX][JMAX];
+  if (idec) {
+    poly_ijacobi(S[1], 1.0, nord, minalpha, 1, HomL, hP, hR);
+    for (int a = 1; a <= nord; ++a)
+      for (int i = 1; i <= nord - (a - 1); ++i)
+        for (int c = 0; c < 3; ++c) DHomL[a][i][c] = hP[a][i - 1] * DS[c][1];
+  } else {
+    poly_ijacobi(S[1], S[0] + S[1], nord, minalpha, 0, HomL, hP, hR);
+    double ds01[3];
+    for (int c = 0; c < 3; ++c) ds01[c] = DS[c][0] + DS[c][1];
+    for (int a = 1; a <= nord; ++a)
+      for (int i = 1; i <= nord - (a - 1); ++i)
+        for (int c = 0; c < 3; ++c)
+          DHomL[a][i][c] = hP[a][i - 1] * DS[c][1] + hR[a][i - 1] * ds01[c];
+  }
+}
+
+/* AncPhiTri (Ancillary.F90:397-442): triangle ancillary functions
+ * phi[i][j] = phiE_i(s0,s1) * L^{2i}_j(s2; s0+s1+s2), i >= 2, j >= 1,
+ * i + j <= nord.  S[k], DS[c][k] for k = 0..2. */
+static void anc_phi_tri(const double *S, const double DS[3][3], int nord, int idec,
+                        double phi[JMAX][JMAX], double dphi[JMAX][JMAX][3]) {
+  double s01[2] = {S[0], S[1]}, ds01[3][2];
+  for (int c = 0; c < 3; ++c) { ds01[c][0] = DS[c][0]; ds01[c][1] = DS[c][1]; }
+  double phiE[16], dphiE[16][3];
+  hom_ilegendre(s01, ds01, nord - 1, 0, phiE, dphiE);
+  double sL[2] = {S[0] + S[1], S[2]}, dsL[3][2];
+  for (int c = 0; c < 3; ++c) { dsL[c][0] = DS[c][0] + DS[c][1]; dsL[c][1] = DS[c][2]; }
+  double hl[JMAX][JMAX], dhl[JMAX][JMAX][3];
+  hom_ijacobi(sL, dsL, nord - 2, 4, idec, hl, dhl);
+  /* homLal(i, j) of the reference is row i-1 of HomIJacobi */
+  for (int nij = 3; nij <= nord; ++nij)
+    for (int i = 2; i <= nij - 1; ++i) {
+      int j = nij - i;
+      phi[i][j] = phiE[i] * hl[i - 1][j];
+      for (int c = 0; c < 3; ++c) dphi[i][j][c] = hl[i - 1][j] * dphiE[i][c] + phiE[i] * dhl[i - 1][j][c];
+    }
+}
+
+/* OrientTri (Orient.F90:119-162): GS(k) = S(Or(nori, k)) */
+static const int ORIENT_TRI[6][3] = {{0, 1, 2}, {1, 2, 0}, {2, 0, 1}, {0, 2, 1}, {1, 0, 2}, {2, 1, 0}};
+
+/* ------------------------------------------------------------------------ */
+/* Tetrahedron H1 (Tetrahedron.F90:33-234; AffineTetrahedron,                */
+/* AffineCoordinates.F90:74-89; BlendTetV / ProjectTetE / ProjectTetF,        */
+/* BlendProject.F90:441-560).                                                 */
+/* ------------------------------------------------------------------------ */
+static const int TET_E[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+static const int TET_F[4][3] = {{0, 1, 2}, {0, 1, 3}, {1, 2, 3}, {0, 2, 3}};
+
+static int tri_ndof(int p) { return p > 2 ? (p - 1) * (p - 2) / 2 : 0; }
+static int tet_nbub(int p) { return p > 3 ? (p - 1) * (p - 2) * (p - 3) / 6 : 0; }
+
+int orc_nrdofH_tet(const int32_t *norder) {
+  int n = 4;
+  for (int e = 0; e < 6; ++e) n += imax(norder[e] - 1, 0);
+  for (int f = 0; f < 4; ++f) n += tri_ndof(norder[6 + f]);
+  return n + tet_nbub(norder[10]);
+}
+
+/* set_3Dint_aux TETRA branch (set_3D_int.F90:305-323) with the Duffy rule of
+ * init_gauss_quadrature (gauss_quadrature.F90:757-787): order = max order
+ * + INTEGRATION capped at MAXP; (p+1) x (p+1) x (p+2) collapsed points. */
 int orc_set_3D_int_tet(const int32_t *norder, int integration, double *xiloc,
                        double *waloc) {
-  (void)norder; (void)integration; (void)xiloc; (void)waloc;
-  return -1;
+  int nord = 0;
+  for (int i = 0; i < 11; ++i) nord = imax(nord, norder[i]);
+  nord = imin(nord + integration, ORC_MAXP);
+  if (nord < 1) return -1;
+  int np = nord;
+  double xz[16], wz[16], xy[16], wy[16];
+  orc_gauss1d(np + 2, xz, wz);
+  orc_gauss1d(np + 1, xy, wy);
+  int l = 0;
+  for (int k = 0; k < np + 2; ++k) {
+    double z = xz[k], wzk = wz[k];
+    for (int j = 0; j < np + 1; ++j) {
+      double y = xy[j], wyj = wy[j];
+      for (int i = 0; i < np + 1; ++i) {
+        double xx = xy[i], wx = wy[i];
+        xiloc[3 * l + 0] = xx * (1.0 - y) * (1.0 - z);
+        xiloc[3 * l + 1] = y * (1.0 - z);
+        xiloc[3 * l + 2] = z;
+        double omz = 1.0 - z;
+        waloc[l] = wx * wyj * wzk * (omz * omz) * (1.0 - y);
+        ++l;
+      }
+    }
+  }
+  return l;
 }
+
 int orc_shape3DH_tet(const double *xi, const int32_t *nord,
                      const int32_t *nori_edge, const int32_t *nori_face,
                      double *shap, double *grad) {
-  (void)xi; (void)nord; (void)nori_edge; (void)nori_face; (void)shap; (void)grad;
-  return -1;
+  double lam[4] = {1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+  static const double DL[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  int m = 0;
+  for (int v = 0; v < 4; ++v, ++m) {
+    shap[m] = lam[v];
+    for (int c = 0; c < 3; ++c) grad[3 * m + c] = DL[v][c];
+  }
+  /* edges: OrientE + AncPhiE (homogenized integrated Legendre, Idec false) */
+  for (int e = 0; e < 6; ++e) {
+    int p = nord[e];
+    if (p - 1 <= 0) continue;
+    int v0 = TET_E[e][0], v1 = TET_E[e][1];
+    if (nori_edge[e] == 1) { int t = v0; v0 = v1; v1 = t; }
+    double S[2] = {lam[v0], lam[v1]}, DS[3][2];
+    for (int c = 0; c < 3; ++c) { DS[c][0] = DL[v0][c]; DS[c][1] = DL[v1][c]; }
+    double phi[16], dphi[16][3];
+    hom_ilegendre(S, DS, p, 0, phi, dphi);
+    for (int i = 2; i <= p; ++i, ++m) {
+      shap[m] = phi[i];
+      for (int c = 0; c < 3; ++c) grad[3 * m + c] = dphi[i][c];
+    }
+  }
+  /* faces: OrientTri + AncPhiTri */
+  for (int f = 0; f < 4; ++f) {
+    int p = nord[6 + f];
+    if (tri_ndof(p) <= 0) continue;
+    const int *o = ORIENT_TRI[nori_face[f]];
+    double S[3], DS[3][3];
+    for (int k = 0; k < 3; ++k) {
+      int v = TET_F[f][o[k]];
+      S[k] = lam[v];
+      for (int c = 0; c < 3; ++c) DS[c][k] = DL[v][c];
+    }
+    double phi[JMAX][JMAX], dphi[JMAX][JMAX][3];
+    anc_phi_tri(S, DS, p, 0, phi, dphi);
+    for (int nij = 3; nij <= p; ++nij)
+      for (int i = 2; i <= nij - 1; ++i, ++m) {
+        int j = nij - i;
+        shap[m] = phi[i][j];
+        for (int c = 0; c < 3; ++c) grad[3 * m + c] = dphi[i][j][c];
+      }
+  }
+  /* bubbles: AncPhiTri(lam0..2) x HomIJacobi((1-lam3, lam3), alpha = 2(i+j)) */
+  int pb = nord[10];
+  if (tet_nbub(pb) > 0) {
+    double S[3] = {lam[0], lam[1], lam[2]}, DS[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) DS[c][k] = DL[k][c];
+    double phi[JMAX][JMAX], dphi[JMAX][JMAX][3];
+    anc_phi_tri(S, DS, pb - 1, 0, phi, dphi);
+    double Sz[2] = {1.0 - lam[3], lam[3]}, DSz[3][2];
+    for (int c = 0; c < 3; ++c) { DSz[c][0] = -DL[3][c]; DSz[c][1] = DL[3][c]; }
+    double hb[JMAX][JMAX], dhb[JMAX][JMAX][3];
+    hom_ijacobi(Sz, DSz, pb - 3, 6, 1, hb, dhb);
+    /* homLbet(nij, k) of the reference is row nij-2 of HomIJacobi */
+    for (int nijk = 4; nijk <= pb; ++nijk)
+      for (int nij = 3; nij <= nijk - 1; ++nij)
+        for (int i = 2; i <= nij - 1; ++i, ++m) {
+          int j = nij - i, k = nijk - nij;
+          double hv = hb[nij - 2][k];
+          shap[m] = phi[i][j] * hv;
+          for (int c = 0; c < 3; ++c)
+            grad[3 * m + c] = hv * dphi[i][j][c] + phi[i][j] * dhb[nij - 2][k][c];
+        }
+  }
+  return m;
 }

@@ -121,6 +121,30 @@ def shape_hexa(xi, norder, nori_edge=None, nori_face=None):
     return shap[:n].copy(), grad[:n].copy()
 
 
+def shape_tet(xi, norder, nori_edge=None, nori_face=None):
+    xi = _f64(xi)
+    norder = _i32(norder)
+    ne = _i32(np.zeros(12) if nori_edge is None else nori_edge)
+    nf = _i32(np.zeros(6) if nori_face is None else nori_face)
+    shap = np.zeros(343); grad = np.zeros((343, 3))
+    n = lib().orc_shape3DH_tet(_p(xi, _f64p), _p(norder, _i32p), _p(ne, _i32p),
+                               _p(nf, _i32p), _p(shap, _f64p), _p(grad, _f64p))
+    return shap[:n].copy(), grad[:n].copy()
+
+
+def shape(etype, xi, norder, nori_edge=None, nori_face=None):
+    if etype == TET:
+        return shape_tet(xi, norder, nori_edge, nori_face)
+    return shape_hexa(xi, norder, nori_edge, nori_face)
+
+
+def quad_tet(norder, integration=0):
+    xi = np.zeros(3 * 400); w = np.zeros(400)
+    n = lib().orc_set_3D_int_tet(_p(_i32(norder), _i32p), integration, _p(xi, _f64p),
+                                 _p(w, _f64p))
+    return xi[: 3 * n].reshape(n, 3).copy(), w[:n].copy()
+
+
 def getf(isol, x):
     return lib().orc_getf(isol, _p(_f64(x), _f64p))
 

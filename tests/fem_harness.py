@@ -22,13 +22,50 @@ HEXA_EDGE_V = [(0, 1), (1, 2), (3, 2), (0, 3), (4, 5), (5, 6), (7, 6), (4, 7),
 # reference coordinate parametrisation of each face: fixed axis/value, (s,t) axes
 HEXA_FACE = [(2, 0.0, 0, 1), (2, 1.0, 0, 1), (1, 0.0, 0, 2), (0, 1.0, 1, 2),
              (1, 1.0, 0, 2), (0, 0.0, 1, 2)]
-# edge: reference coordinates at parameter s in [0,1]
 _VREF = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
                   [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], dtype=float)
+# tetrahedron (BlendProject.F90 BlendTetV / ProjectTetE / ProjectTetF)
+TET_VREF = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+TET_EDGE_V = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
+TET_FACE_V = [(0, 1, 2), (0, 1, 3), (1, 2, 3), (0, 2, 3)]
+
+HEXA, TET = 1, 3
+
+
+def type_info(etype):
+    """(vertex count, node count, reference vertices, edge vertex pairs)."""
+    if etype == TET:
+        return 4, 14, TET_VREF, TET_EDGE_V
+    return 8, 26, _VREF, HEXA_EDGE_V
+
+
+def nnode_of(mesh):
+    return np.array([type_info(int(t))[1] for t in mesh["etype"]], dtype=np.int32)
 
 
 def _xmap(xv, shap):
-    return shap[:8] @ xv
+    return shap[: len(xv)] @ xv
+
+
+def _face_points(etype, f):
+    """Quadrature points (reference coordinates) and weights on face f."""
+    gs, gw = O.gauss1d(8)
+    pts, wts = [], []
+    if etype == TET:
+        a, b, c = (TET_VREF[q] for q in TET_FACE_V[f])
+        for s1, w1 in zip(gs, gw):
+            for t1, w2 in zip(gs, gw):
+                u, v = s1 * (1 - t1), t1  # collapsed square -> triangle
+                pts.append(a + u * (b - a) + v * (c - a))
+                wts.append(w1 * w2 * (1 - t1))
+        return pts, wts
+    ax, v0, sa, ta = HEXA_FACE[f]
+    for s1, w1 in zip(gs, gw):
+        for t1, w2 in zip(gs, gw):
+            xi = np.zeros(3)
+            xi[ax] = v0; xi[sa] = s1; xi[ta] = t1
+            pts.append(xi); wts.append(w1 * w2)
+    return pts, wts
 
 
 def dirichlet_data(mesh, isol):
@@ -43,51 +80,47 @@ def dirichlet_data(mesh, isol):
     known = {}
     out = []
     for e in range(ne):
-        nd = O.node_ndof(1, no[e])
+        et = int(mesh["etype"][e])
+        nv, nn, vref, edges = type_info(et)
+        nd = O.node_ndof(et, no[e])
         first = np.concatenate([[0], np.cumsum(nd)])
         ni = int(first[-1])
         z = np.zeros(ni)
-        xv = mesh["xvert"][e]
+        xv = mesh["xvert"][e][:nv]
         ne_, nf_ = mesh["nori_edge"][e], mesh["nori_face"][e]
-        for i in range(26):
+        nedge = len(edges)
+        for i in range(nn):
             if not bc[e, i] or nd[i] == 0:
                 continue
             g = int(nodes[e, i])
             if g in known:
                 z[first[i]:first[i + 1]] = known[g]
                 continue
-            if i < 8:
-                s, _ = O.shape_hexa(_VREF[i], no[e], ne_, nf_)
+            if i < nv:
+                s, _ = O.shape(et, vref[i], no[e], ne_, nf_)
                 u, _ = O.exact(isol, _xmap(xv, s))
                 val = np.array([u])
-            elif i < 20:
-                ie = i - 8
-                a, b = HEXA_EDGE_V[ie]
+            elif i < nv + nedge:
+                a, b = edges[i - nv]
                 gs, gw = O.gauss1d(8)
                 rows, rhs = [], []
                 for t, w in zip(gs, gw):
-                    xi = (1 - t) * _VREF[a] + t * _VREF[b]
-                    s, _ = O.shape_hexa(xi, no[e], ne_, nf_)
+                    xi = (1 - t) * vref[a] + t * vref[b]
+                    s, _ = O.shape(et, xi, no[e], ne_, nf_)
                     u, _ = O.exact(isol, _xmap(xv, s))
-                    # subtract vertex part (already known)
                     uv = s[a] * z[first[a]] + s[b] * z[first[b]]
                     rows.append(np.sqrt(w) * s[first[i]:first[i + 1]])
                     rhs.append(np.sqrt(w) * (u - uv))
                 val = np.linalg.lstsq(np.array(rows), np.array(rhs), rcond=None)[0]
             else:
-                f = i - 20
-                ax, v0, sa, ta = HEXA_FACE[f]
-                gs, gw = O.gauss1d(8)
+                pts, wts = _face_points(et, i - nv - nedge)
                 rows, rhs = [], []
-                for s1, w1 in zip(gs, gw):
-                    for t1, w2 in zip(gs, gw):
-                        xi = np.zeros(3)
-                        xi[ax] = v0; xi[sa] = s1; xi[ta] = t1
-                        s, _ = O.shape_hexa(xi, no[e], ne_, nf_)
-                        u, _ = O.exact(isol, _xmap(xv, s))
-                        known_part = s[:first[20]] @ z[:first[20]]
-                        rows.append(np.sqrt(w1 * w2) * s[first[i]:first[i + 1]])
-                        rhs.append(np.sqrt(w1 * w2) * (u - known_part))
+                for xi, w in zip(pts, wts):
+                    s, _ = O.shape(et, xi, no[e], ne_, nf_)
+                    u, _ = O.exact(isol, _xmap(xv, s))
+                    known_part = s[:first[nv + nedge]] @ z[:first[nv + nedge]]
+                    rows.append(np.sqrt(w) * s[first[i]:first[i + 1]])
+                    rhs.append(np.sqrt(w) * (u - known_part))
                 val = np.linalg.lstsq(np.array(rows), np.array(rhs), rcond=None)[0]
             known[g] = val
             z[first[i]:first[i + 1]] = val
@@ -100,11 +133,13 @@ def oracle_element_outputs(mesh, isol, integration=0, zdofd=None, stc_method=0):
     compressed system, Schur blocks and per-node active dof counts."""
     res = []
     for e in range(mesh["nelem"]):
-        K, b, rc = O.elem(1, mesh["norder"][e], mesh["nori_edge"][e], mesh["nori_face"][e],
-                          mesh["xvert"][e], mesh["kappa"][e], isol=isol,
+        et = int(mesh["etype"][e])
+        nv = type_info(et)[0]
+        K, b, rc = O.elem(et, mesh["norder"][e], mesh["nori_edge"][e], mesh["nori_face"][e],
+                          mesh["xvert"][e][:nv], mesh["kappa"][e], isol=isol,
                           integration=integration)
         assert rc == 0
-        nb = O.nrdof_bubble(1, mesh["norder"][e])
+        nb = O.nrdof_bubble(et, mesh["norder"][e])
         if nb > 0:
             aii, bi, asch, bsch, rc = O.stc_fwd(K, b, nb, stc_method)
             assert rc == 0
@@ -112,9 +147,11 @@ def oracle_element_outputs(mesh, isol, integration=0, zdofd=None, stc_method=0):
             aii, bi = K, b
             asch = np.zeros((0, K.shape[0])); bsch = np.zeros(0)
         zd = None if zdofd is None else zdofd[e]
-        nextract, zb, zs, ndofm = O.celem_compress(1, mesh["norder"][e], mesh["bcflag"][e],
+        nextract, zb, zs, ndofm = O.celem_compress(et, mesh["norder"][e], mesh["bcflag"][e],
                                                    aii, bi, zd)
-        res.append(dict(nextract=nextract, zbload=zb, zastif=zs, ndofm=ndofm[:26].copy(),
+        nd26 = np.zeros(26, dtype=np.int32)
+        nd26[: len(ndofm)] = ndofm[:26]
+        res.append(dict(nextract=nextract, zbload=zb, zastif=zs, ndofm=nd26,
                         aschur=asch, bschur=bsch, ni=aii.shape[0], nb=nb))
     return res
 
@@ -124,7 +161,7 @@ def assemble_solve(mesh, elems):
     (mumps_sc.F90:300-321 triplets) and solve it; returns the global interface
     solution x and the index maps."""
     ne = mesh["nelem"]
-    nnode = np.full(ne, 26, dtype=np.int32)
+    nnode = nnode_of(mesh)
     ndofm = np.stack([el["ndofm"] for el in elems]).astype(np.int32)
     nrdof, nfirst, lcon, lcon_off, elem_nnz = O.index_maps(nnode, mesh["nodes"], ndofm,
                                                            mesh["nnodes"])
@@ -150,7 +187,7 @@ def solve_and_error(mesh, elems, isol, zdofd=None):
     back-substitute bubbles and return (H1 error, H1 norm, global solution,
     per-element full dof vectors)."""
     ne = mesh["nelem"]
-    nnode = np.full(ne, 26, dtype=np.int32)
+    nnode = nnode_of(mesh)
     ndofm = np.stack([el["ndofm"] for el in elems]).astype(np.int32)
     nrdof, nfirst, lcon, lcon_off, elem_nnz = O.index_maps(nnode, mesh["nodes"], ndofm,
                                                            mesh["nnodes"])
@@ -179,13 +216,35 @@ def solve_and_error(mesh, elems, isol, zdofd=None):
         dof = np.concatenate([xi, xb])
         dofs.append(dof)
         n = len(dof)
-        xn = np.zeros((n, 3)); xn[:8] = mesh["xvert"][e]
+        et = int(mesh["etype"][e])
+        nv = type_info(et)[0]
+        xn = np.zeros((n, 3)); xn[:nv] = mesh["xvert"][e][:nv]
         e2 = np.zeros(1); r2 = np.zeros(1)
         L = O.lib()
-        L.orc_element_error(1, O._p(O._i32(mesh["norder"][e]), O._i32p),
+        L.orc_element_error(et, O._p(O._i32(mesh["norder"][e]), O._i32p),
                             O._p(O._i32(mesh["nori_edge"][e]), O._i32p),
                             O._p(O._i32(mesh["nori_face"][e]), O._i32p),
                             O._p(O._f64(xn), O._f64p), O._p(O._f64(dof), O._f64p), isol,
                             O._p(e2, O._f64p), O._p(r2, O._f64p))
         err2 += e2[0]; nrm2 += r2[0]
     return np.sqrt(err2), np.sqrt(nrm2), x, dofs
+
+
+def gpu_elements(ep, m):
+    """Per-element outputs of the GPU library in the form the harness
+    assembles (NEXTRACT rebuilt from the node dof counts: nodes in reverse
+    order, Dirichlet nodes skipped)."""
+    out = []
+    for e in range(m["nelem"]):
+        zb, zs = ep.condensed(e)
+        a, b = ep.schur(e)
+        et = int(m["etype"][e])
+        nd = O.node_ndof(et, m["norder"][e])
+        nn = len(nd)
+        ndofm = np.zeros(26, dtype=np.int32)
+        ndofm[:nn] = nd * (1 - m["bcflag"][e][:nn])
+        first = np.concatenate([[0], np.cumsum(nd)])
+        nx = [first[i] + q for i in range(nn - 1, -1, -1) for q in range(ndofm[i])]
+        out.append(dict(nextract=np.array(nx, dtype=np.int64), zbload=zb, zastif=zs, ndofm=ndofm,
+                        aschur=a, bschur=b, ni=int(nd.sum()), nb=a.shape[0]))
+    return out

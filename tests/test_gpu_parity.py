@@ -81,18 +81,7 @@ def test_dirichlet_lift_matches_oracle():
         assert _rel(zb, ref[e]["zbload"]) < TOL
 
 
-def _gpu_elements(ep, m):
-    out = []
-    for e in range(m["nelem"]):
-        zb, zs = ep.condensed(e)
-        a, b = ep.schur(e)
-        nd = O.node_ndof(1, m["norder"][e])
-        ndofm = (nd * (1 - m["bcflag"][e])).astype(np.int32)
-        first = np.concatenate([[0], np.cumsum(nd)])
-        nx = [first[i] + q for i in range(25, -1, -1) for q in range(ndofm[i])]
-        out.append(dict(nextract=np.array(nx, dtype=np.int64), zbload=zb, zastif=zs, ndofm=ndofm,
-                        aschur=a, bschur=b, ni=int(nd.sum()), nb=a.shape[0]))
-    return out
+_gpu_elements = FH.gpu_elements
 
 
 @pytest.mark.parametrize("n", [2, 4])
