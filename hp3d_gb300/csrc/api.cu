@@ -118,12 +118,93 @@ int tet_quadrature(int pm, int integration, std::vector<double>& xi, std::vector
   return (int)w.size();
 }
 
+// Triangle rules of the prism: Dunavant's symmetric rules of degree 2..12 in
+// the 15-digit form of init_gauss_quadrature (gauss_quadrature.F90:130-270:
+// per orbit a weight, a barycentric triple and the orbit size 1, 3 or 6),
+// expanded into points in the order of gauss_quadrature.F90:663-700.
+struct TriOrbit { int degree, size; double w, b[3]; };
+const TriOrbit TRI_ORBITS[] = {
+    {2, 3, 0.333333333333333, {0.666666666666667, 0.166666666666667, 0.166666666666667}},
+    {4, 3, 0.223381589678011, {0.10810301816807, 0.445948490915965, 0.445948490915965}},
+    {4, 3, 0.109951743655322, {0.816847572980459, 0.091576213509771, 0.091576213509771}},
+    {6, 3, 0.116786275726379, {0.501426509658179, 0.24928674517091, 0.24928674517091}},
+    {6, 3, 0.050844906370207, {0.873821971016996, 0.063089014491502, 0.063089014491502}},
+    {6, 6, 0.082851075618374, {0.053145049844817, 0.310352451033784, 0.636502499121399}},
+    {8, 1, 0.144315607677787, {0.333333333333333, 0.333333333333333, 0.333333333333333}},
+    {8, 3, 0.095091634267285, {0.081414823414554, 0.459292588292723, 0.459292588292723}},
+    {8, 3, 0.103217370534718, {0.65886138449648, 0.17056930775176, 0.17056930775176}},
+    {8, 3, 0.032458497623198, {0.898905543365938, 0.050547228317031, 0.050547228317031}},
+    {8, 6, 0.027230314174435, {0.008394777409958, 0.263112829634638, 0.728492392955404}},
+    {10, 1, 0.090817990382754, {0.333333333333333, 0.333333333333333, 0.333333333333333}},
+    {10, 3, 0.036725957756467, {0.028844733232685, 0.485577633383657, 0.485577633383657}},
+    {10, 3, 0.045321059435528, {0.781036849029926, 0.109481575485037, 0.109481575485037}},
+    {10, 6, 0.07275791684542, {0.14170721941488, 0.307939838764121, 0.550352941820999}},
+    {10, 6, 0.028327242531057, {0.025003534762686, 0.246672560639903, 0.728323904597411}},
+    {10, 6, 0.009421666963733, {0.009540815400299, 0.0668032510122, 0.9236559335875}},
+    {12, 3, 0.025731066440455, {0.02356522045239, 0.488217389773805, 0.488217389773805}},
+    {12, 3, 0.043692544538038, {0.120551215411079, 0.43972439229446, 0.43972439229446}},
+    {12, 3, 0.062858224217885, {0.457579229975768, 0.271210385012116, 0.271210385012116}},
+    {12, 3, 0.034796112930709, {0.744847708916828, 0.127576145541586, 0.127576145541586}},
+    {12, 3, 0.006166261051559, {0.957365299093579, 0.02131735045321, 0.02131735045321}},
+    {12, 6, 0.040371557766381, {0.115343494534698, 0.275713269685514, 0.608943235779788}},
+    {12, 6, 0.022356773202303, {0.022838332222257, 0.28132558098994, 0.695836086787803}},
+    {12, 6, 0.017316231108659, {0.02573405054833, 0.116251915907597, 0.858014033544073}},
+};
+
+int tri_rule(int degree, std::vector<double>& bar, std::vector<double>& w) {
+  bar.clear(); w.clear();
+  for (const TriOrbit& r : TRI_ORBITS) {
+    if (r.degree != degree) continue;
+    const double x[6] = {r.b[0], r.b[1], r.b[2], r.b[0], r.b[1], r.b[2]};
+    const int rot = r.size == 1 ? 1 : 3;
+    for (int q = 0; q < rot; ++q) {  // identity, then the two cyclic shifts
+      for (int k = 0; k < 3; ++k) bar.push_back(x[k + q]);
+      w.push_back(r.w);
+    }
+    if (r.size == 6)
+      for (int l = 1; l <= 3; ++l) {  // the three reflections
+        for (int k = 1; k <= 3; ++k) bar.push_back(x[3 + l - k - 1]);
+        w.push_back(r.w);
+      }
+  }
+  return (int)w.size();
+}
+
+// set_3Dint_aux PRISM branch (set_3D_int.F90:264-300) on the bin orders
+// (horizontal ph, vertical pz): the triangle rule NSELECT(ph) = degree 2ph
+// times Gauss with pz+1 points; xi = (bar2, bar3, z), w = w_tri/2 * w_z.
+int prism_quadrature(int ph, int pz, int integration, std::vector<double>& xi,
+                     std::vector<double>& w) {
+  int nh = std::min(ph + integration, MAXP), nz = std::min(pz + integration, MAXP) + 1;
+  std::vector<double> bar, wt;
+  int nt = tri_rule(2 * nh, bar, wt);
+  xi.clear(); w.clear();
+  for (int l2 = 0; l2 < nz; ++l2)
+    for (int l1 = 0; l1 < nt; ++l1) {
+      xi.push_back(bar[3 * l1 + 1]);
+      xi.push_back(bar[3 * l1 + 2]);
+      xi.push_back(0.5 * (1.0 + GX[nz - 1][l2]));
+      w.push_back(wt[l1] / 2.0 * (0.5 * GW[nz - 1][l2]));
+    }
+  return (int)w.size();
+}
+
 // ---- per element type (element_data.F90 node tables, ndof_nod 808-884) ----
 int type_nvert(int t) { return t == HP3DG_HEXA ? 8 : (t == HP3DG_PRISM ? 6 : 4); }
 int type_nnode(int t) { return t == HP3DG_HEXA ? 26 : (t == HP3DG_PRISM ? 20 : 14); }
 
 // dof per vertex / edge / face node in element node order; returns node count
 int node_ndof(int t, const int* no, int* nd) {
+  if (t == HP3DG_PRISM) {
+    for (int v = 0; v < 6; ++v) nd[v] = 1;
+    for (int e = 0; e < 9; ++e) nd[6 + e] = no[e] > 1 ? no[e] - 1 : 0;
+    for (int f = 0; f < 2; ++f) nd[15 + f] = tri_ndof(no[9 + f]);
+    for (int f = 0; f < 3; ++f) {
+      int h, v; decod2(no[11 + f], h, v);
+      nd[17 + f] = (h > 1 && v > 1) ? (h - 1) * (v - 1) : 0;
+    }
+    return 20;
+  }
   if (t == HP3DG_TET) {
     for (int v = 0; v < 4; ++v) nd[v] = 1;
     for (int e = 0; e < 6; ++e) nd[4 + e] = no[e] > 1 ? no[e] - 1 : 0;
@@ -135,8 +216,12 @@ int node_ndof(int t, const int* no, int* nd) {
   for (int f = 0; f < 6; ++f) { int h, v; decod2(no[12 + f], h, v); nd[20 + f] = (h - 1) * (v - 1); }
   return 26;
 }
-int elem_nbub(int t, const int* no) { return t == HP3DG_TET ? tet_nbub(no[10]) : hexa_nbub(no); }
-int elem_ndof(int t, const int* no) { return t == HP3DG_TET ? tet_ndof(no) : hexa_ndof(no); }
+int elem_nbub(int t, const int* no) {
+  return t == HP3DG_TET ? tet_nbub(no[10]) : (t == HP3DG_PRISM ? prism_nbub(no) : hexa_nbub(no));
+}
+int elem_ndof(int t, const int* no) {
+  return t == HP3DG_TET ? tet_ndof(no) : (t == HP3DG_PRISM ? prism_ndof(no) : hexa_ndof(no));
+}
 
 // descriptor checks (CheckOrder / the reference's order and orientation ranges)
 int validate_desc(const hp3dg_elem_desc& d, int nnodes) {
@@ -158,6 +243,19 @@ int validate_desc(const hp3dg_elem_desc& d, int nnodes) {
       if (d.nori_edge[e] & ~1) return HP3DG_ERR_BAD_ORDER;
     for (int f = 0; f < 4; ++f)
       if (d.nori_face[f] < 0 || d.nori_face[f] > 5) return HP3DG_ERR_BAD_ORDER;
+  } else if (d.etype == HP3DG_PRISM) {
+    for (int i = 0; i < 11; ++i)
+      if (d.norder[i] < 1 || d.norder[i] > MAXP) return HP3DG_ERR_BAD_ORDER;
+    for (int i = 11; i < 15; ++i) {
+      int h, v; decod2(d.norder[i], h, v);
+      if (h < 1 || h > MAXP || v < 1 || v > MAXP || d.norder[i] > 99) return HP3DG_ERR_BAD_ORDER;
+    }
+    for (int e = 0; e < 9; ++e)
+      if (d.nori_edge[e] & ~1) return HP3DG_ERR_BAD_ORDER;
+    for (int f = 0; f < 2; ++f)
+      if (d.nori_face[f] < 0 || d.nori_face[f] > 5) return HP3DG_ERR_BAD_ORDER;
+    for (int f = 2; f < 5; ++f)
+      if (d.nori_face[f] < 0 || d.nori_face[f] > 7) return HP3DG_ERR_BAD_ORDER;
   } else {
     return HP3DG_ERR_BAD_ORDER;
   }
@@ -172,6 +270,12 @@ int validate_desc(const hp3dg_elem_desc& d, int nnodes) {
 void bin_key(const hp3dg_elem_desc& d, std::vector<int>& key, int* full, int* fo) {
   for (int i = 0; i < 19; ++i) full[i] = 0;
   for (int f = 0; f < 6; ++f) fo[f] = 0;
+  if (d.etype == HP3DG_PRISM) {
+    prism_bin_orders(d.norder, d.nori_face, full);
+    for (int f = 0; f < 2; ++f) fo[f] = tri_class(d.nori_face[f]);
+    key = {HP3DG_PRISM, full[14], fo[0], fo[1]};
+    return;
+  }
   if (d.etype == HP3DG_TET) {
     int pm = 0;
     for (int i = 0; i < 11; ++i) pm = std::max(pm, (int)d.norder[i]);
@@ -190,6 +294,7 @@ void bin_key(const hp3dg_elem_desc& d, std::vector<int>& key, int* full, int* fo
 int bin_quadrature(int t, const int* full, int integration, std::vector<double>& xi,
                    std::vector<double>& w) {
   if (t == HP3DG_TET) return tet_quadrature(full[0], integration, xi, w);
+  if (t == HP3DG_PRISM) return prism_quadrature(full[14] / 10, full[14] % 10, integration, xi, w);
   return hexa_quadrature(full, integration, xi, w);
 }
 
@@ -745,9 +850,10 @@ int hp3dg_get_elem(const hp3dg_ctx* c, int32_t iel, double* aloc, int32_t ld, do
   cudaMemcpy(of, c->d_nori_f + 6 * (size_t)iel, sizeof(of), cudaMemcpyDeviceToHost);
   const double* PK = c->h_PK + c->pk_off[iel];
   const double* b0 = c->h_b0 + c->b0_off[iel];
-  const bool tet = B.etype == HP3DG_TET;
   auto dmap = [&](int a) {
-    return tet ? tet_dof_map(a, no, oe, of, B.nord_loc[0]) : hexa_dof_map(a, no, oe, of, B.nord_loc);
+    if (B.etype == HP3DG_TET) return tet_dof_map(a, no, oe, of, B.nord_loc[0]);
+    if (B.etype == HP3DG_PRISM) return prism_dof_map(a, no, oe, of, B.nord_loc);
+    return hexa_dof_map(a, no, oe, of, B.nord_loc);
   };
   for (int a = 0; a < n; ++a) {
     uint32_t ma = dmap(a);

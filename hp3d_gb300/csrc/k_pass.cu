@@ -2,9 +2,10 @@
 //
 // Each kernel restates one stage of hp3D's per-element work as a batched
 // device pass over one bin (elements with the same type and local orders):
-//   k_tables_*      shape3DHHexa / shape3DHTet at the set_3D_int points, once
-//                   per bin (shape_1/Hexahedron.F90:33-210,
-//                   shape_1/Tetrahedron.F90:33-234, quadrature/set_3D_int.F90)
+//   k_tables_*      shape3DHHexa / shape3DHTet / shape3DHPris at the
+//                   set_3D_int points, once per bin (shape_1/Hexahedron.F90:
+//                   33-210, Tetrahedron.F90:33-234, Prism.F90:33-330,
+//                   quadrature/set_3D_int.F90)
 //   k_orient_*      signed permutation of the element's oriented dof onto the
 //                   bin's reference enumeration (shape_1/Orient.F90:9-162)
 //   k_geom          geom3D + geom + getf per point (util/geom3D.F90:30-112,
@@ -47,6 +48,17 @@ __global__ void k_tables_tet(Ord19 ord, Ord19 fo, int nint, int n, const double*
   tet_shape(x, ord.v, oe, fo.v, tab_shap + (size_t)l * n, tab_grad + (size_t)l * 3 * n, n);
 }
 
+// prism tables: edge and quad-face orientation 0, triangle faces in the
+// bin's orientation classes (fo[0..1])
+__global__ void k_tables_prism(Ord19 ord, Ord19 fo, int nint, int n, const double* __restrict__ xi,
+                               double* __restrict__ tab_shap, double* __restrict__ tab_grad) {
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nint) return;
+  double x[3] = {xi[3 * l], xi[3 * l + 1], xi[3 * l + 2]};
+  const int oe[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  prism_shape(x, ord.v, oe, fo.v, tab_shap + (size_t)l * n, tab_grad + (size_t)l * 3 * n, n);
+}
+
 void launch_tables(int etype, const int* nord_loc, const int* face_nori, int nint, int n,
                    const double* d_xi, double* d_shap, double* d_grad, cudaStream_t st) {
   Ord19 o, f;
@@ -54,6 +66,8 @@ void launch_tables(int etype, const int* nord_loc, const int* face_nori, int nin
   for (int i = 0; i < 19; ++i) f.v[i] = i < 6 ? face_nori[i] : 0;
   if (etype == ETYPE_TET)
     k_tables_tet<<<(nint + 63) / 64, 64, 0, st>>>(o, f, nint, n, d_xi, d_shap, d_grad);
+  else if (etype == ETYPE_PRISM)
+    k_tables_prism<<<(nint + 63) / 64, 64, 0, st>>>(o, f, nint, n, d_xi, d_shap, d_grad);
   else
     k_tables_hexa<<<(nint + 63) / 64, 64, 0, st>>>(o, nint, n, d_xi, d_shap, d_grad);
 }
@@ -93,10 +107,32 @@ __global__ void k_orient_tet(int nel, const int* __restrict__ elist, const int* 
     perm[(size_t)j * nfull + a] = a < n ? tet_dof_map(a, no, oe, of, pm) : 0u;
 }
 
+__global__ void k_orient_prism(int nel, const int* __restrict__ elist, const int* __restrict__ norder,
+                               const int* __restrict__ nori_e, const int* __restrict__ nori_f,
+                               Ord19 full, int nfull, uint32_t* __restrict__ perm) {
+  int j = blockIdx.x;
+  if (j >= nel) return;
+  int e = elist[j];
+  __shared__ int no[19], oe[12], of[6];
+  if (threadIdx.x < 19) no[threadIdx.x] = norder[19 * e + threadIdx.x];
+  if (threadIdx.x < 12) oe[threadIdx.x] = nori_e[12 * e + threadIdx.x];
+  if (threadIdx.x < 6) of[threadIdx.x] = nori_f[6 * e + threadIdx.x];
+  __syncthreads();
+  const int n = prism_ndof(no);
+  for (int a = threadIdx.x; a < nfull; a += blockDim.x)
+    perm[(size_t)j * nfull + a] = a < n ? prism_dof_map(a, no, oe, of, full.v) : 0u;
+}
+
 void launch_orient(int etype, int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
                    const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
                    cudaStream_t st) {
   if (nel <= 0) return;
+  if (etype == ETYPE_PRISM) {
+    Ord19 o;
+    for (int i = 0; i < 19; ++i) o.v[i] = full[i];
+    k_orient_prism<<<nel, 128, 0, st>>>(nel, d_elist, d_norder, d_nori_e, d_nori_f, o, nfull, d_perm);
+    return;
+  }
   if (etype == ETYPE_TET) {
     k_orient_tet<<<nel, 128, 0, st>>>(nel, d_elist, d_norder, d_nori_e, d_nori_f, full[0], nfull,
                                       d_perm);

@@ -59,7 +59,7 @@ void launch_backsub(int nel, int nif, const int* d_elist, const int* d_ni_e, con
                                                     d_bub_off, d_aschur, d_bschur, d_dof_off, d_dofs);
 }
 
-// manufactured solutions (common/solution.F90:45-134, plus 10 and 12)
+// manufactured solutions (common/solution.F90:45-134, plus 10, 12 and 13)
 __device__ inline void exact_dev(int isol, const double* X, double& u, double* g) {
   const double PI = 3.141592653589793238462643383279502884;
   double x1 = X[0], x2 = X[1], x3 = X[2];
@@ -91,6 +91,9 @@ __device__ inline void exact_dev(int isol, const double* X, double& u, double* g
     }
     case 12:
       u = x1 * x2 * x3; g[0] = x2 * x3; g[1] = x1 * x3; g[2] = x1 * x2;
+      break;
+    case 13:
+      u = 1.0 + x1 + 2.0 * x2 + 3.0 * x3; g[0] = 1.0; g[1] = 2.0; g[2] = 3.0;
       break;
     default: break;
   }

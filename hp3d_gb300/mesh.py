@@ -356,3 +356,255 @@ def hp_tet(n, seed=2024, perturb=0.0, kappa_logrange=(-1, 1), pmax=6, dirichlet=
     orders = np.minimum(rng.geometric(1.0 / np.maximum(mean, 1.0)), pmax).astype(np.int32)
     return structured_tet(n, None, perturb=perturb, kappa_logrange=kappa_logrange, seed=seed,
                           dirichlet=dirichlet, orders=orders)
+
+
+PRISM = 2
+# local topology in each element's own frame (shape_1/BlendProject.F90):
+#   edges: (from, to) in the local direction, and the element axis of the edge
+#   faces: triangles (w0, w1, w2) in OrientTri order; quads (w0, w1, w2, w3)
+#          with S along w0->w1 and T along w0->w3, and the element axes of S, T
+# Hexa axes are x/y/z (orders px, py, pz); prism axes are 0 = horizontal
+# (ph), 2 = vertical (pz); tet orders have one axis.
+_HEXA_EDGES = [((0, 1), 0), ((1, 2), 1), ((3, 2), 0), ((0, 3), 1), ((4, 5), 0), ((5, 6), 1),
+               ((7, 6), 0), ((4, 7), 1), ((0, 4), 2), ((1, 5), 2), ((2, 6), 2), ((3, 7), 2)]
+_HEXA_FACES = [((0, 1, 2, 3), (0, 1)), ((4, 5, 6, 7), (0, 1)), ((0, 1, 5, 4), (0, 2)),
+               ((1, 2, 6, 5), (1, 2)), ((3, 2, 6, 7), (0, 2)), ((0, 3, 7, 4), (1, 2))]
+_PRISM_EDGES = [((0, 1), 0), ((1, 2), 0), ((0, 2), 0), ((3, 4), 0), ((4, 5), 0), ((3, 5), 0),
+                ((0, 3), 2), ((1, 4), 2), ((2, 5), 2)]
+_PRISM_FACES = [((0, 1, 2), (0, 0)), ((3, 4, 5), (0, 0)), ((0, 1, 4, 3), (0, 2)),
+                ((1, 2, 5, 4), (0, 2)), ((0, 2, 5, 3), (0, 2))]
+_TET_EDGES = [(e, 0) for e in TET_EDGES]
+_TET_FACES = [(f, (0, 0)) for f in TET_FACES]
+_TOPO = {HEXA: (8, _HEXA_EDGES, _HEXA_FACES), PRISM: (6, _PRISM_EDGES, _PRISM_FACES),
+         TET: (4, _TET_EDGES, _TET_FACES)}
+
+# OrientQuad (shape_1/Orient.F90:39-116): OrPa(1:2)-1, OrGS(0:1), OrGT(0:1)
+ORIENT_QUAD = [(0, 1, 0, 1, 0, 1), (1, 0, 0, 1, 1, 0), (0, 1, 1, 0, 1, 0), (1, 0, 1, 0, 0, 1),
+               (1, 0, 0, 1, 0, 1), (0, 1, 1, 0, 0, 1), (1, 0, 1, 0, 1, 0), (0, 1, 0, 1, 1, 0)]
+_QUAD_ST = [(0, 0), (1, 0), (1, 1), (0, 1)]
+
+
+def quad_orientation(local, glob):
+    """Orientation code o under which the element's face functions use the
+    face node's frame: with (s, t) the element's face coordinates, the
+    OrientQuad map of o sends every local vertex to the global (S, T)
+    coordinates of the same vertex."""
+    for o, (pa1, pa2, _, gs1, _, gt1) in enumerate(ORIENT_QUAD):
+        ok = True
+        for k, w in enumerate(local):
+            st = _QUAD_ST[k]
+            S = st[pa1] if gs1 == 1 else 1 - st[pa1]
+            T = st[pa2] if gt1 == 1 else 1 - st[pa2]
+            if glob[_QUAD_ST.index((S, T))] != w:
+                ok = False
+                break
+        if ok:
+            return o
+    raise ValueError("quad face vertices do not match")
+
+
+def build_mesh(etypes, verts, X, grid, n, orders, kappa_logrange=None, seed=12345,
+               dirichlet=True):
+    """Conforming mesh from elements given by type and local vertex list.
+
+    X: vertex coordinates; grid: integer grid coordinates on [0, n]^3 (for
+    the Dirichlet boundary); orders: per element (px, py, pz) for a hexa,
+    (ph, pz) for a prism, (p,) for a tet.  Edge nodes run from the lower to
+    the higher vertex id, triangle faces list their vertices in increasing
+    id, quad faces take the frame of the first element that reaches them;
+    each element's NoriE / NoriF follow.  Edge and face orders follow the
+    minimum rule of the element orders along each global direction
+    (adapt/enforce_min_rule.F90); a face's (h, v) is in its own frame.
+    """
+    rng = np.random.default_rng(seed)
+    ne = len(etypes)
+    nverts = len(X)
+    edge_id, face_id, face_frame = {}, {}, {}
+    emin, fmin = {}, {}
+    enode = [[] for _ in range(ne)]
+    fnode = [[] for _ in range(ne)]
+    nori_e = np.zeros((ne, 12), np.int32)
+    nori_f = np.zeros((ne, 6), np.int32)
+    ford = [[] for _ in range(ne)]
+
+    def axis_order(t, o, ax):
+        if t == HEXA:
+            return int(o[ax])
+        if t == PRISM:
+            return int(o[0] if ax == 0 else o[1])
+        return int(o[0])
+
+    for e in range(ne):
+        t, v, o = etypes[e], verts[e], orders[e]
+        nv, edges, faces = _TOPO[t]
+        for q, ((a, b), ax) in enumerate(edges):
+            key = (min(v[a], v[b]), max(v[a], v[b]))
+            if key not in edge_id:
+                edge_id[key] = len(edge_id)
+            enode[e].append(key)
+            nori_e[e, q] = 0 if v[a] < v[b] else 1
+            emin[key] = min(emin.get(key, 99), axis_order(t, o, ax))
+        for q, (fv, (a1, a2)) in enumerate(faces):
+            loc = tuple(v[r] for r in fv)
+            key = tuple(sorted(loc))
+            if key not in face_id:
+                face_id[key] = len(face_id)
+                face_frame[key] = key if len(loc) == 3 else loc
+            fnode[e].append(key)
+            if len(loc) == 3:
+                nori_f[e, q] = tri_orientation(loc, face_frame[key])
+                h = (axis_order(t, o, a1), 0)
+            else:
+                oq = quad_orientation(loc, face_frame[key])
+                nori_f[e, q] = oq
+                ps, pt = axis_order(t, o, a1), axis_order(t, o, a2)
+                h = (pt, ps) if ORIENT_QUAD[oq][0] == 1 else (ps, pt)
+            cur = fmin.get(key, (99, 99))
+            fmin[key] = (min(cur[0], h[0]), min(cur[1], h[1]))
+    nedges = len(edge_id)
+    nnodes = nverts + nedges + len(face_id)
+    nodes = np.full((ne, 26), 0, np.int32)
+    bcflag = np.zeros((ne, 26), np.int32)
+    xvert = np.zeros((ne, 8, 3))
+    norder = np.zeros((ne, 19), np.int32)
+    grid = np.asarray(grid)
+    for e in range(ne):
+        t, v, o = etypes[e], verts[e], orders[e]
+        nv, edges, faces = _TOPO[t]
+        xvert[e, :nv] = X[list(v)]
+        k = 0
+        for q in range(nv):
+            nodes[e, k] = v[q]
+            bcflag[e, k] = int(_on_boundary(grid[[v[q]]], n))
+            k += 1
+        for q, key in enumerate(enode[e]):
+            nodes[e, k] = nverts + edge_id[key]
+            bcflag[e, k] = int(_on_boundary(grid[list(key)], n))
+            norder[e, q] = emin[key]
+            k += 1
+        for q, key in enumerate(fnode[e]):
+            nodes[e, k] = nverts + nedges + face_id[key]
+            bcflag[e, k] = int(_on_boundary(grid[list(key)], n))
+            h, vv = fmin[key]
+            norder[e, len(edges) + q] = h if len(key) == 3 else 10 * h + vv
+            k += 1
+        mid = len(edges) + len(faces)
+        if t == HEXA:
+            norder[e, mid] = 100 * o[0] + 10 * o[1] + o[2]
+        elif t == PRISM:
+            norder[e, mid] = 10 * o[0] + o[1]
+        else:
+            norder[e, mid] = o[0]
+    if not dirichlet:
+        bcflag[:] = 0
+    return dict(
+        nelem=ne, n=n, nnodes=nnodes, nverts=nverts, etype=np.asarray(etypes, np.int32),
+        norder=norder, nori_edge=nori_e, nori_face=nori_f, nodes=nodes, bcflag=bcflag,
+        xvert=xvert, kappa=_kappa(rng, ne, kappa_logrange), vertex_xyz=X,
+        orders=[tuple(int(x) for x in o) for o in orders],
+    )
+
+
+def _grid(n, perturb, rng):
+    nv1 = n + 1
+    idx = np.arange(nv1)
+    I, J, K = np.meshgrid(idx, idx, idx, indexing="ij")
+    coords = np.stack([I.ravel(order="F"), J.ravel(order="F"), K.ravel(order="F")], axis=1)
+    X = coords.astype(np.float64) / n
+    if perturb > 0.0:
+        interior = np.all((coords > 0) & (coords < n), axis=1)
+        d = rng.uniform(-perturb / n, perturb / n, size=X.shape)
+        X[interior] += d[interior]
+    return coords, X
+
+
+def _signed_volume(x, t):
+    # a positive Jacobian at the reference origin for the type's first corner
+    if t == TET:
+        return np.linalg.det(np.stack([x[1] - x[0], x[2] - x[0], x[3] - x[0]]))
+    return np.linalg.det(np.stack([x[1] - x[0], x[2] - x[0], x[3] - x[0]]))
+
+
+def _prism_cells(vid, c, axis):
+    """The two prisms of the unit cell at c extruded along `axis`, their
+    cross-section squares split along the diagonal through the cell's low
+    corner (matching the Kuhn split of the neighbouring tetrahedra)."""
+    u, w = [a for a in range(3) if a != axis]
+    e = np.eye(3, dtype=int)
+    p00, p10, p11, p01 = c, c + e[u], c + e[u] + e[w], c + e[w]
+    out = []
+    for tri in ((p00, p10, p11), (p00, p11, p01)):
+        bot = [vid(*q) for q in tri]
+        top = [vid(*(q + e[axis])) for q in tri]
+        out.append(bot + top)
+    return out
+
+
+def _hp_order(rng, centre, pmax, k):
+    r = np.linalg.norm(centre) / np.sqrt(3.0)
+    mean = 1.0 + (pmax - 1) * r
+    return tuple(int(min(x, pmax)) for x in rng.geometric(1.0 / max(mean, 1.0), size=k))
+
+
+def structured_prism(n, ph, pz, perturb=0.0, kappa_logrange=None, seed=12345, dirichlet=True):
+    """n^3 cells of [0,1]^3, each split into two prisms extruded along z."""
+    rng = np.random.default_rng(seed)
+    coords, X = _grid(n, perturb, rng)
+    nv1 = n + 1
+    vid = lambda i, j, k: int(i + nv1 * (j + nv1 * k))  # noqa: E731
+    verts = []
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                verts += _prism_cells(vid, np.array([i, j, k]), 2)
+    et = [PRISM] * len(verts)
+    return build_mesh(et, verts, X, coords, n, [(ph, pz)] * len(verts), kappa_logrange, seed,
+                      dirichlet)
+
+
+def mixed_mesh(n, a=0.875, b=0.875, p=None, pmax=6, perturb=0.0, kappa_logrange=(-1, 1),
+               seed=2024, dirichlet=True):
+    """Mixed hexa / prism / tet mesh of [0,1]^3 on an n^3 grid of cells:
+
+      x < a, z < b : hexahedra
+      x > a, z < b : prisms extruded along z
+      x > a, z > b : tetrahedra (Kuhn split of each cell)
+      x < a, z > b : prisms extruded along x
+
+    Every interface is conforming: hexa faces meet prism quads, prism
+    triangles meet tetrahedron faces split along the same diagonals.  With
+    p=None the orders are drawn per element in 1..pmax from a seeded
+    geometric distribution whose mean falls toward (0,0,0) -- (px,py,pz) for
+    a hexa, (ph,pz) for a prism, p for a tet -- and edges/faces take the
+    minimum rule; otherwise every order is p.
+    """
+    rng = np.random.default_rng(seed)
+    coords, X = _grid(n, perturb, rng)
+    nv1 = n + 1
+    vid = lambda i, j, k: int(i + nv1 * (j + nv1 * k))  # noqa: E731
+    ia, kb = int(round(a * n)), int(round(b * n))
+    et, verts, orders = [], [], []
+    e3 = np.eye(3, dtype=int)
+    perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
+    for k in range(n):
+        for j in range(n):
+            for i in range(n):
+                c = np.array([i, j, k])
+                centre = (c + 0.5) / n
+                if i < ia and k < kb:
+                    v = [vid(*(c + d)) for d in _VOFF]
+                    et.append(HEXA); verts.append(v)
+                    orders.append((p, p, p) if p else _hp_order(rng, centre, pmax, 3))
+                elif k < kb or i < ia:
+                    for v in _prism_cells(vid, c, 2 if k < kb else 0):
+                        et.append(PRISM); verts.append(v)
+                        orders.append((p, p) if p else _hp_order(rng, centre, pmax, 2))
+                else:
+                    for pa in perms:
+                        path = [c, c + e3[pa[0]], c + e3[pa[0]] + e3[pa[1]], c + 1]
+                        v = [vid(*q) for q in path]
+                        if _signed_volume(X[v], TET) < 0:
+                            v[2], v[3] = v[3], v[2]
+                        et.append(TET); verts.append(v)
+                        orders.append((p,) if p else _hp_order(rng, centre, pmax, 1))
+    return build_mesh(et, verts, X, coords, n, orders, kappa_logrange, seed, dirichlet)

@@ -66,7 +66,8 @@ typedef struct hp3dg_opts {
                           (set_3D_int.F90:236-244), capped at MAXP */
   int32_t isol;        /* source selector of getf (common/getf.F90:63):
                           0,1,2 as common/solution.F90; 10 = sin sin sin;
-                          11 = f == 1; 12 = u = xyz (f = 0) */
+                          11 = f == 1; 12 = u = xyz (f = 0);
+                          13 = u = 1 + x + 2y + 3z (f = 0) */
   int32_t keep_elem;   /* 1: keep the unconstrained element matrices so that
                           hp3dg_get_elem can serve the elem() contract */
   int32_t timing;      /* 1: record per-phase CUDA-event timings */

@@ -256,6 +256,10 @@ int orc_nrdofH_bubble(int etype, const int32_t *norder) {
     int p = norder[10];
     return (p - 3) * (p - 2) * (p - 1) / 6 > 0 ? (p - 3) * (p - 2) * (p - 1) / 6 : 0;
   }
+  if (etype == ORC_PRISM) {
+    int ph = norder[14] / 10, pz = norder[14] % 10;
+    return (ph > 2 && pz > 1) ? (ph - 1) * (ph - 2) / 2 * (pz - 1) : 0;
+  }
   return -1;
 }
 
@@ -479,6 +483,11 @@ static void solution(int isol, const double *X, double *u, double *gu,
       gu[0] = x2 * x3; gu[1] = x1 * x3; gu[2] = x1 * x2;
       *hess_trace = 0.0;
       break;
+    case 13: /* u = 1 + x + 2y + 3z: in the space of every order (f = 0) */
+      *u = 1.0 + x1 + 2.0 * x2 + 3.0 * x3;
+      gu[0] = 1.0; gu[1] = 2.0; gu[2] = 3.0;
+      *hess_trace = 0.0;
+      break;
     default:
       break;
   }
@@ -503,6 +512,7 @@ static int shape_dispatch(int etype, const double *xi, const int32_t *norder,
                           double *shap, double *grad) {
   if (etype == ORC_HEXA) return orc_shape3DH_hexa(xi, norder, noriE, noriF, shap, grad);
   if (etype == ORC_TET) return orc_shape3DH_tet(xi, norder, noriE, noriF, shap, grad);
+  if (etype == ORC_PRISM) return orc_shape3DH_prism(xi, norder, noriE, noriF, shap, grad);
   return -1;
 }
 
@@ -510,6 +520,7 @@ static int quad_dispatch(int etype, const int32_t *norder, const int32_t *noriF,
                          int integration, double *xi, double *w) {
   if (etype == ORC_HEXA) return orc_set_3D_int_hexa(norder, noriF, integration, xi, w);
   if (etype == ORC_TET) return orc_set_3D_int_tet(norder, integration, xi, w);
+  if (etype == ORC_PRISM) return orc_set_3D_int_prism(norder, noriF, integration, xi, w);
   return -1;
 }
 
@@ -736,6 +747,19 @@ int orc_node_ndof(int etype, const int32_t *norder, int32_t *ndof) {
     }
     return 14;
   }
+  if (etype == ORC_PRISM) {
+    for (int v = 0; v < 6; ++v) ndof[v] = 1;
+    for (int e = 0; e < 9; ++e) ndof[6 + e] = imax(norder[e] - 1, 0);
+    for (int f = 0; f < 2; ++f) {
+      int p = norder[9 + f];
+      ndof[15 + f] = (p - 2) * (p - 1) / 2 > 0 ? (p - 2) * (p - 1) / 2 : 0;
+    }
+    for (int f = 0; f < 3; ++f) {
+      int h = norder[11 + f] / 10, v = norder[11 + f] % 10;
+      ndof[17 + f] = imax(h - 1, 0) * imax(v - 1, 0);
+    }
+    return 20;
+  }
   return -1;
 }
 
@@ -848,7 +872,8 @@ int orc_element_pass(int nelem, const int32_t *etype, const int32_t *norder,
     for (int e = 0; e < nelem; ++e) {
       int et = etype[e];
       const int32_t *no = &norder[19 * (size_t)e];
-      int n = (et == ORC_HEXA) ? orc_nrdofH_hexa(no) : orc_nrdofH_tet(no);
+      int n = (et == ORC_HEXA) ? orc_nrdofH_hexa(no)
+              : (et == ORC_TET) ? orc_nrdofH_tet(no) : orc_nrdofH_prism(no);
       int nb = orc_nrdofH_bubble(et, no);
       int ni = n - nb;
       int nv = nvert_of(et);
@@ -1158,6 +1183,258 @@ int orc_shape3DH_tet(const double *xi, const int32_t *nord,
           shap[m] = phi[i][j] * hv;
           for (int c = 0; c < 3; ++c)
             grad[3 * m + c] = hv * dphi[i][j][c] + phi[i][j] * dhb[nij - 2][k][c];
+        }
+  }
+  return m;
+}
+
+
+/* ------------------------------------------------------------------------ */
+/* Triangle rules for the prism: Dunavant's symmetric rules of degree        */
+/* 2,4,...,12 as tabulated in init_gauss_quadrature (gauss_quadrature.F90:  */
+/* 130-270: barcoo = weight + barycentric triple per orbit, nnod = orbit     */
+/* size), expanded into points as at gauss_quadrature.F90:663-700.  Only the */
+/* sets NSELECT(1..MAXP) = 2,4,...,12 are needed.                            */
+/* ------------------------------------------------------------------------ */
+typedef struct { int set, size; double w, b1, b2, b3; } orc_orbit;
+static const orc_orbit ORC_TRI_ORBITS[] = {
+    {2, 3, 0.333333333333333, 0.666666666666667, 0.166666666666667, 0.166666666666667},
+    {4, 3, 0.223381589678011, 0.10810301816807, 0.445948490915965, 0.445948490915965},
+    {4, 3, 0.109951743655322, 0.816847572980459, 0.091576213509771, 0.091576213509771},
+    {6, 3, 0.116786275726379, 0.501426509658179, 0.24928674517091, 0.24928674517091},
+    {6, 3, 0.050844906370207, 0.873821971016996, 0.063089014491502, 0.063089014491502},
+    {6, 6, 0.082851075618374, 0.053145049844817, 0.310352451033784, 0.636502499121399},
+    {8, 1, 0.144315607677787, 0.333333333333333, 0.333333333333333, 0.333333333333333},
+    {8, 3, 0.095091634267285, 0.081414823414554, 0.459292588292723, 0.459292588292723},
+    {8, 3, 0.103217370534718, 0.65886138449648, 0.17056930775176, 0.17056930775176},
+    {8, 3, 0.032458497623198, 0.898905543365938, 0.050547228317031, 0.050547228317031},
+    {8, 6, 0.027230314174435, 0.008394777409958, 0.263112829634638, 0.728492392955404},
+    {10, 1, 0.090817990382754, 0.333333333333333, 0.333333333333333, 0.333333333333333},
+    {10, 3, 0.036725957756467, 0.028844733232685, 0.485577633383657, 0.485577633383657},
+    {10, 3, 0.045321059435528, 0.781036849029926, 0.109481575485037, 0.109481575485037},
+    {10, 6, 0.07275791684542, 0.14170721941488, 0.307939838764121, 0.550352941820999},
+    {10, 6, 0.028327242531057, 0.025003534762686, 0.246672560639903, 0.728323904597411},
+    {10, 6, 0.009421666963733, 0.009540815400299, 0.0668032510122, 0.9236559335875},
+    {12, 3, 0.025731066440455, 0.02356522045239, 0.488217389773805, 0.488217389773805},
+    {12, 3, 0.043692544538038, 0.120551215411079, 0.43972439229446, 0.43972439229446},
+    {12, 3, 0.062858224217885, 0.457579229975768, 0.271210385012116, 0.271210385012116},
+    {12, 3, 0.034796112930709, 0.744847708916828, 0.127576145541586, 0.127576145541586},
+    {12, 3, 0.006166261051559, 0.957365299093579, 0.02131735045321, 0.02131735045321},
+    {12, 6, 0.040371557766381, 0.115343494534698, 0.275713269685514, 0.608943235779788},
+    {12, 6, 0.022356773202303, 0.022838332222257, 0.28132558098994, 0.695836086787803},
+    {12, 6, 0.017316231108659, 0.02573405054833, 0.116251915907597, 0.858014033544073},
+};
+static const int ORC_NSELECT[7] = {0, 2, 4, 6, 8, 10, 12}; /* NSELECT(1:6) */
+
+/* Points (barycentric, 3 per point) and weights (summing to 1) of set np. */
+static int tri_rule(int np, double *bar, double *w) {
+  int i = 0;
+  for (size_t o = 0; o < sizeof(ORC_TRI_ORBITS) / sizeof(ORC_TRI_ORBITS[0]); ++o) {
+    const orc_orbit *r = &ORC_TRI_ORBITS[o];
+    if (r->set != np) continue;
+    double x[6] = {r->b1, r->b2, r->b3, r->b1, r->b2, r->b3};
+    for (int k = 0; k < 3; ++k) bar[3 * i + k] = x[k];
+    w[i++] = r->w;
+    if (r->size == 1) continue;
+    for (int k = 0; k < 3; ++k) {
+      bar[3 * i + k] = x[k + 1];
+      bar[3 * (i + 1) + k] = x[k + 2];
+    }
+    w[i] = r->w;
+    w[i + 1] = r->w;
+    i += 2;
+    if (r->size == 3) continue;
+    for (int l = 1; l <= 3; ++l) {
+      for (int k = 1; k <= 3; ++k) bar[3 * (i + l - 1) + (k - 1)] = x[3 + l - k - 1];
+      w[i + l - 1] = r->w;
+    }
+    i += 3;
+  }
+  return i;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Prism H1 (Prism.F90:33-330; AffinePrism, AffineCoordinates.F90:91-110;    */
+/* BlendPrisV / BlendProjectPrisME / QE / TF / ProjectPrisQF,                 */
+/* BlendProject.F90:562-804; OrientQuad, Orient.F90:39-116; AncPhiQuad,       */
+/* Ancillary.F90:171-206).  Norder(15): 6 mixed (horizontal) edges, 3 quad    */
+/* (vertical) edges, 2 triangle faces, 3 quad faces (h*10+v), interior        */
+/* (ph*10+pz).                                                                */
+/* ------------------------------------------------------------------------ */
+static const int PRIS_NUPAIR[3][2] = {{0, 1}, {1, 2}, {0, 2}}; /* ME 1-3 (4-6), QF 1-3 */
+
+static void decod2i(int v, int *a, int *b) { *a = v / 10; *b = v % 10; }
+
+int orc_nrdofH_prism(const int32_t *norder) {
+  int n = 6;
+  for (int e = 0; e < 9; ++e) n += imax(norder[e] - 1, 0);
+  for (int f = 0; f < 2; ++f) n += tri_ndof(norder[9 + f]);
+  for (int f = 0; f < 3; ++f) {
+    int h, v;
+    decod2i(norder[11 + f], &h, &v);
+    n += imax(h - 1, 0) * imax(v - 1, 0);
+  }
+  int ph, pz;
+  decod2i(norder[14], &ph, &pz);
+  return n + tri_ndof(ph) * imax(pz - 1, 0);
+}
+
+/* set_3Dint_aux PRISM branch (set_3D_int.F90:264-300) on find_order_loc
+ * orders (find_order.F90:88-94: quad faces swap (h,v) when NFAXES says so). */
+int orc_set_3D_int_prism(const int32_t *norder, const int32_t *nori_face, int integration,
+                         double *xiloc, double *waloc) {
+  int32_t loc[19];
+  for (int i = 0; i < 19; ++i) loc[i] = norder[i];
+  static const int NFAXES3[8] = {0, 1, 0, 1, 1, 0, 1, 0};
+  for (int j = 0; j < 3; ++j)
+    if (nori_face && NFAXES3[nori_face[2 + j] & 7]) {
+      int h, v;
+      decod2i(norder[11 + j], &h, &v);
+      loc[11 + j] = v * 10 + h;
+    }
+  int nordh = 0, nordz = 0;
+  for (int i = 1; i <= 15; ++i) {
+    if ((i >= 1 && i <= 6) || i == 10 || i == 11) nordh = imax(nordh, loc[i - 1]);
+    else if (i >= 7 && i <= 9) nordz = imax(nordz, loc[i - 1]);
+    else {
+      int h, v;
+      decod2i(loc[i - 1], &h, &v);
+      nordh = imax(nordh, h);
+      nordz = imax(nordz, v);
+    }
+  }
+  nordh = imin(nordh + integration, ORC_MAXP);
+  nordz = imin(nordz + integration, ORC_MAXP);
+  if (nordh < 1 || nordz < 1) return -1;
+  double bar[3 * 40], wt[40], xz[16], wz[16];
+  int nintx = tri_rule(ORC_NSELECT[nordh], bar, wt);
+  int nintz = nordz + 1;
+  orc_gauss1d(nintz, xz, wz);
+  int l = 0;
+  for (int l2 = 0; l2 < nintz; ++l2)
+    for (int l1 = 0; l1 < nintx; ++l1) {
+      xiloc[3 * l + 0] = bar[3 * l1 + 1];
+      xiloc[3 * l + 1] = bar[3 * l1 + 2];
+      xiloc[3 * l + 2] = xz[l2];
+      waloc[l] = wt[l1] / 2.0 * wz[l2];
+      ++l;
+    }
+  return l;
+}
+
+int orc_shape3DH_prism(const double *xi, const int32_t *nord,
+                       const int32_t *nori_edge, const int32_t *nori_face,
+                       double *shap, double *grad) {
+  const double Nu[3] = {1.0 - xi[0] - xi[1], xi[0], xi[1]};
+  const double DNu[3][3] = {{-1.0, -1.0, 0.0}, {1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}};
+  const double Mu[2] = {1.0 - xi[2], xi[2]};
+  const double DMu[2][3] = {{0.0, 0.0, -1.0}, {0.0, 0.0, 1.0}};
+  int m = 0;
+  /* vertices: Nu(v mod 3) * Mu(v / 3) */
+  for (int v = 0; v < 6; ++v, ++m) {
+    int a = v % 3, b = v / 3;
+    shap[m] = Nu[a] * Mu[b];
+    for (int c = 0; c < 3; ++c) grad[3 * m + c] = DNu[a][c] * Mu[b] + Nu[a] * DMu[b][c];
+  }
+  /* mixed edges: homogenized Legendre of the oriented Nu pair (Idec false) x Mu */
+  for (int e = 0; e < 6; ++e) {
+    int p = nord[e];
+    if (p - 1 <= 0) continue;
+    int a = PRIS_NUPAIR[e % 3][0], b = PRIS_NUPAIR[e % 3][1], mb = e / 3;
+    if (nori_edge[e] == 1) { int t = a; a = b; b = t; }
+    double S[2] = {Nu[a], Nu[b]}, DS[3][2];
+    for (int c = 0; c < 3; ++c) { DS[c][0] = DNu[a][c]; DS[c][1] = DNu[b][c]; }
+    double phi[16], dphi[16][3];
+    hom_ilegendre(S, DS, p, 0, phi, dphi);
+    for (int i = 2; i <= p; ++i, ++m) {
+      shap[m] = phi[i] * Mu[mb];
+      for (int c = 0; c < 3; ++c) grad[3 * m + c] = dphi[i][c] * Mu[mb] + phi[i] * DMu[mb][c];
+    }
+  }
+  /* quad (vertical) edges: Legendre of the oriented Mu pair (Idec true) x Nu */
+  for (int e = 0; e < 3; ++e) {
+    int p = nord[6 + e];
+    if (p - 1 <= 0) continue;
+    int o0 = nori_edge[6 + e] == 1 ? 1 : 0, o1 = 1 - o0;
+    double S[2] = {Mu[o0], Mu[o1]}, DS[3][2];
+    for (int c = 0; c < 3; ++c) { DS[c][0] = DMu[o0][c]; DS[c][1] = DMu[o1][c]; }
+    double phi[16], dphi[16][3];
+    hom_ilegendre(S, DS, p, 1, phi, dphi);
+    for (int i = 2; i <= p; ++i, ++m) {
+      shap[m] = phi[i] * Nu[e];
+      for (int c = 0; c < 3; ++c) grad[3 * m + c] = dphi[i][c] * Nu[e] + phi[i] * DNu[e][c];
+    }
+  }
+  /* triangle faces: AncPhiTri of the oriented Nu triple (Idec true) x Mu */
+  for (int f = 0; f < 2; ++f) {
+    int p = nord[9 + f];
+    if (tri_ndof(p) <= 0) continue;
+    const int *o = ORIENT_TRI[nori_face[f]];
+    double S[3], DS[3][3];
+    for (int k = 0; k < 3; ++k) {
+      S[k] = Nu[o[k]];
+      for (int c = 0; c < 3; ++c) DS[c][k] = DNu[o[k]][c];
+    }
+    double phi[JMAX][JMAX], dphi[JMAX][JMAX][3];
+    anc_phi_tri(S, DS, p, 1, phi, dphi);
+    for (int nij = 3; nij <= p; ++nij)
+      for (int i = 2; i <= nij - 1; ++i, ++m) {
+        int j = nij - i;
+        shap[m] = phi[i][j] * Mu[f];
+        for (int c = 0; c < 3; ++c) grad[3 * m + c] = dphi[i][j][c] * Mu[f] + phi[i][j] * DMu[f][c];
+      }
+  }
+  /* quad faces: OrientQuad of ((Nu pair; Idec false), (Mu pair; Idec true)), AncPhiQuad */
+  for (int f = 0; f < 3; ++f) {
+    int nf[2];
+    decod2i(nord[11 + f], &nf[0], &nf[1]);
+    if (nf[0] < 2 || nf[1] < 2) continue;
+    /* ST(k, pair): pair 0 = Nu pair, pair 1 = Mu pair */
+    double ST[2][2], DST[2][2][3];
+    int idec[2] = {0, 1};
+    int a = PRIS_NUPAIR[f][0], b = PRIS_NUPAIR[f][1];
+    ST[0][0] = Nu[a]; ST[1][0] = Nu[b];
+    ST[0][1] = Mu[0]; ST[1][1] = Mu[1];
+    for (int c = 0; c < 3; ++c) {
+      DST[0][0][c] = DNu[a][c]; DST[1][0][c] = DNu[b][c];
+      DST[0][1][c] = DMu[0][c]; DST[1][1][c] = DMu[1][c];
+    }
+    const int *oq = ORQ[nori_face[2 + f] & 7];
+    int pa1 = oq[0], pa2 = oq[1];
+    double GS[2] = {ST[oq[2]][pa1], ST[oq[3]][pa1]}, GT[2] = {ST[oq[4]][pa2], ST[oq[5]][pa2]};
+    double GDS[3][2], GDT[3][2];
+    for (int c = 0; c < 3; ++c) {
+      GDS[c][0] = DST[oq[2]][pa1][c]; GDS[c][1] = DST[oq[3]][pa1][c];
+      GDT[c][0] = DST[oq[4]][pa2][c]; GDT[c][1] = DST[oq[5]][pa2][c];
+    }
+    double phs[16], dphs[16][3], pht[16], dpht[16][3];
+    hom_ilegendre(GS, GDS, nf[0], idec[pa1], phs, dphs);
+    hom_ilegendre(GT, GDT, nf[1], idec[pa2], pht, dpht);
+    for (int j = 2; j <= nf[1]; ++j)
+      for (int i = 2; i <= nf[0]; ++i, ++m) {
+        shap[m] = phs[i] * pht[j];
+        for (int c = 0; c < 3; ++c) grad[3 * m + c] = phs[i] * dpht[j][c] + pht[j] * dphs[i][c];
+      }
+  }
+  /* bubbles: AncPhiTri(Nu; Idec true) x AncPhiE(Mu; Idec true) */
+  int ph, pz;
+  decod2i(nord[14], &ph, &pz);
+  if (tri_ndof(ph) > 0 && pz >= 2) {
+    double S[3] = {Nu[0], Nu[1], Nu[2]}, DS[3][3];
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) DS[c][k] = DNu[k][c];
+    double phi[JMAX][JMAX], dphi[JMAX][JMAX][3];
+    anc_phi_tri(S, DS, ph, 1, phi, dphi);
+    double Sz[2] = {Mu[0], Mu[1]}, DSz[3][2];
+    for (int c = 0; c < 3; ++c) { DSz[c][0] = DMu[0][c]; DSz[c][1] = DMu[1][c]; }
+    double pe[16], dpe[16][3];
+    hom_ilegendre(Sz, DSz, pz, 1, pe, dpe);
+    for (int k = 2; k <= pz; ++k)
+      for (int nij = 3; nij <= ph; ++nij)
+        for (int i = 2; i <= nij - 1; ++i, ++m) {
+          int j = nij - i;
+          shap[m] = phi[i][j] * pe[k];
+          for (int c = 0; c < 3; ++c) grad[3 * m + c] = dphi[i][j][c] * pe[k] + phi[i][j] * dpe[k][c];
         }
   }
   return m;

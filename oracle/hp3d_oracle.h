@@ -68,13 +68,22 @@ int orc_shape3DH_tet(const double *xi, const int32_t *nord,
                      const int32_t *nori_edge, const int32_t *nori_face,
                      double *shap, double *grad);
 
+/* Prism: celndof count, set_3D_int (triangle rule x Gauss, set_3D_int.F90:
+ * 264-300 on find_order_loc orders) and shape3DHPris (Prism.F90:33-330). */
+int orc_nrdofH_prism(const int32_t *norder);
+int orc_set_3D_int_prism(const int32_t *norder, const int32_t *nori_face, int integration,
+                         double *xiloc, double *waloc);
+int orc_shape3DH_prism(const double *xi, const int32_t *nord,
+                       const int32_t *nori_edge, const int32_t *nori_face,
+                       double *shap, double *grad);
+
 /* geom (geom.F90:30-138): det and cofactor inverse; returns Iflag. */
 int orc_geom(const double *dxdxi, double *dxidx, double *rjac);
 
 /* source term f = -Laplace(u) of the manufactured solution
  * (common/getf.F90:63, common/solution.F90:45-134).  isol 0,1,2 are the
  * reference's cases; 10 = sin(pi x)sin(pi y)sin(pi z), 11 = f==1,
- * 12 = u = x*y*z (test/poly_pois.F90:390-395). */
+ * 12 = u = x*y*z (test/poly_pois.F90:390-395), 13 = u = 1 + x + 2y + 3z. */
 double orc_getf(int isol, const double *x);
 /* exact solution value and gradient (for error evaluation) */
 void orc_exact(int isol, const double *x, double *u, double *gradu);

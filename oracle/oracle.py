@@ -43,8 +43,10 @@ def lib():
         L.orc_set_3D_int_tet.argtypes = [_i32p, ctypes.c_int, _f64p, _f64p]
         L.orc_nrdofH_hexa.argtypes = [_i32p]
         L.orc_nrdofH_tet.argtypes = [_i32p]
+        L.orc_nrdofH_prism.argtypes = [_i32p]
+        L.orc_set_3D_int_prism.argtypes = [_i32p, _i32p, ctypes.c_int, _f64p, _f64p]
         L.orc_nrdofH_bubble.argtypes = [ctypes.c_int, _i32p]
-        for f in (L.orc_shape3DH_hexa, L.orc_shape3DH_tet):
+        for f in (L.orc_shape3DH_hexa, L.orc_shape3DH_tet, L.orc_shape3DH_prism):
             f.argtypes = [_f64p, _i32p, _i32p, _i32p, _f64p, _f64p]
         L.orc_geom.argtypes = [_f64p, _f64p, _f64p]
         L.orc_getf.argtypes = [ctypes.c_int, _f64p]
@@ -103,6 +105,8 @@ def nrdofH(etype, norder):
     norder = _i32(norder)
     if etype == HEXA:
         return lib().orc_nrdofH_hexa(_p(norder, _i32p))
+    if etype == PRISM:
+        return lib().orc_nrdofH_prism(_p(norder, _i32p))
     return lib().orc_nrdofH_tet(_p(norder, _i32p))
 
 
@@ -132,9 +136,30 @@ def shape_tet(xi, norder, nori_edge=None, nori_face=None):
     return shap[:n].copy(), grad[:n].copy()
 
 
+def shape_prism(xi, norder, nori_edge=None, nori_face=None):
+    xi = _f64(xi)
+    norder = _i32(norder)
+    ne = _i32(np.zeros(12) if nori_edge is None else nori_edge)
+    nf = _i32(np.zeros(6) if nori_face is None else nori_face)
+    shap = np.zeros(343); grad = np.zeros((343, 3))
+    n = lib().orc_shape3DH_prism(_p(xi, _f64p), _p(norder, _i32p), _p(ne, _i32p),
+                                 _p(nf, _i32p), _p(shap, _f64p), _p(grad, _f64p))
+    return shap[:n].copy(), grad[:n].copy()
+
+
+def quad_prism(norder, nori_face=None, integration=0):
+    nf = _i32(np.zeros(6) if nori_face is None else nori_face)
+    xi = np.zeros(3 * 400); w = np.zeros(400)
+    n = lib().orc_set_3D_int_prism(_p(_i32(norder), _i32p), _p(nf, _i32p), integration,
+                                   _p(xi, _f64p), _p(w, _f64p))
+    return xi[: 3 * n].reshape(n, 3).copy(), w[:n].copy()
+
+
 def shape(etype, xi, norder, nori_edge=None, nori_face=None):
     if etype == TET:
         return shape_tet(xi, norder, nori_edge, nori_face)
+    if etype == PRISM:
+        return shape_prism(xi, norder, nori_edge, nori_face)
     return shape_hexa(xi, norder, nori_edge, nori_face)
 
 

@@ -15,6 +15,7 @@ import scipy.sparse as sp
 import scipy.sparse.linalg as spla
 
 from oracle import oracle as O
+from hp3d_gb300 import mesh as M
 
 # local vertex numbers of each hexa edge / face (element_data.F90 hexa tables)
 HEXA_EDGE_V = [(0, 1), (1, 2), (3, 2), (0, 3), (4, 5), (5, 6), (7, 6), (4, 7),
@@ -24,19 +25,22 @@ HEXA_FACE = [(2, 0.0, 0, 1), (2, 1.0, 0, 1), (1, 0.0, 0, 2), (0, 1.0, 1, 2),
              (1, 1.0, 0, 2), (0, 0.0, 1, 2)]
 _VREF = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0],
                   [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]], dtype=float)
-# tetrahedron (BlendProject.F90 BlendTetV / ProjectTetE / ProjectTetF)
+# tetrahedron and prism reference vertices (BlendProject.F90 BlendTetV, BlendPrisV)
 TET_VREF = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], dtype=float)
+PRISM_VREF = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [0, 1, 1]],
+                      dtype=float)
 TET_EDGE_V = [(0, 1), (1, 2), (0, 2), (0, 3), (1, 3), (2, 3)]
 TET_FACE_V = [(0, 1, 2), (0, 1, 3), (1, 2, 3), (0, 2, 3)]
 
-HEXA, TET = 1, 3
+HEXA, PRISM, TET = 1, 2, 3
 
 
 def type_info(etype):
-    """(vertex count, node count, reference vertices, edge vertex pairs)."""
-    if etype == TET:
-        return 4, 14, TET_VREF, TET_EDGE_V
-    return 8, 26, _VREF, HEXA_EDGE_V
+    """(vertex count, node count, reference vertices, edge vertex pairs,
+    face vertex lists in the element's frame order)."""
+    nv, edges, faces = M._TOPO[etype]
+    vref = {HEXA: _VREF, PRISM: PRISM_VREF, TET: TET_VREF}[etype]
+    return nv, nv + len(edges) + len(faces), vref, [e for e, _ in edges], [f for f, _ in faces]
 
 
 def nnode_of(mesh):
@@ -48,23 +52,23 @@ def _xmap(xv, shap):
 
 
 def _face_points(etype, f):
-    """Quadrature points (reference coordinates) and weights on face f."""
+    """Quadrature points (reference coordinates) and weights on face f:
+    a collapsed Gauss rule on triangles, a bilinear map of the unit square
+    through the face's vertices on quadrilaterals."""
+    vref, fv = type_info(etype)[2], type_info(etype)[4][f]
     gs, gw = O.gauss1d(8)
     pts, wts = [], []
-    if etype == TET:
-        a, b, c = (TET_VREF[q] for q in TET_FACE_V[f])
-        for s1, w1 in zip(gs, gw):
-            for t1, w2 in zip(gs, gw):
-                u, v = s1 * (1 - t1), t1  # collapsed square -> triangle
-                pts.append(a + u * (b - a) + v * (c - a))
-                wts.append(w1 * w2 * (1 - t1))
-        return pts, wts
-    ax, v0, sa, ta = HEXA_FACE[f]
+    V = [vref[q] for q in fv]
     for s1, w1 in zip(gs, gw):
         for t1, w2 in zip(gs, gw):
-            xi = np.zeros(3)
-            xi[ax] = v0; xi[sa] = s1; xi[ta] = t1
-            pts.append(xi); wts.append(w1 * w2)
+            if len(V) == 3:
+                u, v = s1 * (1 - t1), t1
+                pts.append(V[0] + u * (V[1] - V[0]) + v * (V[2] - V[0]))
+                wts.append(w1 * w2 * (1 - t1))
+            else:
+                pts.append((1 - s1) * (1 - t1) * V[0] + s1 * (1 - t1) * V[1] + s1 * t1 * V[2]
+                           + (1 - s1) * t1 * V[3])
+                wts.append(w1 * w2)
     return pts, wts
 
 
@@ -81,7 +85,7 @@ def dirichlet_data(mesh, isol):
     out = []
     for e in range(ne):
         et = int(mesh["etype"][e])
-        nv, nn, vref, edges = type_info(et)
+        nv, nn, vref, edges, _ = type_info(et)
         nd = O.node_ndof(et, no[e])
         first = np.concatenate([[0], np.cumsum(nd)])
         ni = int(first[-1])
