@@ -245,14 +245,25 @@ def main():
     nel = mesh["nelem"]
     value = world * nel / (ms_step / 1000.0)
 
-    # end to end through the C ABI with host buffers (submit + run + download)
+    # end to end through the C ABI with host buffers (submit + run + download).
+    # Each step resubmits the mesh with this step's geometry and coefficient:
+    # the descriptors equal the batch's, so submit uploads xvert and kappa
+    # (the per-step inputs) and keeps the device state; download copies the
+    # condensed matrices, loads, Schur blocks and LCON into pinned buffers.
     nnz, nl, ns, nbub = ep.sizes()
-    h2d = int(ep.desc.nbytes + ep.xvert.nbytes + ep.kappa.nbytes)
     d2h = int(8 * (nnz + nl + ns + nbub) + 4 * nl)
+    rng = np.random.default_rng(7 + rank)
+    steps_in = []
+    for _ in range(args.e2e_steps):
+        mk = dict(mesh)
+        mk["kappa"] = mesh["kappa"] * (1.0 + 0.01 * rng.random(mesh["nelem"]))
+        steps_in.append(mk)
+    h2d = int(mesh["xvert"].nbytes + mesh["kappa"].nbytes)
+    ep.submit(mesh); ep.run(); ep.download()  # pinned result buffers exist from here on
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        ep.submit(mesh)
+    for mk in steps_in:
+        ep.submit(mk)
         ep.run()
         ep.download()
     torch.cuda.synchronize()
@@ -261,8 +272,21 @@ def main():
         t = torch.tensor([e2e_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_s = float(t.item())
+    # one cold step: a new context (descriptor processing, allocations, bin
+    # tables, operand digits, graph capture, pinned buffers) for reference
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    epc = H.ElementPass(prec, integration=args.integration, isol=args.isol, device=local)
+    epc.set_stream(stream.cuda_stream)
+    epc.submit(mesh); epc.run(); epc.download()
+    torch.cuda.synchronize()
+    cold_ms = 1000 * (time.perf_counter() - t0)
+    epc.close()
     e2e = {"value": world * nel / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * e2e_s}
+           "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * e2e_s,
+           "cold_step_ms": cold_ms,
+           "note": "resubmit of the mesh with new kappa each step (upload xvert+kappa, "
+                   "run, download all condensed outputs); cold_step_ms = new context"}
 
     # the plain FP64 GPU form on the same mesh (the comparison the metric names)
     fp64 = None

@@ -375,7 +375,8 @@ struct hp3dg_ctx {
   bool have_dofs = false;
   cudaEvent_t ev[8] = {};
   float times[6] = {0, 0, 0, 0, 0, 0};
-  cudaGraphExec_t graph = nullptr;  // the captured pass; rebuilt after every submit
+  cudaGraphExec_t graph = nullptr;  // the captured pass; rebuilt after every new structure
+  std::vector<hp3dg_elem_desc> last_desc;  // descriptors of the current batch
 };
 
 namespace {
@@ -482,7 +483,28 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
                        int32_t nnodes) {
   if (!c || nel < 0 || (nel > 0 && (!desc || !xvert)) || nnodes < 0) return HP3DG_ERR_ARG;
   cudaSetDevice(c->device);
+  // Resubmit of the same mesh (identical descriptors, node count and
+  // Dirichlet layout) with new geometry / coefficients / Dirichlet values:
+  // keep every buffer, the bin tables, the tensor-core operand digits, the
+  // captured graph and the pinned host buffers; upload the numeric inputs.
+  if (c->submitted && nel == c->nel && nnodes == c->nnodes && (zdofd != nullptr) == c->have_zdofd &&
+      nel > 0 && c->last_desc.size() == (size_t)nel &&
+      std::memcmp(c->last_desc.data(), desc, sizeof(hp3dg_elem_desc) * (size_t)nel) == 0) {
+    cudaStream_t st = c->stream;
+    CK(cudaMemcpyAsync(c->d_xvert, xvert, (size_t)nel * 24 * 8, cudaMemcpyHostToDevice, st));
+    if (kappa) {
+      CK(cudaMemcpyAsync(c->d_kappa, kappa, (size_t)nel * 8, cudaMemcpyHostToDevice, st));
+    } else {
+      std::vector<double> one(nel, 1.0);
+      CK(cudaMemcpyAsync(c->d_kappa, one.data(), (size_t)nel * 8, cudaMemcpyHostToDevice, st));
+      CK(cudaStreamSynchronize(st));
+    }
+    if (zdofd) CK(cudaMemcpyAsync(c->d_zdofd, zdofd, c->zd_off[nel] * 8, cudaMemcpyHostToDevice, st));
+    c->ran = c->downloaded = c->have_dofs = false;
+    return HP3DG_OK;
+  }
   free_batch(c);
+  c->last_desc.clear();
   c->nel = nel;
   c->nnodes = nnodes;
   c->n_e.assign(nel, 0); c->nb_e.assign(nel, 0); c->ni_e.assign(nel, 0);
@@ -658,6 +680,7 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
     }
   }
   CK(cudaStreamSynchronize(st));
+  c->last_desc.assign(desc, desc + nel);
   c->submitted = true;
   return HP3DG_OK;
 }

@@ -86,16 +86,19 @@ typedef struct hp3dg_opts {
  * find_orient (datstrs/find_orient.F90:8), elem_nodes and get_index
  * (datstrs/get_index.F90:27) return for element Mdle. */
 typedef struct hp3dg_elem_desc {
-  int32_t etype;         /* HP3DG_HEXA or HP3DG_TET */
+  int32_t etype;         /* HP3DG_HEXA, HP3DG_PRISM or HP3DG_TET */
   int32_t mdle;          /* middle node id, returned back for bookkeeping */
   int32_t norder[19];    /* Norder.  hexa: 12 edges, 6 faces (MODORDER=10
-                            packed), interior (3 digits); tet: 6 edges,
-                            4 faces, interior (one order each, 11 used) */
-  int32_t nori_edge[12]; /* NoriE: 0/1 (tet: 6 used) */
-  int32_t nori_face[6];  /* NoriF: hexa 0..7 (OrientQuad); tet 0..5
-                            (OrientTri, 4 used) */
+                            packed), interior (3 digits); prism: 6 mixed and
+                            3 vertical edges, 2 triangle faces, 3 quad faces
+                            (packed), interior (ph*10+pz), 15 used; tet:
+                            6 edges, 4 faces, interior, 11 used */
+  int32_t nori_edge[12]; /* NoriE: 0/1 (prism 9, tet 6 used) */
+  int32_t nori_face[6];  /* NoriF: quad faces 0..7 (OrientQuad), triangle
+                            faces 0..5 (OrientTri); prism: 2 triangles then
+                            3 quads; tet: 4 triangles */
   int32_t nodes[26];     /* global ids of vertex, edge, face nodes in element
-                            order (hexa 26, tet 14 used; the rest ignored) */
+                            order (hexa 26, prism 20, tet 14 used) */
   int32_t bcflag[26];    /* 1: every dof of this node is Dirichlet (index=1) */
 } hp3dg_elem_desc;
 
@@ -110,11 +113,15 @@ int hp3dg_set_stream(hp3dg_ctx *ctx, void *stream);
 /* Submit a batch: n_elem descriptors in ELEM_ORDER, vertex coordinates
  * xvert (n_elem x 8 x 3, the nodcor geometry dof of a trilinear map, a
  * tetrahedron using the first 4 vertex slots; higher-order geometry dof are
- * zero), per-element coefficient kappa
+ * zero; a prism the first 6), per-element coefficient kappa
  * (NULL = 1), Dirichlet data zdofd (NULL = homogeneous; else for each
  * element its interface dof values in element dof order, concatenated),
  * and the number of global nodes (size of NFIRST_DOF).
- * Validates orders and copies the batch to the device.
+ * Validates orders and copies the batch to the device.  A resubmit whose
+ * descriptors, node count and Dirichlet layout equal the current batch's
+ * (a new geometry, coefficient or Dirichlet data on the same mesh) only
+ * uploads xvert, kappa and zdofd: device buffers, bin tables, the captured
+ * pass and the pinned result buffers are kept.
  * Replaces: mumps_sc.F90 STEP 1 (102-188). */
 int hp3dg_batch_submit(hp3dg_ctx *ctx, int32_t n_elem, const hp3dg_elem_desc *desc,
                        const double *xvert, const double *kappa, const double *zdofd,

@@ -56,3 +56,19 @@ def test_graph_rebuilt_after_resubmit():
     ep2 = H.ElementPass(H.FP64, isol=10, graph=False)
     ep2.submit(m2); ep2.run(); ep2.download()
     _same(o_graph, _outputs(ep2))
+
+
+def test_resubmit_same_mesh_reuses_and_matches_fresh_submit():
+    """A resubmit with identical descriptors and new geometry / kappa takes
+    the upload-only path; its results equal a fresh context's bit for bit."""
+    m1 = M.hp_hexa(3, seed=3, perturb=0.1, kappa_logrange=(-1, 1))
+    m2 = dict(m1)
+    rng = np.random.default_rng(5)
+    m2["xvert"] = m1["xvert"] + rng.uniform(-0.01, 0.01, m1["xvert"].shape) / 3
+    m2["kappa"] = m1["kappa"] * 1.7
+    ep = H.ElementPass(H.MIXED, isol=10)
+    ep.submit(m1); ep.run(); ep.download()
+    ep.submit(m2); ep.run(); ep.download()
+    ref = H.ElementPass(H.MIXED, isol=10)
+    ref.submit(m2); ref.run(); ref.download()
+    _same(_outputs(ep), _outputs(ref))
