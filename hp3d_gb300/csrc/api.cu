@@ -330,6 +330,12 @@ struct Bin {
   OzakiPlan plan{};
   uint16_t *d_mdig = nullptr, *d_ddig = nullptr;
   double *d_mscale = nullptr, *d_dscale = nullptr;
+  // tensor-core Schur update (mixed): Y digits, column exponents, condensed load
+  bool tc_schur = false;
+  TcFactorOut tco{};
+  uint8_t* d_ydig = nullptr;
+  int* d_yexp = nullptr;
+  double* d_bi = nullptr;
 };
 
 }  // namespace
@@ -388,6 +394,7 @@ void free_bin(Bin& b) {
   cudaFree(b.d_perm); cudaFree(b.d_dmask); cudaFree(b.d_mdig); cudaFree(b.d_ddig);
   cudaFree(b.d_mscale); cudaFree(b.d_dscale);
   cudaFree(b.d_xi_err); cudaFree(b.d_wq_err); cudaFree(b.d_shap_err); cudaFree(b.d_grad_err);
+  cudaFree(b.d_ydig); cudaFree(b.d_yexp); cudaFree(b.d_bi);
   b = Bin();
 }
 
@@ -676,6 +683,20 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
       if (rc) { free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
       B.d_ddig = (uint16_t*)dalloc<uint8_t>(ozaki_d_bytes(B.plan, (int)ne), &err);
       B.d_dscale = dalloc<double>(ne + 128, &err);
+      B.tc_schur = !c->opts.schur_fp64 && !B.d_Yg &&
+                   schur_tc_supported(B.ni, B.nb, B.plan.digits);
+      if (B.tc_schur) {
+        TcFactorOut& t = B.tco;
+        t.nr = schur_tc_rows(B.ni);
+        t.nkb = schur_tc_kblocks(B.nb);
+        t.digits = B.plan.digits;
+        t.radix = B.plan.radix;
+        t.ebytes = schur_tc_elem_bytes(B.ni, B.nb, B.plan.digits);
+        B.d_ydig = dalloc<uint8_t>(ne * t.ebytes, &err);
+        B.d_yexp = dalloc<int>(ne * (size_t)t.nr, &err);
+        B.d_bi = dalloc<double>(ne * (size_t)B.ni, &err);
+        t.ydig = B.d_ydig; t.yexp = B.d_yexp; t.bi = B.d_bi;
+      }
       if (err) { free_batch(c); return err; }
     }
   }
@@ -726,12 +747,22 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
   mark(c, 3, st, capturing);
   for (auto& B : c->bins) {
     int ne = (int)B.elems.size();
+    const double* zd = c->have_zdofd ? c->d_zdofd : nullptr;
     if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
                         B.d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
-                        c->d_bub_off, c->d_zd_off, c->have_zdofd ? c->d_zdofd : nullptr, B.d_dmask,
-                        B.d_S, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur, B.d_Yg,
-                        c->d_flags + 1, st))
+                        c->d_bub_off, c->d_zd_off, zd, B.d_dmask, B.d_S, c->d_zastif,
+                        c->d_zbload, c->d_aschur, c->d_bschur, B.d_Yg, c->d_flags + 1, st,
+                        B.tc_schur ? &B.tco : nullptr))
       return HP3DG_ERR_CUDA;
+    if (B.tc_schur) {
+      // S = K_ii - Y^T Y on tensor cores, then the compression
+      if (launch_schur_tc(ne, B.n, B.ni, B.nb, B.tco.radix, B.tco.digits, B.d_ydig, B.d_yexp,
+                          B.d_elist, c->d_ni_e, B.d_S, c->d_flags + 2, st))
+        return HP3DG_ERR_CUDA;
+      launch_compress(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, B.d_PK, B.d_perm, B.d_S, B.d_bi,
+                      c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd, B.d_dmask,
+                      c->d_zastif, c->d_zbload, st);
+    }
   }
   mark(c, 4, st, capturing);
   launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,

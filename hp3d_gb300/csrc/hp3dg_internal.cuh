@@ -270,4 +270,14 @@ __host__ __device__ inline int64_t pk_index(int a, int b, int ni, int nb) {
   return (int64_t)c * (c + 1) / 2 + r;
 }
 
+// entry (a, b) of an element's matrix (element dof a, b) from the bin
+// element's packed matrix through the element's signed dof map pm
+__device__ inline double pk_get(const double* PKj, const uint32_t* pm, int a, int b, int ni,
+                                int nb) {
+  uint32_t ma = pm[a], mb = pm[b];
+  int ra = (int)(ma & 0x7fffffffu), rb = (int)(mb & 0x7fffffffu);
+  double v = PKj[pk_index(ra, rb, ni, nb)];
+  return ((ma ^ mb) & 0x80000000u) ? -v : v;
+}
+
 }  // namespace hp3dg

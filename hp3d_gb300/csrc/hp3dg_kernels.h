@@ -26,6 +26,17 @@ void launch_contract_fp64(int nel, int nint, int n, int ni, int nb, const double
                           const double* d_D, double* d_PK, cudaStream_t st);
 size_t condense_smem(int ni, int nb);
 size_t condense_smem_small(int ni, int nb);
+// Factor mode of the condensation (mixed pass): instead of the FP64 Schur
+// update and the compression, write Y = L^-1 K_bi as balanced BF16 digits
+// (per element ebytes: digit, k-block, nr x 16 canonical tile) with one
+// power-of-two exponent per column, and the condensed load bi (nif per element).
+struct TcFactorOut {
+  uint8_t* ydig = nullptr;
+  int* yexp = nullptr;
+  double* bi = nullptr;
+  int nr = 0, nkb = 0, digits = 0, radix = 0;
+  size_t ebytes = 0;
+};
 int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
                     const int* d_nb_e, const double* d_PK, const double* d_b0,
                     const uint32_t* d_perm, const int* d_nextract, const int64_t* d_lcon_off,
@@ -33,7 +44,22 @@ int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, co
                     const int64_t* d_bub_off, const int64_t* d_zd_off, const double* d_zdofd,
                     const uint8_t* d_dmask, double* d_S, double* d_zastif, double* d_zbload,
                     double* d_aschur, double* d_bschur, double* d_Yg, int* d_bad_spd,
-                    cudaStream_t st);
+                    cudaStream_t st, const TcFactorOut* tco = nullptr);
+// compression after the tensor-core update: S = K_ii (through the dof map)
+// - W, then Zastif / Zbload as compress_out
+void launch_compress(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
+                     const double* d_PK, const uint32_t* d_perm, const double* d_W,
+                     const double* d_bi, const int* d_nextract, const int64_t* d_lcon_off,
+                     const int64_t* d_elem_nnz, const int64_t* d_zd_off, const double* d_zdofd,
+                     const uint8_t* d_dmask, double* d_zastif, double* d_zbload, cudaStream_t st);
+// tensor-core Schur update S = K_ii - Y^T Y -- k_schur.cu
+int schur_tc_rows(int nif);
+int schur_tc_kblocks(int nbf);
+size_t schur_tc_elem_bytes(int nif, int nbf, int digits);
+bool schur_tc_supported(int nif, int nbf, int digits);
+int launch_schur_tc(int nel, int nfull, int nif, int nbf, int radix, int digits,
+                    const uint8_t* d_ydig, const int* d_yexp, const int* d_elist,
+                    const int* d_ni_e, double* d_W, int* d_flag, cudaStream_t st);
 int launch_index_maps(int nel, int nnode, int nnodes_global, const int* d_nodes, const int* d_ndofm,
                       const int64_t* d_lcon_off, int* d_first, int* d_cnt, int64_t* d_scan,
                       int64_t* d_blk, int64_t* d_total, int* d_nfirst, int* d_lcon,

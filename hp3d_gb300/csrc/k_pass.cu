@@ -354,14 +354,6 @@ void launch_contract_fp64(int nel, int nint, int n, int ni, int nb, const double
 // Bi = b_i - Y^T y_b, then ASchur = L^-T Y, BSchur = L^-T y_b.
 constexpr int CND_THREADS = 256;
 
-__device__ inline double pk_get(const double* PKj, const uint32_t* pm, int a, int b, int ni,
-                                int nb) {
-  uint32_t ma = pm[a], mb = pm[b];
-  int ra = (int)(ma & 0x7fffffffu), rb = (int)(mb & 0x7fffffffu);
-  double v = PKj[pk_index(ra, rb, ni, nb)];
-  return ((ma ^ mb) & 0x80000000u) ? -v : v;
-}
-
 __device__ inline void upper_decode(int64_t idx, int& a, int& b) {
   int bb = (int)((sqrtf(8.0f * (float)idx + 1.0f) - 1.0f) * 0.5f);
   while ((int64_t)(bb + 1) * (bb + 2) / 2 <= idx) ++bb;
@@ -369,6 +361,48 @@ __device__ inline void upper_decode(int64_t idx, int& a, int& b) {
   b = bb;
   a = (int)(idx - (int64_t)bb * (bb + 1) / 2);
 }
+
+// celem_systemI compression (constrs/celem_systemI.F90:800-845) of one
+// element: Zastif row-major over the extracted dof (NEXTRACT), Zbload with
+// the Dirichlet lift bi - S zd over the Dirichlet dof.  S is the element's
+// packed upper Schur complement, bi its condensed load.
+__device__ inline void compress_out(int e, int j, int ni, int nif, const double* __restrict__ S,
+                                    const double* __restrict__ bi, const int* __restrict__ nextract,
+                                    const int64_t* __restrict__ lcon_off,
+                                    const int64_t* __restrict__ elem_nnz,
+                                    const int64_t* __restrict__ zd_off,
+                                    const double* __restrict__ zdofd,
+                                    const uint8_t* __restrict__ dmask, double* __restrict__ zastif,
+                                    double* __restrict__ zbload) {
+  const int tid = threadIdx.x;
+  {
+    const int64_t lo = lcon_off[e];
+    const int nc = (int)(lcon_off[e + 1] - lo);
+    const int* nx = nextract + lo;
+    double* Z = zastif + elem_nnz[e];
+    for (int64_t idx = tid; idx < (int64_t)nc * nc; idx += CND_THREADS) {
+      int l1 = (int)(idx / nc), l2 = (int)(idx % nc);
+      int k1 = nx[l1], k2 = nx[l2];
+      int a = k1 < k2 ? k1 : k2, b = k1 < k2 ? k2 : k1;
+      Z[idx] = S[(int64_t)b * (b + 1) / 2 + a];
+    }
+    const double* zd = zdofd ? zdofd + zd_off[e] : nullptr;
+    const uint8_t* dm = dmask + (size_t)j * nif;
+    for (int l1 = tid; l1 < nc; l1 += CND_THREADS) {
+      int k1 = nx[l1];
+      double v = bi[k1];
+      if (zd) {
+        for (int k2 = 0; k2 < ni; ++k2)
+          if (dm[k2]) {
+            int a = k1 < k2 ? k1 : k2, b = k1 < k2 ? k2 : k1;
+            v -= S[(int64_t)b * (b + 1) / 2 + a] * zd[k2];
+          }
+      }
+      zbload[lo + l1] = v;
+    }
+  }
+}
+
 
 __global__ void __launch_bounds__(CND_THREADS) k_condense(
     int nfull, int nif, int nbf, const int* __restrict__ elist, const int* __restrict__ ni_e,
@@ -379,7 +413,7 @@ __global__ void __launch_bounds__(CND_THREADS) k_condense(
     const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
     const uint8_t* __restrict__ dmask, double* __restrict__ Sbuf, double* __restrict__ zastif,
     double* __restrict__ zbload, double* __restrict__ aschur, double* __restrict__ bschur,
-    double* __restrict__ Yg, int* __restrict__ bad_spd) {
+    double* __restrict__ Yg, int* __restrict__ bad_spd, TcFactorOut tco) {
   extern __shared__ double sm[];
   const int j = blockIdx.x;
   const int e = elist[j];
@@ -412,16 +446,20 @@ __global__ void __launch_bounds__(CND_THREADS) k_condense(
     Ys[r * ld + ni] = (m & 0x80000000u) ? -v : v;
   }
   __syncthreads();
-  // ---- Cholesky K_bb = L L^T ----
+  // ---- Cholesky K_bb = L L^T (reciprocals of the pivots kept in rd: the
+  // FP64 pipe is the bound, one division per pivot instead of per entry) ----
+  __shared__ double rd[128];
   for (int k = 0; k < nb; ++k) {
     if (tid == 0) {
       double d = L[k * nb + k];
       if (!(d > 0.0)) { fail = 1; d = 1.0; }
-      L[k * nb + k] = sqrt(d);
+      d = sqrt(d);
+      L[k * nb + k] = d;
+      rd[k] = 1.0 / d;
     }
     __syncthreads();
-    double dk = L[k * nb + k];
-    for (int i = k + 1 + tid; i < nb; i += CND_THREADS) L[i * nb + k] /= dk;
+    const double rk = rd[k];
+    for (int i = k + 1 + tid; i < nb; i += CND_THREADS) L[i * nb + k] *= rk;
     __syncthreads();
     int m = nb - k - 1;
     for (int idx = tid; idx < m * m; idx += CND_THREADS) {
@@ -436,7 +474,7 @@ __global__ void __launch_bounds__(CND_THREADS) k_condense(
     for (int r = 0; r < nb; ++r) {
       double s = Ys[r * ld + c];
       for (int k = 0; k < r; ++k) s -= L[r * nb + k] * Ys[k * ld + c];
-      Ys[r * ld + c] = s / L[r * nb + r];
+      Ys[r * ld + c] = s * rd[r];
     }
   }
   __syncthreads();
@@ -449,49 +487,98 @@ __global__ void __launch_bounds__(CND_THREADS) k_condense(
     for (int r = 0; r < nb; ++r) s += Ys[r * ld + a] * Ys[r * ld + ni];
     bi[a] = v - s;
   }
-  const int64_t nup = (int64_t)ni * (ni + 1) / 2;
-  for (int64_t idx = tid; idx < nup; idx += CND_THREADS) {
-    int a, b;
-    upper_decode(idx, a, b);
-    double v = pk_get(PKj, pm, a, b, nif, nbf);
-    double s = 0.0;
-    for (int r = 0; r < nb; ++r) s += Ys[r * ld + a] * Ys[r * ld + b];
-    S[idx] = v - s;
-  }
-  __syncthreads();
-  // ---- compression: Zastif (row-major), Zbload with Dirichlet lift ----
-  {
-    const int64_t lo = lcon_off[e];
-    const int nc = (int)(lcon_off[e + 1] - lo);
-    const int* nx = nextract + lo;
-    double* Z = zastif + elem_nnz[e];
-    for (int64_t idx = tid; idx < (int64_t)nc * nc; idx += CND_THREADS) {
-      int l1 = (int)(idx / nc), l2 = (int)(idx % nc);
-      int k1 = nx[l1], k2 = nx[l2];
-      int a = k1 < k2 ? k1 : k2, b = k1 < k2 ? k2 : k1;
-      Z[idx] = S[(int64_t)b * (b + 1) / 2 + a];
+  if (tco.ydig) {
+    // ---- factor mode: Y's columns as balanced digits for the tensor-core
+    // Schur update, the condensed load for the compression kernel ----
+    __shared__ int yex[256];
+    // column exponents e_c (max |Y[:, c]| = m 2^e_c, m in [0.5, 1)), from the
+    // bit patterns: magnitudes of finite doubles order like their bits
+    for (int c = tid; c < tco.nr; c += CND_THREADS) {
+      unsigned long long mb = 0;
+      if (c < ni)
+        for (int r = 0; r < nb; ++r) {
+          unsigned long long bits = (unsigned long long)__double_as_longlong(Ys[r * ld + c]) &
+                                    0x7fffffffffffffffull;
+          mb = bits > mb ? bits : mb;
+        }
+      const int E = (int)(mb >> 52);
+      const int ex = mb ? E - 1022 : 0;
+      yex[c] = ex;
+      tco.yexp[(size_t)j * tco.nr + c] = ex;
     }
-    const double* zd = zdofd ? zdofd + zd_off[e] : nullptr;
-    const uint8_t* dm = dmask + (size_t)j * nif;
-    for (int l1 = tid; l1 < nc; l1 += CND_THREADS) {
-      int k1 = nx[l1];
-      double v = bi[k1];
-      if (zd) {
-        for (int k2 = 0; k2 < ni; ++k2)
-          if (dm[k2]) {
-            int a = k1 < k2 ? k1 : k2, b = k1 < k2 ? k2 : k1;
-            v -= S[(int64_t)b * (b + 1) / 2 + a] * zd[k2];
+    for (int a = tid; a < ni; a += CND_THREADS) tco.bi[(size_t)j * nif + a] = bi[a];
+    __syncthreads();
+    // balanced digits in integer arithmetic: X = round(Y 2^(radix*D - e_c)),
+    // a fixed-point integer below 2^(radix*D) in magnitude, then
+    // X = sum_i d_i 2^(radix (D-i)) with |d_1| <= 2^radix, |d_i| <= 2^(radix-1)
+    uint8_t* Yd = tco.ydig + (size_t)j * tco.ebytes;
+    const int R = tco.radix, DG = tco.digits, half = 1 << (R - 1);
+    for (int it = tid; it < tco.nr * tco.nkb * 2; it += CND_THREADS) {
+      const int c = it % tco.nr, kg = (it / tco.nr) & 1, kb = it / (2 * tco.nr);
+      long long X[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int r = kb * 16 + kg * 8 + t;
+        X[t] = 0;
+        if (c < ni && r < nb) {
+          const long long bits = __double_as_longlong(Ys[r * ld + c]);
+          const int E = (int)((bits >> 52) & 0x7ff);
+          if (E > 0) {
+            const long long M = (bits & 0xfffffffffffffLL) | (1LL << 52);
+            const int sh = E - 1075 - yex[c] + R * DG;  // X = M 2^sh
+            long long v = 0;
+            if (sh >= 0) v = M << sh;
+            else if (sh > -54) v = (M + (1LL << (-sh - 1))) >> (-sh);
+            X[t] = bits < 0 ? -v : v;
           }
+        }
       }
-      zbload[lo + l1] = v;
+      uint8_t* dst = Yd + (size_t)kb * tco.nr * 32 + (size_t)(c >> 3) * 256 + (size_t)kg * 128 +
+                     (size_t)(c & 7) * 16;
+      for (int dg = DG - 1; dg >= 0; --dg) {  // least significant digit first
+        uint32_t h[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          long long d;
+          if (dg > 0) {
+            const long long q = (X[t] + half) >> R;  // floor division
+            d = X[t] - (q << R);
+            X[t] = q;
+          } else {
+            d = X[t];
+          }
+          h[t] = __float_as_uint((float)(int)d) >> 16;  // exact in BF16
+        }
+        uint4 w;
+        w.x = h[0] | (h[1] << 16);
+        w.y = h[2] | (h[3] << 16);
+        w.z = h[4] | (h[5] << 16);
+        w.w = h[6] | (h[7] << 16);
+        *(uint4*)(dst + (size_t)dg * tco.nkb * tco.nr * 32) = w;
+      }
     }
+    __syncthreads();  // the backward solve below overwrites Y in place
+  } else {
+    // ---- Schur complement (upper, col-major), then compression ----
+    const int64_t nup = (int64_t)ni * (ni + 1) / 2;
+    for (int64_t idx = tid; idx < nup; idx += CND_THREADS) {
+      int a, b;
+      upper_decode(idx, a, b);
+      double v = pk_get(PKj, pm, a, b, nif, nbf);
+      double s = 0.0;
+      for (int r = 0; r < nb; ++r) s += Ys[r * ld + a] * Ys[r * ld + b];
+      S[idx] = v - s;
+    }
+    __syncthreads();
+    compress_out(e, j, ni, nif, S, bi, nextract, lcon_off, elem_nnz, zd_off, zdofd, dmask, zastif,
+                 zbload);
   }
   // ---- ASchur = L^-T Y, BSchur = L^-T y_b ----
   for (int c = tid; c < ld; c += CND_THREADS) {
     for (int r = nb - 1; r >= 0; --r) {
       double s = Ys[r * ld + c];
       for (int k = r + 1; k < nb; ++k) s -= L[k * nb + r] * Ys[k * ld + c];
-      Ys[r * ld + c] = s / L[r * nb + r];
+      Ys[r * ld + c] = s * rd[r];
     }
   }
   __syncthreads();
@@ -520,19 +607,57 @@ int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, co
                     const int64_t* d_bub_off, const int64_t* d_zd_off, const double* d_zdofd,
                     const uint8_t* d_dmask, double* d_S, double* d_zastif, double* d_zbload,
                     double* d_aschur, double* d_bschur, double* d_Yg, int* d_bad_spd,
-                    cudaStream_t st) {
+                    cudaStream_t st, const TcFactorOut* tco) {
   if (nel <= 0) return 0;
   size_t smem = d_Yg ? condense_smem_small(nif, nbf) : condense_smem(nif, nbf);
   if (smem > 227 * 1024) return -2;
   if (cudaFuncSetAttribute(k_condense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return -1;
+  TcFactorOut none{};
   k_condense<<<nel, CND_THREADS, smem, st>>>(nfull, nif, nbf, d_elist, d_ni_e, d_nb_e, d_PK, d_b0,
                                               d_perm, d_nextract, d_lcon_off, d_elem_nnz,
                                               d_schur_off, d_bub_off, d_zd_off, d_zdofd, d_dmask,
                                               d_S, d_zastif, d_zbload, d_aschur, d_bschur,
-                                              d_Yg, d_bad_spd);
+                                              d_Yg, d_bad_spd, tco ? *tco : none);
   return 0;
+}
+
+// compression after the tensor-core Schur update: one block per element.
+// S = K_ii - W is formed in place (K_ii gathered through the dof map), then
+// compressed as in the FP64 path.
+__global__ void __launch_bounds__(CND_THREADS) k_compress(
+    int nfull, int nif, int nbf, const int* __restrict__ elist, const int* __restrict__ ni_e,
+    const double* __restrict__ PK, const uint32_t* __restrict__ perm, double* __restrict__ Wbuf,
+    const double* __restrict__ Bi, const int* __restrict__ nextract,
+    const int64_t* __restrict__ lcon_off, const int64_t* __restrict__ elem_nnz,
+    const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
+    const uint8_t* __restrict__ dmask, double* __restrict__ zastif, double* __restrict__ zbload) {
+  const int j = blockIdx.x, e = elist[j];
+  const int ni = ni_e[e];
+  const double* PKj = PK + (size_t)j * ((size_t)nfull * (nfull + 1) / 2);
+  const uint32_t* pm = perm + (size_t)j * nfull;
+  double* S = Wbuf + (size_t)j * ((size_t)nif * (nif + 1) / 2);
+  const int64_t nup = (int64_t)ni * (ni + 1) / 2;
+  for (int64_t idx = threadIdx.x; idx < nup; idx += CND_THREADS) {
+    int a, b;
+    upper_decode(idx, a, b);
+    S[idx] = pk_get(PKj, pm, a, b, nif, nbf) - S[idx];
+  }
+  __syncthreads();
+  compress_out(e, j, ni, nif, S, Bi + (size_t)j * nif, nextract, lcon_off, elem_nnz, zd_off, zdofd,
+               dmask, zastif, zbload);
+}
+
+void launch_compress(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
+                     const double* d_PK, const uint32_t* d_perm, const double* d_W,
+                     const double* d_bi, const int* d_nextract, const int64_t* d_lcon_off,
+                     const int64_t* d_elem_nnz, const int64_t* d_zd_off, const double* d_zdofd,
+                     const uint8_t* d_dmask, double* d_zastif, double* d_zbload, cudaStream_t st) {
+  if (nel <= 0) return;
+  k_compress<<<nel, CND_THREADS, 0, st>>>(nfull, nif, nbf, d_elist, d_ni_e, d_PK, d_perm,
+                                          (double*)d_W, d_bi, d_nextract, d_lcon_off, d_elem_nnz,
+                                          d_zd_off, d_zdofd, d_dmask, d_zastif, d_zbload);
 }
 
 // ---------------------------------------------------------------------------

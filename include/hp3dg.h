@@ -79,7 +79,10 @@ typedef struct hp3dg_opts {
   int32_t launch_mode; /* 0 = hp3dg_batch_run replays one CUDA graph of the pass
                           (captured on the first run after a submit);
                           1 = direct stream launches */
-  int32_t reserved[6];
+  int32_t schur_fp64;  /* HP3DG_MIXED only: 0 = the Schur update of the
+                          condensation (K_ii - Y^T Y) on tensor cores with
+                          split-BF16 digits where the bin fits, 1 = FP64 */
+  int32_t reserved[5];
 } hp3dg_opts;
 
 /* Element descriptor: what find_order (datstrs/find_order.F90:5),

@@ -1,0 +1,48 @@
+"""Schur update of the condensation on tensor cores (mixed pass): the
+condensed matrices, loads and Schur blocks equal those of the FP64 Schur
+update to 1e-12 relative, for hexahedra at p=5 (two 128-row tiles), hp
+bins, prisms and tetrahedra (one tile), with Dirichlet data; and against the
+oracle at the mixed-pass tolerance (1e-10)."""
+import numpy as np
+import pytest
+
+from hp3d_gb300 import hp3dg as H
+from hp3d_gb300 import mesh as M
+import fem_harness as FH
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _meshes():
+    yield "hexa_p5", M.random_orientations(M.structured_hexa(3, 5, perturb=0.15,
+                                                             kappa_logrange=(-2, 2)), seed=2)
+    yield "hp_hexa", M.hp_hexa(3, seed=4, perturb=0.1)
+    yield "mixed", M.mixed_mesh(4, a=0.5, b=0.5, perturb=0.1, seed=13)
+    yield "prism_6_5", M.structured_prism(2, 6, 5, perturb=0.1, seed=3)
+
+
+@pytest.mark.parametrize("name,m", list(_meshes()))
+def test_tensor_schur_matches_fp64_schur(name, m):
+    zd = FH.dirichlet_data(m, 10)
+    out = []
+    for tc in (True, False):
+        ep = H.ElementPass(H.MIXED, isol=10, schur_tc=tc)
+        ep.submit(m, zdofd=zd)
+        ep.run(); ep.download()
+        out.append([(ep.condensed(e), ep.schur(e)) for e in range(m["nelem"])])
+        ep.close()
+    for ((zb1, zs1), (a1, b1)), ((zb0, zs0), (a0, b0)) in zip(out[0], out[1]):
+        if zs0.size:
+            assert _rel(zs1, zs0) < 1e-12
+            assert _rel(zb1, zb0) < 1e-12
+        if a0.size:
+            assert np.array_equal(a1, a0) and np.array_equal(b1, b0)
+    ref = FH.oracle_element_outputs(m, 10, zdofd=zd)
+    for e, ((zb, zs), _) in enumerate(out[0]):
+        if zs.size:
+            assert _rel(zs, ref[e]["zastif"]) < 1e-10, (name, e)
+            assert _rel(zb, ref[e]["zbload"]) < 1e-10, (name, e)
