@@ -44,7 +44,8 @@ def make_mesh(n, p, seed=12345):
 
 
 def per_element_work(n, nint):
-    """Algorithmic work per element (roofline)."""
+    """Algorithmic work per element: SYRK flop count of elem_opt, one D.M
+    product of the mixed contraction, condensation flops, output bytes."""
     nb = (round(n ** (1 / 3)) - 1) ** 3
     ni = n - nb
     ncols = n * (n + 1) // 2

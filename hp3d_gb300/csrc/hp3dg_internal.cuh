@@ -1,7 +1,7 @@
 // hp3dg_internal.cuh -- shared device helpers of the GB300 element pass.
 //
 // Data layout in HBM (one "bin" = elements of one type and one local order
-// tuple; see the design doc for the full map):
+// tuple, plus, for triangle faces, one orientation class per face):
 //   tab_shap [nint][n]          reference-element H1 values (orientation 0)
 //   tab_grad [nint][3][n]       reference gradients, row (l,c) contiguous in k
 //   D        [E][nint][6]       kappa*w*detJ*(dxi/dx)(dxi/dx)^T, upper (00,11,22,01,02,12)

@@ -2,7 +2,7 @@
 
 This is the host-side interface a Python caller (tests, benchmark, the torch
 autograd harness) uses; the Fortran host binds the same entry points through
-ISO_C_BINDING (INTEGRATION.md).  Loading fails loudly when libhp3dg.so is
+ISO_C_BINDING.  Loading fails loudly when libhp3dg.so is
 missing: there is no CPU fallback.
 """
 from __future__ import annotations
