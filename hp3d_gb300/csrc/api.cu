@@ -330,6 +330,9 @@ struct Bin {
   OzakiPlan plan{};
   uint16_t *d_mdig = nullptr, *d_ddig = nullptr;
   double *d_mscale = nullptr, *d_dscale = nullptr;
+  // condensation with every product on tensor cores (mixed, nb <= 64)
+  bool cond_tc = false;
+  CondTcBufs ctb{};
   // tensor-core Schur update (mixed): Y digits, column exponents, condensed load
   bool tc_schur = false;
   TcFactorOut tco{};
@@ -395,6 +398,8 @@ void free_bin(Bin& b) {
   cudaFree(b.d_mscale); cudaFree(b.d_dscale);
   cudaFree(b.d_xi_err); cudaFree(b.d_wq_err); cudaFree(b.d_shap_err); cudaFree(b.d_grad_err);
   cudaFree(b.d_ydig); cudaFree(b.d_yexp); cudaFree(b.d_bi);
+  cudaFree(b.ctb.kbd); cudaFree(b.ctb.lid); cudaFree(b.ctb.ltd);
+  cudaFree(b.ctb.ekb); cudaFree(b.ctb.eli); cudaFree(b.ctb.elt); cudaFree(b.ctb.bi);
   b = Bin();
 }
 
@@ -683,7 +688,22 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
       if (rc) { free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
       B.d_ddig = (uint16_t*)dalloc<uint8_t>(ozaki_d_bytes(B.plan, (int)ne), &err);
       B.d_dscale = dalloc<double>(ne + 128, &err);
-      B.tc_schur = !c->opts.schur_fp64 && !B.d_Yg &&
+      // the condensation products have K = nb <= 64: radix 8, 6 digits keep
+      // every level sum exact (below 2^23) with 21 digit pairs
+      B.cond_tc = !c->opts.schur_fp64 && !B.d_Yg &&
+                  cond_tc_supported(B.ni, B.nb, COND_TC_DIGITS);
+      if (B.cond_tc) {
+        CondTcBufs& t = B.ctb;
+        cond_tc_make_out(B.ni, B.nb, COND_TC_RADIX, COND_TC_DIGITS, t);
+        t.kbd = dalloc<uint8_t>(ne * t.bytes_a, &err);
+        t.lid = dalloc<uint8_t>(ne * t.bytes_b, &err);
+        t.ltd = dalloc<uint8_t>(ne * t.bytes_b, &err);
+        t.ekb = dalloc<int>(ne * (size_t)t.nr, &err);
+        t.eli = dalloc<int>(ne * (size_t)t.nbr, &err);
+        t.elt = dalloc<int>(ne * (size_t)t.nbr, &err);
+        t.bi = dalloc<double>(ne * (size_t)B.ni, &err);
+      }
+      B.tc_schur = !B.cond_tc && !c->opts.schur_fp64 && !B.d_Yg &&
                    schur_tc_supported(B.ni, B.nb, B.plan.digits);
       if (B.tc_schur) {
         TcFactorOut& t = B.tco;
@@ -748,6 +768,18 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
   for (auto& B : c->bins) {
     int ne = (int)B.elems.size();
     const double* zd = c->have_zdofd ? c->d_zdofd : nullptr;
+    if (B.cond_tc) {
+      // Cholesky + explicit inverse in FP64; Y, W = Y^T Y and ASchur on tensor
+      // cores; then S = K_ii - W and the compression
+      if (launch_cond_tc(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
+                         B.d_perm, c->d_schur_off, c->d_bub_off, B.d_S, c->d_aschur,
+                         c->d_bschur, B.ctb, c->d_flags + 1, c->d_flags + 2, st))
+        return HP3DG_ERR_CUDA;
+      launch_compress(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, B.d_PK, B.d_perm, B.d_S,
+                      B.ctb.bi, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd,
+                      B.d_dmask, c->d_zastif, c->d_zbload, st);
+      continue;
+    }
     if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
                         B.d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
                         c->d_bub_off, c->d_zd_off, zd, B.d_dmask, B.d_S, c->d_zastif,

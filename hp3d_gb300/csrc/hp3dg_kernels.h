@@ -52,6 +52,24 @@ void launch_compress(int nel, int nfull, int nif, int nbf, const int* d_elist, c
                      const double* d_bi, const int* d_nextract, const int64_t* d_lcon_off,
                      const int64_t* d_elem_nnz, const int64_t* d_zd_off, const double* d_zdofd,
                      const uint8_t* d_dmask, double* d_zastif, double* d_zbload, cudaStream_t st);
+// condensation with every product on tensor cores (nb <= 64) -- k_cond_tc.cu
+// Digits of its operands: with K = nb <= 64 a level sum of radix-8 digits is
+// at most (2^16 + 4 * 2^14) * 64 = 2^23 < 2^24 (exact in FP32).
+constexpr int COND_TC_RADIX = 8, COND_TC_DIGITS = 6;
+struct CondTcBufs {
+  uint8_t *kbd = nullptr, *lid = nullptr, *ltd = nullptr;  // digits of K_bi^T, Li, Li^T
+  int *ekb = nullptr, *eli = nullptr, *elt = nullptr;      // row exponents
+  double* bi = nullptr;                                     // condensed load
+  int nr = 0, nbr = 0, nkb = 0, digits = 0, radix = 0;
+  size_t bytes_a = 0, bytes_b = 0;                          // per element
+};
+bool cond_tc_supported(int nif, int nbf, int digits);
+void cond_tc_make_out(int nif, int nbf, int radix, int digits, CondTcBufs& b);
+int launch_cond_tc(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
+                   const int* d_nb_e, const double* d_PK, const double* d_b0,
+                   const uint32_t* d_perm, const int64_t* d_schur_off, const int64_t* d_bub_off,
+                   double* d_W, double* d_aschur, double* d_bschur, const CondTcBufs& b,
+                   int* d_bad_spd, int* d_flag, cudaStream_t st);
 // tensor-core Schur update S = K_ii - Y^T Y -- k_schur.cu
 int schur_tc_rows(int nif);
 int schur_tc_kblocks(int nbf);

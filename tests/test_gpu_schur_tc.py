@@ -1,8 +1,10 @@
-"""Schur update of the condensation on tensor cores (mixed pass): the
-condensed matrices, loads and Schur blocks equal those of the FP64 Schur
-update to 1e-12 relative, for hexahedra at p=5 (two 128-row tiles), hp
-bins, prisms and tetrahedra (one tile), with Dirichlet data; and against the
-oracle at the mixed-pass tolerance (1e-10)."""
+"""Condensation of the mixed pass on tensor cores (Y = L^-1 K_bi, W = Y^T Y
+and ASchur = L^-T Y as split-BF16 products; the Schur-update-only path for
+bins with more than 64 bubbles): the condensed matrices, loads and Schur
+blocks equal those of the FP64 condensation to 1e-12 relative, for
+hexahedra at p=5 (two 128-row tiles), hp bins, prisms and tetrahedra (one
+tile), with Dirichlet data; and against the oracle at the mixed-pass
+tolerance (1e-10)."""
 import numpy as np
 import pytest
 
@@ -40,7 +42,10 @@ def test_tensor_schur_matches_fp64_schur(name, m):
             assert _rel(zs1, zs0) < 1e-12
             assert _rel(zb1, zb0) < 1e-12
         if a0.size:
-            assert np.array_equal(a1, a0) and np.array_equal(b1, b0)
+            # ASchur / BSchur through the explicit inverse of the Cholesky
+            # factor: cond(K_bb)-dependent (2.4e-11 measured at p=5); they
+            # only enter the bubble back-substitution
+            assert _rel(a1, a0) < 1e-10 and _rel(b1, b0) < 1e-10
     ref = FH.oracle_element_outputs(m, 10, zdofd=zd)
     for e, ((zb, zs), _) in enumerate(out[0]):
         if zs.size:
