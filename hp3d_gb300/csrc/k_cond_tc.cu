@@ -126,114 +126,121 @@ struct CondTcOut {
   uint32_t bytes_a, bytes_b;
 };
 
-// Per element: gather K_bb and b_b through the dof map, Cholesky, Li = L^-1,
-// BSchur = K_bb^-1 b_b, and the digits of Li and Li^T (rows = bubble dof).
-__global__ void __launch_bounds__(F2_THREADS) k_cond_chol(
+// Per element, one warp: gather K_bb (lower triangle, packed) and b_b through
+// the dof map; right-looking Cholesky K_bb = L L^T and the inverse Li = L^-1
+// in place (columns from the last to the first, the original column kept in
+// a scratch vector); BSchur = Li^T (Li b_b); the digits of Li and Li^T.
+// Warp-synchronous: no block barrier.
+constexpr int CH_WARPS = 4;
+__device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+
+__global__ void __launch_bounds__(CH_WARPS * 32) k_cond_chol(
     int nfull, int nif, int nbf, const int* __restrict__ elist, const int* __restrict__ ni_e,
     const int* __restrict__ nb_e, const double* __restrict__ PK, const double* __restrict__ b0,
     const uint32_t* __restrict__ perm, const int64_t* __restrict__ bub_off,
-    double* __restrict__ bschur, CondTcOut o, int* __restrict__ bad_spd) {
+    double* __restrict__ bschur, CondTcOut o, int nel, int* __restrict__ bad_spd) {
   extern __shared__ double sm[];
-  const int j = blockIdx.x, e = elist[j];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * CH_WARPS + w;
+  if (j >= nel) return;
+  const int e = elist[j];
   const int ni = ni_e[e], nb = nb_e[e];
   const double* PKj = PK + (size_t)j * ((size_t)nfull * (nfull + 1) / 2);
   const uint32_t* pm = perm + (size_t)j * nfull;
   const double* bj = b0 + (size_t)j * nfull;
-  const int tid = threadIdx.x;
-  double* L = sm;                       // nb x nb
-  double* Li = L + (size_t)nbf * nbf;   // nb x nb
-  __shared__ double rd[64], bb[64], yv[64];
-  __shared__ int eli_s[64], elt_s[64];
-  __shared__ int fail;
-  if (tid == 0) fail = 0;
-  for (int idx = tid; idx < nb * nb; idx += F2_THREADS) {
-    int r = idx / nb, c = idx % nb;
-    L[idx] = pk_get(PKj, pm, ni + r, ni + c, nif, nbf);
-    Li[idx] = 0.0;
+  const size_t per = (size_t)nbf * (nbf + 1) / 2 + 3 * (size_t)nbf;
+  double* A = sm + (size_t)w * per;        // packed lower triangle
+  double* col = A + (size_t)nbf * (nbf + 1) / 2;
+  double* bb = col + nbf;
+  double* yv = bb + nbf;
+  for (int idx = lane; idx < nb * (nb + 1) / 2; idx += 32) {
+    int i = (int)((sqrtf(8.0f * idx + 1.0f) - 1.0f) * 0.5f);
+    while (tri(i + 1, 0) <= idx) ++i;
+    while (tri(i, 0) > idx) --i;
+    const int c = idx - tri(i, 0);
+    A[idx] = pk_get(PKj, pm, ni + i, ni + c, nif, nbf);
   }
-  for (int r = tid; r < nb; r += F2_THREADS) {
+  for (int r = lane; r < nb; r += 32) {
     uint32_t m = pm[ni + r];
     double v = bj[m & 0x7fffffffu];
     bb[r] = (m & 0x80000000u) ? -v : v;
   }
-  __syncthreads();
-  // Cholesky K_bb = L L^T (pivot reciprocals in rd)
+  __syncwarp();
+  bool fail = false;
+  // Cholesky: lane owns columns jj = k+1+lane (+32)
   for (int k = 0; k < nb; ++k) {
-    if (tid == 0) {
-      double d = L[k * nb + k];
-      if (!(d > 0.0)) { fail = 1; d = 1.0; }
-      d = sqrt(d);
-      L[k * nb + k] = d;
-      rd[k] = 1.0 / d;
+    double d = A[tri(k, k)];
+    if (!(d > 0.0)) { fail = true; d = 1.0; }
+    d = sqrt(d);
+    const double rk = 1.0 / d;
+    __syncwarp();
+    if (lane == 0) A[tri(k, k)] = d;
+    for (int i = k + 1 + lane; i < nb; i += 32) A[tri(i, k)] *= rk;
+    __syncwarp();
+    for (int jj = k + 1 + lane; jj < nb; jj += 32) {
+      const double ljk = A[tri(jj, k)];
+      for (int i = jj; i < nb; ++i) A[tri(i, jj)] -= A[tri(i, k)] * ljk;
     }
-    __syncthreads();
-    const double rk = rd[k];
-    for (int i = k + 1 + tid; i < nb; i += F2_THREADS) L[i * nb + k] *= rk;
-    __syncthreads();
-    const int m = nb - k - 1;
-    for (int idx = tid; idx < m * m; idx += F2_THREADS) {
-      int ii = k + 1 + idx / m, jj = k + 1 + idx % m;
-      if (jj <= ii) L[ii * nb + jj] -= L[ii * nb + k] * L[jj * nb + k];
-    }
-    __syncthreads();
+    __syncwarp();
   }
-  if (fail && tid == 0) atomicMin(bad_spd, e);
-  // Li = L^-1 row by row: Li[i][c] = (delta_ic - sum_{k=c}^{i-1} L[i][k] Li[k][c]) / L[i][i]
-  for (int i = 0; i < nb; ++i) {
-    for (int c = tid; c <= i; c += F2_THREADS) {
-      double s = (c == i) ? 1.0 : 0.0;
-      for (int k = c; k < i; ++k) s -= L[i * nb + k] * Li[k * nb + c];
-      Li[i * nb + c] = s * rd[i];
+  if (fail && lane == 0) atomicMin(bad_spd, e);
+  // inverse in place, column c from the last: Li[c][c] = 1 / L[c][c],
+  // Li[i][c] = -(sum_{k=c+1..i} Li[i][k] L[k][c]) Li[c][c]
+  for (int c = nb - 1; c >= 0; --c) {
+    for (int k = c + lane; k < nb; k += 32) col[k] = A[tri(k, c)];
+    __syncwarp();
+    const double dc = 1.0 / col[c];
+    for (int i = c + 1 + lane; i < nb; i += 32) {
+      double s = 0.0;
+      for (int k = c + 1; k <= i; ++k) s += A[tri(i, k)] * col[k];
+      A[tri(i, c)] = -s * dc;
     }
-    __syncthreads();
+    if (lane == 0) A[tri(c, c)] = dc;
+    __syncwarp();
   }
-  // y = Li b_b, BSchur = Li^T y = K_bb^-1 b_b
-  for (int r = tid; r < nb; r += F2_THREADS) {
+  // y = Li b_b, BSchur = Li^T y
+  for (int r = lane; r < nb; r += 32) {
     double s = 0.0;
-    for (int k = 0; k <= r; ++k) s += Li[r * nb + k] * bb[k];
+    for (int k = 0; k <= r; ++k) s += A[tri(r, k)] * bb[k];
     yv[r] = s;
   }
-  __syncthreads();
-  for (int r = tid; r < nb; r += F2_THREADS) {
+  __syncwarp();
+  for (int r = lane; r < nb; r += 32) {
     double s = 0.0;
-    for (int k = r; k < nb; ++k) s += Li[k * nb + r] * yv[k];
+    for (int k = r; k < nb; ++k) s += A[tri(k, r)] * yv[k];
     bschur[bub_off[e] + r] = s;
   }
-  // row exponents and digits of Li and Li^T
-  for (int r = tid; r < o.nbr; r += F2_THREADS) {
-    unsigned long long m1 = 0, m2 = 0;
-    if (r < nb)
-      for (int k = 0; k < nb; ++k) {
-        unsigned long long b1 = mag_bits(Li[r * nb + k]), b2 = mag_bits(Li[k * nb + r]);
-        m1 = b1 > m1 ? b1 : m1;
-        m2 = b2 > m2 ? b2 : m2;
-      }
-    eli_s[r] = row_exponent(m1);
-    elt_s[r] = row_exponent(m2);
-    o.eli[(size_t)j * o.nbr + r] = eli_s[r];
-    o.elt[(size_t)j * o.nbr + r] = elt_s[r];
-  }
-  __syncthreads();
+  // row exponents and digits of Li (row r: A[r][0..r]) and Li^T (row r: A[r..][r])
   const int fb = o.radix * o.digits;
   uint8_t* bl = o.lid + (size_t)j * o.bytes_b;
   uint8_t* bt = o.ltd + (size_t)j * o.bytes_b;
   const size_t dstride = (size_t)o.nkb * o.nbr * 32;
-  for (int it = tid; it < o.nbr * o.nkb * 2; it += F2_THREADS) {
-    const int r = it % o.nbr, g = it / o.nbr;
-    long long X[8], Z[8];
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-      const int k = g * 8 + t;
-      const bool ok = r < nb && k < nb;
-      X[t] = ok ? fixed_of(Li[r * nb + k], eli_s[r], fb) : 0;
-      Z[t] = ok ? fixed_of(Li[k * nb + r], elt_s[r], fb) : 0;
+  for (int r = lane; r < o.nbr; r += 32) {
+    unsigned long long m1 = 0, m2 = 0;
+    if (r < nb) {
+      for (int k = 0; k <= r; ++k) { unsigned long long b = mag_bits(A[tri(r, k)]); m1 = b > m1 ? b : m1; }
+      for (int k = r; k < nb; ++k) { unsigned long long b = mag_bits(A[tri(k, r)]); m2 = b > m2 ? b : m2; }
     }
-    store_digits8(X, o.radix, o.digits, bl + tile_off(r, g, o.nbr), dstride);
-    store_digits8(Z, o.radix, o.digits, bt + tile_off(r, g, o.nbr), dstride);
+    const int e1 = row_exponent(m1), e2 = row_exponent(m2);
+    o.eli[(size_t)j * o.nbr + r] = e1;
+    o.elt[(size_t)j * o.nbr + r] = e2;
+    for (int g = 0; g < o.nkb * 2; ++g) {
+      long long X[8], Z[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int k = g * 8 + t;
+        X[t] = (r < nb && k <= r) ? fixed_of(A[tri(r, k)], e1, fb) : 0;
+        Z[t] = (r < nb && k >= r && k < nb) ? fixed_of(A[tri(k, r)], e2, fb) : 0;
+      }
+      store_digits8(X, o.radix, o.digits, bl + tile_off(r, g, o.nbr), dstride);
+      store_digits8(Z, o.radix, o.digits, bt + tile_off(r, g, o.nbr), dstride);
+    }
   }
 }
 
-size_t cond_chol_smem(int nbf) { return (size_t)2 * nbf * nbf * sizeof(double); }
+size_t cond_chol_smem(int nbf) {
+  return (size_t)CH_WARPS * ((size_t)nbf * (nbf + 1) / 2 + 3 * (size_t)nbf) * sizeof(double);
+}
 
 // Per (element, 128 interface columns): K_bi column c gathered through the
 // dof map (twice: the row exponent first, then the digits), the condensed
@@ -666,8 +673,9 @@ int launch_cond_tc(int nel, int nfull, int nif, int nbf, const int* d_elist, con
   if (cudaFuncSetAttribute(k_cond_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1) !=
       cudaSuccess)
     return -1;
-  k_cond_chol<<<nel, F2_THREADS, sm1, st>>>(nfull, nif, nbf, d_elist, d_ni_e, d_nb_e, d_PK, d_b0,
-                                            d_perm, d_bub_off, d_bschur, o, d_bad_spd);
+  k_cond_chol<<<(nel + CH_WARPS - 1) / CH_WARPS, CH_WARPS * 32, sm1, st>>>(
+      nfull, nif, nbf, d_elist, d_ni_e, d_nb_e, d_PK, d_b0, d_perm, d_bub_off, d_bschur, o, nel,
+      d_bad_spd);
   k_cond_kbi<<<dim3(nel, (o.nr + 127) / 128), 128, 0, st>>>(nfull, nif, nbf, d_elist, d_ni_e,
                                                             d_nb_e, d_PK, d_b0, d_perm, d_bub_off,
                                                             d_bschur, o);
