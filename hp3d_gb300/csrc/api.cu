@@ -385,6 +385,12 @@ struct hp3dg_ctx {
   cudaEvent_t ev[8] = {};
   float times[6] = {0, 0, 0, 0, 0, 0};
   cudaGraphExec_t graph = nullptr;  // the captured pass; rebuilt after every new structure
+  // pipelined download: the pass in element chunks, each recording an event
+  int nchunk = 1;
+  int chunk_lo[9] = {0};            // chunk boundaries (element positions of the single bin)
+  cudaEvent_t chunk_ev[8] = {};
+  cudaStream_t copy_stream = nullptr;
+  bool chunked_run = false;
   std::vector<hp3dg_elem_desc> last_desc;  // descriptors of the current batch
 };
 
@@ -469,6 +475,7 @@ int hp3dg_batch_begin(const hp3dg_opts* opts, hp3dg_ctx** out) {
   else c->opts.isol = 10;
   if (c->opts.precision != HP3DG_FP64 && c->opts.precision != HP3DG_MIXED) { delete c; return HP3DG_ERR_ARG; }
   if (c->opts.integration < 0 || c->opts.integration > MAXP) { delete c; return HP3DG_ERR_ARG; }
+  if (c->opts.download_chunks < 0 || c->opts.download_chunks > 8) { delete c; return HP3DG_ERR_ARG; }
   c->device = c->opts.device;
   if (cudaSetDevice(c->device) != cudaSuccess) { delete c; return HP3DG_ERR_CUDA; }
   if (c->opts.precision == HP3DG_MIXED) {
@@ -479,6 +486,11 @@ int hp3dg_batch_begin(const hp3dg_opts* opts, hp3dg_ctx** out) {
   if (cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) { delete c; return HP3DG_ERR_CUDA; }
   c->stream = c->own;
   for (auto& e : c->ev) cudaEventCreate(&e);
+  for (auto& e : c->chunk_ev) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+  if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return HP3DG_ERR_CUDA;
+  }
   if (cudaMalloc(&c->d_flags, 4 * sizeof(int)) != cudaSuccess) { delete c; return HP3DG_ERR_ALLOC; }
   *out = c;
   return HP3DG_OK;
@@ -722,6 +734,19 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   }
   CK(cudaStreamSynchronize(st));
   c->last_desc.assign(desc, desc + nel);
+  // pipelined download: chunks of the single bin at 128-element boundaries
+  c->nchunk = 1;
+  c->chunk_lo[0] = 0;
+  c->chunk_lo[1] = nel;
+  const int want = std::min(std::max((int)c->opts.download_chunks, 1), 8);
+  if (want > 1 && c->bins.size() == 1 && nel >= 256 && !c->opts.keep_elem) {
+    const int cs = (nel + want - 1) / want;
+    const int step = (cs + 127) / 128 * 128;
+    int k = 0;
+    for (int lo = 0; lo < nel && k < 8; lo += step) c->chunk_lo[k++] = lo;
+    c->nchunk = k;
+    c->chunk_lo[k] = nel;
+  }
   c->submitted = true;
   return HP3DG_OK;
 }
@@ -738,65 +763,116 @@ void mark(hp3dg_ctx* c, int i, cudaStream_t st, bool capturing) {
   else cudaEventRecord(c->ev[i], st);
 }
 
-// The per-run work of the pass, enqueued on st: flags reset, per bin the
-// orientation map, geometry, load, (mixed) digit slicing, contraction and
-// condensation, then the global index maps.  Bin tables are built beforehand.
-int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
-  if (cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st) != cudaSuccess) return HP3DG_ERR_CUDA;
-  for (auto& B : c->bins) {
-    int ne = (int)B.elems.size();
-    launch_orient(B.etype, ne, B.d_elist, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n,
-                  B.d_perm, st);
-    launch_geom(ne, B.nvert, B.d_elist, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert,
-                c->d_kappa, c->opts.isol, B.d_D, B.d_F, c->d_flags, st);
-    launch_load_hexa(ne, B.nint, B.n, B.d_shap, B.d_F, B.d_b0, st);
-    if (c->opts.precision == HP3DG_MIXED)
-      launch_ozaki_slice_d(B.plan, ne, B.nint, B.d_D, B.d_ddig, B.d_dscale, st);
+// One stage of the pass for positions [j0, j1) of bin B (every per-bin
+// buffer is indexed by the position in the bin, so a range is the same
+// launches on offset base pointers; j0 is a multiple of 128, the block of the
+// D digit tiles).  stage 0: orientation map, geometry, load, digit slicing;
+// 1: contraction; 2: condensation and compression.
+int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t st) {
+  const int ne = j1 - j0;
+  if (ne <= 0) return HP3DG_OK;
+  const size_t npk = (size_t)B.n * (B.n + 1) / 2, nsu = (size_t)B.ni * (B.ni + 1) / 2;
+  const int* el = B.d_elist + j0;
+  uint32_t* perm = B.d_perm + (size_t)j0 * B.n;
+  double* D = B.d_D + (size_t)j0 * B.nint * 6;
+  double* F = B.d_F + (size_t)j0 * B.nint;
+  double* b0 = B.d_b0 + (size_t)j0 * B.n;
+  double* PK = B.d_PK + (size_t)j0 * npk;
+  double* S = B.d_S + (size_t)j0 * nsu;
+  uint8_t* dm = B.d_dmask + (size_t)j0 * B.ni;
+  const double* zd = c->have_zdofd ? c->d_zdofd : nullptr;
+  const bool mixed = c->opts.precision == HP3DG_MIXED;
+  const size_t dblk = mixed ? ozaki_d_bytes(B.plan, 128) : 0;  // D digits of 128 elements
+  uint16_t* ddig = mixed ? (uint16_t*)((uint8_t*)B.d_ddig + (size_t)(j0 / 128) * dblk) : nullptr;
+  double* dscale = mixed ? B.d_dscale + j0 : nullptr;
+  if (stage == 0) {
+    launch_orient(B.etype, ne, el, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n, perm, st);
+    launch_geom(ne, B.nvert, el, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert, c->d_kappa,
+                c->opts.isol, D, F, c->d_flags, st);
+    launch_load_hexa(ne, B.nint, B.n, B.d_shap, F, b0, st);
+    if (mixed) launch_ozaki_slice_d(B.plan, ne, B.nint, D, ddig, dscale, st);
+    return HP3DG_OK;
   }
-  mark(c, 2, st, capturing);
-  for (auto& B : c->bins) {
-    int ne = (int)B.elems.size();
-    if (c->opts.precision == HP3DG_MIXED) {
-      if (launch_ozaki_gemm(B.plan, ne, B.n, B.d_ddig, B.d_dscale, B.d_mdig, B.d_mscale, B.d_PK,
-                            c->d_flags + 2, st))
+  if (stage == 1) {
+    if (mixed) {
+      if (launch_ozaki_gemm(B.plan, ne, B.n, ddig, dscale, B.d_mdig, B.d_mscale, PK, c->d_flags + 2,
+                            st))
         return HP3DG_ERR_CUDA;
     } else {
-      launch_contract_fp64(ne, B.nint, B.n, B.ni, B.nb, B.d_grad, B.d_D, B.d_PK, st);
+      launch_contract_fp64(ne, B.nint, B.n, B.ni, B.nb, B.d_grad, D, PK, st);
     }
+    return HP3DG_OK;
   }
-  mark(c, 3, st, capturing);
-  for (auto& B : c->bins) {
-    int ne = (int)B.elems.size();
-    const double* zd = c->have_zdofd ? c->d_zdofd : nullptr;
-    if (B.cond_tc) {
-      // Cholesky + explicit inverse in FP64; Y, W = Y^T Y and ASchur on tensor
-      // cores; then S = K_ii - W and the compression
-      if (launch_cond_tc(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
-                         B.d_perm, c->d_schur_off, c->d_bub_off, B.d_S, c->d_aschur,
-                         c->d_bschur, B.ctb, c->d_flags + 1, c->d_flags + 2, st))
-        return HP3DG_ERR_CUDA;
-      launch_compress(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, B.d_PK, B.d_perm, B.d_S,
-                      B.ctb.bi, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd,
-                      B.d_dmask, c->d_zastif, c->d_zbload, st);
-      continue;
-    }
-    if (launch_condense(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, c->d_nb_e, B.d_PK, B.d_b0,
-                        B.d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
-                        c->d_bub_off, c->d_zd_off, zd, B.d_dmask, B.d_S, c->d_zastif,
-                        c->d_zbload, c->d_aschur, c->d_bschur, B.d_Yg, c->d_flags + 1, st,
-                        B.tc_schur ? &B.tco : nullptr))
+  if (B.cond_tc) {
+    // Cholesky + explicit inverse in FP64; Y, W = Y^T Y and ASchur on tensor
+    // cores; then S = K_ii - W and the compression
+    CondTcBufs t = B.ctb;
+    t.kbd += (size_t)j0 * t.bytes_a;
+    t.lid += (size_t)j0 * t.bytes_b;
+    t.ltd += (size_t)j0 * t.bytes_b;
+    t.ekb += (size_t)j0 * t.nr;
+    t.eli += (size_t)j0 * t.nbr;
+    t.elt += (size_t)j0 * t.nbr;
+    t.bi += (size_t)j0 * B.ni;
+    if (launch_cond_tc(ne, B.n, B.ni, B.nb, el, c->d_ni_e, c->d_nb_e, PK, b0, perm,
+                       c->d_schur_off, c->d_bub_off, S, c->d_aschur, c->d_bschur, t,
+                       c->d_flags + 1, c->d_flags + 2, st))
       return HP3DG_ERR_CUDA;
-    if (B.tc_schur) {
-      // S = K_ii - Y^T Y on tensor cores, then the compression
-      if (launch_schur_tc(ne, B.n, B.ni, B.nb, B.tco.radix, B.tco.digits, B.d_ydig, B.d_yexp,
-                          B.d_elist, c->d_ni_e, B.d_S, c->d_flags + 2, st))
-        return HP3DG_ERR_CUDA;
-      launch_compress(ne, B.n, B.ni, B.nb, B.d_elist, c->d_ni_e, B.d_PK, B.d_perm, B.d_S, B.d_bi,
-                      c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd, B.d_dmask,
-                      c->d_zastif, c->d_zbload, st);
+    launch_compress(ne, B.n, B.ni, B.nb, el, c->d_ni_e, PK, perm, S, t.bi, c->d_nextract,
+                    c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd, dm, c->d_zastif, c->d_zbload, st);
+    return HP3DG_OK;
+  }
+  TcFactorOut tco = B.tco;
+  if (B.tc_schur) {
+    tco.ydig += (size_t)j0 * tco.ebytes;
+    tco.yexp += (size_t)j0 * tco.nr;
+    tco.bi += (size_t)j0 * B.ni;
+  }
+  double* Yg = B.d_Yg ? B.d_Yg + (size_t)j0 * B.nb * (B.ni + 1) : nullptr;
+  if (launch_condense(ne, B.n, B.ni, B.nb, el, c->d_ni_e, c->d_nb_e, PK, b0, perm, c->d_nextract,
+                      c->d_lcon_off, c->d_elem_nnz, c->d_schur_off, c->d_bub_off, c->d_zd_off, zd,
+                      dm, S, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur, Yg,
+                      c->d_flags + 1, st, B.tc_schur ? &tco : nullptr))
+    return HP3DG_ERR_CUDA;
+  if (B.tc_schur) {
+    // S = K_ii - Y^T Y on tensor cores, then the compression
+    if (launch_schur_tc(ne, B.n, B.ni, B.nb, tco.radix, tco.digits, tco.ydig, tco.yexp, el,
+                        c->d_ni_e, S, c->d_flags + 2, st))
+      return HP3DG_ERR_CUDA;
+    launch_compress(ne, B.n, B.ni, B.nb, el, c->d_ni_e, PK, perm, S, tco.bi, c->d_nextract,
+                    c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd, dm, c->d_zastif, c->d_zbload, st);
+  }
+  return HP3DG_OK;
+}
+
+// The per-run work of the pass, enqueued on st: flags reset, the three stages
+// over every bin (stage-major, with the phase timers between them) or, for a
+// pipelined download, all stages chunk by chunk with an event after each
+// chunk; then the global index maps.  Bin tables are built beforehand.
+int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
+  if (cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st) != cudaSuccess) return HP3DG_ERR_CUDA;
+  if (c->nchunk > 1) {
+    Bin& B = c->bins[0];
+    for (int k = 0; k < c->nchunk; ++k) {
+      for (int stage = 0; stage < 3; ++stage) {
+        int rc = enqueue_range(c, B, c->chunk_lo[k], c->chunk_lo[k + 1], stage, st);
+        if (rc) return rc;
+      }
+      if (capturing) cudaEventRecordWithFlags(c->chunk_ev[k], st, cudaEventRecordExternal);
+      else cudaEventRecord(c->chunk_ev[k], st);
+    }
+    mark(c, 2, st, capturing);
+    mark(c, 3, st, capturing);
+    mark(c, 4, st, capturing);
+  } else {
+    for (int stage = 0; stage < 3; ++stage) {
+      for (auto& B : c->bins) {
+        int rc = enqueue_range(c, B, 0, (int)B.elems.size(), stage, st);
+        if (rc) return rc;
+      }
+      mark(c, 2 + stage, st, capturing);
     }
   }
-  mark(c, 4, st, capturing);
   launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,
                     c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon, st);
   mark(c, 5, st, capturing);
@@ -856,6 +932,7 @@ int hp3dg_batch_run(hp3dg_ctx* c) {
   }
   c->ran = true;
   c->downloaded = false;
+  c->chunked_run = c->nchunk > 1;
   return HP3DG_OK;
 }
 
@@ -882,8 +959,6 @@ int hp3dg_batch_download(hp3dg_ctx* c) {
   if (!c) return HP3DG_ERR_ARG;
   if (!c->ran) return HP3DG_ERR_STATE;
   cudaSetDevice(c->device);
-  int rc = hp3dg_batch_sync(c);
-  if (rc != HP3DG_OK) return rc;
   int nel = c->nel;
   auto hal = [](void** p, size_t bytes) {
     if (*p) return true;
@@ -894,6 +969,35 @@ int hp3dg_batch_download(hp3dg_ctx* c) {
       !hal((void**)&c->h_lcon, c->lcon_off[nel] * 4) || !hal((void**)&c->h_nfirst, (size_t)c->nnodes * 4))
     return HP3DG_ERR_ALLOC;
   cudaStream_t st = c->stream;
+  if (c->chunked_run) {
+    // each chunk's outputs (contiguous in element order) as soon as its event
+    // fires, on the copy stream, while the pass continues on st
+    cudaStream_t cs = c->copy_stream;
+    for (int k = 0; k < c->nchunk; ++k) {
+      const int e0 = c->chunk_lo[k], e1 = c->chunk_lo[k + 1];
+      CK(cudaStreamWaitEvent(cs, c->chunk_ev[k], 0));
+      CK(cudaMemcpyAsync(c->h_zastif + c->elem_nnz[e0], c->d_zastif + c->elem_nnz[e0],
+                         (c->elem_nnz[e1] - c->elem_nnz[e0]) * 8, cudaMemcpyDeviceToHost, cs));
+      CK(cudaMemcpyAsync(c->h_zbload + c->lcon_off[e0], c->d_zbload + c->lcon_off[e0],
+                         (c->lcon_off[e1] - c->lcon_off[e0]) * 8, cudaMemcpyDeviceToHost, cs));
+      CK(cudaMemcpyAsync(c->h_aschur + c->schur_off[e0], c->d_aschur + c->schur_off[e0],
+                         (c->schur_off[e1] - c->schur_off[e0]) * 8, cudaMemcpyDeviceToHost, cs));
+      CK(cudaMemcpyAsync(c->h_bschur + c->bub_off[e0], c->d_bschur + c->bub_off[e0],
+                         (c->bub_off[e1] - c->bub_off[e0]) * 8, cudaMemcpyDeviceToHost, cs));
+    }
+    // the index maps come last in the pass
+    int rc = hp3dg_batch_sync(c);
+    if (rc != HP3DG_OK) { cudaStreamSynchronize(cs); return rc; }
+    CK(cudaMemcpyAsync(c->h_lcon, c->d_lcon, c->lcon_off[nel] * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(c->h_nfirst, c->d_nfirst, (size_t)c->nnodes * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&c->h_nrdof, c->d_total, 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(cs));
+    CK(cudaStreamSynchronize(st));
+    c->downloaded = true;
+    return HP3DG_OK;
+  }
+  int rc = hp3dg_batch_sync(c);
+  if (rc != HP3DG_OK) return rc;
   CK(cudaMemcpyAsync(c->h_zastif, c->d_zastif, c->elem_nnz[nel] * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(c->h_zbload, c->d_zbload, c->lcon_off[nel] * 8, cudaMemcpyDeviceToHost, st));
   CK(cudaMemcpyAsync(c->h_aschur, c->d_aschur, c->schur_off[nel] * 8, cudaMemcpyDeviceToHost, st));
@@ -1133,6 +1237,8 @@ void hp3dg_batch_end(hp3dg_ctx* c) {
   free_batch(c);
   cudaFree(c->d_flags);
   for (auto& e : c->ev) cudaEventDestroy(e);
+  for (auto& e : c->chunk_ev) cudaEventDestroy(e);
+  cudaStreamDestroy(c->copy_stream);
   cudaStreamDestroy(c->own);
   delete c;
 }

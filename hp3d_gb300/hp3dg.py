@@ -36,7 +36,8 @@ class Opts(ctypes.Structure):
                 ("timing", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("ozaki_radix", ctypes.c_int32), ("ozaki_digits", ctypes.c_int32),
                 ("stc_method", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
-                ("schur_fp64", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("schur_fp64", ctypes.c_int32), ("download_chunks", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 DESC_DTYPE = np.dtype([("etype", np.int32), ("mdle", np.int32), ("norder", np.int32, 19),
@@ -114,7 +115,8 @@ class ElementPass:
     """One batched element pass (a context of the C ABI)."""
 
     def __init__(self, precision=FP64, integration=0, isol=10, keep_elem=False, timing=False,
-                 device=0, ozaki_radix=0, ozaki_digits=0, graph=True, schur_tc=True):
+                 device=0, ozaki_radix=0, ozaki_digits=0, graph=True, schur_tc=True,
+                 download_chunks=0):
         self.L = lib()
         o = Opts()
         o.precision = precision
@@ -127,6 +129,7 @@ class ElementPass:
         o.ozaki_digits = ozaki_digits
         o.launch_mode = 0 if graph else 1
         o.schur_fp64 = 0 if schur_tc else 1
+        o.download_chunks = download_chunks
         self.ctx = _vp()
         self._check(self.L.hp3dg_batch_begin(ctypes.byref(o), ctypes.byref(self.ctx)), "begin")
         self.nel = 0

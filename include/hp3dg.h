@@ -82,7 +82,12 @@ typedef struct hp3dg_opts {
   int32_t schur_fp64;  /* HP3DG_MIXED only: 0 = the Schur update of the
                           condensation (K_ii - Y^T Y) on tensor cores with
                           split-BF16 digits where the bin fits, 1 = FP64 */
-  int32_t reserved[5];
+  int32_t download_chunks; /* 0/1: one piece; N = 2..8: for a batch of one bin
+                          the pass runs in N element chunks and
+                          hp3dg_batch_download copies each chunk's outputs
+                          as soon as it is done, overlapping the copies with
+                          the rest of the pass (same results) */
+  int32_t reserved[4];
 } hp3dg_opts;
 
 /* Element descriptor: what find_order (datstrs/find_order.F90:5),

@@ -72,3 +72,38 @@ def test_resubmit_same_mesh_reuses_and_matches_fresh_submit():
     ref = H.ElementPass(H.MIXED, isol=10)
     ref.submit(m2); ref.run(); ref.download()
     _same(_outputs(ep), _outputs(ref))
+
+
+@pytest.mark.parametrize("prec,graph", [(H.MIXED, True), (H.MIXED, False), (H.FP64, True)])
+def test_pipelined_download_matches_one_piece(prec, graph):
+    """download_chunks: the pass runs in element chunks and each chunk's
+    outputs are copied as soon as it is done; the results are the same bytes
+    as the one-piece download (chunks at 128-element boundaries; 343 and 729
+    elements, so that the last chunk is ragged)."""
+    for n in (7, 9):
+        m = M.random_orientations(M.structured_hexa(n, 3, perturb=0.1, seed=2), seed=6)
+        ref = H.ElementPass(prec, isol=10, graph=graph)
+        ref.submit(m); ref.run(); ref.download()
+        o_ref = _outputs(ref)
+        for chunks in (2, 3, 8):
+            ep = H.ElementPass(prec, isol=10, graph=graph, download_chunks=chunks)
+            ep.submit(m)
+            for _ in range(2):
+                ep.run(); ep.download()
+                _same(o_ref, _outputs(ep))
+            ep.close()
+        ref.close()
+
+
+def test_pipelined_download_with_several_bins_falls_back():
+    m = M.hp_hexa(3, seed=3, perturb=0.1)
+    ref = H.ElementPass(H.MIXED, isol=10)
+    ref.submit(m); ref.run(); ref.download()
+    ep = H.ElementPass(H.MIXED, isol=10, download_chunks=4)
+    ep.submit(m); ep.run(); ep.download()
+    _same(_outputs(ref), _outputs(ep))
+
+
+def test_download_chunks_out_of_range_is_rejected():
+    with pytest.raises(H.HP3DGError):
+        H.ElementPass(H.MIXED, download_chunks=9)
