@@ -38,24 +38,16 @@ sys.path.insert(0, ROOT)
 METRIC = "condensed elements/s at p=5: mixed-precision vs plain FP64 GPU at 1e-10 rel err"
 
 
-def make_mesh(n, p, seed=12345):
+def make_mesh(args, seed=12345):
+    """hexa: the metric's uniform mesh.  mixed: the hp-adaptive mesh of
+    hexahedra, prisms and tetrahedra (orders 1..6 drawn per element, minimum
+    rule on shared edges and faces), n^3 cells of which the x > 21/24 and
+    z > 21/24 slabs are split into prisms and tetrahedra."""
     from hp3d_gb300 import mesh as M
-    return M.structured_hexa(n, p, perturb=0.15, kappa_logrange=(-2, 2), seed=seed)
-
-
-def per_element_work(n, nint):
-    """Algorithmic work per element: SYRK flop count of elem_opt, one D.M
-    product of the mixed contraction, condensation flops, output bytes."""
-    nb = (round(n ** (1 / 3)) - 1) ** 3
-    ni = n - nb
-    ncols = n * (n + 1) // 2
-    f_syrk = n * (n + 1) * 3 * nint
-    f_dm = 2 * 6 * nint * ncols          # one D.M product (FLOP)
-    f_stc = (2 / 3) * nb ** 3 + 2 * nb * nb * (ni + 1) + 2 * ni * ni * nb + 2 * ni * nb
-    bytes_out = 8 * (ni * ni + ni + nb * ni + nb) + 4 * ni
-    bytes_in = 8 * (24 + 1) + 364
-    return dict(nb=nb, ni=ni, ncols=ncols, f_syrk=f_syrk, f_dm=f_dm, f_stc=f_stc,
-                bytes=bytes_out + bytes_in)
+    if args.workload == "mixed":
+        return M.mixed_mesh(args.n, a=21 / 24, b=21 / 24, pmax=6, perturb=0.1,
+                            kappa_logrange=(-2, 2), seed=seed)
+    return M.structured_hexa(args.n, args.p, perturb=0.15, kappa_logrange=(-2, 2), seed=seed)
 
 
 class ClockSampler:
@@ -123,23 +115,26 @@ def cpu_baseline(mesh, isol, integration, seconds=15.0, nthreads=0):
     """Time the oracle (OpenMP, all host cores) on a bounded sample."""
     from oracle import oracle as O
     cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
-    # size the sample: one probe round of `cores` elements
-    probe = np.arange(min(cores, mesh["nelem"]))
+    # size the sample: one probe round of `cores` elements, spread evenly over
+    # the mesh (an hp mesh's orders vary with position)
+    nel = mesh["nelem"]
+    spread = lambda k: np.unique(np.round(np.linspace(0, nel - 1, k)).astype(np.int64))  # noqa: E731
+    probe = spread(min(cores, nel))
     t0 = time.perf_counter()
     O.element_pass(mesh, isol=isol, integration=integration, stc_method=0, nthreads=cores,
                    elements=probe)
     dt = time.perf_counter() - t0
     per_round = max(dt, 1e-3)
     rounds = max(1, int(seconds / per_round))
-    ns = min(mesh["nelem"], rounds * len(probe))
-    sample = np.arange(ns)
+    sample = spread(min(nel, rounds * len(probe)))
+    ns = len(sample)
     t0 = time.perf_counter()
     r = O.element_pass(mesh, isol=isol, integration=integration, stc_method=0, nthreads=cores,
                        elements=sample)
     dt = time.perf_counter() - t0
     assert r["rc"] == 0
     return {"value": ns / dt, "unit": "elements/s", "cores": cores, "kind": "port",
-            "sample": f"{ns} of {mesh['nelem']} elements (first in ELEM_ORDER), one pass, "
+            "sample": f"{ns} of {nel} elements (evenly spread over ELEM_ORDER), one pass, "
                       f"{dt:.1f} s, oracle C restatement (elem_opt DSYRK form + LU condensation "
                       f"+ compression), OpenMP"}
 
@@ -147,11 +142,13 @@ def cpu_baseline(mesh, isol, integration, seconds=15.0, nthreads=0):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    mesh = make_mesh(args.n, args.p)
+    mesh = make_mesh(args)
     vals = []
     cb = None
+    # each step a bounded sample, the whole run about two minutes at most
+    sec = min(args.cpu_seconds, 120.0 / max(1, args.warmup + args.steps))
     for i in range(args.warmup + args.steps):
-        c = cpu_baseline(mesh, args.isol, args.integration, seconds=args.cpu_seconds)
+        c = cpu_baseline(mesh, args.isol, args.integration, seconds=sec)
         if i >= args.warmup:
             vals.append(c["value"])
             cb = c
@@ -160,14 +157,23 @@ def run_reference(args, rank, world):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * mesh["nelem"] / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_dict(args, world),
+            "config": config_dict(args, world, mesh),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def config_dict(args, world):
+def config_dict(args, world, mesh):
+    if args.workload == "mixed":
+        cnt = np.bincount(mesh["etype"], minlength=4)[1:]
+        return {"workload": f"galerkin_poisson_hp_mixed_{args.n}^3_cells_pmax6_integration{args.integration}",
+                "elements_per_gpu": int(mesh["nelem"]),
+                "hexa_prism_tet": [int(x) for x in cnt], "orders": "1..6 per element, min rule",
+                "perturbation": "U(-0.1h,0.1h) interior vertices", "kappa": "10**U(-2,2)",
+                "precision": args.precision,
+                "parallelism": f"replicas{world}" if world > 1 else "single",
+                "l2": "working set per step > L2, no flush needed"}
     return {"workload": f"galerkin_poisson_hexa_{args.n}^3_p{args.p}_integration{args.integration}",
             "elements_per_gpu": args.n ** 3, "p": args.p, "quadrature_points": (min(args.p + args.integration, 6) + 1) ** 3,
             "perturbation": "U(-0.15h,0.15h) interior vertices", "kappa": "10**U(-2,2)",
@@ -182,6 +188,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="hexa", choices=["hexa", "mixed"],
+                    help="hexa: uniform p hexahedra (the metric's mesh); mixed: hp-adaptive "
+                         "hexa/prism/tet mesh")
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--p", type=int, default=5)
     ap.add_argument("--integration", type=int, default=1)
@@ -210,7 +219,7 @@ def main():
     B.build()
     from hp3d_gb300 import hp3dg as H
 
-    mesh = make_mesh(args.n, args.p, seed=12345 + rank)
+    mesh = make_mesh(args, seed=12345 + rank)
     prec = H.MIXED if args.precision == "mixed" else H.FP64
     stream = torch.cuda.current_stream()
 
@@ -292,7 +301,9 @@ def main():
     epc.close()
     e2e = {"value": world * nel / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * e2e_s,
-           "cold_step_ms": cold_ms, "download_chunks": args.download_chunks,
+           "cold_step_ms": cold_ms,
+           # the chunked pass applies to a batch of one bin (the uniform mesh)
+           "download_chunks": args.download_chunks if args.workload == "hexa" else 1,
            "note": "resubmit of the mesh with new kappa each step (upload xvert+kappa, "
                    "run, download all condensed outputs, each element chunk copied as "
                    "soon as it is done); cold_step_ms = new context"}
@@ -305,21 +316,25 @@ def main():
                 "unit": "elements/s", "phase_ms": [round(x, 3) for x in ph64[-1]]}
         ep64.close()
 
-    nint = (min(args.p + args.integration, 6) + 1) ** 3
-    n = (args.p + 1) ** 3
-    w = per_element_work(n, nint)
     ph = np.median(np.array(phases), axis=0)
     hbm, bf16, peak_kind = measured_peaks()
-    # dominant kernel = contraction phase (one launch per bin; one bin here)
+    # dominant kernel = the contraction (one launch per bin; one bin for the
+    # uniform mesh); its algorithmic FLOPs per run come from the library
+    kernels, flops = ep.pass_stats()
     t_con = ph[2] / 1000.0
+    con_note = ""
+    if args.workload == "mixed":
+        # bins run on parallel branches: the contraction's own time is not
+        # separable, so the whole pass bounds it from above
+        t_con = ph[5] / 1000.0
+        con_note = "; time = whole pass (bins run concurrently), a lower bound on the rate"
     if prec == H.MIXED:
-        pairs = ep.ozaki_pairs() if hasattr(ep, "ozaki_pairs") else None
-        flops = nel * w["f_dm"] * (pairs or 0)
+        pairs = ep.ozaki_pairs()
         roof = {"bound": "tensor", "achieved": flops / t_con / 1e12 if t_con > 0 else None,
                 "peak": bf16, "unit": "TFLOP/s", "kernel": "k_ozaki_gemm",
-                "note": f"{pairs} digit-pair products of the D.M contraction; peak {peak_kind}"}
+                "note": f"{pairs} digit-pair products of the D.M contraction, "
+                        f"2*(6*nint)*n(n+1)/2 each per element; peak {peak_kind}{con_note}"}
     else:
-        flops = nel * w["f_syrk"]
         roof = {"bound": "tensor", "achieved": flops / t_con / 1e12 if t_con > 0 else None,
                 "peak": bf16, "unit": "TFLOP/s", "kernel": "k_contract_fp64",
                 "note": "FP64 CUDA-core contraction measured against the bf16 peak"}
@@ -331,16 +346,16 @@ def main():
     if rank == 0 and not args.no_cpu_baseline:
         cb = cpu_baseline(mesh, args.isol, args.integration, seconds=args.cpu_seconds)
 
-    # kernels per pass: orient, geom, load, contraction (+ d_scale, slice_d when mixed),
-    # condense, and 7 index-map kernels
-    launches_per_step = 12 if prec == H.FP64 else 14
+    # kernel launches per pass: the kernel nodes of the captured graph
+    launches_per_step = kernels
     line = {"metric": METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if prec == H.FP64 else "bf16-digits->f64", "data": "synthetic",
-            "config": config_dict(args, world), "e2e": e2e, "roofline": roof,
+            "config": config_dict(args, world, mesh), "e2e": e2e, "roofline": roof,
             "cpu_baseline": cb, "clocks": clocks,
-            "gpu_launches": launches_per_step * args.steps,
+            "gpu_launches": launches_per_step * args.steps if launches_per_step > 0 else None,
+            "launches_per_pass": launches_per_step,
             "phase_ms": {"tables": float(ph[0]), "geometry_load": float(ph[1]),
                          "contraction": float(ph[2]), "condensation": float(ph[3]),
                          "index_maps": float(ph[4]), "pass": float(ph[5])},

@@ -385,12 +385,18 @@ struct hp3dg_ctx {
   cudaEvent_t ev[8] = {};
   float times[6] = {0, 0, 0, 0, 0, 0};
   cudaGraphExec_t graph = nullptr;  // the captured pass; rebuilt after every new structure
+  int64_t graph_kernels = -1;        // kernel nodes of the captured pass
   // pipelined download: the pass in element chunks, each recording an event
   int nchunk = 1;
   int chunk_lo[9] = {0};            // chunk boundaries (element positions of the single bin)
   cudaEvent_t chunk_ev[8] = {};
   cudaStream_t copy_stream = nullptr;
   bool chunked_run = false;
+  // a batch of several bins runs them on parallel branches: the bins are
+  // spread over NBRANCH streams forked from the library stream
+  static constexpr int NBRANCH = 4;
+  cudaStream_t branch[NBRANCH] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[NBRANCH] = {};
   std::vector<hp3dg_elem_desc> last_desc;  // descriptors of the current batch
 };
 
@@ -412,6 +418,7 @@ void free_bin(Bin& b) {
 void free_batch(hp3dg_ctx* c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
   c->graph = nullptr;
+  c->graph_kernels = -1;
   for (auto& b : c->bins) free_bin(b);
   c->bins.clear();
   void* dev[] = {c->d_norder, c->d_nori_e, c->d_nori_f, c->d_nodes, c->d_ndofm, c->d_nextract,
@@ -490,6 +497,14 @@ int hp3dg_batch_begin(const hp3dg_opts* opts, hp3dg_ctx** out) {
   if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return HP3DG_ERR_CUDA;
+  }
+  cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
+  for (int b = 0; b < hp3dg_ctx::NBRANCH; ++b) {
+    cudaEventCreateWithFlags(&c->join_ev[b], cudaEventDisableTiming);
+    if (cudaStreamCreateWithFlags(&c->branch[b], cudaStreamNonBlocking) != cudaSuccess) {
+      delete c;
+      return HP3DG_ERR_CUDA;
+    }
   }
   if (cudaMalloc(&c->d_flags, 4 * sizeof(int)) != cudaSuccess) { delete c; return HP3DG_ERR_ALLOC; }
   *out = c;
@@ -864,14 +879,51 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
     mark(c, 2, st, capturing);
     mark(c, 3, st, capturing);
     mark(c, 4, st, capturing);
-  } else {
+  } else if (c->bins.size() == 1) {
     for (int stage = 0; stage < 3; ++stage) {
-      for (auto& B : c->bins) {
-        int rc = enqueue_range(c, B, 0, (int)B.elems.size(), stage, st);
-        if (rc) return rc;
-      }
+      int rc = enqueue_range(c, c->bins[0], 0, (int)c->bins[0].elems.size(), stage, st);
+      if (rc) return rc;
       mark(c, 2 + stage, st, capturing);
     }
+  } else {
+    // bins on parallel branches (largest estimated work first, each to the
+    // least loaded branch); a captured graph keeps the branches as
+    // independent paths, so small bins' kernels run side by side
+    const int nb = (int)c->bins.size();
+    std::vector<int> order(nb);
+    std::vector<double> work(nb);
+    for (int b = 0; b < nb; ++b) {
+      order[b] = b;
+      const Bin& B = c->bins[b];
+      work[b] = (double)B.elems.size() * B.nint * B.n * (double)B.n + 1e6;
+    }
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return work[a] > work[b]; });
+    double load[hp3dg_ctx::NBRANCH] = {0};
+    std::vector<int> owner(nb);
+    for (int b : order) {
+      int k = 0;
+      for (int j = 1; j < hp3dg_ctx::NBRANCH; ++j)
+        if (load[j] < load[k]) k = j;
+      owner[b] = k;
+      load[k] += work[b];
+    }
+    if (cudaEventRecord(c->fork_ev, st) != cudaSuccess) return HP3DG_ERR_CUDA;
+    for (int k = 0; k < hp3dg_ctx::NBRANCH; ++k)
+      if (cudaStreamWaitEvent(c->branch[k], c->fork_ev, 0) != cudaSuccess) return HP3DG_ERR_CUDA;
+    for (int b : order)
+      for (int stage = 0; stage < 3; ++stage) {
+        Bin& B = c->bins[b];
+        int rc = enqueue_range(c, B, 0, (int)B.elems.size(), stage, c->branch[owner[b]]);
+        if (rc) return rc;
+      }
+    for (int k = 0; k < hp3dg_ctx::NBRANCH; ++k) {
+      if (cudaEventRecord(c->join_ev[k], c->branch[k]) != cudaSuccess) return HP3DG_ERR_CUDA;
+      if (cudaStreamWaitEvent(st, c->join_ev[k], 0) != cudaSuccess) return HP3DG_ERR_CUDA;
+    }
+    // the per-stage timers are not meaningful across branches
+    mark(c, 2, st, capturing);
+    mark(c, 3, st, capturing);
+    mark(c, 4, st, capturing);
   }
   launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,
                     c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon, st);
@@ -923,6 +975,17 @@ int hp3dg_batch_run(hp3dg_ctx* c) {
         if (g) cudaGraphDestroy(g);
         cudaGetLastError();
         return rc ? rc : HP3DG_ERR_CUDA;
+      }
+      size_t nn = 0;
+      c->graph_kernels = 0;
+      if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+        std::vector<cudaGraphNode_t> nodes(nn);
+        if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+          for (size_t i = 0; i < nn; ++i) {
+            cudaGraphNodeType ty;
+            if (cudaGraphNodeGetType(nodes[i], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+              ++c->graph_kernels;
+          }
       }
       ce = cudaGraphInstantiate(&c->graph, g, 0);
       cudaGraphDestroy(g);
@@ -1228,6 +1291,24 @@ int hp3dg_mixed_config(const hp3dg_ctx* c, int32_t* radix, int32_t* digits, int3
   return HP3DG_OK;
 }
 
+int hp3dg_pass_stats(const hp3dg_ctx* c, int64_t* kernels, double* contraction_flops) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  if (kernels) *kernels = c->graph ? c->graph_kernels : -1;
+  if (contraction_flops) {
+    double f = 0.0;
+    for (const auto& B : c->bins) {
+      const double ne = (double)B.elems.size(), n = B.n, nint = B.nint;
+      if (c->opts.precision == HP3DG_MIXED)
+        f += ne * ozaki_pairs(B.plan) * 2.0 * (6.0 * nint) * (n * (n + 1) / 2);
+      else
+        f += ne * n * (n + 1) * 3.0 * nint;
+    }
+    *contraction_flops = f;
+  }
+  return HP3DG_OK;
+}
+
 int32_t hp3dg_last_bad_element(const hp3dg_ctx* c) { return c ? c->last_bad : -1; }
 
 void hp3dg_batch_end(hp3dg_ctx* c) {
@@ -1239,6 +1320,11 @@ void hp3dg_batch_end(hp3dg_ctx* c) {
   for (auto& e : c->ev) cudaEventDestroy(e);
   for (auto& e : c->chunk_ev) cudaEventDestroy(e);
   cudaStreamDestroy(c->copy_stream);
+  cudaEventDestroy(c->fork_ev);
+  for (int b = 0; b < hp3dg_ctx::NBRANCH; ++b) {
+    cudaEventDestroy(c->join_ev[b]);
+    cudaStreamDestroy(c->branch[b]);
+  }
   cudaStreamDestroy(c->own);
   delete c;
 }

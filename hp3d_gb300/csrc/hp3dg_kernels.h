@@ -5,6 +5,12 @@
 
 namespace hp3dg {
 
+// Raises the dynamic shared-memory limit of a kernel (on the current device)
+// to at least `bytes`.  The limit only grows, so a launch enqueued earlier
+// (into a graph being captured, or a stream that has not reached it) stays
+// valid when a later launch of the same kernel needs less.
+cudaError_t raise_smem_limit(const void* func, size_t bytes);
+
 // element types as in the C ABI (HP3DG_HEXA / HP3DG_PRISM / HP3DG_TET)
 constexpr int ETYPE_HEXA = 1, ETYPE_PRISM = 2, ETYPE_TET = 3;
 

@@ -670,9 +670,7 @@ int launch_cond_tc(int nel, int nfull, int nif, int nbf, const int* d_elist, con
   o.nr = b.nr; o.nbr = b.nbr; o.nkb = b.nkb; o.digits = b.digits; o.radix = b.radix;
   o.bytes_a = (uint32_t)b.bytes_a; o.bytes_b = (uint32_t)b.bytes_b;
   size_t sm1 = cond_chol_smem(nbf);
-  if (cudaFuncSetAttribute(k_cond_chol, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm1) !=
-      cudaSuccess)
-    return -1;
+  if (raise_smem_limit((const void*)k_cond_chol, sm1) != cudaSuccess) return -1;
   k_cond_chol<<<(nel + CH_WARPS - 1) / CH_WARPS, CH_WARPS * 32, sm1, st>>>(
       nfull, nif, nbf, d_elist, d_ni_e, d_nb_e, d_PK, d_b0, d_perm, d_bub_off, d_bschur, o, nel,
       d_bad_spd);
@@ -706,9 +704,7 @@ int launch_cond_tc(int nel, int nfull, int nif, int nbf, const int* d_elist, con
     }
   P.npair = np;
   size_t sm2 = b.bytes_a + b.bytes_b + 1024;
-  if (cudaFuncSetAttribute(k_cond_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2) !=
-      cudaSuccess)
-    return -1;
+  if (raise_smem_limit((const void*)k_cond_tc, sm2) != cudaSuccess) return -1;
   int grid = nel < num_sms ? nel : num_sms;
   k_cond_tc<<<grid, CT_THREADS, sm2, st>>>(b.kbd, b.lid, b.ltd, b.ekb, b.eli, b.elt, P, d_elist,
                                            d_ni_e, d_nb_e, d_schur_off, d_W, d_aschur, d_flag);

@@ -24,6 +24,7 @@
 // capture begins.
 #include "../../include/hp3dg.h"
 #include "hp3dg_internal.cuh"
+#include "hp3dg_kernels.h"
 
 #include <cuda_runtime.h>
 
@@ -172,9 +173,7 @@ extern "C" int hp3dg_condense_noalloc(int32_t n_elem, int32_t n, int32_t nb, con
   int* status = (int*)(scratch + kScratchDoubles - 1);
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemsetAsync(status, 0x7f, sizeof(int), st) != cudaSuccess) return HP3DG_ERR_CUDA;
-  if (cudaFuncSetAttribute(k_condense_dense, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess)
-    return HP3DG_ERR_CUDA;
+  if (hp3dg::raise_smem_limit((const void*)k_condense_dense, smem) != cudaSuccess) return HP3DG_ERR_CUDA;
   k_condense_dense<<<n_elem, NT, smem, st>>>(n, ni, nb, K, b, scratch, aii, bi, aschur, bschur,
                                              status);
   if (cudaPeekAtLastError() != cudaSuccess) return HP3DG_ERR_CUDA;

@@ -21,7 +21,25 @@
 
 #include <math.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 namespace hp3dg {
+
+cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, size_t> cur;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& have = cur[{dev, func}];
+  if (bytes <= have) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) have = bytes;
+  return e;
+}
+
 
 // ---------------------------------------------------------------------------
 // tables
@@ -611,9 +629,7 @@ int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, co
   if (nel <= 0) return 0;
   size_t smem = d_Yg ? condense_smem_small(nif, nbf) : condense_smem(nif, nbf);
   if (smem > 227 * 1024) return -2;
-  if (cudaFuncSetAttribute(k_condense, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return -1;
+  if (raise_smem_limit((const void*)k_condense, smem) != cudaSuccess) return -1;
   TcFactorOut none{};
   k_condense<<<nel, CND_THREADS, smem, st>>>(nfull, nif, nbf, d_elist, d_ni_e, d_nb_e, d_PK, d_b0,
                                               d_perm, d_nextract, d_lcon_off, d_elem_nnz,

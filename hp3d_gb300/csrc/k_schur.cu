@@ -251,9 +251,7 @@ int launch_schur_tc(int nel, int nfull, int nif, int nbf, int radix, int digits,
     }
   P.npair = np;
   size_t smem = schur_tc_elem_bytes(nif, nbf, digits) + 1024;
-  if (cudaFuncSetAttribute(k_schur_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return -1;
+  if (raise_smem_limit((const void*)k_schur_tc, smem) != cudaSuccess) return -1;
   int grid = nel < num_sms ? nel : num_sms;
   k_schur_tc<<<grid, SC_THREADS, smem, st>>>(d_ydig, d_yexp, P, d_elist, d_ni_e, d_W, d_flag);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;

@@ -55,7 +55,7 @@ EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit", "hp3dg
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
            "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_output_sizes", "hp3dg_device_outputs",
-           "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_last_bad_element", "hp3dg_batch_end", "hp3dg_strerror"]
+           "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_pass_stats", "hp3dg_last_bad_element", "hp3dg_batch_end", "hp3dg_strerror"]
 
 
 def lib():
@@ -83,6 +83,7 @@ def lib():
         L.hp3dg_device_outputs.argtypes = [_vp] + [ctypes.POINTER(_vp)] * 5
         L.hp3dg_phase_times.argtypes = [_vp, _f32p, ctypes.c_int32]
         L.hp3dg_mixed_config.argtypes = [_vp, _i32p, _i32p, _i32p]
+        L.hp3dg_pass_stats.argtypes = [_vp, _i64p, _f64p]
         L.hp3dg_last_bad_element.argtypes = [_vp]
         L.hp3dg_last_bad_element.restype = ctypes.c_int32
         L.hp3dg_batch_end.argtypes = [_vp]
@@ -240,6 +241,13 @@ class ElementPass:
         self._check(self.L.hp3dg_mixed_config(self.ctx, ctypes.byref(r), ctypes.byref(d),
                                               ctypes.byref(p)), "mixed_config")
         return r.value, d.value, p.value
+
+    def pass_stats(self):
+        """(kernel launches per run from the captured graph, or -1; algorithmic
+        contraction FLOPs per run)."""
+        k, f = ctypes.c_int64(), ctypes.c_double()
+        self._check(self.L.hp3dg_pass_stats(self.ctx, ctypes.byref(k), ctypes.byref(f)), "stats")
+        return k.value, f.value
 
     def ozaki_pairs(self):
         return self.mixed_config()[2]

@@ -220,6 +220,16 @@ int hp3dg_phase_times(const hp3dg_ctx *ctx, float *ms, int32_t n);
  * Returns HP3DG_ERR_STATE before a mixed-precision submit. */
 int hp3dg_mixed_config(const hp3dg_ctx *ctx, int32_t *radix, int32_t *digits, int32_t *pairs);
 
+/* Statistics of the pass as it runs after the last submit.
+ * kernels: kernel launches per hp3dg_batch_run, counted from the kernel nodes
+ *   of the captured CUDA graph (-1 before the first run or with launch_mode
+ *   = 1, where nothing is captured).
+ * contraction_flops: algorithmic floating-point operations of the contraction
+ *   per run, summed over the bins: mixed precision, digit-pair products x
+ *   2 (6 nint) n(n+1)/2 per element; FP64, n(n+1) 3 nint per element (the
+ *   DSYRK count of elem_opt). */
+int hp3dg_pass_stats(const hp3dg_ctx *ctx, int64_t *kernels, double *contraction_flops);
+
 /* Size of the fixed device scratch array used by hp3dg_condense_noalloc:
  * 2^20 doubles (8 MiB), resident on every GPU that loads the library. */
 #define HP3DG_NOALLOC_SCRATCH_DOUBLES (1 << 20)

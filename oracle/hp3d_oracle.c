@@ -1439,3 +1439,19 @@ int orc_shape3DH_prism(const double *xi, const int32_t *nord,
   }
   return m;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Helpers shared with hp3d_oracle_dpg.c (hp3d_oracle_int.h)                  */
+/* ------------------------------------------------------------------------ */
+void orc_i_decod(int nick, int mod, int n, int *arr) { decod(nick, mod, n, arr); }
+void orc_i_poly_legendre(double x, double t, int nord, double *p) { poly_legendre(x, t, nord, p); }
+void orc_i_poly_ilegendre(double x, double t, int nord, int idec, double *L, double *P, double *R) {
+  poly_ilegendre(x, t, nord, idec, L, P, R);
+}
+void orc_i_hom_ilegendre(const double *S, const double DS[3][2], int nord, int idec, double *homL,
+                         double dhomL[][3]) {
+  hom_ilegendre(S, DS, nord, idec, homL, dhomL);
+}
+const int (*orc_i_hexa_e(void))[5] { return HEXA_E; }
+const int (*orc_i_hexa_f(void))[4] { return HEXA_F; }
+const int (*orc_i_orq(void))[6] { return ORQ; }

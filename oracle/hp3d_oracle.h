@@ -168,6 +168,67 @@ int orc_element_pass(int nelem, const int32_t *etype, const int32_t *norder,
                      double *zastif, double *zbload, double *aschur,
                      double *bschur);
 
+/* ------------------------------------------------------------------------ */
+/* Ultraweak DPG Maxwell on hexahedra (problems/MAXWELL/ULTRAWEAK_DPG),       */
+/* hp3d_oracle_dpg.c.  Complex arrays are interleaved (re, im) doubles.       */
+/* ------------------------------------------------------------------------ */
+
+/* commonParam.F90 / set_environment.F90: OMEGA, MU, EPSILON, GAMMA,
+ * ALPHA_NORM, IBCFLAG (0 Dirichlet, 2 impedance by penalty), NORD_ADD,
+ * ISOL (mfd_solutions cases 0-2) and ICOMP_EXACT (1-based component of E). */
+typedef struct {
+  double omega, mu, epsilon, gamma, alpha;
+  int32_t ibcflag, nord_add, isol, icomp;
+} orc_maxw_params;
+
+/* H(curl) count of shape3DEHexa for Norder (celndof E branch) */
+int orc_nrdofE_hexa(const int32_t *norder);
+/* shape3DEHexa (Hexahedron.F90:240-440): values and curls (3,k) */
+int orc_shape3DE_hexa(const double *xi, const int32_t *nord, const int32_t *nori_edge,
+                      const int32_t *nori_face, double *shapE, double *curlE);
+/* shape3DQHexa (Hexahedron.F90:640-698) */
+int orc_shape3DQ_hexa(const double *xi, const int32_t *nord, double *shapQ);
+/* shape3EE for a brick -> shape3DEBrokenHexa (BrokenHexahedron.F90:139-258);
+ * nordP = the enriched middle-node order code (e.g. 444) */
+int orc_shape3EE_hexa(const double *xi, int nordP, double *shapE, double *curlE);
+/* set_2D_int(_DPG) of a quad face (set_2D_int.F90:72-247): norderf = face_order
+ * (4 edge orders + face code), maxp = MAXP (6) or MAXPP (7) */
+int orc_set_2D_int_quad(const int32_t *norderf, int nori, int integration, int maxp,
+                        double *tloc, double *wtloc);
+/* exact E, H and source J of mfd_solutions case isol (exact.F90, getf.F90);
+ * eps = EPSILON * eps_r of the element */
+void orc_maxw_exact(int isol, int icomp, double omega, double mu, double eps_re, double eps_im,
+                    const double *X, double *E, double *H, double *J);
+/* sizes[5] = {NrdofEi, NrdofQ, NrdofEE, NrTest, NrTrial} (elem.F90:78-103) */
+int orc_dpg_sizes(const int32_t *norder, int nord_add, int32_t *sizes);
+/* elem_maxwell (elem/elem_maxwell.F90:24-676) with the impedance penalty
+ * (imp_penalty 679-876) on the faces of imp_mask (bit f: ibc(f,2) = 2) and a
+ * scalar complex relative permittivity eps_r per element (get_permittivity
+ * returns eps_r * I).  zaloc: NrTrial x NrTrial, column-major, rows/columns
+ * [E,H traces interleaved per shape function | 6 L2 components per shape
+ * function]; zbloc: NrTrial.  Returns NrTrial, -1 (negative Jacobian) or -2
+ * (Gram not positive definite). */
+int orc_dpg_maxwell_elem(const int32_t *norder, const int32_t *nori_edge, const int32_t *nori_face,
+                         const double *xvert, double eps_re, double eps_im, int32_t imp_mask,
+                         const orc_maxw_params *prm, double *zaloc, double *zbloc);
+/* stc_fwd_herm (stc.F90:338-416), complex Hermitian */
+int orc_stc_fwd_z(int ni, int nb, const double *a, int lda, const double *b, double *aii,
+                  double *bi, double *aschur, double *bschur);
+/* H(curl) shape functions per element node (26: vertices, edges, faces) */
+int orc_node_nshapeE(const int32_t *norder, int32_t *nsh);
+/* celem_systemI H(curl) branch with the two EHtrc components + compression;
+ * bcflag bit 0 = E known, bit 1 = H known.  Returns nrdofc. */
+int orc_celem_compress_z(const int32_t *norder, const int32_t *bcflag, const double *aii,
+                         const double *bi, const double *zdofd, int32_t *nextract,
+                         double *zbload, double *zastif, int32_t *ndofm);
+/* batch pass elem_maxwell -> stc_fwd_herm -> compression (OpenMP) */
+int orc_dpg_pass(int nelem, const int32_t *norder, const int32_t *nori_edge,
+                 const int32_t *nori_face, const int32_t *bcflag, const int32_t *imp_mask,
+                 const double *xvert, const double *eps, const orc_maxw_params *prm, int nthreads,
+                 const int64_t *elem_nnz, const int64_t *lcon_off, const int64_t *schur_off,
+                 const int64_t *bub_off, double *zastif, double *zbload, double *aschur,
+                 double *bschur);
+
 #ifdef __cplusplus
 }
 #endif

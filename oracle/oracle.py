@@ -26,8 +26,10 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 
 def build(force: bool = False) -> str:
     """Compile liborc.so with the Makefile beside this file."""
-    src = os.path.join(_HERE, "hp3d_oracle.c")
-    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < os.path.getmtime(src):
+    srcs = [os.path.join(_HERE, f) for f in ("hp3d_oracle.c", "hp3d_oracle_dpg.c",
+                                             "hp3d_oracle.h", "hp3d_oracle_int.h")]
+    newest = max(os.path.getmtime(f) for f in srcs)
+    if force or not os.path.exists(_LIB) or os.path.getmtime(_LIB) < newest:
         subprocess.run(["make", "-C", _HERE, "-B", "liborc.so"], check=True,
                        stdout=subprocess.DEVNULL)
     return _LIB
@@ -68,8 +70,45 @@ def lib():
                                        _f64p, _f64p, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, _i64p, _i64p, _i64p,
                                        _i64p, _f64p, _f64p, _f64p, _f64p]
+        L.orc_nrdofE_hexa.argtypes = [_i32p]
+        L.orc_shape3DE_hexa.argtypes = [_f64p, _i32p, _i32p, _i32p, _f64p, _f64p]
+        L.orc_shape3DQ_hexa.argtypes = [_f64p, _i32p, _f64p]
+        L.orc_shape3EE_hexa.argtypes = [_f64p, ctypes.c_int, _f64p, _f64p]
+        L.orc_set_2D_int_quad.argtypes = [_i32p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                          _f64p, _f64p]
+        L.orc_maxw_exact.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, ctypes.c_double, _f64p,
+                                     _f64p, _f64p, _f64p]
+        L.orc_maxw_exact.restype = None
+        L.orc_dpg_sizes.argtypes = [_i32p, ctypes.c_int, _i32p]
+        L.orc_dpg_maxwell_elem.argtypes = [_i32p, _i32p, _i32p, _f64p, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_int32,
+                                           ctypes.POINTER(MaxwParams), _f64p, _f64p]
+        L.orc_stc_fwd_z.argtypes = [ctypes.c_int, ctypes.c_int, _f64p, ctypes.c_int, _f64p,
+                                    _f64p, _f64p, _f64p, _f64p]
+        L.orc_node_nshapeE.argtypes = [_i32p, _i32p]
+        L.orc_celem_compress_z.argtypes = [_i32p, _i32p, _f64p, _f64p, _f64p, _i32p, _f64p,
+                                           _f64p, _i32p]
+        L.orc_dpg_pass.argtypes = [ctypes.c_int, _i32p, _i32p, _i32p, _i32p, _i32p, _f64p,
+                                   _f64p, ctypes.POINTER(MaxwParams), ctypes.c_int, _i64p,
+                                   _i64p, _i64p, _i64p, _f64p, _f64p, _f64p, _f64p]
         _lib = L
     return _lib
+
+
+class MaxwParams(ctypes.Structure):
+    """orc_maxw_params: OMEGA, MU, EPSILON, GAMMA, ALPHA_NORM, IBCFLAG,
+    NORD_ADD, ISOL, ICOMP_EXACT (defaults of set_environment.F90)."""
+    _fields_ = [("omega", ctypes.c_double), ("mu", ctypes.c_double),
+                ("epsilon", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("ibcflag", ctypes.c_int32),
+                ("nord_add", ctypes.c_int32), ("isol", ctypes.c_int32),
+                ("icomp", ctypes.c_int32)]
+
+
+def maxw_params(omega=2 * np.pi, mu=1.0, epsilon=1.0, gamma=1.0, alpha=1.0, ibcflag=0,
+                nord_add=1, isol=1, icomp=1):
+    return MaxwParams(omega, mu, epsilon, gamma, alpha, ibcflag, nord_add, isol, icomp)
 
 
 def _p(a, t):
@@ -286,3 +325,100 @@ def element_pass(mesh, isol=10, integration=0, stc_method=0, nthreads=0,
     return dict(rc=rc, zastif=zastif, zbload=zbload, aschur=aschur, bschur=bschur,
                 elem_nnz=elem_nnz, lcon_off=lcon_off, schur_off=schur_off, bub_off=bub_off,
                 nrdofc=nrdofc, nb=nb, ni=ni)
+
+
+# --------------------------------------------------------------------------
+# ultraweak DPG Maxwell (hexahedra)
+# --------------------------------------------------------------------------
+def _z(a):
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+def shapeE_hexa(xi, norder, nori_edge=None, nori_face=None):
+    ne = _i32(np.zeros(12) if nori_edge is None else nori_edge)
+    nf = _i32(np.zeros(6) if nori_face is None else nori_face)
+    s = np.zeros((800, 3)); c = np.zeros((800, 3))
+    n = lib().orc_shape3DE_hexa(_p(_f64(xi), _f64p), _p(_i32(norder), _i32p), _p(ne, _i32p),
+                                _p(nf, _i32p), _p(s, _f64p), _p(c, _f64p))
+    return s[:n].copy(), c[:n].copy()
+
+
+def shapeQ_hexa(xi, norder):
+    q = np.zeros(512)
+    n = lib().orc_shape3DQ_hexa(_p(_f64(xi), _f64p), _p(_i32(norder), _i32p), _p(q, _f64p))
+    return q[:n].copy()
+
+
+def shapeEE_hexa(xi, nordP):
+    s = np.zeros((800, 3)); c = np.zeros((800, 3))
+    n = lib().orc_shape3EE_hexa(_p(_f64(xi), _f64p), int(nordP), _p(s, _f64p), _p(c, _f64p))
+    return s[:n].copy(), c[:n].copy()
+
+
+def quad_face(norderf, nori=0, integration=1, maxp=7):
+    t = np.zeros((100, 2)); w = np.zeros(100)
+    n = lib().orc_set_2D_int_quad(_p(_i32(norderf), _i32p), int(nori), integration, maxp,
+                                  _p(t, _f64p), _p(w, _f64p))
+    return t[:n].copy(), w[:n].copy()
+
+
+def maxw_exact(x, prm, eps=1.0 + 0j):
+    E = np.zeros(6); H = np.zeros(6); J = np.zeros(6)
+    lib().orc_maxw_exact(prm.isol, prm.icomp, prm.omega, prm.mu, prm.epsilon * eps.real,
+                         prm.epsilon * eps.imag, _p(_f64(x), _f64p), _p(E, _f64p),
+                         _p(H, _f64p), _p(J, _f64p))
+    return E.view(np.complex128), H.view(np.complex128), J.view(np.complex128)
+
+
+def dpg_sizes(norder, nord_add=1):
+    sz = np.zeros(5, dtype=np.int32)
+    lib().orc_dpg_sizes(_p(_i32(norder), _i32p), nord_add, _p(sz, _i32p))
+    return dict(nEi=int(sz[0]), nQ=int(sz[1]), nEE=int(sz[2]), ntest=int(sz[3]),
+                ntrial=int(sz[4]))
+
+
+def dpg_elem(norder, nori_edge, nori_face, xvert, eps=1.0 + 0j, imp_mask=0, prm=None):
+    """DPG element matrix (NrTrial x NrTrial, complex) and load."""
+    prm = maxw_params() if prm is None else prm
+    n = dpg_sizes(norder, prm.nord_add)["ntrial"]
+    A = np.zeros((n, n), dtype=np.complex128, order="F"); b = np.zeros(n, dtype=np.complex128)
+    xv = _f64(np.asarray(xvert)[:8])
+    rc = lib().orc_dpg_maxwell_elem(_p(_i32(norder), _i32p), _p(_i32(nori_edge), _i32p),
+                                    _p(_i32(nori_face), _i32p), _p(xv, _f64p), eps.real,
+                                    eps.imag, int(imp_mask), ctypes.byref(prm),
+                                    A.ctypes.data_as(_f64p), b.ctypes.data_as(_f64p))
+    return A, b, rc
+
+
+def stc_fwd_z(A, b, nb):
+    n = A.shape[0]
+    ni = n - nb
+    Af = np.asfortranarray(A, dtype=np.complex128)
+    aii = np.zeros((ni, ni), dtype=np.complex128, order="F"); bi = np.zeros(ni, np.complex128)
+    asch = np.zeros((nb, ni), dtype=np.complex128, order="F"); bsch = np.zeros(nb, np.complex128)
+    rc = lib().orc_stc_fwd_z(ni, nb, Af.ctypes.data_as(_f64p), n, _z(b).ctypes.data_as(_f64p),
+                             aii.ctypes.data_as(_f64p), bi.ctypes.data_as(_f64p),
+                             asch.ctypes.data_as(_f64p), bsch.ctypes.data_as(_f64p))
+    return aii, bi, asch, bsch, rc
+
+
+def node_nshapeE(norder):
+    ns = np.zeros(26, dtype=np.int32)
+    lib().orc_node_nshapeE(_p(_i32(norder), _i32p), _p(ns, _i32p))
+    return ns
+
+
+def celem_compress_z(norder, bcflag, aii, bi, zdofd=None):
+    ni = aii.shape[0]
+    a = np.asfortranarray(aii, dtype=np.complex128)
+    bc = _i32(np.pad(np.asarray(bcflag), (0, 26 - len(bcflag))))
+    nx = np.zeros(max(ni, 1), dtype=np.int32)
+    zb = np.zeros(max(ni, 1), np.complex128); zs = np.zeros(max(ni * ni, 1), np.complex128)
+    ndofm = np.zeros(26, dtype=np.int32)
+    zd = None if zdofd is None else _z(zdofd)
+    nc = lib().orc_celem_compress_z(_p(_i32(norder), _i32p), _p(bc, _i32p),
+                                    a.ctypes.data_as(_f64p), _z(bi).ctypes.data_as(_f64p),
+                                    None if zd is None else zd.ctypes.data_as(_f64p),
+                                    _p(nx, _i32p), zb.ctypes.data_as(_f64p),
+                                    zs.ctypes.data_as(_f64p), _p(ndofm, _i32p))
+    return nx[:nc].copy(), zb[:nc].copy(), zs[: nc * nc].reshape(nc, nc).copy(), ndofm

@@ -107,3 +107,27 @@ def test_pipelined_download_with_several_bins_falls_back():
 def test_download_chunks_out_of_range_is_rejected():
     with pytest.raises(H.HP3DGError):
         H.ElementPass(H.MIXED, download_chunks=9)
+
+
+@pytest.mark.parametrize("prec,chunks,expect", [
+    # orient, geom, load, D scale, D digits, contraction, Cholesky+inverse,
+    # K_bi digits, tensor-core condensation, compression; 7 index-map kernels
+    (H.MIXED, 0, 10 + 7),
+    (H.MIXED, 3, 3 * 10 + 7),
+    # orient, geom, load, FP64 contraction, FP64 condensation; index maps
+    (H.FP64, 0, 5 + 7),
+])
+def test_pass_stats_counts_graph_kernels(prec, chunks, expect):
+    m = M.structured_hexa(7, 3, perturb=0.1, seed=2)
+    ep = H.ElementPass(prec, isol=10, download_chunks=chunks)
+    ep.submit(m)
+    assert ep.pass_stats()[0] == -1          # nothing captured yet
+    ep.run(); ep.download()
+    k, f = ep.pass_stats()
+    assert k == expect
+    n, nint, ne = 64, 4 ** 3, 343             # p = 3, INTEGRATION = 0: 4^3 points
+    if prec == H.MIXED:
+        assert f == pytest.approx(ne * ep.ozaki_pairs() * 2 * 6 * nint * n * (n + 1) / 2)
+    else:
+        assert f == pytest.approx(ne * n * (n + 1) * 3 * nint)
+    ep.close()
