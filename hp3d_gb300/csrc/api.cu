@@ -63,6 +63,20 @@ const double GW[10][10] = {
      .2692667193099963550912269, .2190863625159820439955349, .1494513491505805931457763,
      .0666713443086881375935688}};
 
+}  // namespace
+
+// the rule with n points on [0,1] (gauss_quadrature.F90:749-750)
+int hp3dg::gauss_rule01(int n, double* x, double* w) {
+  if (n < 1 || n > 10) return -1;
+  for (int i = 0; i < n; ++i) {
+    x[i] = 0.5 * (1.0 + GX[n - 1][i]);
+    w[i] = 0.5 * GW[n - 1][i];
+  }
+  return n;
+}
+
+namespace {
+
 // set_3Dint_aux BRICK branch (set_3D_int.F90:155-245) on local orders.
 int hexa_quadrature(const int* nl, int integration, std::vector<double>& xi,
                     std::vector<double>& w) {

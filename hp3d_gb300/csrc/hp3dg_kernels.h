@@ -11,6 +11,9 @@ namespace hp3dg {
 // valid when a later launch of the same kernel needs less.
 cudaError_t raise_smem_limit(const void* func, size_t bytes);
 
+// 1D Gauss-Legendre rule of the reference's tables on [0,1] (n <= 10)
+int gauss_rule01(int n, double* x, double* w);
+
 // element types as in the C ABI (HP3DG_HEXA / HP3DG_PRISM / HP3DG_TET)
 constexpr int ETYPE_HEXA = 1, ETYPE_PRISM = 2, ETYPE_TET = 3;
 
@@ -132,5 +135,43 @@ int ozaki_pairs(const OzakiPlan& plan);
 int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
                       double* d_PK, int* d_flag, cudaStream_t st);
+
+// ultraweak DPG Maxwell on hexahedra -- k_dpg.cu
+constexpr int DPG_GV = 36;  // doubles per volume point: D1(6) D2(6) wJ^-1(9) wJ/detJ(9) g(6)
+struct DpgDims {
+  int p, q;            // trial order, test order p + NORD_ADD
+  int nEE, nEi, nQ;    // test functions per field, trace functions, L2 functions
+  int nr;              // trial dof: 2 nEi + 6 nQ
+  int nv, nfp, nip;    // volume points, face points per face (DPG rule), impedance points per face
+  double dxidt[6][3][2];  // face parametrisations (face_param)
+  double nsign[6];        // outward normal signs (Nsign_param)
+};
+struct DpgPhys {
+  double omega, mu, epsilon, gamma, alpha;
+  int ibcflag, isol, icomp;
+};
+struct DpgTables {
+  double *vs = nullptr, *vc = nullptr, *vq = nullptr;     // volume: test values, curls, L2
+  double *fs = nullptr, *fscratch = nullptr, *ft = nullptr;  // faces: test values, traces
+  double* it = nullptr;                                   // impedance points: traces
+};
+struct DpgWork {
+  const double *xiV, *wV, *xiF, *wF, *xiI, *wI;
+  double *gV, *gF, *gI;            // per element point data
+  double *MFF, *MCC, *MFC;         // real Gram parts (MFC per bin)
+  double *P, *R, *T, *load;        // real coupling blocks, complex load
+  double *G, *S, *Z;               // complex: Gram, [B|l] -> X, DPG matrix (nr+1)^2
+};
+void launch_dpg_tables(const DpgDims& d, const double* xiV, const double* wV, const double* xiF,
+                       const double* xiI, const DpgTables& t, double* mfc, cudaStream_t st);
+// stage 0: geometry, real contractions, assembly of G and [B|l];
+// 1: Cholesky of G, forward solve, Z = X^H X, impedance penalty;
+// 2: condensation of the L2 fields and compression
+void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
+                      const DpgTables& t, const DpgWork& w, const double* xvert, const double* eps,
+                      const int* imp_mask, const uint32_t* perm, const int* nextract,
+                      const int64_t* lcon_off, const int64_t* elem_nnz, const int64_t* schur_off,
+                      const int64_t* bub_off, double* zastif, double* zbload, double* aschur,
+                      double* bschur, int* flags, cudaStream_t st);
 
 }  // namespace hp3dg

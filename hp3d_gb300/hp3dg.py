@@ -55,7 +55,11 @@ EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit", "hp3dg
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
            "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_output_sizes", "hp3dg_device_outputs",
-           "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_pass_stats", "hp3dg_last_bad_element", "hp3dg_batch_end", "hp3dg_strerror"]
+           "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_pass_stats", "hp3dg_last_bad_element",
+           "hp3dg_dpg_begin", "hp3dg_dpg_submit", "hp3dg_dpg_run", "hp3dg_dpg_sync",
+           "hp3dg_dpg_download", "hp3dg_dpg_sizes", "hp3dg_dpg_get_elem",
+           "hp3dg_dpg_get_condensed", "hp3dg_dpg_get_schur", "hp3dg_dpg_index_map",
+           "hp3dg_dpg_phase_times", "hp3dg_dpg_last_bad_element", "hp3dg_dpg_end", "hp3dg_batch_end", "hp3dg_strerror"]
 
 
 def lib():
@@ -90,6 +94,20 @@ def lib():
         L.hp3dg_batch_end.restype = None
         L.hp3dg_strerror.argtypes = [ctypes.c_int]
         L.hp3dg_strerror.restype = ctypes.c_char_p
+        L.hp3dg_dpg_begin.argtypes = [ctypes.POINTER(DpgOpts), ctypes.POINTER(_vp)]
+        L.hp3dg_dpg_submit.argtypes = [_vp, ctypes.c_int32, _vp, _f64p, _f64p, ctypes.c_int32]
+        for f in (L.hp3dg_dpg_run, L.hp3dg_dpg_sync, L.hp3dg_dpg_download):
+            f.argtypes = [_vp]
+        L.hp3dg_dpg_sizes.argtypes = [_vp, _i32p, _i32p, _i32p]
+        L.hp3dg_dpg_get_elem.argtypes = [_vp, ctypes.c_int32, _f64p, ctypes.c_int32, _f64p]
+        L.hp3dg_dpg_get_condensed.argtypes = [_vp, ctypes.c_int32, _f64p, _f64p, _i32p]
+        L.hp3dg_dpg_get_schur.argtypes = [_vp, ctypes.c_int32, _f64p, _f64p, _i32p, _i32p]
+        L.hp3dg_dpg_index_map.argtypes = [_vp, _i32p, _i64p, _i64p, _i32p, _i64p]
+        L.hp3dg_dpg_phase_times.argtypes = [_vp, _f32p, ctypes.c_int32]
+        L.hp3dg_dpg_last_bad_element.argtypes = [_vp]
+        L.hp3dg_dpg_last_bad_element.restype = ctypes.c_int32
+        L.hp3dg_dpg_end.argtypes = [_vp]
+        L.hp3dg_dpg_end.restype = None
         _lib = L
     return _lib
 
@@ -255,6 +273,121 @@ class ElementPass:
     def close(self):
         if self.ctx:
             self.L.hp3dg_batch_end(self.ctx)
+            self.ctx = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --------------------------------------------------------------------------
+# ultraweak DPG Maxwell (hexahedra), hp3dg_dpg_*
+# --------------------------------------------------------------------------
+class DpgOpts(ctypes.Structure):
+    _fields_ = [("omega", ctypes.c_double), ("mu", ctypes.c_double),
+                ("epsilon", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("alpha", ctypes.c_double), ("ibcflag", ctypes.c_int32),
+                ("nord_add", ctypes.c_int32), ("isol", ctypes.c_int32),
+                ("icomp", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("timing", ctypes.c_int32), ("keep_elem", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
+
+
+class DPGPass:
+    """One batch of the DPG Maxwell element pass (a context of the C ABI)."""
+
+    def __init__(self, omega=2 * np.pi, mu=1.0, epsilon=1.0, gamma=1.0, alpha=1.0, ibcflag=0,
+                 nord_add=1, isol=1, icomp=1, device=0, timing=False, keep_elem=False):
+        self.L = lib()
+        o = DpgOpts(omega, mu, epsilon, gamma, alpha, ibcflag, nord_add, isol, icomp, device,
+                    int(timing), int(keep_elem))
+        self.ctx = _vp()
+        self._check(self.L.hp3dg_dpg_begin(ctypes.byref(o), ctypes.byref(self.ctx)), "begin")
+        self.nel = 0
+
+    def _check(self, rc, what):
+        if rc != 0:
+            bad = self.L.hp3dg_dpg_last_bad_element(self.ctx) if self.ctx else -1
+            raise HP3DGError(rc, f"{what}: {self.L.hp3dg_strerror(rc).decode()}", bad)
+
+    def submit(self, mesh, eps, bcflag):
+        """mesh: a hexa mesh dict; eps: complex relative permittivity per
+        element; bcflag: (n_elem, 26) DPG node flags (bit 0 E known, bit 1 H
+        known, bit 2 impedance face)."""
+        self.mesh = mesh
+        d = mesh_descriptors(mesh)
+        d["bcflag"] = np.asarray(bcflag, dtype=np.int32)
+        self.desc = d
+        self.xvert = np.ascontiguousarray(np.asarray(mesh["xvert"])[:, :8], dtype=np.float64)
+        self.eps = np.ascontiguousarray(np.asarray(eps, dtype=np.complex128))
+        self.nel = mesh["nelem"]
+        self._check(self.L.hp3dg_dpg_submit(self.ctx, self.nel, self.desc.ctypes.data_as(_vp),
+                                            _p(self.xvert, _f64p),
+                                            self.eps.ctypes.data_as(_f64p),
+                                            int(mesh["nnodes"])), "submit")
+
+    def run(self):
+        self._check(self.L.hp3dg_dpg_run(self.ctx), "run")
+
+    def sync(self):
+        self._check(self.L.hp3dg_dpg_sync(self.ctx), "sync")
+
+    def download(self):
+        self._check(self.L.hp3dg_dpg_download(self.ctx), "download")
+
+    def sizes(self):
+        v = [ctypes.c_int32() for _ in range(3)]
+        self._check(self.L.hp3dg_dpg_sizes(self.ctx, *[ctypes.byref(x) for x in v]), "sizes")
+        return [x.value for x in v]
+
+    def elem(self, e):
+        n = self.sizes()[0]
+        a = np.zeros((n, n), dtype=np.complex128, order="F"); b = np.zeros(n, np.complex128)
+        self._check(self.L.hp3dg_dpg_get_elem(self.ctx, e, a.ctypes.data_as(_f64p), n,
+                                              b.ctypes.data_as(_f64p)), "elem")
+        return a, b
+
+    def condensed(self, e):
+        nc = ctypes.c_int32()
+        self._check(self.L.hp3dg_dpg_get_condensed(self.ctx, e, None, None, ctypes.byref(nc)),
+                    "cond")
+        n = nc.value
+        zb = np.zeros(max(n, 1), np.complex128); zs = np.zeros(max(n * n, 1), np.complex128)
+        self._check(self.L.hp3dg_dpg_get_condensed(self.ctx, e, zb.ctypes.data_as(_f64p),
+                                                   zs.ctypes.data_as(_f64p),
+                                                   ctypes.byref(nc)), "cond")
+        return zb[:n], zs[: n * n].reshape(n, n)
+
+    def schur(self, e):
+        _, ni, nb = self.sizes()
+        a = np.zeros(nb * ni, np.complex128); b = np.zeros(nb, np.complex128)
+        self._check(self.L.hp3dg_dpg_get_schur(self.ctx, e, a.ctypes.data_as(_f64p),
+                                               b.ctypes.data_as(_f64p), None, None), "schur")
+        return a.reshape(ni, nb).T.copy(), b
+
+    def index_map(self):
+        lo = np.zeros(self.nel + 1, dtype=np.int64)
+        en = np.zeros(self.nel + 1, dtype=np.int64)
+        nr = ctypes.c_int64()
+        self._check(self.L.hp3dg_dpg_index_map(self.ctx, None, None, _p(lo, _i64p), None,
+                                               ctypes.byref(nr)), "index_map")
+        nf = np.zeros(self.mesh["nnodes"], dtype=np.int32)
+        lc = np.zeros(max(int(lo[-1]), 1), dtype=np.int32)
+        self._check(self.L.hp3dg_dpg_index_map(self.ctx, _p(nf, _i32p), _p(en, _i64p),
+                                               _p(lo, _i64p), _p(lc, _i32p), ctypes.byref(nr)),
+                    "index_map")
+        return nr.value, nf, lc[: lo[-1]], lo, en
+
+    def phase_times(self):
+        t = (ctypes.c_float * 5)()
+        self._check(self.L.hp3dg_dpg_phase_times(self.ctx, t, 5), "times")
+        return list(t)
+
+    def close(self):
+        if self.ctx:
+            self.L.hp3dg_dpg_end(self.ctx)
             self.ctx = _vp()
 
     def __del__(self):

@@ -270,6 +270,69 @@ void hp3dg_batch_end(hp3dg_ctx *ctx);
 /* Message for a status code. */
 const char *hp3dg_strerror(int status);
 
+/* ------------------------------------------------------------------------ */
+/* Ultraweak DPG Maxwell on hexahedra (problems/MAXWELL/ULTRAWEAK_DPG).       */
+/* Replaces elem (elem/elem.F90:15 -> elem_maxwell / elem_opt, complex) with  */
+/* the automatic static condensation of the L2 fields (stc_fwd_herm,          */
+/* HERM_STC) and celem_systemI's compression for the EHtrc attribute, over    */
+/* a batch of hexahedra of one isotropic trial order p (1..5, test order      */
+/* p + NORD_ADD).  Complex arrays are interleaved (re, im) doubles, the       */
+/* layout of Fortran complex(8).                                              */
+/* ------------------------------------------------------------------------ */
+typedef struct hp3dg_dpg_ctx hp3dg_dpg_ctx;
+
+typedef struct hp3dg_dpg_opts {
+  double omega;      /* OMEGA (commonParam.F90; default 2 pi) */
+  double mu;         /* MU */
+  double epsilon;    /* EPSILON (times the element's relative permittivity) */
+  double gamma;      /* GAMMA, impedance constant */
+  double alpha;      /* ALPHA_NORM of the scaled adjoint graph test norm */
+  int32_t ibcflag;   /* IBCFLAG: 0 Dirichlet only, 2 impedance by penalty */
+  int32_t nord_add;  /* NORD_ADD: test enrichment (1) */
+  int32_t isol;      /* source: mfd_solutions case 0 (none), 1 (sin), 2 (polynomial) */
+  int32_t icomp;     /* ICOMP_EXACT: component (1..3) of E in the manufactured solution */
+  int32_t device;
+  int32_t timing;    /* record phase times */
+  int32_t keep_elem; /* keep the uncondensed DPG element matrices (hp3dg_dpg_get_elem) */
+  int32_t reserved[5];
+} hp3dg_dpg_opts;
+
+int hp3dg_dpg_begin(const hp3dg_dpg_opts *opts, hp3dg_dpg_ctx **ctx);
+/* desc: as for hp3dg_batch_submit with etype HP3DG_HEXA and isotropic order p
+ * on every edge, face and the interior.  bcflag per node: bit 0 = the E
+ * trace is known (perfect conductor, homogeneous), bit 1 = the H trace is
+ * known; on a face node bit 2 = the face lies on the impedance boundary
+ * (ibc = 2).  xvert: 3 x 8 vertex coordinates per element (trilinear
+ * geometry).  eps: complex relative permittivity per element (the
+ * permittivity tensor is EPSILON * eps * I). */
+int hp3dg_dpg_submit(hp3dg_dpg_ctx *ctx, int32_t n_elem, const hp3dg_elem_desc *desc,
+                     const double *xvert, const double *eps, int32_t nnodes);
+int hp3dg_dpg_run(hp3dg_dpg_ctx *ctx);
+int hp3dg_dpg_sync(hp3dg_dpg_ctx *ctx);
+int hp3dg_dpg_download(hp3dg_dpg_ctx *ctx);
+/* Sizes of one element: trial dof (2 nEi + 6 nQ), interface (2 nEi), L2 (6 nQ). */
+int hp3dg_dpg_sizes(const hp3dg_dpg_ctx *ctx, int32_t *ntrial, int32_t *ni, int32_t *nb);
+/* The DPG element matrix B^H G^-1 B (ld x ntrial, column-major, complex) and
+ * load before condensation, rows/columns [E,H traces per trace function |
+ * six L2 components per L2 function] (needs keep_elem). */
+int hp3dg_dpg_get_elem(const hp3dg_dpg_ctx *ctx, int32_t iel, double *zaloc, int32_t ld,
+                       double *zbloc);
+/* Condensed and compressed element system (row-major, complex), as
+ * celem_systemI returns it to the MUMPS driver. */
+int hp3dg_dpg_get_condensed(const hp3dg_dpg_ctx *ctx, int32_t iel, double *zbload,
+                            double *zastif, int32_t *nrdofc);
+/* ASchur (nb x ni, column-major) and BSchur (nb), complex. */
+int hp3dg_dpg_get_schur(const hp3dg_dpg_ctx *ctx, int32_t iel, double *aschur, double *bschur,
+                        int32_t *nb, int32_t *ni);
+/* NFIRST_DOF / LCON of the EHtrc unknowns, as hp3dg_index_map. */
+int hp3dg_dpg_index_map(const hp3dg_dpg_ctx *ctx, int32_t *nfirst, int64_t *elem_nnz,
+                        int64_t *lcon_off, int32_t *lcon, int64_t *nrdof);
+/* [0] geometry + contractions + assembly, [1] Cholesky + solve + X^H X,
+ * [2] condensation + compression, [3] index maps, [4] whole pass (ms). */
+int hp3dg_dpg_phase_times(const hp3dg_dpg_ctx *ctx, float *ms, int32_t n);
+int32_t hp3dg_dpg_last_bad_element(const hp3dg_dpg_ctx *ctx);
+void hp3dg_dpg_end(hp3dg_dpg_ctx *ctx);
+
 #ifdef __cplusplus
 }
 #endif
