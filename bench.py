@@ -181,6 +181,154 @@ def config_dict(args, world, mesh):
             "l2": "working set per step > L2 (condensed outputs 3.7 GB), no flush needed"}
 
 
+DPG_METRIC = "DPG Maxwell elements/s (complex FP64, trial p=3, test p=4, condensed)"
+
+
+def dpg_flops(ntest, ntrial, ni, nb):
+    """Dense algebra of the DPG element per element (real FLOPs): Cholesky of
+    the Gram matrix (ZPPTRF), the triangular solve of [B|l] (ZTPTRS), X^H X
+    (ZHERK), then the condensation of the L2 fields (Cholesky, two solves,
+    Schur update)."""
+    n1 = ntrial + 1
+    f = 4.0 / 3.0 * ntest ** 3 + 4.0 * ntest ** 2 * n1 + 4.0 * n1 * (n1 + 1) * ntest
+    f += 4.0 / 3.0 * nb ** 3 + 8.0 * nb ** 2 * (ni + 1) + 4.0 * ni * ni * nb
+    return f
+
+
+def run_dpg(args, rank, world):
+    """Ultraweak DPG Maxwell on 10^3 hexahedra of the unit cube: trial p = 3,
+    test p + 1, omega = 2 pi, eps_r = U[1,4] (1 - i tan d), tan d = U[0, 0.1]
+    per element, impedance on the wall x = 1 (IBCFLAG = 2), perfect conductor
+    elsewhere, sin source (mfd_solutions case 1); interior vertices perturbed
+    by U(-0.1h, 0.1h).  Seeded synthetic mesh."""
+    from hp3d_gb300 import mesh as M
+    from oracle import oracle as O
+    n = 10 if args.n == 24 else args.n
+    mesh = M.structured_hexa(n, 3, perturb=0.1, seed=4321 + rank)
+    rng = np.random.default_rng(99 + rank)
+    ne = mesh["nelem"]
+    eps = rng.uniform(1, 4, ne) * (1 - 1j * rng.uniform(0, 0.1, ne))
+    flags = M.dpg_boundary_flags(mesh, ((0, 1),))
+    imp = np.zeros(ne, np.int32)
+    for f in range(6):
+        imp |= ((flags[:, 20 + f] >> 2) & 1) << f
+    prm = O.maxw_params(isol=1, ibcflag=2)
+    cfg = {"workload": f"ultraweak_dpg_maxwell_hexa_{n}^3_p3_impedance", "elements_per_gpu": ne,
+           "p": 3, "test_order": 4, "quadrature_points": 125, "omega": "2 pi",
+           "eps_r": "U[1,4](1 - i U[0,0.1])", "precision": "fp64",
+           "parallelism": f"replicas{world}" if world > 1 else "single",
+           "l2": "working set per step > L2 (Gram matrices 5.8 GB), no flush needed"}
+    s = O.dpg_sizes([3] * 12 + [33] * 6 + [333])
+    fl_el = dpg_flops(s["ntest"], s["ntrial"], 2 * s["nEi"], 6 * s["nQ"])
+
+    def cpu(seconds):
+        cores = os.cpu_count() or 1
+        probe = np.arange(min(cores, ne))
+        t0 = time.perf_counter()
+        O.dpg_pass(mesh, eps, flags & 3, imp, prm, elements=probe, nthreads=cores)
+        dt = max(time.perf_counter() - t0, 1e-3)
+        k = max(1, int(seconds / dt)) * len(probe)
+        sample = np.unique(np.round(np.linspace(0, ne - 1, min(ne, k))).astype(np.int64))
+        t0 = time.perf_counter()
+        r = O.dpg_pass(mesh, eps, flags & 3, imp, prm, elements=sample, nthreads=cores)
+        dt = time.perf_counter() - t0
+        assert r["rc"] == 0
+        return {"value": len(sample) / dt, "unit": "elements/s", "cores": cores, "kind": "port",
+                "sample": f"{len(sample)} of {ne} elements (evenly spread), one pass, {dt:.1f} s, "
+                          f"oracle C restatement of elem_maxwell (ZPPTRF/ZTPTRS/ZHERK) + "
+                          f"stc_fwd_herm + compression, OpenMP"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        vals, cb = [], None
+        sec = min(args.cpu_seconds, 120.0 / max(1, args.warmup + args.steps))
+        for i in range(args.warmup + args.steps):
+            c = cpu(sec)
+            if i >= args.warmup:
+                vals.append(c["value"])
+                cb = c
+        v = statistics.median(vals)
+        print(json.dumps({"impl": "reference", "metric": DPG_METRIC, "value": v,
+                          "unit": "elements/s", "n_gpus": world, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": 1000.0 * ne / v,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "c128", "data": "synthetic", "config": cfg, "cpu_baseline": cb,
+                          "e2e": {"value": v, "unit": "elements/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}), flush=True)
+        return
+
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from hp3d_gb300 import build as B
+    B.build()
+    from hp3d_gb300 import hp3dg as H
+    ep = H.DPGPass(omega=prm.omega, ibcflag=2, isol=1, timing=True, device=local)
+    ep.submit(mesh, eps, flags)
+    for _ in range(args.warmup):
+        ep.run(); ep.sync()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    ph = []
+    for _ in range(args.steps):
+        ep.run(); ep.sync()
+        ph.append(ep.phase_times())
+    clocks = clk.stop()
+    ph = np.array(ph)
+    ms = float(np.median(ph[:, 4]))
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * ne / (ms / 1000.0)
+    # end to end: submit (descriptors, vertices, permittivities), run, download
+    ep.download()
+    ntrial, ni, nb = ep.sizes()
+    nr, _, _, lo, en = ep.index_map()
+    d2h = int(16 * (en[-1] + lo[-1] + ne * (ni * nb + nb)) + 4 * lo[-1])
+    h2d = int(ep.desc.nbytes + ep.xvert.nbytes + ep.eps.nbytes)
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.e2e_steps)):
+        ep.submit(mesh, eps, flags); ep.run(); ep.download()
+    e2e_s = (time.perf_counter() - t0) / max(1, args.e2e_steps)
+    med = np.median(ph, axis=0)
+    t_la = (med[1] + med[2]) / 1000.0
+    hbm, bf16, peak_kind = measured_peaks()
+    achieved = ne * fl_el / t_la / 1e12 if t_la > 0 else None
+    roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+            "frac": achieved / 1.25 if achieved else None, "traffic": None,
+            "kernel": "k_dpg_dpg + k_dpg_condense",
+            "note": "dense DPG algebra (Gram Cholesky, forward solve of [B|l], X^H X, L2-field "
+                    "condensation) per element over the two kernels' time; peak = nominal GB300 "
+                    "FP64 (not in the measured peaks)"}
+    cb = cpu(args.cpu_seconds) if (rank == 0 and not args.no_cpu_baseline) else None
+    line = {"metric": DPG_METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+            "data": "synthetic", "config": cfg,
+            "e2e": {"value": world * ne / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * e2e_s,
+                    "note": "submit (descriptors, vertices, permittivities), run, download of "
+                            "the condensed systems, Schur blocks and LCON"},
+            "roofline": roof, "cpu_baseline": cb, "clocks": clocks,
+            "gpu_launches": 9 * args.steps,
+            "phase_ms": {"geometry_contractions_assembly": float(med[0]),
+                         "gram_cholesky_solve_herk_impedance": float(med[1]),
+                         "condensation_compression": float(med[2]),
+                         "index_maps": float(med[3]), "pass": float(med[4])}}
+    ep.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -188,9 +336,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="hexa", choices=["hexa", "mixed"],
+    ap.add_argument("--workload", default="hexa", choices=["hexa", "mixed", "dpg"],
                     help="hexa: uniform p hexahedra (the metric's mesh); mixed: hp-adaptive "
-                         "hexa/prism/tet mesh")
+                         "hexa/prism/tet mesh; dpg: ultraweak DPG Maxwell, 10^3 hexahedra p=3")
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--p", type=int, default=5)
     ap.add_argument("--integration", type=int, default=1)
@@ -207,6 +355,8 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.workload == "dpg":
+        return run_dpg(args, rank, world)
     if args.impl == "reference":
         return run_reference(args, rank, world)
 

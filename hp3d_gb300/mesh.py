@@ -608,3 +608,30 @@ def mixed_mesh(n, a=0.875, b=0.875, p=None, pmax=6, perturb=0.0, kappa_logrange=
                         et.append(TET); verts.append(v)
                         orders.append((p,) if p else _hp_order(rng, centre, pmax, 1))
     return build_mesh(et, verts, X, coords, n, orders, kappa_logrange, seed, dirichlet)
+
+
+def dpg_boundary_flags(mesh, imp_planes=(), tol=1e-12):
+    """Node flags of the ultraweak DPG Maxwell pass on a hexa mesh of the unit
+    cube: bit 0 (E trace known) on every edge and face node of a perfect
+    conductor wall, bit 2 on the face nodes of impedance walls (ibc = 2).
+    imp_planes: (axis, side) walls with the impedance condition; the other
+    walls are perfect conductors.  An edge shared by both kinds of wall is a
+    conductor edge.  Returns (n_elem, 26) int32."""
+    ne = mesh["nelem"]
+    out = np.zeros((ne, 26), np.int32)
+    edges = [e for e, _ in _HEXA_EDGES]
+    faces = [f for f, _ in _HEXA_FACES]
+
+    def planes(x):
+        return [(a, s) for a in range(3) for s in (0, 1) if abs(x[a] - s) < tol]
+
+    for e in range(ne):
+        xv = np.asarray(mesh["xvert"][e])[:8]
+        pts = [xv[list(q)].mean(0) for q in edges] + [xv[list(q)].mean(0) for q in faces]
+        for k, x in enumerate(pts):
+            pl = planes(x)
+            if any(q not in imp_planes for q in pl):
+                out[e, 8 + k] |= 1
+            elif pl and k >= 12:
+                out[e, 8 + k] |= 4
+    return out

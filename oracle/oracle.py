@@ -422,3 +422,35 @@ def celem_compress_z(norder, bcflag, aii, bi, zdofd=None):
                                     _p(nx, _i32p), zb.ctypes.data_as(_f64p),
                                     zs.ctypes.data_as(_f64p), _p(ndofm, _i32p))
     return nx[:nc].copy(), zb[:nc].copy(), zs[: nc * nc].reshape(nc, nc).copy(), ndofm
+
+
+def dpg_pass(mesh, eps, bcflag, imp_mask, prm, elements=None, nthreads=0):
+    """elem_maxwell -> stc_fwd_herm -> compression over (a subset of) a hexa
+    mesh with OpenMP; returns the oracle's return code and the outputs."""
+    idx = np.arange(mesh["nelem"]) if elements is None else np.asarray(elements)
+    ne = len(idx)
+    no = _i32(mesh["norder"][idx]); ned = _i32(mesh["nori_edge"][idx])
+    nfc = _i32(mesh["nori_face"][idx]); bc = _i32(np.asarray(bcflag)[idx])
+    im = _i32(np.asarray(imp_mask)[idx]); xv = _f64(np.asarray(mesh["xvert"])[idx, :8])
+    ep = _z(np.asarray(eps)[idx])
+    nc = np.zeros(ne, np.int64); s = dpg_sizes(no[0], prm.nord_add)
+    ni, nb = 2 * s["nEi"], 6 * s["nQ"]
+    for j in range(ne):
+        nsh = node_nshapeE(no[j])
+        nc[j] = sum(int(nsh[i]) * (2 - bin(int(bc[j][i]) & 3).count("1")) for i in range(26))
+    elem_nnz = np.concatenate([[0], np.cumsum(nc * nc)]).astype(np.int64)
+    lcon_off = np.concatenate([[0], np.cumsum(nc)]).astype(np.int64)
+    schur_off = (np.arange(ne + 1) * nb * ni).astype(np.int64)
+    bub_off = (np.arange(ne + 1) * nb).astype(np.int64)
+    zs = np.zeros(max(int(elem_nnz[-1]), 1), np.complex128)
+    zb = np.zeros(max(int(lcon_off[-1]), 1), np.complex128)
+    asch = np.zeros(max(int(schur_off[-1]), 1), np.complex128)
+    bsch = np.zeros(max(int(bub_off[-1]), 1), np.complex128)
+    rc = lib().orc_dpg_pass(ne, _p(no, _i32p), _p(ned, _i32p), _p(nfc, _i32p), _p(bc, _i32p),
+                            _p(im, _i32p), _p(xv, _f64p), ep.ctypes.data_as(_f64p),
+                            ctypes.byref(prm), nthreads, _p(elem_nnz, _i64p),
+                            _p(lcon_off, _i64p), _p(schur_off, _i64p), _p(bub_off, _i64p),
+                            zs.ctypes.data_as(_f64p), zb.ctypes.data_as(_f64p),
+                            asch.ctypes.data_as(_f64p), bsch.ctypes.data_as(_f64p))
+    return dict(rc=rc, zastif=zs, zbload=zb, aschur=asch, bschur=bsch, elem_nnz=elem_nnz,
+                lcon_off=lcon_off)

@@ -62,46 +62,14 @@ def rotated_hexa_mesh(n, p, seed=0, grading=1.0, rotate=True):
     return M.build_mesh(et, verts, X, grid, n, orders)
 
 
-_EDGE_V = [e for e, _ in M._HEXA_EDGES]
-_FACE_V = [f for f, _ in M._HEXA_FACES]
-
-
-def node_points(xvert):
-    """Centres of the 26 nodes of a hexa (vertices, edges, faces)."""
-    pts = [xvert[v] for v in range(8)]
-    pts += [xvert[list(e)].mean(0) for e in _EDGE_V]
-    pts += [xvert[list(f)].mean(0) for f in _FACE_V]
-    return np.array(pts)
-
-
-def _planes(x, tol=1e-12):
-    out = []
-    for a in range(3):
-        if abs(x[a]) < tol:
-            out.append((a, 0))
-        if abs(x[a] - 1.0) < tol:
-            out.append((a, 1))
-    return out
-
-
 def boundary_flags(mesh, imp_planes=()):
-    """Per element: bcflag (26 nodes; bit 0 = E trace known: perfect
-    conductor) and the impedance face mask (bit f: face f on an impedance
-    plane).  imp_planes: (axis, side) planes with the impedance condition."""
-    ne = mesh["nelem"]
-    bc = np.zeros((ne, 26), np.int32)
-    imp = np.zeros(ne, np.int32)
-    for e in range(ne):
-        xv = mesh["xvert"][e, :8]
-        pts = node_points(xv)
-        for k in range(8, 26):
-            pl = _planes(pts[k])
-            if any(q not in imp_planes for q in pl):
-                bc[e, k] = 1
-        for f in range(6):
-            pl = _planes(pts[20 + f])
-            if pl and all(q in imp_planes for q in pl):
-                imp[e] |= 1 << f
+    """Per element: bcflag (26 nodes; bit 0 = E trace known) and the impedance
+    face mask, from the library's node flags (hp3d_gb300.mesh)."""
+    fl = M.dpg_boundary_flags(mesh, imp_planes)
+    bc = fl & 3
+    imp = np.zeros(mesh["nelem"], np.int32)
+    for f in range(6):
+        imp |= ((fl[:, 20 + f] >> 2) & 1) << f
     return bc, imp
 
 
