@@ -412,6 +412,17 @@ struct hp3dg_ctx {
   cudaStream_t branch[NBRANCH] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[NBRANCH] = {};
   std::vector<hp3dg_elem_desc> last_desc;  // descriptors of the current batch
+  // constrained approximation: the compression writes a work layout (every
+  // element; constrained elements with all their interface dof), which
+  // k_constrain turns into the final outputs.  Without constraints the work
+  // pointers alias the final ones.
+  bool constrained = false;
+  int node_stride = 26;  // node slots per element of the index maps
+  int* d_wnextract = nullptr;
+  int64_t *d_wlcon_off = nullptr, *d_welem_nnz = nullptr;
+  double *d_zwork = nullptr, *d_bwork = nullptr;
+  ConstrainArgs cargs{};
+  std::vector<void*> cbufs;  // allocations of the constraint data
 };
 
 namespace {
@@ -430,6 +441,16 @@ void free_bin(Bin& b) {
 }
 
 void free_batch(hp3dg_ctx* c) {
+  for (void* p : c->cbufs) cudaFree(p);
+  c->cbufs.clear();
+  if (c->constrained) {
+    c->d_wnextract = nullptr;
+    c->d_wlcon_off = c->d_welem_nnz = nullptr;
+    c->d_zwork = c->d_bwork = nullptr;
+  }
+  c->constrained = false;
+  c->node_stride = 26;
+  c->cargs = ConstrainArgs{};
   if (c->graph) cudaGraphExecDestroy(c->graph);
   c->graph = nullptr;
   c->graph_kernels = -1;
@@ -534,13 +555,22 @@ int hp3dg_set_stream(hp3dg_ctx* c, void* stream) {
 int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
                        const double* xvert, const double* kappa, const double* zdofd,
                        int32_t nnodes) {
+  return hp3dg_batch_submit_constrained(c, nel, desc, xvert, kappa, zdofd, nnodes, nullptr);
+}
+
+int hp3dg_batch_submit_constrained(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
+                                   const double* xvert, const double* kappa,
+                                   const double* zdofd, int32_t nnodes,
+                                   const hp3dg_constraints* cons) {
   if (!c || nel < 0 || (nel > 0 && (!desc || !xvert)) || nnodes < 0) return HP3DG_ERR_ARG;
+  if (cons && cons->n == 0) cons = nullptr;
   cudaSetDevice(c->device);
   // Resubmit of the same mesh (identical descriptors, node count and
   // Dirichlet layout) with new geometry / coefficients / Dirichlet values:
   // keep every buffer, the bin tables, the tensor-core operand digits, the
   // captured graph and the pinned host buffers; upload the numeric inputs.
-  if (c->submitted && nel == c->nel && nnodes == c->nnodes && (zdofd != nullptr) == c->have_zdofd &&
+  if (!cons && !c->constrained && c->submitted && nel == c->nel && nnodes == c->nnodes &&
+      (zdofd != nullptr) == c->have_zdofd &&
       nel > 0 && c->last_desc.size() == (size_t)nel &&
       std::memcmp(c->last_desc.data(), desc, sizeof(hp3dg_elem_desc) * (size_t)nel) == 0) {
     cudaStream_t st = c->stream;
@@ -627,6 +657,114 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   }
   c->dof_off.assign(nel + 1, 0);
   for (int e = 0; e < nel; ++e) c->dof_off[e + 1] = c->dof_off[e] + c->n_e[e];
+  // ---- constrained approximation ----
+  std::vector<int> wnextract, cidx, cnmod, cgptr, cgk;
+  std::vector<int64_t> wlcon_off, welem_nnz, cgptr_off, caux_off, cmdof_off;
+  std::vector<double> cgv, cmzd;
+  std::vector<uint8_t> cmdir;
+  if (cons) {
+    const int nc_el = cons->n;
+    if (!cons->iel || !cons->node_off || !cons->nodm || !cons->ndof || !cons->bcflag ||
+        !cons->coef_off || !cons->coef_k || !cons->coef_l || !cons->coef_v || nc_el < 0)
+      { free_batch(c); return HP3DG_ERR_ARG; }
+    cidx.assign(nel, -1);
+    int stride = 26;
+    for (int j = 0; j < nc_el; ++j) {
+      const int e = cons->iel[j];
+      if (e < 0 || e >= nel || (j > 0 && e <= cons->iel[j - 1])) { free_batch(c); return HP3DG_ERR_ARG; }
+      cidx[e] = j;
+      const int64_t nn = cons->node_off[j + 1] - cons->node_off[j];
+      if (nn <= 0 || nn > 4096) { free_batch(c); return HP3DG_ERR_ARG; }
+      stride = std::max(stride, (int)nn);
+    }
+    // final extraction, offsets and index-map node lists
+    std::vector<int> nodes2((size_t)nel * stride, -1), ndofm2((size_t)nel * stride, 0);
+    std::vector<int> fnext;
+    std::vector<int64_t> flcon(nel + 1, 0), fnnz(nel + 1, 0);
+    wlcon_off.assign(nel + 1, 0);
+    welem_nnz.assign(nel + 1, 0);
+    cgptr_off.assign(nc_el, 0);
+    caux_off.assign(nc_el + 1, 0);
+    cmdof_off.assign(nc_el + 1, 0);
+    cnmod.assign(nc_el, 0);
+    int64_t pos = 0;  // running position in c->nextract (conforming extraction)
+    for (int e = 0; e < nel; ++e) {
+      const int j = cidx[e];
+      const int ni = c->ni_e[e];
+      const int nconf = (int)(c->lcon_off[e + 1] - c->lcon_off[e]);
+      int nrdofc;
+      if (j < 0) {
+        for (int i = 0; i < 26; ++i) {
+          nodes2[(size_t)e * stride + i] = nodes[(size_t)e * 26 + i];
+          ndofm2[(size_t)e * stride + i] = ndofm[(size_t)e * 26 + i];
+        }
+        for (int q = 0; q < nconf; ++q) {
+          fnext.push_back(c->nextract[pos + q]);
+          wnextract.push_back(c->nextract[pos + q]);
+        }
+        nrdofc = nconf;
+        wlcon_off[e + 1] = wlcon_off[e] + nrdofc;
+        welem_nnz[e + 1] = welem_nnz[e] + (int64_t)nrdofc * nrdofc;
+      } else {
+        const int64_t n0 = cons->node_off[j], nn = cons->node_off[j + 1] - n0;
+        std::vector<int> mfirst(nn + 1, 0);
+        for (int64_t i = 0; i < nn; ++i) {
+          const int g = cons->nodm[n0 + i], nd = cons->ndof[n0 + i];
+          if (g < 0 || g >= nnodes || nd < 0) { free_batch(c); return HP3DG_ERR_ARG; }
+          mfirst[i + 1] = mfirst[i] + nd;
+          nodes2[(size_t)e * stride + i] = g;
+          ndofm2[(size_t)e * stride + i] = cons->bcflag[n0 + i] ? 0 : nd;
+        }
+        const int nmod = mfirst[nn];
+        cnmod[j] = nmod;
+        nrdofc = 0;
+        for (int64_t i = nn - 1; i >= 0; --i)
+          if (!cons->bcflag[n0 + i])
+            for (int q = 0; q < cons->ndof[n0 + i]; ++q) { fnext.push_back(mfirst[i] + q); ++nrdofc; }
+        for (int q = 0; q < ni; ++q) wnextract.push_back(q);
+        wlcon_off[e + 1] = wlcon_off[e] + ni;
+        welem_nnz[e + 1] = welem_nnz[e] + (int64_t)ni * ni;
+        // gather lists by modified dof, stable in the given (reference) order
+        const int64_t c0 = cons->coef_off[j], c1 = cons->coef_off[j + 1];
+        std::vector<int> cnt(nmod + 1, 0);
+        for (int64_t q = c0; q < c1; ++q) {
+          const int k = cons->coef_k[q], l = cons->coef_l[q];
+          if (k < 0 || k >= ni || l < 0 || l >= nmod) { free_batch(c); return HP3DG_ERR_ARG; }
+          ++cnt[l + 1];
+        }
+        for (int l = 0; l < nmod; ++l) cnt[l + 1] += cnt[l];
+        cgptr_off[j] = (int64_t)cgptr.size();
+        const int base = (int)cgk.size();
+        for (int l = 0; l <= nmod; ++l) cgptr.push_back(base + cnt[l]);
+        cgk.resize(base + (c1 - c0));
+        cgv.resize(base + (c1 - c0));
+        std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+        for (int64_t q = c0; q < c1; ++q) {
+          const int l = cons->coef_l[q];
+          cgk[base + fill[l]] = cons->coef_k[q];
+          cgv[base + fill[l]] = cons->coef_v[q];
+          ++fill[l];
+        }
+        caux_off[j + 1] = caux_off[j] + (int64_t)nmod * ni;
+        cmdof_off[j + 1] = cmdof_off[j] + nmod;
+        for (int64_t i = 0; i < nn; ++i)
+          for (int q = 0; q < cons->ndof[n0 + i]; ++q) {
+            cmdir.push_back(cons->bcflag[n0 + i] ? 1 : 0);
+            cmzd.push_back(cons->zdofd ? cons->zdofd[cmdof_off[j] + mfirst[i] + q] : 0.0);
+          }
+      }
+      pos += nconf;
+      flcon[e + 1] = flcon[e] + nrdofc;
+      fnnz[e + 1] = fnnz[e] + (int64_t)nrdofc * nrdofc;
+    }
+    c->nextract.swap(fnext);
+    c->lcon_off.swap(flcon);
+    c->elem_nnz.swap(fnnz);
+    nodes.swap(nodes2);
+    ndofm.swap(ndofm2);
+    c->node_stride = stride;
+    c->constrained = true;
+  }
   int err = 0;
   // ---- device inputs ----
   c->d_norder = dalloc<int>(norder.size(), &err);
@@ -655,7 +793,7 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   c->d_bschur = dalloc<double>(c->bub_off[nel], &err);
   c->d_lcon = dalloc<int>(c->lcon_off[nel], &err);
   c->d_nfirst = dalloc<int>(nnodes, &err);
-  int64_t ns = (int64_t)nel * 26;
+  int64_t ns = (int64_t)nel * c->node_stride;
   c->d_first = dalloc<int>(nnodes, &err);
   c->d_cnt = dalloc<int>(ns, &err);
   c->d_scan = dalloc<int64_t>(ns, &err);
@@ -691,6 +829,68 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   }
   if (zdofd)
     CK(cudaMemcpyAsync(c->d_zdofd, zdofd, c->zd_off[nel] * 8, cudaMemcpyHostToDevice, st));
+  // ---- work layout and constraint data ----
+  if (!c->constrained) {
+    c->d_wnextract = c->d_nextract;
+    c->d_wlcon_off = c->d_lcon_off;
+    c->d_welem_nnz = c->d_elem_nnz;
+    c->d_zwork = c->d_zastif;
+    c->d_bwork = c->d_zbload;
+  } else {
+    auto calloc_ = [&](size_t bytes) -> void* {
+      void* p = nullptr;
+      if (cudaMalloc(&p, bytes ? bytes : 8) != cudaSuccess) { err = HP3DG_ERR_ALLOC; return nullptr; }
+      c->cbufs.push_back(p);
+      return p;
+    };
+    auto upc = [&](void* dst, const void* src, size_t bytes) {
+      if (!err && bytes && cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        err = HP3DG_ERR_CUDA;
+    };
+    const int nc_el = cons->n;
+    c->d_wnextract = (int*)calloc_(wnextract.size() * 4);
+    c->d_wlcon_off = (int64_t*)calloc_((nel + 1) * 8);
+    c->d_welem_nnz = (int64_t*)calloc_((nel + 1) * 8);
+    c->d_zwork = (double*)calloc_(welem_nnz[nel] * 8);
+    c->d_bwork = (double*)calloc_(wlcon_off[nel] * 8);
+    ConstrainArgs& a = c->cargs;
+    int* d_cidx = (int*)calloc_((size_t)nel * 4);
+    int* d_nmod = (int*)calloc_((size_t)nc_el * 4);
+    int64_t* d_gptr_off = (int64_t*)calloc_((size_t)nc_el * 8);
+    int* d_gptr = (int*)calloc_(cgptr.size() * 4);
+    int* d_gk = (int*)calloc_(cgk.size() * 4);
+    double* d_gv = (double*)calloc_(cgv.size() * 8);
+    int64_t* d_aux_off = (int64_t*)calloc_((size_t)(nc_el + 1) * 8);
+    double* d_aux = (double*)calloc_(caux_off[nc_el] * 8);
+    int64_t* d_mdof_off = (int64_t*)calloc_((size_t)(nc_el + 1) * 8);
+    uint8_t* d_mdir = (uint8_t*)calloc_(cmdir.size());
+    double* d_mzd = cons->zdofd ? (double*)calloc_(cmzd.size() * 8) : nullptr;
+    if (err) { free_batch(c); return err; }
+    upc(c->d_wnextract, wnextract.data(), wnextract.size() * 4);
+    upc(c->d_wlcon_off, wlcon_off.data(), (nel + 1) * 8);
+    upc(c->d_welem_nnz, welem_nnz.data(), (nel + 1) * 8);
+    upc(d_cidx, cidx.data(), (size_t)nel * 4);
+    upc(d_nmod, cnmod.data(), (size_t)nc_el * 4);
+    upc(d_gptr_off, cgptr_off.data(), (size_t)nc_el * 8);
+    upc(d_gptr, cgptr.data(), cgptr.size() * 4);
+    upc(d_gk, cgk.data(), cgk.size() * 4);
+    upc(d_gv, cgv.data(), cgv.size() * 8);
+    upc(d_aux_off, caux_off.data(), (size_t)(nc_el + 1) * 8);
+    upc(d_mdof_off, cmdof_off.data(), (size_t)(nc_el + 1) * 8);
+    upc(d_mdir, cmdir.data(), cmdir.size());
+    if (d_mzd) upc(d_mzd, cmzd.data(), cmzd.size() * 8);
+    if (!err && cudaStreamSynchronize(st) != cudaSuccess) err = HP3DG_ERR_CUDA;
+    if (err) { free_batch(c); return err; }
+    a.cidx = d_cidx;
+    a.lcon_off = c->d_lcon_off; a.elem_nnz = c->d_elem_nnz;
+    a.zastif = c->d_zastif; a.zbload = c->d_zbload;
+    a.wlcon_off = c->d_wlcon_off; a.welem_nnz = c->d_welem_nnz;
+    a.zwork = c->d_zwork; a.bwork = c->d_bwork;
+    a.nmod = d_nmod; a.gptr_off = d_gptr_off; a.gptr = d_gptr; a.gk = d_gk; a.gv = d_gv;
+    a.aux_off = d_aux_off; a.aux = d_aux;
+    a.cnextract = c->d_nextract;
+    a.mdof_off = d_mdof_off; a.mdir = d_mdir; a.mzd = d_mzd;
+  }
   // ---- per-bin buffers ----
   for (auto& B : c->bins) {
     size_t ne = B.elems.size();
@@ -719,7 +919,8 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
         int nd[26];
         int nn = node_ndof(d.etype, d.norder, nd), k = 0;
         for (int i = 0; i < nn; ++i)
-          for (int q = 0; q < nd[i]; ++q) dm[j * B.ni + k++] = d.bcflag[i] ? 1 : 0;
+          for (int q = 0; q < nd[i]; ++q)
+            dm[j * B.ni + k++] = (d.bcflag[i] && !(c->constrained && cidx[B.elems[j]] >= 0)) ? 1 : 0;
       }
       CK(cudaMemcpyAsync(B.d_dmask, dm.data(), dm.size(), cudaMemcpyHostToDevice, st));
       CK(cudaStreamSynchronize(st));
@@ -768,7 +969,7 @@ int hp3dg_batch_submit(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   c->chunk_lo[0] = 0;
   c->chunk_lo[1] = nel;
   const int want = std::min(std::max((int)c->opts.download_chunks, 1), 8);
-  if (want > 1 && c->bins.size() == 1 && nel >= 256 && !c->opts.keep_elem) {
+  if (want > 1 && c->bins.size() == 1 && nel >= 256 && !c->opts.keep_elem && !c->constrained) {
     const int cs = (nel + want - 1) / want;
     const int step = (cs + 127) / 128 * 128;
     int k = 0;
@@ -847,8 +1048,9 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
                        c->d_schur_off, c->d_bub_off, S, c->d_aschur, c->d_bschur, t,
                        c->d_flags + 1, c->d_flags + 2, st))
       return HP3DG_ERR_CUDA;
-    launch_compress(ne, B.n, B.ni, B.nb, el, c->d_ni_e, PK, perm, S, t.bi, c->d_nextract,
-                    c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd, dm, c->d_zastif, c->d_zbload, st);
+    launch_compress(ne, B.n, B.ni, B.nb, el, c->d_ni_e, PK, perm, S, t.bi, c->d_wnextract,
+                    c->d_wlcon_off, c->d_welem_nnz, c->d_zd_off, zd, dm, c->d_zwork, c->d_bwork,
+                    st);
     return HP3DG_OK;
   }
   TcFactorOut tco = B.tco;
@@ -858,9 +1060,9 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
     tco.bi += (size_t)j0 * B.ni;
   }
   double* Yg = B.d_Yg ? B.d_Yg + (size_t)j0 * B.nb * (B.ni + 1) : nullptr;
-  if (launch_condense(ne, B.n, B.ni, B.nb, el, c->d_ni_e, c->d_nb_e, PK, b0, perm, c->d_nextract,
-                      c->d_lcon_off, c->d_elem_nnz, c->d_schur_off, c->d_bub_off, c->d_zd_off, zd,
-                      dm, S, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur, Yg,
+  if (launch_condense(ne, B.n, B.ni, B.nb, el, c->d_ni_e, c->d_nb_e, PK, b0, perm, c->d_wnextract,
+                      c->d_wlcon_off, c->d_welem_nnz, c->d_schur_off, c->d_bub_off, c->d_zd_off, zd,
+                      dm, S, c->d_zwork, c->d_bwork, c->d_aschur, c->d_bschur, Yg,
                       c->d_flags + 1, st, B.tc_schur ? &tco : nullptr))
     return HP3DG_ERR_CUDA;
   if (B.tc_schur) {
@@ -868,8 +1070,9 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
     if (launch_schur_tc(ne, B.n, B.ni, B.nb, tco.radix, tco.digits, tco.ydig, tco.yexp, el,
                         c->d_ni_e, S, c->d_flags + 2, st))
       return HP3DG_ERR_CUDA;
-    launch_compress(ne, B.n, B.ni, B.nb, el, c->d_ni_e, PK, perm, S, tco.bi, c->d_nextract,
-                    c->d_lcon_off, c->d_elem_nnz, c->d_zd_off, zd, dm, c->d_zastif, c->d_zbload, st);
+    launch_compress(ne, B.n, B.ni, B.nb, el, c->d_ni_e, PK, perm, S, tco.bi, c->d_wnextract,
+                    c->d_wlcon_off, c->d_welem_nnz, c->d_zd_off, zd, dm, c->d_zwork, c->d_bwork,
+                    st);
   }
   return HP3DG_OK;
 }
@@ -939,8 +1142,10 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
     mark(c, 3, st, capturing);
     mark(c, 4, st, capturing);
   }
-  launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,
-                    c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon, st);
+  if (c->constrained) launch_constrain(c->nel, c->cargs, st);
+  launch_index_maps(c->nel, c->node_stride, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off,
+                    c->d_first, c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon,
+                    st);
   mark(c, 5, st, capturing);
   return cudaPeekAtLastError() == cudaSuccess ? HP3DG_OK : HP3DG_ERR_CUDA;
 }
@@ -1175,6 +1380,7 @@ int hp3dg_index_map(const hp3dg_ctx* c, int32_t* nfirst_dof, int64_t* elem_nnz,
 int hp3dg_backsub(hp3dg_ctx* c, const double* x_global) {
   if (!c || !x_global) return HP3DG_ERR_ARG;
   if (!c->ran) return HP3DG_ERR_STATE;
+  if (c->constrained) return HP3DG_ERR_UNSUPPORTED;
   cudaSetDevice(c->device);
   int rc = hp3dg_batch_sync(c);
   if (rc != HP3DG_OK) return rc;
@@ -1247,6 +1453,7 @@ int hp3dg_element_error(hp3dg_ctx* c, int32_t isol, double* err2, double* nrm2) 
 int hp3dg_adjoint(hp3dg_ctx* c, const double* dofs, double* djdkappa, double* djdx) {
   if (!c || !djdkappa || !djdx) return HP3DG_ERR_ARG;
   if (!c->ran) return HP3DG_ERR_STATE;
+  if (c->constrained) return HP3DG_ERR_UNSUPPORTED;
   if (!dofs && !c->have_dofs) return HP3DG_ERR_STATE;
   cudaSetDevice(c->device);
   cudaStream_t st = c->stream;

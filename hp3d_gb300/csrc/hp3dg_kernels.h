@@ -136,6 +136,27 @@ int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_d
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
                       double* d_PK, int* d_flag, cudaStream_t st);
 
+// constrained approximation (hanging nodes) -- k_constrain.cu
+struct ConstrainArgs {
+  const int* cidx;                 // per element: constrained index j, or -1
+  const int64_t *lcon_off, *elem_nnz;    // final layout
+  double *zastif, *zbload;
+  const int64_t *wlcon_off, *welem_nnz;  // work layout of the compression
+  const double *zwork, *bwork;
+  const int* nmod;                 // per constrained element: modified dof
+  const int64_t* gptr_off;         // per constrained element: offset of its nmod+1 row pointers
+  const int* gptr;                 // row pointers into gk / gv (absolute)
+  const int* gk;                   // element interface dof
+  const double* gv;                // coefficient
+  const int64_t* aux_off;          // scratch nmod x ni per constrained element
+  double* aux;
+  const int* cnextract;            // final extraction over the modified dof (at lcon_off)
+  const int64_t* mdof_off;         // per constrained element: offset into mdir / mzd
+  const uint8_t* mdir;             // modified dof is Dirichlet
+  const double* mzd;               // Dirichlet values (or nullptr)
+};
+void launch_constrain(int nel, const ConstrainArgs& a, cudaStream_t st);
+
 // ultraweak DPG Maxwell on hexahedra -- k_dpg.cu
 constexpr int DPG_GV = 36;  // doubles per volume point: D1(6) D2(6) wJ^-1(9) wJ/detJ(9) g(6)
 struct DpgDims {

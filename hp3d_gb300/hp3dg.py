@@ -51,7 +51,8 @@ _i64p = ctypes.POINTER(ctypes.c_int64)
 _f64p = ctypes.POINTER(ctypes.c_double)
 _f32p = ctypes.POINTER(ctypes.c_float)
 
-EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit", "hp3dg_batch_run",
+EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit",
+           "hp3dg_batch_submit_constrained", "hp3dg_batch_run",
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
            "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_output_sizes", "hp3dg_device_outputs",
@@ -72,6 +73,9 @@ def lib():
         L.hp3dg_set_stream.argtypes = [_vp, _vp]
         L.hp3dg_batch_submit.argtypes = [_vp, ctypes.c_int32, _vp, _f64p, _f64p, _f64p,
                                          ctypes.c_int32]
+        L.hp3dg_batch_submit_constrained.argtypes = [_vp, ctypes.c_int32, _vp, _f64p, _f64p,
+                                                     _f64p, ctypes.c_int32,
+                                                     ctypes.POINTER(Constraints)]
         L.hp3dg_batch_run.argtypes = [_vp]
         L.hp3dg_batch_sync.argtypes = [_vp]
         L.hp3dg_batch_download.argtypes = [_vp]
@@ -110,6 +114,41 @@ def lib():
         L.hp3dg_dpg_end.restype = None
         _lib = L
     return _lib
+
+
+class Constraints(ctypes.Structure):
+    """hp3dg_constraints: logic's data of the constrained elements."""
+    _fields_ = [("n", ctypes.c_int32), ("iel", _i32p), ("node_off", _i64p), ("nodm", _i32p),
+                ("ndof", _i32p), ("bcflag", _i32p), ("coef_off", _i64p), ("coef_k", _i32p),
+                ("coef_l", _i32p), ("coef_v", _f64p), ("zdofd", _f64p)]
+
+
+def pack_constraints(cons):
+    """Constraints struct (and the arrays it points to) from a list with, per
+    element, None or a dict with nodm, ndof, bc, ck, cl, cv (and optionally
+    zd, the Dirichlet values of the modified dof)."""
+    iel = [e for e, c in enumerate(cons) if c is not None]
+    arrs = {}
+    arrs["iel"] = np.array(iel, np.int32)
+    arrs["node_off"] = np.concatenate([[0], np.cumsum([len(cons[e]["nodm"]) for e in iel])]).astype(np.int64)
+    arrs["nodm"] = np.concatenate([cons[e]["nodm"] for e in iel]).astype(np.int32)
+    arrs["ndof"] = np.concatenate([cons[e]["ndof"] for e in iel]).astype(np.int32)
+    arrs["bcflag"] = np.concatenate([cons[e]["bc"] for e in iel]).astype(np.int32)
+    arrs["coef_off"] = np.concatenate([[0], np.cumsum([len(cons[e]["ck"]) for e in iel])]).astype(np.int64)
+    arrs["coef_k"] = np.concatenate([cons[e]["ck"] for e in iel]).astype(np.int32)
+    arrs["coef_l"] = np.concatenate([cons[e]["cl"] for e in iel]).astype(np.int32)
+    arrs["coef_v"] = np.concatenate([cons[e]["cv"] for e in iel]).astype(np.float64)
+    zd = None
+    if any("zd" in cons[e] for e in iel):
+        zd = np.concatenate([cons[e].get("zd", np.zeros(int(np.sum(cons[e]["ndof"]))))
+                             for e in iel]).astype(np.float64)
+    arrs["zdofd"] = zd
+    st = Constraints(len(iel), *[_p(arrs[k], t) for k, t in
+                                 (("iel", _i32p), ("node_off", _i64p), ("nodm", _i32p),
+                                  ("ndof", _i32p), ("bcflag", _i32p), ("coef_off", _i64p),
+                                  ("coef_k", _i32p), ("coef_l", _i32p), ("coef_v", _f64p),
+                                  ("zdofd", _f64p))])
+    return st, arrs
 
 
 def mesh_descriptors(mesh):
@@ -161,16 +200,26 @@ class ElementPass:
     def set_stream(self, stream_ptr):
         self._check(self.L.hp3dg_set_stream(self.ctx, _vp(stream_ptr)), "set_stream")
 
-    def submit(self, mesh, zdofd=None, desc=None):
+    def submit(self, mesh, zdofd=None, desc=None, constraints=None):
+        """constraints: None, or per element None / dict (see pack_constraints)."""
         self.mesh = mesh
         self.desc = mesh_descriptors(mesh) if desc is None else desc
         self.xvert = np.ascontiguousarray(mesh["xvert"], dtype=np.float64)
         self.kappa = np.ascontiguousarray(mesh["kappa"], dtype=np.float64)
         self.zd = None if zdofd is None else np.ascontiguousarray(np.concatenate(zdofd), np.float64)
         self.nel = mesh["nelem"]
-        self._check(self.L.hp3dg_batch_submit(self.ctx, self.nel, self.desc.ctypes.data_as(_vp),
-                                              _p(self.xvert, _f64p), _p(self.kappa, _f64p),
-                                              _p(self.zd, _f64p), int(mesh["nnodes"])), "submit")
+        if constraints is None:
+            self._check(self.L.hp3dg_batch_submit(self.ctx, self.nel,
+                                                  self.desc.ctypes.data_as(_vp),
+                                                  _p(self.xvert, _f64p), _p(self.kappa, _f64p),
+                                                  _p(self.zd, _f64p), int(mesh["nnodes"])),
+                        "submit")
+        else:
+            self._cons, self._cons_arrs = pack_constraints(constraints)
+            self._check(self.L.hp3dg_batch_submit_constrained(
+                self.ctx, self.nel, self.desc.ctypes.data_as(_vp), _p(self.xvert, _f64p),
+                _p(self.kappa, _f64p), _p(self.zd, _f64p), int(mesh["nnodes"]),
+                ctypes.byref(self._cons)), "submit")
 
     def run(self):
         self._check(self.L.hp3dg_batch_run(self.ctx), "run")

@@ -135,6 +135,41 @@ int hp3dg_batch_submit(hp3dg_ctx *ctx, int32_t n_elem, const hp3dg_elem_desc *de
                        const double *xvert, const double *kappa, const double *zdofd,
                        int32_t n_nodes_global);
 
+/* Constrained approximation (hanging nodes): for each constrained element,
+ * what logic (constrs/logic.F90) returns for it, as celem_systemI consumes it
+ * (celem_systemI.F90:541-760):
+ *   the modified element nodes Nodm (without the middle node), their H1 dof
+ *   counts and Dirichlet flags; and the coefficients constrH of every
+ *   element interface dof k (element order, 0-based) on the modified dof l
+ *   (modified nodes in order, each node's dof forward, 0-based) as triplets,
+ *   listed per element in the order logic gives them (k, then its connected
+ *   dof).
+ * The condensed element system becomes C^T A C, C^T b; extraction,
+ * Dirichlet lift and compression run over the modified nodes, and the index
+ * maps walk Nodm (mumps_sc.F90:102-188 with celem's Nodm). */
+typedef struct hp3dg_constraints {
+  int32_t n;               /* number of constrained elements */
+  const int32_t *iel;      /* their batch indices, strictly increasing */
+  const int64_t *node_off; /* n+1 offsets into nodm / ndof / bcflag */
+  const int32_t *nodm;     /* modified element nodes (global ids) */
+  const int32_t *ndof;     /* H1 dof per modified node */
+  const int32_t *bcflag;   /* 1: the node's dof are Dirichlet */
+  const int64_t *coef_off; /* n+1 offsets into coef_k / coef_l / coef_v */
+  const int32_t *coef_k;
+  const int32_t *coef_l;
+  const double *coef_v;
+  const double *zdofd;     /* Dirichlet values per modified dof, concatenated
+                              per element (node_off order); NULL = 0 */
+} hp3dg_constraints;
+
+/* hp3dg_batch_submit for a batch with constrained elements (cons may be
+ * NULL).  Back-substitution, element errors and the adjoint are not
+ * available for a constrained batch (HP3DG_ERR_UNSUPPORTED). */
+int hp3dg_batch_submit_constrained(hp3dg_ctx *ctx, int32_t n_elem, const hp3dg_elem_desc *desc,
+                                   const double *xvert, const double *kappa,
+                                   const double *zdofd, int32_t nnodes,
+                                   const hp3dg_constraints *cons);
+
 /* Run the whole element pass on the device (asynchronous on the context's
  * stream; errors of the pass are reported by hp3dg_batch_sync).
  * Replaces: the STEP 2 element loop (mumps_sc.F90:253-330). */

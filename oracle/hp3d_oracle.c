@@ -769,7 +769,16 @@ int orc_celem_compress(int etype, const int32_t *norder, const int32_t *bcflag,
                        double *zastif, int32_t *ndofm) {
   int32_t nd[32];
   int nn = orc_node_ndof(etype, norder, nd);
-  int first[32], ni = 0;
+  return orc_celem_compress_nodes(nn, nd, bcflag, aii, bi, zdofd, nextract, zbload, zastif,
+                                  ndofm);
+}
+
+int orc_celem_compress_nodes(int nn, const int32_t *nd, const int32_t *bcflag,
+                             const double *aii, const double *bi, const double *zdofd,
+                             int32_t *nextract, double *zbload, double *zastif,
+                             int32_t *ndofm) {
+  int first[256], ni = 0;
+  if (nn > 256) return -1;
   for (int i = 0; i < nn; ++i) { first[i] = ni; ni += nd[i]; }
   /* NEXTRACT: nodes in reverse order, dof in forward order, skip Dirichlet
    * (celem_systemI.F90:290-350) */
@@ -1438,6 +1447,33 @@ int orc_shape3DH_prism(const double *xi, const int32_t *nord,
         }
   }
   return m;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Constrained approximation (celem_systemI.F90:541-760)                      */
+/* ------------------------------------------------------------------------ */
+int orc_constrain(int ni, const double *aii, const double *bi, int ncoef, const int32_t *ck,
+                  const int32_t *cl, const double *cv, int nmod, double *amod, double *bmod) {
+  /* rows: ZBMOD(l) += BLOC(k) c, AAUX(l,:) += ALOC(k,:) c (loop over k, then
+   * its connected modified dof); columns: ZAMOD(:,l) += AAUX(:,k) c */
+  double *aux = (double *)calloc((size_t)nmod * (ni > 0 ? ni : 1), sizeof(double));
+  if (!aux) return -1;
+  for (int i = 0; i < nmod; ++i) bmod[i] = 0.0;
+  for (size_t i = 0; i < (size_t)nmod * nmod; ++i) amod[i] = 0.0;
+  for (int q = 0; q < ncoef; ++q) {
+    const int k = ck[q], l = cl[q];
+    if (k < 0 || k >= ni || l < 0 || l >= nmod) { free(aux); return -2; }
+    bmod[l] = bmod[l] + bi[k] * cv[q];
+    for (int j = 0; j < ni; ++j)
+      aux[l + (size_t)nmod * j] = aux[l + (size_t)nmod * j] + aii[k + (size_t)ni * j] * cv[q];
+  }
+  for (int q = 0; q < ncoef; ++q) {
+    const int k = ck[q], l = cl[q];
+    for (int i = 0; i < nmod; ++i)
+      amod[i + (size_t)nmod * l] = amod[i + (size_t)nmod * l] + aux[i + (size_t)nmod * k] * cv[q];
+  }
+  free(aux);
+  return 0;
 }
 
 /* ------------------------------------------------------------------------ */

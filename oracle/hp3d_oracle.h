@@ -132,6 +132,23 @@ int orc_celem_compress(int etype, const int32_t *norder, const int32_t *bcflag,
                        const double *zdofd, int32_t *nextract, double *zbload,
                        double *zastif, int32_t *ndofm);
 
+/* The same over an arbitrary node list (the modified element nodes of a
+ * constrained element): nn nodes with nd dof each (modified dof numbered node
+ * by node, forward), bcflag per node. */
+int orc_celem_compress_nodes(int nn, const int32_t *nd, const int32_t *bcflag,
+                             const double *aii, const double *bi, const double *zdofd,
+                             int32_t *nextract, double *zbload, double *zastif,
+                             int32_t *ndofm);
+
+/* Constraint transform of the condensed element system (celem_systemI.F90:
+ * 541-760, CONTIN branch): amod = C^T aii C, bmod = C^T bi with the
+ * coefficients of logic (constrs/logic.F90) given as triplets (element
+ * interface dof k, modified dof l, coefficient), in the reference's loop
+ * order (k, then its connected dof).  aii ni x ni and amod nmod x nmod,
+ * column-major.  Returns 0, or <0 for an index out of range. */
+int orc_constrain(int ni, const double *aii, const double *bi, int ncoef, const int32_t *ck,
+                  const int32_t *cl, const double *cv, int nmod, double *amod, double *bmod);
+
 /* mumps_sc STEP 1 offsets + STEP 2 connectivities
  * (solver/omp_mumps/mumps_sc.F90:102-188, 266-299).
  * nodes: nelem x nnode_max global node ids (element node order),

@@ -70,6 +70,10 @@ def lib():
                                        _f64p, _f64p, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, ctypes.c_int, _i64p, _i64p, _i64p,
                                        _i64p, _f64p, _f64p, _f64p, _f64p]
+        L.orc_celem_compress_nodes.argtypes = [ctypes.c_int, _i32p, _i32p, _f64p, _f64p, _f64p,
+                                               _i32p, _f64p, _f64p, _i32p]
+        L.orc_constrain.argtypes = [ctypes.c_int, _f64p, _f64p, ctypes.c_int, _i32p, _i32p,
+                                    _f64p, ctypes.c_int, _f64p, _f64p]
         L.orc_nrdofE_hexa.argtypes = [_i32p]
         L.orc_shape3DE_hexa.argtypes = [_f64p, _i32p, _i32p, _i32p, _f64p, _f64p]
         L.orc_shape3DQ_hexa.argtypes = [_f64p, _i32p, _f64p]
@@ -454,3 +458,29 @@ def dpg_pass(mesh, eps, bcflag, imp_mask, prm, elements=None, nthreads=0):
                             asch.ctypes.data_as(_f64p), bsch.ctypes.data_as(_f64p))
     return dict(rc=rc, zastif=zs, zbload=zb, aschur=asch, bschur=bsch, elem_nnz=elem_nnz,
                 lcon_off=lcon_off)
+
+
+def constrain(aii, bi, ck, cl, cv, nmod):
+    """amod = C^T aii C, bmod = C^T bi (celem_systemI.F90:541-760)."""
+    ni = aii.shape[0]
+    a = np.asfortranarray(aii, dtype=np.float64)
+    am = np.zeros((nmod, nmod), order="F"); bm = np.zeros(nmod)
+    rc = lib().orc_constrain(ni, a.ctypes.data_as(_f64p), _p(_f64(bi), _f64p), len(ck),
+                             _p(_i32(ck), _i32p), _p(_i32(cl), _i32p), _p(_f64(cv), _f64p), nmod,
+                             am.ctypes.data_as(_f64p), _p(bm, _f64p))
+    assert rc == 0, rc
+    return am, bm
+
+
+def celem_compress_nodes(nd, bcflag, amod, bmod, zdofd=None):
+    """Compression over a node list (modified element nodes)."""
+    n = amod.shape[0]
+    a = np.asfortranarray(amod, dtype=np.float64)
+    nx = np.zeros(max(n, 1), dtype=np.int32)
+    zb = np.zeros(max(n, 1)); zs = np.zeros(max(n * n, 1)); ndofm = np.zeros(len(nd), np.int32)
+    zd = None if zdofd is None else _f64(zdofd)
+    nc = lib().orc_celem_compress_nodes(len(nd), _p(_i32(nd), _i32p), _p(_i32(bcflag), _i32p),
+                                        a.ctypes.data_as(_f64p), _p(_f64(bmod), _f64p),
+                                        _p(zd, _f64p), _p(nx, _i32p), _p(zb, _f64p),
+                                        _p(zs, _f64p), _p(ndofm, _i32p))
+    return nx[:nc].copy(), zb[:nc].copy(), zs[: nc * nc].reshape(nc, nc).copy(), ndofm
