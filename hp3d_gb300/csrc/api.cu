@@ -1530,6 +1530,54 @@ int hp3dg_pass_stats(const hp3dg_ctx* c, int64_t* kernels, double* contraction_f
   return HP3DG_OK;
 }
 
+int hp3dg_dirichlet_dofs(hp3dg_ctx* c, int32_t isol, double* zdofd, int64_t* n) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  const int nel = c->nel;
+  if (n) *n = nel > 0 ? c->zd_off[nel] : 0;
+  if (!zdofd || nel == 0) return HP3DG_OK;
+  if ((int)c->last_desc.size() != nel) return HP3DG_ERR_STATE;
+  for (int e = 0; e < nel; ++e)
+    if (c->etype_e[e] != HP3DG_HEXA) return HP3DG_ERR_UNSUPPORTED;
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  std::vector<int> bc((size_t)nel * 26);
+  for (int e = 0; e < nel; ++e)
+    for (int i = 0; i < 26; ++i) bc[(size_t)e * 26 + i] = c->last_desc[e].bcflag[i] ? 1 : 0;
+  std::vector<double> gx(16 * 11, 0.0), gw(16 * 11, 0.0);
+  for (int m = 1; m <= 10; ++m) gauss_rule01(m, &gx[16 * m], &gw[16 * m]);
+  int *d_bc = nullptr, *d_bad = nullptr;
+  double *d_gx = nullptr, *d_gw = nullptr, *d_work = nullptr, *d_zd = nullptr;
+  int rc = HP3DG_OK;
+  const size_t nz = c->zd_off[nel];
+  if (cudaMalloc(&d_bc, bc.size() * 4) != cudaSuccess || cudaMalloc(&d_bad, 4) != cudaSuccess ||
+      cudaMalloc(&d_gx, gx.size() * 8) != cudaSuccess || cudaMalloc(&d_gw, gw.size() * 8) != cudaSuccess ||
+      cudaMalloc(&d_work, dirichlet_work_doubles(nel) * 8) != cudaSuccess ||
+      cudaMalloc(&d_zd, nz * 8) != cudaSuccess)
+    rc = HP3DG_ERR_ALLOC;
+  int badv = 0x7f7f7f7f;
+  if (rc == HP3DG_OK &&
+      (cudaMemcpyAsync(d_bc, bc.data(), bc.size() * 4, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+       cudaMemcpyAsync(d_gx, gx.data(), gx.size() * 8, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+       cudaMemcpyAsync(d_gw, gw.data(), gw.size() * 8, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+       cudaMemcpyAsync(d_bad, &badv, 4, cudaMemcpyHostToDevice, st) != cudaSuccess))
+    rc = HP3DG_ERR_CUDA;
+  if (rc == HP3DG_OK) {
+    launch_dirichlet(nel, c->d_norder, c->d_nori_e, c->d_nori_f, d_bc, c->d_xvert, c->d_zd_off,
+                     d_gx, d_gw, isol, d_work, d_zd, d_bad, st);
+    if (cudaMemcpyAsync(zdofd, d_zd, nz * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&badv, d_bad, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = HP3DG_ERR_CUDA;
+    else if (badv != 0x7f7f7f7f) {
+      c->last_bad = badv;
+      rc = HP3DG_ERR_NOT_SPD;
+    }
+  }
+  cudaFree(d_bc); cudaFree(d_bad); cudaFree(d_gx); cudaFree(d_gw); cudaFree(d_work); cudaFree(d_zd);
+  return rc;
+}
+
 int32_t hp3dg_last_bad_element(const hp3dg_ctx* c) { return c ? c->last_bad : -1; }
 
 void hp3dg_batch_end(hp3dg_ctx* c) {

@@ -112,6 +112,14 @@ void launch_adjoint(int nel, int nvert, int nint, int n, int isol, const int* d_
                     const double* d_kappa, const uint32_t* d_perm, const int64_t* d_dof_off,
                     const double* d_dofs, double* d_djdk, double* d_djdx, cudaStream_t st);
 
+// Dirichlet data by projection-based interpolation (hexahedra) -- k_post.cu.
+// d_gx / d_gw: the n-point Gauss rules on [0,1] at [16 n + l], n <= 10.
+size_t dirichlet_work_doubles(int nel);
+void launch_dirichlet(int nel, const int* d_norder, const int* d_nori_e, const int* d_nori_f,
+                      const int* d_bc, const double* d_xvert, const int64_t* d_zd_off,
+                      const double* d_gx, const double* d_gw, int isol, double* d_work,
+                      double* d_zdofd, int* d_bad, cudaStream_t st);
+
 // mixed precision (split-BF16 digits on tcgen05) -- k_ozaki.cu
 struct OzakiPlan {
   int radix;      // bits per digit

@@ -313,4 +313,212 @@ void launch_adjoint(int nel, int nvert, int nint, int n, int isol, const int* d_
                                                   d_djdx);
 }
 
+// ---------------------------------------------------------------------------
+// Dirichlet data by projection-based interpolation (update_Ddof.F90:70-250):
+// vertex values (dhpvert.F90), then tangential H1-seminorm projections on
+// the boundary edges (edge/dhpedgeH.F90) and faces (face/dhpfaceH.F90) of
+// what the lower-order part leaves, in the element's reference coordinates
+// (the element is its own geometry block: eta = xi, x(eta) trilinear).  The
+// values depend only on the node's trace, so every element computes its own
+// boundary nodes; one thread per element.  Output per interface dof in
+// element order (zeros on non-Dirichlet nodes).
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ inline int lu_small(int n, double* A, double* b) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
+    if (A[p + n * k] == 0.0) return -1;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) { double t = A[k + n * j]; A[k + n * j] = A[p + n * j]; A[p + n * j] = t; }
+      double t = b[k]; b[k] = b[p]; b[p] = t;
+    }
+    for (int i = k + 1; i < n; ++i) {
+      double f = A[i + n * k] / A[k + n * k];
+      A[i + n * k] = f;
+      for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
+      b[i] -= f * b[k];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    double t = b[k];
+    for (int j = k + 1; j < n; ++j) t -= A[k + n * j] * b[j];
+    b[k] = t / A[k + n * k];
+  }
+  return 0;
+}
+
+__device__ const double DBRICK_XI[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                           {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+__device__ const int DBRICK_E2V[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {4, 5}, {5, 6},
+                                          {7, 6}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+__device__ const int DBRICK_F2V[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                                         {1, 2, 6, 5}, {3, 2, 6, 7}, {0, 3, 7, 4}};
+__device__ const int DBRICK_F2E[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 9, 4, 8},
+                                         {1, 10, 5, 9}, {2, 10, 6, 11}, {3, 11, 7, 8}};
+
+// gradient (in xi) of the element's oriented function a at xi, from the
+// reference-enumeration gradients of the element's local orders
+__device__ inline void grad_oriented(int a, const int* nord, const int* ne, const int* nf,
+                                     const int* loc, const double* grad, double* g) {
+  const uint32_t m = hexa_dof_map(a, nord, ne, nf, loc);
+  const int r = (int)(m & 0x7fffffffu);
+  const double sg = (m >> 31) ? -1.0 : 1.0;
+  for (int c = 0; c < 3; ++c) g[c] = sg * grad[c * MAXN + r];
+}
+
+__device__ void trilin_dev(const double* xv, const double* xi, double* x, double J[3][3]) {
+  double Mu[2][3];
+  for (int a = 0; a < 3; ++a) { Mu[0][a] = 1.0 - xi[a]; Mu[1][a] = xi[a]; }
+  for (int i = 0; i < 3; ++i) {
+    x[i] = 0.0;
+    for (int j = 0; j < 3; ++j) J[i][j] = 0.0;
+  }
+  for (int v = 0; v < 8; ++v) {
+    const int s0 = hexa_v(v, 0), s1 = hexa_v(v, 1), s2 = hexa_v(v, 2);
+    const double b0 = Mu[s0][0], b1 = Mu[s1][1], b2 = Mu[s2][2];
+    const double gg[3] = {(s0 ? 1.0 : -1.0) * b1 * b2, b0 * (s1 ? 1.0 : -1.0) * b2,
+                          b0 * b1 * (s2 ? 1.0 : -1.0)};
+    for (int i = 0; i < 3; ++i) {
+      x[i] += xv[3 * v + i] * b0 * b1 * b2;
+      for (int j = 0; j < 3; ++j) J[i][j] += xv[3 * v + i] * gg[j];
+    }
+  }
+}
+
+__global__ void k_dirichlet(int nel, const int* __restrict__ norder, const int* __restrict__ nori_e,
+                            const int* __restrict__ nori_f, const int* __restrict__ nodes_bc,
+                            const double* __restrict__ xvert, const int64_t* __restrict__ zd_off,
+                            const double* __restrict__ gx, const double* __restrict__ gw,
+                            int isol, double* __restrict__ work, double* __restrict__ zdofd,
+                            int* __restrict__ bad) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nel) return;
+  const int* bc = nodes_bc + (size_t)26 * e;
+  bool any = false;
+  for (int i = 0; i < 26; ++i) any |= bc[i] != 0;
+  double* zd = zdofd + zd_off[e];
+  const int ni = (int)(zd_off[e + 1] - zd_off[e]);
+  for (int k = 0; k < ni; ++k) zd[k] = 0.0;
+  if (!any) return;
+  int nord[19], ne[12], nf[6], loc[19];
+  for (int i = 0; i < 19; ++i) nord[i] = norder[19 * (size_t)e + i];
+  for (int i = 0; i < 12; ++i) ne[i] = nori_e[12 * (size_t)e + i];
+  for (int i = 0; i < 6; ++i) nf[i] = nori_f[6 * (size_t)e + i];
+  hexa_order_loc(nord, nf, loc);
+  const double* xv = xvert + (size_t)24 * e;
+  // per-thread scratch: shape values and gradients, the small system
+  double* shap = work + (size_t)e * (4 * MAXN + 64 * 64 + 64);
+  double* grad = shap + MAXN;
+  double* A = grad + 3 * MAXN;
+  double* rhs = A + 64 * 64;
+  int nd[26], first[27];
+  first[0] = 0;
+  for (int i = 0; i < 26; ++i) {
+    if (i < 8) nd[i] = 1;
+    else if (i < 20) nd[i] = nord[i - 8] > 1 ? nord[i - 8] - 1 : 0;
+    else { int a, b; decod2(nord[12 + i - 20], a, b); nd[i] = (a > 1 && b > 1) ? (a - 1) * (b - 1) : 0; }
+    first[i + 1] = first[i] + nd[i];
+  }
+  for (int v = 0; v < 8; ++v)
+    if (bc[v]) {
+      double u, g[3];
+      exact_dev(isol, &xv[3 * v], u, g);
+      zd[v] = u;
+    }
+  // edges, then faces (the faces subtract the edges' values)
+  for (int node = 8; node < 26; ++node) {
+    const int n = nd[node];
+    if (!bc[node] || n == 0) continue;
+    const bool edge = node < 20;
+    const int id = edge ? node - 8 : node - 20;
+    int nx, ny;
+    double x1[3], t1[3], t2[3];
+    if (edge) {
+      const int p = nord[id];
+      nx = min(p + 1, MAXP) + 1;
+      ny = 1;
+      for (int c = 0; c < 3; ++c) {
+        x1[c] = DBRICK_XI[DBRICK_E2V[id][0]][c];
+        t1[c] = DBRICK_XI[DBRICK_E2V[id][1]][c] - x1[c];
+        t2[c] = 0.0;
+      }
+    } else {
+      int h, v; decod2(nord[12 + id], h, v);
+      const int* fe = DBRICK_F2E[id];
+      nx = min(max(max(nord[fe[0]], nord[fe[2]]), h) + 1, MAXP) + 1;
+      ny = min(max(max(nord[fe[1]], nord[fe[3]]), v) + 1, MAXP) + 1;
+      for (int c = 0; c < 3; ++c) {
+        x1[c] = DBRICK_XI[DBRICK_F2V[id][0]][c];
+        t1[c] = DBRICK_XI[DBRICK_F2V[id][1]][c] - x1[c];
+        t2[c] = DBRICK_XI[DBRICK_F2V[id][3]][c] - x1[c];
+      }
+    }
+    // the lower part: vertices (edges) or vertices and all edges (faces)
+    const int nlow = edge ? 8 : first[20];
+    const int a0 = first[node];
+    for (int q = 0; q < n * n; ++q) A[q] = 0.0;
+    for (int q = 0; q < n; ++q) rhs[q] = 0.0;
+    double rn[3] = {t1[1] * t2[2] - t1[2] * t2[1], t1[2] * t2[0] - t1[0] * t2[2],
+                    t1[0] * t2[1] - t1[1] * t2[0]};
+    double bjac;
+    if (edge) {
+      bjac = sqrt(t1[0] * t1[0] + t1[1] * t1[1] + t1[2] * t1[2]);
+      for (int c = 0; c < 3; ++c) rn[c] = t1[c] / bjac;  // the unit tangent
+    } else {
+      bjac = sqrt(rn[0] * rn[0] + rn[1] * rn[1] + rn[2] * rn[2]);
+      for (int c = 0; c < 3; ++c) rn[c] /= bjac;  // the unit normal (its sign is immaterial)
+    }
+    for (int l2 = 0; l2 < ny; ++l2)
+      for (int l1 = 0; l1 < nx; ++l1) {
+        const double s1 = gx[16 * nx + l1], s2 = edge ? 0.0 : gx[16 * ny + l2];
+        const double w = gw[16 * nx + l1] * (edge ? 1.0 : gw[16 * ny + l2]) * bjac;
+        double xi[3];
+        for (int c = 0; c < 3; ++c) xi[c] = x1[c] + s1 * t1[c] + s2 * t2[c];
+        hexa_shape0(xi, loc, shap, grad, MAXN);
+        double x[3], J[3][3];
+        trilin_dev(xv, xi, x, J);
+        double u, gu[3];
+        exact_dev(isol, x, u, gu);
+        double du[3];
+        for (int i = 0; i < 3; ++i) du[i] = gu[0] * J[0][i] + gu[1] * J[1][i] + gu[2] * J[2][i];
+        for (int k = 0; k < nlow; ++k) {
+          if (zd[k] == 0.0) continue;
+          double g[3];
+          grad_oriented(k, nord, ne, nf, loc, grad, g);
+          for (int i = 0; i < 3; ++i) du[i] -= zd[k] * g[i];
+        }
+        for (int j = 0; j < n; ++j) {
+          double gj[3], dv[3];
+          grad_oriented(a0 + j, nord, ne, nf, loc, grad, gj);
+          const double pr = gj[0] * rn[0] + gj[1] * rn[1] + gj[2] * rn[2];
+          for (int c = 0; c < 3; ++c) dv[c] = edge ? pr * rn[c] : gj[c] - pr * rn[c];
+          rhs[j] += (du[0] * dv[0] + du[1] * dv[1] + du[2] * dv[2]) * w;
+          for (int i = 0; i < n; ++i) {
+            double gi[3];
+            grad_oriented(a0 + i, nord, ne, nf, loc, grad, gi);
+            A[j + n * i] += (dv[0] * gi[0] + dv[1] * gi[1] + dv[2] * gi[2]) * w;
+          }
+        }
+      }
+    if (lu_small(n, A, rhs)) { atomicMin(bad, e); return; }
+    for (int j = 0; j < n; ++j) zd[a0 + j] = rhs[j];
+  }
+}
+
+}  // namespace
+
+size_t dirichlet_work_doubles(int nel) { return (size_t)nel * (4 * MAXN + 64 * 64 + 64); }
+
+void launch_dirichlet(int nel, const int* d_norder, const int* d_nori_e, const int* d_nori_f,
+                      const int* d_bc, const double* d_xvert, const int64_t* d_zd_off,
+                      const double* d_gx, const double* d_gw, int isol, double* d_work,
+                      double* d_zdofd, int* d_bad, cudaStream_t st) {
+  if (nel <= 0) return;
+  k_dirichlet<<<(nel + 63) / 64, 64, 0, st>>>(nel, d_norder, d_nori_e, d_nori_f, d_bc, d_xvert,
+                                              d_zd_off, d_gx, d_gw, isol, d_work, d_zdofd, d_bad);
+}
+
 }  // namespace hp3dg

@@ -52,7 +52,7 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 _f32p = ctypes.POINTER(ctypes.c_float)
 
 EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit",
-           "hp3dg_batch_submit_constrained", "hp3dg_batch_run",
+           "hp3dg_batch_submit_constrained", "hp3dg_dirichlet_dofs", "hp3dg_batch_run",
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
            "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_output_sizes", "hp3dg_device_outputs",
@@ -76,6 +76,7 @@ def lib():
         L.hp3dg_batch_submit_constrained.argtypes = [_vp, ctypes.c_int32, _vp, _f64p, _f64p,
                                                      _f64p, ctypes.c_int32,
                                                      ctypes.POINTER(Constraints)]
+        L.hp3dg_dirichlet_dofs.argtypes = [_vp, ctypes.c_int32, _f64p, _i64p]
         L.hp3dg_batch_run.argtypes = [_vp]
         L.hp3dg_batch_sync.argtypes = [_vp]
         L.hp3dg_batch_download.argtypes = [_vp]
@@ -223,6 +224,25 @@ class ElementPass:
 
     def run(self):
         self._check(self.L.hp3dg_batch_run(self.ctx), "run")
+
+    def dirichlet_dofs(self, isol):
+        """Per element Dirichlet values of the interface dof (update_Ddof on
+        the GPU), split per element (the zdofd layout of submit)."""
+        n = ctypes.c_int64()
+        self._check(self.L.hp3dg_dirichlet_dofs(self.ctx, isol, None, ctypes.byref(n)), "dirichlet")
+        z = np.zeros(max(n.value, 1))
+        self._check(self.L.hp3dg_dirichlet_dofs(self.ctx, isol, _p(z, _f64p), ctypes.byref(n)),
+                    "dirichlet")
+        ni = [int(sum(self._node_ndof(e))) for e in range(self.nel)]
+        return np.split(z[: n.value], np.cumsum(ni)[:-1])
+
+    def _node_ndof(self, e):
+        no = self.mesh["norder"][e]
+        nd = [1] * 8 + [max(int(no[i]) - 1, 0) for i in range(12)]
+        for f in range(6):
+            a, b = int(no[12 + f]) // 10, int(no[12 + f]) % 10
+            nd.append(max(a - 1, 0) * max(b - 1, 0))
+        return nd
 
     def sync(self):
         self._check(self.L.hp3dg_batch_sync(self.ctx), "sync")

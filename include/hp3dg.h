@@ -296,6 +296,16 @@ int hp3dg_condense_noalloc(int32_t n_elem, int32_t n, int32_t nb, const double *
                            const double *b, double *aii, double *bi, double *aschur,
                            double *bschur, int32_t *bad_element, void *stream);
 
+/* Dirichlet data of the submitted batch by projection-based interpolation
+ * (update_Ddof, hpinterp/update_Ddof.F90 with dhpvert, dhpedgeH, dhpfaceH)
+ * of the manufactured solution isol, computed on the GPU: for every element
+ * the values of its interface dof on the nodes with bcflag set (vertex
+ * values, then tangential H1-seminorm projections on edges and faces), in
+ * the layout hp3dg_batch_submit takes as zdofd (element order, n_i per
+ * element; zeros elsewhere).  Hexahedra whose geometry block is the element
+ * (trilinear vertex geometry).  zdofd = NULL returns the length in *n. */
+int hp3dg_dirichlet_dofs(hp3dg_ctx *ctx, int32_t isol, double *zdofd, int64_t *n);
+
 /* First element (0-based) that failed in the last run, or -1. */
 int32_t hp3dg_last_bad_element(const hp3dg_ctx *ctx);
 

@@ -1477,6 +1477,193 @@ int orc_constrain(int ni, const double *aii, const double *bi, int ncoef, const 
 }
 
 /* ------------------------------------------------------------------------ */
+/* Dirichlet data by projection-based interpolation (update_Ddof.F90:70-250,  */
+/* dhpvert.F90, edge/dhpedgeH.F90, face/dhpfaceH.F90) for a hexahedron whose  */
+/* geometry block is the element itself (eta = xi, trilinear x(eta)).        */
+/* ------------------------------------------------------------------------ */
+static const int BRICK_E2V[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {4, 5}, {5, 6},
+                                     {7, 6}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+static const int BRICK_F2V[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                                    {1, 2, 6, 5}, {3, 2, 6, 7}, {0, 3, 7, 4}};
+static const int BRICK_F2E[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 9, 4, 8},
+                                    {1, 10, 5, 9}, {2, 10, 6, 11}, {3, 11, 7, 8}};
+static const double BRICK_XI[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                      {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+
+static void trilin(const double *xvert, const double *xi, double *x, double J[3][3]) {
+  double Mu[2][3];
+  for (int d = 0; d < 3; ++d) { Mu[0][d] = 1.0 - xi[d]; Mu[1][d] = xi[d]; }
+  for (int i = 0; i < 3; ++i) {
+    x[i] = 0.0;
+    for (int j = 0; j < 3; ++j) J[i][j] = 0.0;
+  }
+  for (int v = 0; v < 8; ++v) {
+    const int *s = HEXA_V[v];
+    double b0 = Mu[s[0]][0], b1 = Mu[s[1]][1], b2 = Mu[s[2]][2];
+    double g[3] = {(s[0] ? 1.0 : -1.0) * b1 * b2, b0 * (s[1] ? 1.0 : -1.0) * b2,
+                   b0 * b1 * (s[2] ? 1.0 : -1.0)};
+    for (int i = 0; i < 3; ++i) {
+      x[i] += xvert[3 * v + i] * b0 * b1 * b2;
+      for (int j = 0; j < 3; ++j) J[i][j] += xvert[3 * v + i] * g[j];
+    }
+  }
+}
+
+/* dgetrf + dgetrs on a small system (n <= 36), partial pivoting */
+static int lu_solve(int n, double *A, double *b) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
+    if (A[p + n * k] == 0.0) return -1;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) { double t = A[k + n * j]; A[k + n * j] = A[p + n * j]; A[p + n * j] = t; }
+      double t = b[k]; b[k] = b[p]; b[p] = t;
+    }
+    for (int i = k + 1; i < n; ++i) {
+      double f = A[i + n * k] / A[k + n * k];
+      A[i + n * k] = f;
+      for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
+      b[i] -= f * b[k];
+    }
+  }
+  for (int k = n - 1; k >= 0; --k) {
+    double t = b[k];
+    for (int j = k + 1; j < n; ++j) t -= A[k + n * j] * b[j];
+    b[k] = t / A[k + n * k];
+  }
+  return 0;
+}
+
+int orc_dirichlet_hexa(const int32_t *norder, const int32_t *nori_edge, const int32_t *nori_face,
+                       const double *xvert, const int32_t *bcflag, int isol, double *zd) {
+  int32_t nd[32];
+  orc_node_ndof(ORC_HEXA, norder, nd);
+  int first[27];
+  first[0] = 0;
+  for (int i = 0; i < 26; ++i) first[i + 1] = first[i] + nd[i];
+  for (int k = 0; k < first[26]; ++k) zd[k] = 0.0;
+  double shap[ORC_MAXBRICKH], grad[3 * ORC_MAXBRICKH];
+  /* vertices (dhpvert) */
+  for (int v = 0; v < 8; ++v) {
+    if (!bcflag[v]) continue;
+    double u, gu[3];
+    orc_exact(isol, &xvert[3 * v], &u, gu);
+    zd[first[v]] = u;
+  }
+  /* edges (dhpedgeH): tangential H1-seminorm projection of u - u_vertex */
+  for (int e = 0; e < 12; ++e) {
+    const int n = nd[8 + e];
+    if (!bcflag[8 + e] || n == 0) continue;
+    int32_t no1[19];
+    for (int i = 0; i < 12; ++i) no1[i] = 1;
+    for (int i = 12; i < 18; ++i) no1[i] = 11;
+    no1[18] = 111;
+    no1[e] = norder[e];
+    int nint = imin(norder[e] + 1, ORC_MAXP) + 1; /* set_1Dint, INTEGRATION = 1 */
+    double xg[16], wg[16];
+    orc_gauss1d(nint, xg, wg);
+    double A[64], b[8];
+    for (int i = 0; i < n * n; ++i) A[i] = 0.0;
+    for (int i = 0; i < n; ++i) b[i] = 0.0;
+    const double *x1 = BRICK_XI[BRICK_E2V[e][0]], *x2 = BRICK_XI[BRICK_E2V[e][1]];
+    for (int l = 0; l < nint; ++l) {
+      double xi[3], dxidt[3];
+      for (int c = 0; c < 3; ++c) { dxidt[c] = x2[c] - x1[c]; xi[c] = x1[c] + xg[l] * dxidt[c]; }
+      int nr = orc_shape3DH_hexa(xi, no1, nori_edge, nori_face, shap, grad);
+      double bjac = sqrt(dxidt[0] * dxidt[0] + dxidt[1] * dxidt[1] + dxidt[2] * dxidt[2]);
+      double rt[3] = {dxidt[0] / bjac, dxidt[1] / bjac, dxidt[2] / bjac};
+      const double w = wg[l] * bjac;
+      double x[3], J[3][3];
+      trilin(xvert, xi, x, J);
+      double u, gu[3];
+      orc_exact(isol, x, &u, gu);
+      double du[3];
+      for (int i = 0; i < 3; ++i) du[i] = gu[0] * J[0][i] + gu[1] * J[1][i] + gu[2] * J[2][i];
+      const int nlow = nr - n;
+      for (int k = 0; k < nlow; ++k)
+        for (int i = 0; i < 3; ++i) du[i] -= zd[k] * grad[3 * k + i];
+      for (int j = 0; j < n; ++j) {
+        const double *gj = &grad[3 * (nlow + j)];
+        double pr = gj[0] * rt[0] + gj[1] * rt[1] + gj[2] * rt[2];
+        double dv[3] = {pr * rt[0], pr * rt[1], pr * rt[2]};
+        b[j] += (du[0] * dv[0] + du[1] * dv[1] + du[2] * dv[2]) * w;
+        for (int i = 0; i < n; ++i) {
+          const double *gi = &grad[3 * (nlow + i)];
+          A[j + n * i] += (dv[0] * gi[0] + dv[1] * gi[1] + dv[2] * gi[2]) * w;
+        }
+      }
+    }
+    if (lu_solve(n, A, b)) return -1;
+    for (int j = 0; j < n; ++j) zd[first[8 + e] + j] = b[j];
+  }
+  /* faces (dhpfaceH): tangential H1-seminorm projection of u - u_vertex - u_edges */
+  for (int f = 0; f < 6; ++f) {
+    const int n = nd[20 + f];
+    if (!bcflag[20 + f] || n == 0) continue;
+    int32_t no1[19];
+    for (int i = 0; i < 12; ++i) no1[i] = norder[i];
+    for (int i = 12; i < 18; ++i) no1[i] = 11;
+    no1[18] = 111;
+    no1[12 + f] = norder[12 + f];
+    int hv[2];
+    decod(norder[12 + f], 10, 2, hv);
+    const int *fe = BRICK_F2E[f];
+    int nx = imin(imax(imax(norder[fe[0]], norder[fe[2]]), hv[0]) + 1, ORC_MAXP) + 1;
+    int ny = imin(imax(imax(norder[fe[1]], norder[fe[3]]), hv[1]) + 1, ORC_MAXP) + 1;
+    double xa[16], wa[16], xb[16], wb[16];
+    orc_gauss1d(nx, xa, wa);
+    orc_gauss1d(ny, xb, wb);
+    double *A = (double *)calloc((size_t)n * n, sizeof(double));
+    double *b = (double *)calloc((size_t)n, sizeof(double));
+    const double *v1 = BRICK_XI[BRICK_F2V[f][0]], *v2 = BRICK_XI[BRICK_F2V[f][1]],
+                 *v3 = BRICK_XI[BRICK_F2V[f][3]];
+    const double nsign = (f == 0 || f == 4 || f == 5) ? -1.0 : 1.0;
+    for (int l2 = 0; l2 < ny; ++l2)
+      for (int l1 = 0; l1 < nx; ++l1) {
+        double xi[3], t1[3], t2[3];
+        for (int c = 0; c < 3; ++c) {
+          t1[c] = v2[c] - v1[c];
+          t2[c] = v3[c] - v1[c];
+          xi[c] = v1[c] + xa[l1] * t1[c] + xb[l2] * t2[c];
+        }
+        int nr = orc_shape3DH_hexa(xi, no1, nori_edge, nori_face, shap, grad);
+        double rn[3] = {t1[1] * t2[2] - t1[2] * t2[1], t1[2] * t2[0] - t1[0] * t2[2],
+                        t1[0] * t2[1] - t1[1] * t2[0]};
+        double bjac = sqrt(rn[0] * rn[0] + rn[1] * rn[1] + rn[2] * rn[2]);
+        for (int c = 0; c < 3; ++c) rn[c] = rn[c] * nsign / bjac;
+        const double w = wa[l1] * wb[l2] * bjac;
+        double x[3], J[3][3];
+        trilin(xvert, xi, x, J);
+        double u, gu[3];
+        orc_exact(isol, x, &u, gu);
+        double du[3];
+        for (int i = 0; i < 3; ++i) du[i] = gu[0] * J[0][i] + gu[1] * J[1][i] + gu[2] * J[2][i];
+        const int nlow = nr - n;
+        for (int k = 0; k < nlow; ++k)
+          for (int i = 0; i < 3; ++i) du[i] -= zd[k] * grad[3 * k + i];
+        for (int j = 0; j < n; ++j) {
+          const double *gj = &grad[3 * (nlow + j)];
+          double pr = gj[0] * rn[0] + gj[1] * rn[1] + gj[2] * rn[2];
+          double dv[3] = {gj[0] - pr * rn[0], gj[1] - pr * rn[1], gj[2] - pr * rn[2]};
+          b[j] += (du[0] * dv[0] + du[1] * dv[1] + du[2] * dv[2]) * w;
+          for (int i = 0; i < n; ++i) {
+            const double *gi = &grad[3 * (nlow + i)];
+            A[j + n * i] += (dv[0] * gi[0] + dv[1] * gi[1] + dv[2] * gi[2]) * w;
+          }
+        }
+      }
+    int rc = lu_solve(n, A, b);
+    if (!rc)
+      for (int j = 0; j < n; ++j) zd[first[20 + f] + j] = b[j];
+    free(A);
+    free(b);
+    if (rc) return -1;
+  }
+  return first[26];
+}
+
+/* ------------------------------------------------------------------------ */
 /* Helpers shared with hp3d_oracle_dpg.c (hp3d_oracle_int.h)                  */
 /* ------------------------------------------------------------------------ */
 void orc_i_decod(int nick, int mod, int n, int *arr) { decod(nick, mod, n, arr); }

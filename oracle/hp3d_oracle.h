@@ -149,6 +149,16 @@ int orc_celem_compress_nodes(int nn, const int32_t *nd, const int32_t *bcflag,
 int orc_constrain(int ni, const double *aii, const double *bi, int ncoef, const int32_t *ck,
                   const int32_t *cl, const double *cv, int nmod, double *amod, double *bmod);
 
+/* update_Ddof for one hexahedron whose geometry block is the element itself
+ * (eta = xi; x(eta) trilinear in the vertices): Dirichlet values of the
+ * nodes with bcflag set, per interface dof in element order (zeros
+ * elsewhere) -- vertex values (dhpvert.F90), then the tangential
+ * H1-seminorm projections on edges (edge/dhpedgeH.F90) and faces
+ * (face/dhpfaceH.F90) of what the lower-order part leaves.  Returns the
+ * number of interface dof, or -1. */
+int orc_dirichlet_hexa(const int32_t *norder, const int32_t *nori_edge, const int32_t *nori_face,
+                       const double *xvert, const int32_t *bcflag, int isol, double *zd);
+
 /* mumps_sc STEP 1 offsets + STEP 2 connectivities
  * (solver/omp_mumps/mumps_sc.F90:102-188, 266-299).
  * nodes: nelem x nnode_max global node ids (element node order),

@@ -74,6 +74,7 @@ def lib():
                                                _i32p, _f64p, _f64p, _i32p]
         L.orc_constrain.argtypes = [ctypes.c_int, _f64p, _f64p, ctypes.c_int, _i32p, _i32p,
                                     _f64p, ctypes.c_int, _f64p, _f64p]
+        L.orc_dirichlet_hexa.argtypes = [_i32p, _i32p, _i32p, _f64p, _i32p, ctypes.c_int, _f64p]
         L.orc_nrdofE_hexa.argtypes = [_i32p]
         L.orc_shape3DE_hexa.argtypes = [_f64p, _i32p, _i32p, _i32p, _f64p, _f64p]
         L.orc_shape3DQ_hexa.argtypes = [_f64p, _i32p, _f64p]
@@ -484,3 +485,14 @@ def celem_compress_nodes(nd, bcflag, amod, bmod, zdofd=None):
                                         _p(zd, _f64p), _p(nx, _i32p), _p(zb, _f64p),
                                         _p(zs, _f64p), _p(ndofm, _i32p))
     return nx[:nc].copy(), zb[:nc].copy(), zs[: nc * nc].reshape(nc, nc).copy(), ndofm
+
+
+def dirichlet_hexa(norder, nori_edge, nori_face, xvert, bcflag, isol):
+    """update_Ddof restated for one hexahedron: Dirichlet values per interface
+    dof (element order)."""
+    zd = np.zeros(400)
+    n = lib().orc_dirichlet_hexa(_p(_i32(norder), _i32p), _p(_i32(nori_edge), _i32p),
+                                 _p(_i32(nori_face), _i32p), _p(_f64(np.asarray(xvert)[:8]), _f64p),
+                                 _p(_i32(np.asarray(bcflag)[:26]), _i32p), isol, _p(zd, _f64p))
+    assert n >= 0
+    return zd[:n].copy()
