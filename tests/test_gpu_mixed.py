@@ -87,3 +87,25 @@ def test_mixed_radix_digits_options():
                      m["kappa"][0], isol=10, integration=0)
     Kg, _ = ep.elem(0, K.shape[0])
     assert _rel(Kg, K) < 5e-12  # radix 6 x 7 digits carries ~42 bits
+
+
+def test_mixed_final_solution_at_the_fp64_floor():
+    """On 6^3 p=5 (kappa in [1e-2, 1e2]) the global conditioning amplifies
+    element rounding to ~5e-10 in the final solution: the FP64 GPU pass and
+    the FP64 CPU oracle already differ by that much.  The mixed pass must
+    stay within twice that FP64-to-FP64 difference of the FP64 pass."""
+    m = M.structured_hexa(6, 5, perturb=0.15, kappa_logrange=(-2, 2), seed=7)
+    sols = {}
+    for prec in (H.FP64, H.MIXED):
+        ep = H.ElementPass(prec, integration=1, isol=10)
+        ep.submit(m)
+        ep.run(); ep.download()
+        _, _, _, dofs = FH.solve_and_error(m, _gpu_elements(ep, m), 10)
+        sols[prec] = np.concatenate(dofs)
+        ep.close()
+    orc = FH.oracle_element_outputs(m, 10, integration=1, stc_method=1)
+    _, _, _, dofs = FH.solve_and_error(m, orc, 10)
+    cpu = np.concatenate(dofs)
+    floor = np.linalg.norm(sols[H.FP64] - cpu) / np.linalg.norm(cpu)
+    rel = np.linalg.norm(sols[H.MIXED] - sols[H.FP64]) / np.linalg.norm(sols[H.FP64])
+    assert rel <= max(1e-10, 2.0 * floor), (rel, floor)
