@@ -112,12 +112,18 @@ int hp3dg_dpg_begin(const hp3dg_dpg_opts* opts, hp3dg_dpg_ctx** out) {
   if (!opts || !out) return HP3DG_ERR_ARG;
   if (opts->nord_add < 1 || opts->ibcflag < 0 || opts->ibcflag > 2 || opts->ibcflag == 1 ||
       opts->isol < 0 || opts->isol > 2 || opts->icomp < 1 || opts->icomp > 3 ||
-      !(opts->omega > 0.0) || !(opts->mu > 0.0))
+      !(opts->omega > 0.0) || !(opts->mu > 0.0) ||
+      (opts->precision != HP3DG_FP64 && opts->precision != HP3DG_MIXED))
     return HP3DG_ERR_ARG;
   auto* c = new hp3dg_dpg_ctx;
   c->opts = *opts;
   c->device = opts->device;
   if (cudaSetDevice(c->device) != cudaSuccess) { delete c; return HP3DG_ERR_CUDA; }
+  if (opts->precision == HP3DG_MIXED) {
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess) { delete c; return HP3DG_ERR_CUDA; }
+    if (prop.major != 10) { delete c; return HP3DG_ERR_UNSUPPORTED; }  // tcgen05 needs sm_10x
+  }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return HP3DG_ERR_CUDA;
@@ -265,6 +271,14 @@ int hp3dg_dpg_submit(hp3dg_dpg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   w.S = dalloc<double>(c, ne * 2 * nt * n1, &err);
   w.Z = dalloc<double>(c, ne * 2 * n1 * n1, &err);
   if (c->opts.keep_elem) c->d_zkeep = dalloc<double>(c, ne * 2 * n1 * n1, &err);
+  w.tc = c->opts.precision == HP3DG_MIXED;
+  if (w.tc) {
+    const int rmax = (int)std::max(nt, n1);
+    w.tb.a = dalloc<uint8_t>(c, ne * dpg_tc_a_bytes(rmax), &err);
+    w.tb.b = dalloc<uint8_t>(c, ne * dpg_tc_b_bytes(rmax), &err);
+    w.tb.ea = dalloc<int>(c, ne * dpg_tc_ex_slots(rmax), &err);
+    w.tb.eb = dalloc<int>(c, ne * dpg_tc_ex_slots(rmax), &err);
+  }
   c->d_xvert = dalloc<double>(c, xv.size(), &err);
   c->d_eps = dalloc<double>(c, ep.size(), &err);
   c->d_imp = dalloc<int>(c, ne, &err);
@@ -367,6 +381,7 @@ int hp3dg_dpg_sync(hp3dg_dpg_ctx* c) {
   c->last_bad = -1;
   if (fl[0] != NONE) { c->last_bad = fl[0]; return HP3DG_ERR_NEG_JACOBIAN; }
   if (fl[1] != NONE) { c->last_bad = fl[1]; return HP3DG_ERR_NOT_SPD; }
+  if (fl[2] != NONE) return HP3DG_ERR_TIMEOUT;  // a bounded wait of a tensor-core kernel gave up
   return HP3DG_OK;
 }
 

@@ -184,15 +184,28 @@ struct DpgTables {
   double *fs = nullptr, *fscratch = nullptr, *ft = nullptr;  // faces: test values, traces
   double* it = nullptr;                                   // impedance points: traces
 };
+struct DpgTcBufs {
+  uint8_t *a = nullptr, *b = nullptr;  // digit operands (per element dpg_tc_a_bytes / _b_bytes)
+  int *ea = nullptr, *eb = nullptr;    // row exponents (per element dpg_tc_ex_slots)
+};
 struct DpgWork {
   const double *xiV, *wV, *xiF, *wF, *xiI, *wI;
   double *gV, *gF, *gI;            // per element point data
   double *MFF, *MCC, *MFC;         // real Gram parts (MFC per bin)
   double *P, *R, *T, *load;        // real coupling blocks, complex load
   double *G, *S, *Z;               // complex: Gram, [B|l] -> X, DPG matrix (nr+1)^2
+  bool tc = false;                 // dense algebra on tensor cores
+  DpgTcBufs tb;
 };
 void launch_dpg_tables(const DpgDims& d, const double* xiV, const double* wV, const double* xiF,
                        const double* xiI, const DpgTables& t, double* mfc, cudaStream_t st);
+// the dense DPG algebra on tensor cores -- k_dpg_tc.cu
+size_t dpg_tc_ex_slots(int rows);
+size_t dpg_tc_a_bytes(int rows);
+size_t dpg_tc_b_bytes(int rows);
+int launch_dpg_solve_tc(int nel, int nt, int n1, double* G, double* S, double* Z,
+                        const DpgTcBufs& tb, int* bad, int* err, cudaStream_t st);
+
 // stage 0: geometry, real contractions, assembly of G and [B|l];
 // 1: Cholesky of G, forward solve, Z = X^H X, impedance penalty;
 // 2: condensation of the L2 fields and compression

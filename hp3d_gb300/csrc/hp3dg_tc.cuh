@@ -128,4 +128,63 @@ __device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t* r) {
       : "r"(taddr));
 }
 
+// ---------------------------------------------------------------------------
+// split-BF16 digit operands
+// ---------------------------------------------------------------------------
+// exponent e with max |v| = m 2^e, m in [0.5, 1), from the largest magnitude
+// bit pattern (magnitudes of finite doubles order like their bits); 0 for 0
+__device__ __forceinline__ int row_exponent(unsigned long long maxbits) {
+  return maxbits ? (int)(maxbits >> 52) - 1022 : 0;
+}
+__device__ __forceinline__ unsigned long long mag_bits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+}
+
+// X = round(v 2^(radix*digits - e)) for |v| < 2^e, as an integer, from the bits
+__device__ __forceinline__ long long fixed_of(double v, int e, int fbits) {
+  const long long bits = __double_as_longlong(v);
+  const int E = (int)((bits >> 52) & 0x7ff);
+  if (E == 0) return 0;
+  const long long M = (bits & 0xfffffffffffffLL) | (1LL << 52);
+  const int sh = E - 1075 - e + fbits;
+  long long x = 0;
+  if (sh >= 0) x = M << sh;
+  else if (sh > -54) x = (M + (1LL << (-sh - 1))) >> (-sh);
+  return bits < 0 ? -x : x;
+}
+
+// balanced radix-2^R digits of 8 fixed-point integers, written as one
+// 16-byte core-matrix row per digit (least significant digit first)
+__device__ __forceinline__ void store_digits8(long long* X, int R, int D, uint8_t* dst,
+                                              size_t digit_stride) {
+  const long long half = 1LL << (R - 1);
+  for (int dg = D - 1; dg >= 0; --dg) {
+    uint32_t h[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      long long d;
+      if (dg > 0) {
+        const long long q = (X[t] + half) >> R;
+        d = X[t] - (q << R);
+        X[t] = q;
+      } else {
+        d = X[t];
+      }
+      h[t] = __float_as_uint((float)(int)d) >> 16;  // exact in BF16
+    }
+    uint4 w;
+    w.x = h[0] | (h[1] << 16);
+    w.y = h[2] | (h[3] << 16);
+    w.z = h[4] | (h[5] << 16);
+    w.w = h[6] | (h[7] << 16);
+    *(uint4*)(dst + (size_t)dg * digit_stride) = w;
+  }
+}
+
+// byte offset of (row, 8-wide K group g) in a canonical tile set with `nrows` rows
+__host__ __device__ __forceinline__ size_t tile_off(int row, int g, int nrows) {
+  return (size_t)(g >> 1) * nrows * 32 + (size_t)(row >> 3) * 256 + (size_t)(g & 1) * 128 +
+         (size_t)(row & 7) * 16;
+}
+
 }  // namespace hp3dg

@@ -361,17 +361,18 @@ class DpgOpts(ctypes.Structure):
                 ("nord_add", ctypes.c_int32), ("isol", ctypes.c_int32),
                 ("icomp", ctypes.c_int32), ("device", ctypes.c_int32),
                 ("timing", ctypes.c_int32), ("keep_elem", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("precision", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 class DPGPass:
     """One batch of the DPG Maxwell element pass (a context of the C ABI)."""
 
     def __init__(self, omega=2 * np.pi, mu=1.0, epsilon=1.0, gamma=1.0, alpha=1.0, ibcflag=0,
-                 nord_add=1, isol=1, icomp=1, device=0, timing=False, keep_elem=False):
+                 nord_add=1, isol=1, icomp=1, device=0, timing=False, keep_elem=False,
+                 precision=FP64):
         self.L = lib()
         o = DpgOpts(omega, mu, epsilon, gamma, alpha, ibcflag, nord_add, isol, icomp, device,
-                    int(timing), int(keep_elem))
+                    int(timing), int(keep_elem), precision)
         self.ctx = _vp()
         self._check(self.L.hp3dg_dpg_begin(ctypes.byref(o), ctypes.byref(self.ctx)), "begin")
         self.nel = 0

@@ -339,7 +339,10 @@ typedef struct hp3dg_dpg_opts {
   int32_t device;
   int32_t timing;    /* record phase times */
   int32_t keep_elem; /* keep the uncondensed DPG element matrices (hp3dg_dpg_get_elem) */
-  int32_t reserved[5];
+  int32_t precision; /* HP3DG_FP64: the dense algebra in FP64; HP3DG_MIXED: the Cholesky
+                        trailing updates, the solve's block updates and X^H X on tensor
+                        cores from split-BF16 digits (FP64 diagonal blocks) */
+  int32_t reserved[4];
 } hp3dg_dpg_opts;
 
 int hp3dg_dpg_begin(const hp3dg_dpg_opts *opts, hp3dg_dpg_ctx **ctx);

@@ -122,3 +122,44 @@ def test_rejects_anisotropic_or_mixed_orders():
     with pytest.raises(H.HP3DGError):
         ep.submit(m2, np.ones(1, complex), np.zeros((1, 26), np.int32))
     ep.close()
+
+
+@pytest.mark.parametrize("p,imp_planes", [(1, ()), (2, ((0, 1),)), (3, ())])
+def test_tensor_core_dense_algebra_matches_oracle(p, imp_planes):
+    """precision = MIXED: the Gram Cholesky's trailing updates, the solve's
+    block updates and X^H X on tensor cores from split-BF16 digits (FP64
+    diagonal blocks); element matrices and condensed systems within 1e-10 of
+    the FP64 oracle."""
+    m, prm, eps, bc, imp, flags = _setup(2, p, imp_planes)
+    ep = H.DPGPass(omega=prm.omega, ibcflag=prm.ibcflag, isol=prm.isol, keep_elem=True,
+                   precision=H.MIXED)
+    ep.submit(m, eps, flags)
+    ep.run(); ep.download()
+    cond, schur, ni_e = D.oracle_condense(m, prm, eps, bc, imp)
+    for e in range(m["nelem"]):
+        A, b, rc = O.dpg_elem(m["norder"][e], m["nori_edge"][e], m["nori_face"][e],
+                              m["xvert"][e], eps[e], int(imp[e]), prm)
+        Ag, bg = ep.elem(e)
+        assert _rel(Ag, A) < 1e-10 and _rel(bg, b) < 1e-10, (e, _rel(Ag, A), _rel(bg, b))
+        zb, zs = ep.condensed(e)
+        assert _rel(zs, cond[e][2]) < 1e-10 and _rel(zb, cond[e][1]) < 1e-10, e
+    ep.close()
+
+
+def test_tensor_core_polynomial_solution():
+    m, prm, eps, bc, imp, flags = _setup(2, 3, ((0, 1),), isol=2)
+    ep = H.DPGPass(omega=prm.omega, ibcflag=prm.ibcflag, isol=prm.isol, precision=H.MIXED)
+    ep.submit(m, eps, flags)
+    ep.run(); ep.download()
+    ntrial, ni, nb = ep.sizes()
+    cond, schur = [], []
+    for e in range(m["nelem"]):
+        zb, zs = ep.condensed(e)
+        nx, _, _, ndofm = O.celem_compress_z(m["norder"][e], bc[e], np.eye(ni, dtype=complex),
+                                             np.zeros(ni, complex))
+        cond.append((nx, zb, zs, ndofm))
+        schur.append(ep.schur(e))
+    u, lcon, lcon_off, _ = D.solve_condensed(m, cond, m["nnodes"])
+    ee, eh = D.field_errors(m, prm, eps, cond, schur, u, lcon, lcon_off, [ni] * m["nelem"])
+    assert ee < 1e-10 and eh < 1e-10, (ee, eh)
+    ep.close()
