@@ -215,7 +215,7 @@ def run_dpg(args, rank, world):
     prm = O.maxw_params(isol=1, ibcflag=2)
     cfg = {"workload": f"ultraweak_dpg_maxwell_hexa_{n}^3_p3_impedance", "elements_per_gpu": ne,
            "p": 3, "test_order": 4, "quadrature_points": 125, "omega": "2 pi",
-           "eps_r": "U[1,4](1 - i U[0,0.1])", "precision": "fp64",
+           "eps_r": "U[1,4](1 - i U[0,0.1])", "precision": args.precision,
            "parallelism": f"replicas{world}" if world > 1 else "single",
            "l2": "working set per step > L2 (Gram matrices 5.8 GB), no flush needed"}
     s = O.dpg_sizes([3] * 12 + [33] * 6 + [333])
@@ -267,7 +267,8 @@ def run_dpg(args, rank, world):
     from hp3d_gb300 import build as B
     B.build()
     from hp3d_gb300 import hp3dg as H
-    ep = H.DPGPass(omega=prm.omega, ibcflag=2, isol=1, timing=True, device=local)
+    dprec = H.MIXED if args.precision == "mixed" else H.FP64
+    ep = H.DPGPass(omega=prm.omega, ibcflag=2, isol=1, timing=True, device=local, precision=dprec)
     ep.submit(mesh, eps, flags)
     for _ in range(args.warmup):
         ep.run(); ep.sync()
@@ -301,12 +302,24 @@ def run_dpg(args, rank, world):
     t_la = (med[1] + med[2]) / 1000.0
     hbm, bf16, peak_kind = measured_peaks()
     achieved = ne * fl_el / t_la / 1e12 if t_la > 0 else None
-    roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
-            "frac": achieved / 1.25 if achieved else None, "traffic": None,
-            "kernel": "k_dpg_dpg + k_dpg_condense",
-            "note": "dense DPG algebra (Gram Cholesky, forward solve of [B|l], X^H X, L2-field "
-                    "condensation) per element over the two kernels' time; peak = nominal GB300 "
-                    "FP64 (not in the measured peaks)"}
+    if dprec == H.FP64:
+        roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
+                "frac": achieved / 1.25 if achieved else None, "traffic": None,
+                "kernel": "k_dpg_dpg + k_dpg_condense",
+                "note": "dense DPG algebra (Gram Cholesky, forward solve of [B|l], X^H X, L2-field "
+                        "condensation) per element over the two kernels' time; peak = nominal "
+                        "GB300 FP64 (not in the measured peaks)"}
+    else:
+        # tensor work: 28 digit pairs x 2 real products of K = 128 per complex update
+        # (4 real MACs per complex MAC); the algorithmic count is the complex FLOPs
+        tens = fl_el * 28 / 2.0 * 2.0
+        ach = ne * tens / t_la / 1e12 if t_la > 0 else None
+        roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
+                "frac": ach / bf16 if ach else None, "traffic": None,
+                "kernel": "k_zupd + FP64 diagonal blocks + k_dpg_condense",
+                "note": f"BF16 digit-pair MMA work of the dense DPG algebra (28 pairs of the "
+                        f"complex FLOP count) over the stage's time; peak {peak_kind}; the "
+                        f"complex-FP64-equivalent rate is {ne * fl_el / t_la / 1e12:.3f} TFLOP/s"}
     cb = cpu(args.cpu_seconds) if (rank == 0 and not args.no_cpu_baseline) else None
     line = {"metric": DPG_METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,

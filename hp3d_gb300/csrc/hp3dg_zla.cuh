@@ -127,13 +127,16 @@ static __device__ int cta_zpotrf(double2* A, int lda, int n, double2* sm) {
       const int i = x % kb, j = x / kb;
       if (i >= j) A[(k0 + i) + (size_t)(k0 + j) * lda] = D[i * (NB + 1) + j];
     }
-    // panel rows below: x L11^H = a
+    // panel rows below: x L11^H = a (reciprocals of the diagonal: one division each)
+    __shared__ double rdg[NB];
+    if (threadIdx.x < kb) rdg[threadIdx.x] = 1.0 / D[threadIdx.x * (NB + 1) + threadIdx.x].x;
+    __syncthreads();
     for (int r = k0 + kb + threadIdx.x; r < n; r += LA_THREADS) {
       double2 x[NB];
       for (int j = 0; j < kb; ++j) {
         double2 t = A[r + (size_t)(k0 + j) * lda];
         for (int q = 0; q < j; ++q) t = zsub(t, zmul(x[q], zconj(D[j * (NB + 1) + q])));
-        x[j] = zscale(1.0 / D[j * (NB + 1) + j].x, t);
+        x[j] = zscale(rdg[j], t);
       }
       for (int j = 0; j < kb; ++j) A[r + (size_t)(k0 + j) * lda] = x[j];
     }
@@ -158,13 +161,15 @@ static __device__ void cta_ztrsm_fwd(const double2* L, int ldl, int n, double2* 
       const int i = x % kb, j = x / kb;
       if (i >= j) D[i * (NB + 1) + j] = L[(k0 + i) + (size_t)(k0 + j) * ldl];
     }
+    __shared__ double rdf[NB];
+    if (threadIdx.x < kb) rdf[threadIdx.x] = 1.0 / L[(k0 + threadIdx.x) + (size_t)(k0 + threadIdx.x) * ldl].x;
     __syncthreads();
     for (int c = threadIdx.x; c < m; c += LA_THREADS) {
       double2 x[NB];
       for (int i = 0; i < kb; ++i) {
         double2 t = X[(k0 + i) + (size_t)c * ldx];
         for (int q = 0; q < i; ++q) t = zsub(t, zmul(D[i * (NB + 1) + q], x[q]));
-        x[i] = zscale(1.0 / D[i * (NB + 1) + i].x, t);
+        x[i] = zscale(rdf[i], t);
       }
       for (int i = 0; i < kb; ++i) X[(k0 + i) + (size_t)c * ldx] = x[i];
     }
@@ -187,6 +192,8 @@ static __device__ void cta_ztrsm_bwd(const double2* L, int ldl, int n, double2* 
       const int i = x % kb, j = x / kb;
       if (i >= j) D[i * (NB + 1) + j] = L[(k0 + i) + (size_t)(k0 + j) * ldl];
     }
+    __shared__ double rdb[NB];
+    if (threadIdx.x < kb) rdb[threadIdx.x] = 1.0 / L[(k0 + threadIdx.x) + (size_t)(k0 + threadIdx.x) * ldl].x;
     __syncthreads();
     // L11^H x = b: x_j = (b_j - sum_{t>j} conj(L11[t][j]) x_t) / L11[j][j]
     for (int c = threadIdx.x; c < m; c += LA_THREADS) {
@@ -194,7 +201,7 @@ static __device__ void cta_ztrsm_bwd(const double2* L, int ldl, int n, double2* 
       for (int j = kb - 1; j >= 0; --j) {
         double2 t = X[(k0 + j) + (size_t)c * ldx];
         for (int q = j + 1; q < kb; ++q) t = zsub(t, zmul(zconj(D[q * (NB + 1) + j]), x[q]));
-        x[j] = zscale(1.0 / D[j * (NB + 1) + j].x, t);
+        x[j] = zscale(rdb[j], t);
       }
       for (int j = 0; j < kb; ++j) X[(k0 + j) + (size_t)c * ldx] = x[j];
     }

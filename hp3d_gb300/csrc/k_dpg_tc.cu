@@ -217,22 +217,27 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
     const int ea = (i < a.m) ? a.ea[(int64_t)e * a.ea_estride + i] : 0;
     double2* C = a.C + (int64_t)e * a.c_estride;
     for (int cg = 0; cg < ZN / 8; ++cg) {
-      double v[2][8];
+      // exact recombination in integers: levels L = 0..3 (weights 2^7(3-L)) and
+      // L = 4..6 (weights 2^7(6-L)) as two 64-bit sums (below 2^45 / 2^38),
+      // then one FP64 fma per part: v = hi 2^-35 + lo 2^-56
+      long long hi[2][8], lo[2][8];
 #pragma unroll
       for (int part = 0; part < 2; ++part)
 #pragma unroll
-        for (int c = 0; c < 8; ++c) v[part][c] = 0.0;
-      // levels from the least significant up: L = p + q (0-based), weight 2^-7(L+2)
-      for (int L = ZD - 1; L >= 0; --L) {
+        for (int c = 0; c < 8; ++c) hi[part][c] = lo[part][c] = 0;
+#pragma unroll
+      for (int L = 0; L < ZD; ++L) {
         uint32_t r0[8], r1[8];
         tmem_ld8_nowait(tl + (uint32_t)((L * 2 + 0) * ZN + cg * 8), r0);
         tmem_ld8_nowait(tl + (uint32_t)((L * 2 + 1) * ZN + cg * 8), r1);
         tmem_wait();
-        const double w = __longlong_as_double((long long)(1023 - ZR * (L + 2)) << 52);
+        const int sh = ZR * ((L < 4 ? 3 : 6) - L);
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-          v[0][c] = fma((double)__uint_as_float(r0[c]), w, v[0][c]);
-          v[1][c] = fma((double)__uint_as_float(r1[c]), w, v[1][c]);
+          const long long a0 = (long long)__float2int_rn(__uint_as_float(r0[c])) << sh;
+          const long long a1 = (long long)__float2int_rn(__uint_as_float(r1[c])) << sh;
+          if (L < 4) { hi[0][c] += a0; hi[1][c] += a1; }
+          else { lo[0][c] += a0; lo[1][c] += a1; }
         }
       }
       if (!okw || i >= a.m) continue;
@@ -241,10 +246,20 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
         const int j = ct * ZN + cg * 8 + c;
         if (j >= a.n || (a.lower && j > i)) continue;
         const int sx = ea + a.eb[(int64_t)e * a.eb_estride + j];
+        // 2^(sx - 35) and 2^(sx - 56) from the bits, with the sign of the update
+        const double sh1 = a.sgn * __longlong_as_double((long long)(1023 + sx - 5 * ZR) << 52);
+        const double sh2 = a.sgn * __longlong_as_double((long long)(1023 + sx - 8 * ZR) << 52);
         double2* cp = &C[i + (int64_t)j * a.ldc];
         double2 cv = *cp;
-        cv.x = fma(a.sgn, ldexp(v[0][c], sx), cv.x);
-        cv.y = fma(a.sgn, ldexp(v[1][c], sx), cv.y);
+        if (sx > -960 && sx < 960) {
+          cv.x = fma(__ll2double_rn(hi[0][c]), sh1, fma(__ll2double_rn(lo[0][c]), sh2, cv.x));
+          cv.y = fma(__ll2double_rn(hi[1][c]), sh1, fma(__ll2double_rn(lo[1][c]), sh2, cv.y));
+        } else {  // scales outside the normal range of the bit-built powers
+          cv.x += a.sgn * (ldexp(__ll2double_rn(hi[0][c]), sx - 5 * ZR) +
+                           ldexp(__ll2double_rn(lo[0][c]), sx - 8 * ZR));
+          cv.y += a.sgn * (ldexp(__ll2double_rn(hi[1][c]), sx - 5 * ZR) +
+                           ldexp(__ll2double_rn(lo[1][c]), sx - 8 * ZR));
+        }
         *cp = cv;
       }
     }
@@ -259,7 +274,7 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
 
 // FP64 diagonal step of the Cholesky: L11 of the 64-wide block at k0 and the
 // panel below it, x L11^H = a for every row (two 32-column halves)
-constexpr size_t ZP_SMEM = (2 * TK * TM + 64 * 65) * sizeof(double2);
+constexpr size_t ZP_SMEM = (2 * TK * TM + 64 * 65) * sizeof(double2) + 64 * sizeof(double);
 #define LSM(i, j) Ls[(i) * 65 + (j)]
 
 __global__ void __launch_bounds__(LA_THREADS) k_zpanel(double2* G, int64_t estride, int n, int k0,
@@ -271,9 +286,11 @@ __global__ void __launch_bounds__(LA_THREADS) k_zpanel(double2* G, int64_t estri
   double2* A = G + (int64_t)e * estride;
   double2* D = A + k0 + (int64_t)k0 * n;
   if (cta_zpotrf(D, n, kb, sm) && threadIdx.x == 0) atomicMin(bad, e);
+  double* rd = (double*)(Ls + 64 * 65);  // reciprocals of the diagonal
   for (int x = threadIdx.x; x < kb * kb; x += LA_THREADS) {
     const int i = x % kb, j = x / kb;
     LSM(i, j) = i >= j ? D[i + (int64_t)j * n] : make_double2(0.0, 0.0);
+    if (i == j) rd[i] = 1.0 / D[i + (int64_t)i * n].x;
   }
   __syncthreads();
   const int h1 = kb < 32 ? kb : 32;
@@ -282,7 +299,7 @@ __global__ void __launch_bounds__(LA_THREADS) k_zpanel(double2* G, int64_t estri
     for (int j = 0; j < h1; ++j) {
       double2 t = A[r + (int64_t)(k0 + j) * n];
       for (int q = 0; q < j; ++q) t = zsub(t, zmul(x[q], zconj(LSM(j, q))));
-      x[j] = zscale(1.0 / LSM(j, j).x, t);
+      x[j] = zscale(rd[j], t);
     }
     for (int j = 0; j < h1; ++j) A[r + (int64_t)(k0 + j) * n] = x[j];
     if (kb > 32) {
@@ -291,7 +308,7 @@ __global__ void __launch_bounds__(LA_THREADS) k_zpanel(double2* G, int64_t estri
         double2 t = A[r + (int64_t)(k0 + j) * n];
         for (int q = 0; q < 32; ++q) t = zsub(t, zmul(x[q], zconj(LSM(j, q))));
         for (int q = 32; q < j; ++q) t = zsub(t, zmul(y[q - 32], zconj(LSM(j, q))));
-        y[j - 32] = zscale(1.0 / LSM(j, j).x, t);
+        y[j - 32] = zscale(rd[j], t);
       }
       for (int j = 32; j < kb; ++j) A[r + (int64_t)(k0 + j) * n] = y[j - 32];
     }
@@ -307,9 +324,11 @@ __global__ void __launch_bounds__(LA_THREADS) k_zfsolve(const double2* G, int64_
   const int e = blockIdx.x;
   const double2* A = G + (int64_t)e * gstride;
   double2* X = S + (int64_t)e * sstride;
+  double* rd = (double*)(Ls + 64 * 65);
   for (int x = threadIdx.x; x < kb * kb; x += LA_THREADS) {
     const int i = x % kb, j = x / kb;
     LSM(i, j) = i >= j ? A[(k0 + i) + (int64_t)(k0 + j) * n] : make_double2(0.0, 0.0);
+    if (i == j) rd[i] = 1.0 / A[(k0 + i) + (int64_t)(k0 + i) * n].x;
   }
   __syncthreads();
   const int h1 = kb < 32 ? kb : 32;
@@ -319,7 +338,7 @@ __global__ void __launch_bounds__(LA_THREADS) k_zfsolve(const double2* G, int64_
     for (int i = 0; i < h1; ++i) {
       double2 t = xc[i];
       for (int q = 0; q < i; ++q) t = zsub(t, zmul(LSM(i, q), x[q]));
-      x[i] = zscale(1.0 / LSM(i, i).x, t);
+      x[i] = zscale(rd[i], t);
     }
     for (int i = 0; i < h1; ++i) xc[i] = x[i];
     if (kb > 32) {
@@ -328,7 +347,7 @@ __global__ void __launch_bounds__(LA_THREADS) k_zfsolve(const double2* G, int64_
         double2 t = xc[i];
         for (int q = 0; q < 32; ++q) t = zsub(t, zmul(LSM(i, q), x[q]));
         for (int q = 32; q < i; ++q) t = zsub(t, zmul(LSM(i, q), y[q - 32]));
-        y[i - 32] = zscale(1.0 / LSM(i, i).x, t);
+        y[i - 32] = zscale(rd[i], t);
       }
       for (int i = 32; i < kb; ++i) xc[i] = y[i - 32];
     }
