@@ -267,17 +267,23 @@ int hp3dg_dpg_submit(hp3dg_dpg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   w.R = dalloc<double>(c, ne * d.nEE * 3 * d.nQ, &err);
   w.T = dalloc<double>(c, ne * d.nEE * d.nEi, &err);
   w.load = dalloc<double>(c, ne * 2 * d.nEE, &err);
-  w.G = dalloc<double>(c, ne * 2 * nt * nt, &err);
-  w.S = dalloc<double>(c, ne * 2 * nt * n1, &err);
-  w.Z = dalloc<double>(c, ne * 2 * n1 * n1, &err);
-  if (c->opts.keep_elem) c->d_zkeep = dalloc<double>(c, ne * 2 * n1 * n1, &err);
+  w.G = w.S = w.Z = w.M = w.W = w.Y = nullptr;
+  c->d_zkeep = c->opts.keep_elem ? dalloc<double>(c, ne * 2 * n1 * n1, &err) : nullptr;
   w.tc = c->opts.precision == HP3DG_MIXED;
   if (w.tc) {
-    const int rmax = (int)std::max(nt, n1);
-    w.tb.a = dalloc<uint8_t>(c, ne * dpg_tc_a_bytes(rmax), &err);
-    w.tb.b = dalloc<uint8_t>(c, ne * dpg_tc_b_bytes(rmax), &err);
-    w.tb.ea = dalloc<int>(c, ne * dpg_tc_ex_slots(rmax), &err);
-    w.tb.eb = dalloc<int>(c, ne * dpg_tc_ex_slots(rmax), &err);
+    // augmented matrix (nt + n1)^2, inverse diagonal blocks, ASchur workspace
+    const size_t na = nt + n1, nq = 6 * (size_t)d.nQ;
+    w.M = dalloc<double>(c, ne * 2 * na * na, &err);
+    w.W = dalloc<double>(c, ne * 2 * 4096 * (size_t)dpg_aug_wslots((int)nt, (int)nq), &err);
+    w.Y = dalloc<double>(c, ne * 2 * nq * (n1 - nq), &err);
+    w.tb.a = dalloc<uint8_t>(c, ne * dpg_tc_a_bytes((int)na), &err);
+    w.tb.b = dalloc<uint8_t>(c, ne * dpg_tc_b_bytes((int)na), &err);
+    w.tb.ea = dalloc<int>(c, ne * dpg_tc_ex_slots((int)na), &err);
+    w.tb.eb = dalloc<int>(c, ne * dpg_tc_ex_slots((int)na), &err);
+  } else {
+    w.G = dalloc<double>(c, ne * 2 * nt * nt, &err);
+    w.S = dalloc<double>(c, ne * 2 * nt * n1, &err);
+    w.Z = dalloc<double>(c, ne * 2 * n1 * n1, &err);
   }
   c->d_xvert = dalloc<double>(c, xv.size(), &err);
   c->d_eps = dalloc<double>(c, ep.size(), &err);
@@ -345,12 +351,12 @@ int hp3dg_dpg_run(hp3dg_dpg_ctx* c) {
     launch_dpg_stage(s, c->nel, c->d, c->ph, c->t, c->w, c->d_xvert, c->d_eps, c->d_imp,
                      c->d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
                      c->d_bub_off, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur,
-                     c->d_flags, st);
+                     c->w.tc ? c->d_zkeep : nullptr, c->d_flags, st);
   };
   stage(0);
   cudaEventRecord(c->ev[1], st);
   stage(1);
-  if (c->d_zkeep) {
+  if (c->d_zkeep && !c->w.tc) {
     const size_t n1 = c->d.nr + 1;
     CK(cudaMemcpyAsync(c->d_zkeep, c->w.Z, (size_t)c->nel * 2 * n1 * n1 * 8,
                        cudaMemcpyDeviceToDevice, st));

@@ -196,6 +196,9 @@ struct DpgWork {
   double *G, *S, *Z;               // complex: Gram, [B|l] -> X, DPG matrix (nr+1)^2
   bool tc = false;                 // dense algebra on tensor cores
   DpgTcBufs tb;
+  // tensor-core path: augmented matrix (nt + nr + 1)^2 per element, the
+  // inverse diagonal blocks of the panels (64 x 64 each), ASchur workspace
+  double *M = nullptr, *W = nullptr, *Y = nullptr;
 };
 void launch_dpg_tables(const DpgDims& d, const double* xiV, const double* wV, const double* xiF,
                        const double* xiI, const DpgTables& t, double* mfc, cudaStream_t st);
@@ -203,8 +206,16 @@ void launch_dpg_tables(const DpgDims& d, const double* xiV, const double* wV, co
 size_t dpg_tc_ex_slots(int rows);
 size_t dpg_tc_a_bytes(int rows);
 size_t dpg_tc_b_bytes(int rows);
-int launch_dpg_solve_tc(int nel, int nt, int n1, double* G, double* S, double* Z,
-                        const DpgTcBufs& tb, int* bad, int* err, cudaStream_t st);
+// the augmented partial factorization: part 1 eliminates the test unknowns
+// (trailing block -> Z), 2 the L2 fields (-> Schur complement, ASchur), 3
+// writes Z in the interface order [E | Q | l] (full) to zkeep
+int dpg_aug_wslots(int nt, int nq);
+int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& w, double* zkeep,
+                      int* bad, int* err, cudaStream_t st);
+void launch_dpg_aug_out(int nel, int nt, int n1, int nq, const DpgWork& w, const int* nextract,
+                        const int64_t* lcon_off, const int64_t* elem_nnz,
+                        const int64_t* schur_off, const int64_t* bub_off, double* zastif,
+                        double* zbload, double* aschur, double* bschur, cudaStream_t st);
 
 // stage 0: geometry, real contractions, assembly of G and [B|l];
 // 1: Cholesky of G, forward solve, Z = X^H X, impedance penalty;
@@ -214,6 +225,6 @@ void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
                       const int* imp_mask, const uint32_t* perm, const int* nextract,
                       const int64_t* lcon_off, const int64_t* elem_nnz, const int64_t* schur_off,
                       const int64_t* bub_off, double* zastif, double* zbload, double* aschur,
-                      double* bschur, int* flags, cudaStream_t st);
+                      double* bschur, double* zkeep, int* flags, cudaStream_t st);
 
 }  // namespace hp3dg

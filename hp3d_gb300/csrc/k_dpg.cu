@@ -406,6 +406,12 @@ __global__ void __launch_bounds__(128) k_dpg_bmat(DpgDims d, DpgTables t, const 
 }
 
 // G (lower) and [B | l] in complex FP64 from the real parts.
+// AUG = false: G (nt x nt, lower) and S = [B | l] (nt x (nr+1)), column-major.
+// AUG = true: the lower triangle of the augmented Hermitian matrix
+// [[G, S], [S^H, 0]] (N = nt + nr + 1, column-major) with the trial unknowns
+// in the order [L2 fields | traces | load], for the partial factorization of
+// the tensor-core path; the trailing block starts at zero.
+template <bool AUG>
 __global__ void k_dpg_assemble(DpgDims d, DpgPhys ph, const double* eps, const double* MFF,
                                const double* MCC, const double* MFC, const double* P,
                                const double* R, const double* Tm, const double* load,
@@ -418,7 +424,9 @@ __global__ void k_dpg_assemble(DpgDims d, DpgPhys ph, const double* eps, const d
   const double za2 = za.x * za.x + za.y * za.y, zc2 = zc1.y * zc1.y;
   const double* mff = MFF + (size_t)e * nE * nE;
   const double* mcc = MCC + (size_t)e * nE * nE;
-  double2* g = G + (size_t)e * nt * nt;
+  const int n1 = d.nr + 1, NA = nt + n1;
+  const size_t ldg = AUG ? (size_t)NA : (size_t)nt;
+  double2* g = AUG ? G + (size_t)e * NA * NA : G + (size_t)e * nt * nt;
   const size_t ntot = (size_t)nt * nt;
   for (size_t x = blockIdx.y * blockDim.x + threadIdx.x; x < ntot; x += (size_t)gridDim.y * blockDim.x) {
     const int r = (int)(x % nt), c = (int)(x / nt);
@@ -435,15 +443,22 @@ __global__ void k_dpg_assemble(DpgDims d, DpgPhys ph, const double* eps, const d
       else         // -conj(za) M_FC(k2,k1) + zc1 M_FC(k1,k2)
         v = make_double2(-za.x * f21 + zc1.x * f12, za.y * f21 + zc1.y * f12);
     }
-    g[x] = v;
+    g[r + (size_t)c * ldg] = v;
   }
+  if (AUG)  // trailing block (lower): zero
+    for (size_t x = blockIdx.y * blockDim.x + threadIdx.x; x < (size_t)n1 * n1;
+         x += (size_t)gridDim.y * blockDim.x) {
+      const int r = (int)(x % n1), c = (int)(x / n1);
+      if (r >= c) g[(nt + r) + (size_t)(nt + c) * ldg] = make_double2(0.0, 0.0);
+    }
   const int n3q = 3 * d.nQ;
   const double* pe = P + (size_t)e * nE * n3q;
   const double* re = R + (size_t)e * nE * n3q;
   const double* te = Tm + (size_t)e * nE * d.nEi;
   const uint32_t* pm = perm + (size_t)e * d.nEi;
-  double2* s = S + (size_t)e * nt * (nr + 1);
+  double2* s = AUG ? nullptr : S + (size_t)e * nt * (nr + 1);
   const size_t stot = (size_t)nt * (nr + 1);
+  const int nq = nr - ni;
   for (size_t x = blockIdx.y * blockDim.x + threadIdx.x; x < stot; x += (size_t)gridDim.y * blockDim.x) {
     const int r = (int)(x % nt), c = (int)(x / nt);
     const int k1 = r >> 1, a = r & 1;
@@ -464,7 +479,12 @@ __global__ void k_dpg_assemble(DpgDims d, DpgPhys ph, const double* eps, const d
     } else if (a == 0) {
       v = make_double2(load[2 * ((size_t)e * nE + k1)], load[2 * ((size_t)e * nE + k1) + 1]);
     }
-    s[x] = v;
+    if (AUG) {  // row nt + c' of S^H, c' the position of trial unknown c in [Q | E | l]
+      const int ca = c < ni ? nq + c : (c < nr ? c - ni : nr);
+      g[(nt + ca) + (size_t)r * ldg] = make_double2(v.x, -v.y);
+    } else {
+      s[x] = v;
+    }
   }
 }
 
@@ -488,14 +508,16 @@ __global__ void __launch_bounds__(LA_THREADS) k_dpg_dpg(DpgDims d, double2* G, d
 
 // impedance penalty (imp_penalty, elem_maxwell.F90:679-876) on the trace
 // block of Z, in the element's oriented trace functions.
+// the penalty is added to the trace block of Z, which starts at row and
+// column `off` of a column-major matrix with leading dimension n1
 __global__ void k_dpg_imp(DpgDims d, const int* imp_mask, DpgTables t, const double* gI,
-                          const uint32_t* perm, double2* Z) {
+                          const uint32_t* perm, double2* Z, int64_t estride, int off, int n1) {
   const int e = blockIdx.x;
   const int mask = imp_mask[e];
   if (!mask) return;
-  const int n1 = d.nr + 1, nE = d.nEi;
+  const int nE = d.nEi;
   const uint32_t* pm = perm + (size_t)e * nE;
-  double2* z = Z + (size_t)e * n1 * n1;
+  double2* z = Z + (size_t)e * estride + off + (size_t)off * n1;
   for (int x = blockIdx.y * blockDim.x + threadIdx.x; x < nE * nE; x += gridDim.y * blockDim.x) {
     const int m1 = x % nE, m2 = x / nE;
     const uint32_t p1 = pm[m1], p2 = pm[m2];
@@ -578,7 +600,7 @@ void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
                       const int* imp_mask, const uint32_t* perm, const int* nextract,
                       const int64_t* lcon_off, const int64_t* elem_nnz, const int64_t* schur_off,
                       const int64_t* bub_off, double* zastif, double* zbload, double* aschur,
-                      double* bschur, int* flags, cudaStream_t st) {
+                      double* bschur, double* zkeep, int* flags, cudaStream_t st) {
   if (nel <= 0) return;
   if (stage == 0) {
     k_dpg_geom<<<nel, 128, 0, st>>>(d, ph, w.xiV, w.wV, w.xiF, w.wF, w.xiI, w.wI, xvert, eps,
@@ -588,17 +610,38 @@ void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
     const int nzq = (d.nQ + BQ_CH - 1) / BQ_CH, nzt = (d.nEi + BT_CH - 1) / BT_CH;
     k_dpg_bmat<<<dim3(nel, (d.nEE + 127) / 128, nzq + nzt + 1), 128, 0, st>>>(
         d, t, w.gV, w.gF, w.P, w.R, w.T, w.load);
-    k_dpg_assemble<<<dim3(nel, 32), 256, 0, st>>>(d, ph, eps, w.MFF, w.MCC, w.MFC, w.P, w.R, w.T,
-                                                  w.load, perm, (double2*)w.G, (double2*)w.S);
-  } else if (stage == 1) {
     if (w.tc)
-      launch_dpg_solve_tc(nel, 2 * d.nEE, d.nr + 1, w.G, w.S, w.Z, w.tb, flags + 1, flags + 2, st);
+      k_dpg_assemble<true><<<dim3(nel, 32), 256, 0, st>>>(d, ph, eps, w.MFF, w.MCC, w.MFC, w.P,
+                                                          w.R, w.T, w.load, perm,
+                                                          (double2*)w.M, nullptr);
     else
+      k_dpg_assemble<false><<<dim3(nel, 32), 256, 0, st>>>(d, ph, eps, w.MFF, w.MCC, w.MFC, w.P,
+                                                           w.R, w.T, w.load, perm,
+                                                           (double2*)w.G, (double2*)w.S);
+  } else if (stage == 1) {
+    const int n1 = d.nr + 1;
+    const dim3 gimp(nel, (d.nEi * d.nEi + 255) / 256);
+    if (w.tc) {
+      // test block of the augmented matrix -> -Z in the trailing block -> Z
+      const int nt = 2 * d.nEE, na = nt + n1, nq = 6 * d.nQ;
+      launch_dpg_aug_tc(1, nel, nt, n1, nq, w, zkeep, flags + 1, flags + 2, st);
+      if (ph.ibcflag == 2)
+        k_dpg_imp<<<gimp, 256, 0, st>>>(d, imp_mask, t, w.gI, perm, (double2*)w.M,
+                                        (int64_t)na * na, nt + nq, na);
+      if (zkeep) launch_dpg_aug_tc(3, nel, nt, n1, nq, w, zkeep, flags + 1, flags + 2, st);
+    } else {
       k_dpg_dpg<<<nel, LA_THREADS, 0, st>>>(d, (double2*)w.G, (double2*)w.S, (double2*)w.Z,
                                             flags + 1);
-    if (ph.ibcflag == 2)
-      k_dpg_imp<<<dim3(nel, (d.nEi * d.nEi + 255) / 256), 256, 0, st>>>(d, imp_mask, t, w.gI,
-                                                                        perm, (double2*)w.Z);
+      if (ph.ibcflag == 2)
+        k_dpg_imp<<<gimp, 256, 0, st>>>(d, imp_mask, t, w.gI, perm, (double2*)w.Z,
+                                        (int64_t)n1 * n1, 0, n1);
+    }
+  } else if (w.tc) {
+    // L2 block of Z -> Schur complement, ASchur/BSchur, compression
+    const int nt = 2 * d.nEE, n1 = d.nr + 1, nq = 6 * d.nQ;
+    launch_dpg_aug_tc(2, nel, nt, n1, nq, w, nullptr, flags + 1, flags + 2, st);
+    launch_dpg_aug_out(nel, nt, n1, nq, w, nextract, lcon_off, elem_nnz, schur_off, bub_off,
+                       zastif, zbload, aschur, bschur, st);
   } else {
     k_dpg_condense<<<nel, LA_THREADS, 0, st>>>(d, (double2*)w.Z, nextract, lcon_off, elem_nnz,
                                                schur_off, bub_off, (double2*)zastif,

@@ -1,24 +1,29 @@
 // k_dpg_tc.cu -- the dense algebra of the DPG Maxwell element on tcgen05
-// tensor cores: Gram Cholesky G = L L^H, forward solve X = L^-1 [B | l] and
-// Z = X^H X (the steps ZPPTRF / ZTPTRS / ZHERK of elem_maxwell.F90:590-639),
-// blocked in 64-column panels.
+// tensor cores: the steps ZPPTRF / ZTPTRS / ZHERK of elem_maxwell.F90:590-639
+// and the condensation of the L2 fields (stc_fwd_herm, stc.F90:338-416) as one
+// partial Cholesky factorization of the augmented Hermitian matrix
+//     [[G, S], [S^H, 0]],  S = [B | l] with the trial unknowns ordered [Q | E | l],
+// column panel by column panel (64 wide).  Eliminating the test unknowns
+// leaves -Z = -X^H X (X = L^-1 S) in the trailing block; after the sign
+// flip and the impedance penalty, eliminating the L2 fields Q leaves the
+// Schur complement of the interface unknowns with its load.
 //
-// The FP64 work that stays on the CUDA cores is the 64-wide diagonal blocks:
-// the Cholesky of each diagonal block with the solve of the panel below it,
-// and the triangular solve of each 64-row block of X.  Every O(n^3) product
-// -- the trailing updates of the Cholesky, the block updates of the solve
-// and X^H X -- is one kind of update
-//     C (FP64 complex) -= A B^T,   K = 64 complex per step,
+// Per panel the FP64 work is the 64 x 64 diagonal block: its Cholesky factor
+// L11 and W = L11^-H.  Every O(n^3) product -- the panel solve P := P W and
+// the trailing update T -= P P^H, and the blocked backward substitution for
+// ASchur -- is one kind of update
+//     C (FP64 complex) = or -= A B^T,   K = 64 complex per step,
 // computed from split-BF16 digits: each complex row vector of A and B is
 // written as a real vector of length 128 (its real and imaginary parts in a
 // "form": [re|im], [-im|re], [re|-im], [im|re] or [im|-re]) with one
-// power-of-two scale per row and 7 balanced radix-2^7 digits (49 bits).  The
-// real part of the product is A(form [re|im]) . B(one form), the imaginary
-// part A . B(another form); each digit pair (p, q) with p + q <= 8 lands in
-// the FP32 TMEM accumulator of its level, where the sums of at most
-// 7 * 128 products of digits below 2^14 stay below 2^24 (exact); the levels
-// are recombined in FP64 and scaled by the two row exponents, one rounding
-// per term.
+// power-of-two scale per row and 7 balanced radix-2^7 digits of a 48-bit
+// fixed-point value (every digit at most 2^6 in magnitude, exact in BF16).
+// The real part of the product is A(form [re|im]) . B(one form), the
+// imaginary part A . B(another form); each digit pair (p, q) with p + q <= 6
+// lands in the FP32 TMEM accumulator of its level (sums below 2^22, exact).
+// For A digit p one MMA (N up to 256) covers the B digits q = 0..6-p of both
+// forms, whose levels p..6 are contiguous in TMEM.  The levels are
+// recombined exactly in 64-bit integers and added to C with one rounding.
 #include "hp3dg_kernels.h"
 #include "hp3dg_tc.cuh"
 #include "hp3dg_zla.cuh"
@@ -37,7 +42,9 @@ constexpr int ZM = 128, ZN = 32;       // output tile
 constexpr int ZA_BLK = ZM * ZK * 2;    // one A digit block (bytes)
 constexpr int ZB_BLK = ZN * ZK * 2;    // one B digit block
 constexpr int ZB_TILE = 2 * ZD * ZB_BLK;  // both B forms of one column tile
-constexpr int ZU_THREADS = 192;        // loader, MMA, 4 epilogue warps
+constexpr int ZFB = 48;                // fraction bits of the split (|v| < 2^e -> |X| <= 2^48)
+constexpr int ZBROWS = 2 * ZD * ZN;    // rows of one B K-step: [digit q][form][32 rows]
+constexpr int ZU_THREADS = 320;        // loader, MMA, 8 epilogue warps (2 per TMEM lane quarter)
 constexpr uint32_t ZU_TMEM = 512;      // 7 levels x 2 parts x 32 columns = 448
 constexpr size_t ZU_SMEM = 2 * ZA_BLK + ZB_TILE + 1024;
 
@@ -88,19 +95,23 @@ __global__ void k_zslice(ZSlice a) {
     }
   const int ex = row_exponent(mx);
   a.ex[(int64_t)e * a.ex_estride + row] = valid ? ex : 0;
-  const size_t dstride = (size_t)a.nt * ZK * 2;
-  uint8_t* base = a.dst + (int64_t)e * a.dst_estride +
-                  (size_t)(row / a.nt) * a.nforms * ZD * dstride;
   const int r = row % a.nt;
+  const bool isB = a.nt == ZN;
+  // A: [row tile][digit][canonical 128 x 128]; B: [column tile][canonical
+  // 448 x 128], row (digit q, form, r) = 64 q + 32 form + r, so that the
+  // digits q = 0..6-p of both forms are one N = (7 - p) 64 operand
+  const size_t tile_bytes = isB ? (size_t)ZB_TILE : (size_t)ZD * a.nt * ZK * 2;
+  const size_t dstride = isB ? (size_t)(2 * ZN / 8) * 256 : (size_t)a.nt * ZK * 2;
+  uint8_t* base = a.dst + (int64_t)e * a.dst_estride + (size_t)(row / a.nt) * tile_bytes;
   for (int fi = 0; fi < a.nforms; ++fi) {
     const int f = fi == 0 ? a.form0 : a.form1;
-    uint8_t* fb = base + (size_t)fi * ZD * dstride;
     for (int g = 0; g < ZGROUPS; ++g) {
       long long X[8];
 #pragma unroll
       for (int t = 0; t < 8; ++t)
-        X[t] = valid ? fixed_of(form_value(s, a.sk, a.kc, f, 8 * g + t), ex, ZR * ZD) : 0;
-      store_digits8(X, ZR, ZD, fb + tile_off(r, g, a.nt), dstride);
+        X[t] = valid ? fixed_of(form_value(s, a.sk, a.kc, f, 8 * g + t), ex, ZFB) : 0;
+      uint8_t* dst = base + (isB ? tile_off(fi * ZN + r, g, ZBROWS) : tile_off(r, g, a.nt));
+      store_digits8(X, ZR, ZD, dst, dstride);
     }
   }
 }
@@ -119,10 +130,30 @@ struct ZUpd {
   int ldc;
   int m, n;
   int lower;
+  int beta0;  // 1: C = sgn A B^T (C is not read)
   double sgn;
   int nrt;
   int* err;
 };
+
+constexpr int ZX_SKIP = -0x40000000;  // column exponent slot of a skipped output
+
+// V 2^sc rounded to nearest (ties to even), assembled from the bits of V
+// without an FP64 instruction (GB300 issues FP64 and its conversions at
+// about 2 per clock per SM); scales outside the normal range take ldexp
+__device__ __forceinline__ double scaled_i64(long long V, int sc) {
+  if (V == 0) return 0.0;
+  const unsigned long long sb = (unsigned long long)V & 0x8000000000000000ull;
+  unsigned long long u = V < 0 ? (unsigned long long)(-V) : (unsigned long long)V;
+  const int lz = __clzll((long long)u);
+  const int eb = 63 - lz + sc + 1023;  // biased exponent of the leading bit
+  if (eb < 1 || eb > 2045) return ldexp((double)V, sc);
+  u <<= lz;
+  unsigned long long m = u >> 11;  // 53 bits, leading bit at 52
+  const unsigned long long r = u & 0x7ffull;
+  m += (r > 0x400ull || (r == 0x400ull && (m & 1ull))) ? 1ull : 0ull;
+  return __longlong_as_double((long long)(sb | (((unsigned long long)(eb - 1) << 52) + m)));
+}
 
 // one 128 x 32 tile of one element per CTA
 __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
@@ -181,7 +212,6 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
     if (lane == 0) {
       bool ok = mbar_wait(smem_u32(&ldB_bar), 0, &abort_);
       if (!ok) { abort_ = 1; atomicExch(a.err, 42); }
-      const uint32_t idesc = zidesc(ZN);
       const uint64_t dB0 = sdesc_kmajor(smem_u32(regB));
       for (int p = 0; p < ZD && ok; ++p) {
         const int buf = p & 1;
@@ -193,13 +223,16 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
         }
         tc_fence_after();
         const uint64_t dA = sdesc_kmajor(smem_u32(regA0 + buf * ZA_BLK));
-        for (int q = 0; q + p < ZD; ++q) {
-          for (int part = 0; part < 2; ++part) {
-            const uint32_t dt = tbase + (uint32_t)(((p + q) * 2 + part) * ZN);
-            const uint64_t db = dB0 + (uint64_t)(((size_t)part * ZD * ZB_BLK + (size_t)q * ZB_BLK) >> 4);
-            for (int kb = 0; kb < ZK / 16; ++kb)
-              umma_bf16(dt, dA + (uint64_t)((kb * ZM * 32) >> 4), db + (uint64_t)((kb * ZN * 32) >> 4),
-                        idesc, (p > 0 || kb > 0) ? 1u : 0u);
+        // all pairs (p, q), q = 0..6-p, and both parts: B rows [0, 64 (7 - p))
+        // into the TMEM levels p..6 (64 columns each), at most 256 per MMA
+        for (int kb = 0; kb < ZK / 16; ++kb) {
+          const uint64_t a_kb = dA + (uint64_t)((kb * ZM * 32) >> 4);
+          for (int q0 = 0; q0 + p < ZD;) {
+            const int nq = (ZD - p - q0) < 4 ? (ZD - p - q0) : 4;
+            const uint32_t dt = tbase + (uint32_t)((p + q0) * 2 * ZN);
+            const uint64_t db = dB0 + (uint64_t)(((size_t)kb * ZBROWS * 32 + (size_t)q0 * 2 * ZN * 32) >> 4);
+            umma_bf16(dt, a_kb, db, zidesc(nq * 2 * ZN), (p > 0 || kb > 0) ? 1u : 0u);
+            q0 += nq;
           }
         }
         umma_commit(smem_u32(&afree_bar[buf]));
@@ -207,60 +240,73 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
       umma_commit(smem_u32(&accf_bar));
     }
   } else {
-    // epilogue: warps 2..5 -> TMEM lane quarter warp % 4 = rows of the tile
-    const int quarter = warp & 3;
+    // epilogue: warps 2..9; TMEM lane quarter warp % 4 = rows of the tile,
+    // (warp - 2) / 4 = which 16 of the 32 columns
+    const int quarter = warp & 3, half = (warp - 2) >> 2;
     const int i = rt * ZM + quarter * 32 + lane;
+    const bool rowok = i < a.m;
+    const int ea = rowok ? a.ea[(int64_t)e * a.ea_estride + i] : 0;
+    const double2* crow = a.C + (int64_t)e * a.c_estride + i;
+    const int* ebp = a.eb + (int64_t)e * a.eb_estride;
+    // C and the column exponents of the next 8-column group are loaded one
+    // group ahead (independent loads in flight while the levels are combined)
+    double2 cn[8];
+    int xn[8];
+    auto fetch = [&](int cg) {
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const int j = ct * ZN + cg * 8 + c;
+        const bool ok = rowok && j < a.n && !(a.lower && j > i);
+        cn[c] = (ok && !a.beta0) ? crow[(int64_t)j * a.ldc] : make_double2(0.0, 0.0);
+        xn[c] = ok ? ebp[j] : ZX_SKIP;
+      }
+    };
+    const int cg0 = 2 * half;
+    fetch(cg0);
     const bool okw = mbar_wait(smem_u32(&accf_bar), 0, &abort_);
     if (!okw) { abort_ = 1; atomicExch(a.err, 44); }
     tc_fence_after();
     const uint32_t tl = tbase + ((uint32_t)(quarter * 32) << 16);
-    const int ea = (i < a.m) ? a.ea[(int64_t)e * a.ea_estride + i] : 0;
     double2* C = a.C + (int64_t)e * a.c_estride;
-    for (int cg = 0; cg < ZN / 8; ++cg) {
-      // exact recombination in integers: levels L = 0..3 (weights 2^7(3-L)) and
-      // L = 4..6 (weights 2^7(6-L)) as two 64-bit sums (below 2^45 / 2^38),
-      // then one FP64 fma per part: v = hi 2^-35 + lo 2^-56
-      long long hi[2][8], lo[2][8];
+    for (int cg = cg0; cg < cg0 + 2; ++cg) {
+      double2 cv[8];
+      int xs[8];
 #pragma unroll
-      for (int part = 0; part < 2; ++part)
+      for (int c = 0; c < 8; ++c) { cv[c] = cn[c]; xs[c] = xn[c]; }
+      if (cg + 1 < cg0 + 2) fetch(cg + 1);
+      // exact recombination in integers.  Digits are at most 2^6 (48-bit
+      // split), so each level sum s_L (at most 7 pairs x 128 terms) is an
+      // integer below 2^21.8 and (s_L + 1.5 2^23) has it in its low mantissa
+      // bits.  hi = sum_{L<=3} s_L 2^7(3-L) (< 2^42.8), lo = sum_{L>=4}
+      // s_L 2^7(6-L); V = hi 2^19 + lo / 4 (< 2^61.8) carries the product in
+      // units of 2^(sx - 52), below the 2^(sx - 48) of the split itself
+      long long V[2][8];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) hi[part][c] = lo[part][c] = 0;
+      for (int part = 0; part < 2; ++part) {
+        uint32_t r[ZD][8];
 #pragma unroll
-      for (int L = 0; L < ZD; ++L) {
-        uint32_t r0[8], r1[8];
-        tmem_ld8_nowait(tl + (uint32_t)((L * 2 + 0) * ZN + cg * 8), r0);
-        tmem_ld8_nowait(tl + (uint32_t)((L * 2 + 1) * ZN + cg * 8), r1);
+        for (int L = 0; L < ZD; ++L) tmem_ld8_nowait(tl + (uint32_t)((L * 2 + part) * ZN + cg * 8), r[L]);
         tmem_wait();
-        const int sh = ZR * ((L < 4 ? 3 : 6) - L);
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-          const long long a0 = (long long)__float2int_rn(__uint_as_float(r0[c])) << sh;
-          const long long a1 = (long long)__float2int_rn(__uint_as_float(r1[c])) << sh;
-          if (L < 4) { hi[0][c] += a0; hi[1][c] += a1; }
-          else { lo[0][c] += a0; lo[1][c] += a1; }
+          int sl[ZD];
+#pragma unroll
+          for (int L = 0; L < ZD; ++L)
+            sl[L] = __float_as_int(__uint_as_float(r[L][c]) + 12582912.0f) - 0x4B400000;
+          const long long hi = ((long long)(sl[0] * 128 + sl[1]) << 14) + ((long long)sl[2] << 7) + sl[3];
+          const long long lo = ((long long)(sl[4] * 128 + sl[5]) << 7) + sl[6];
+          const long long v = (hi << 19) + (lo >> 2);
+          V[part][c] = a.sgn < 0.0 ? -v : v;
         }
       }
-      if (!okw || i >= a.m) continue;
+      if (!okw || !rowok) continue;
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const int j = ct * ZN + cg * 8 + c;
-        if (j >= a.n || (a.lower && j > i)) continue;
-        const int sx = ea + a.eb[(int64_t)e * a.eb_estride + j];
-        // 2^(sx - 35) and 2^(sx - 56) from the bits, with the sign of the update
-        const double sh1 = a.sgn * __longlong_as_double((long long)(1023 + sx - 5 * ZR) << 52);
-        const double sh2 = a.sgn * __longlong_as_double((long long)(1023 + sx - 8 * ZR) << 52);
-        double2* cp = &C[i + (int64_t)j * a.ldc];
-        double2 cv = *cp;
-        if (sx > -960 && sx < 960) {
-          cv.x = fma(__ll2double_rn(hi[0][c]), sh1, fma(__ll2double_rn(lo[0][c]), sh2, cv.x));
-          cv.y = fma(__ll2double_rn(hi[1][c]), sh1, fma(__ll2double_rn(lo[1][c]), sh2, cv.y));
-        } else {  // scales outside the normal range of the bit-built powers
-          cv.x += a.sgn * (ldexp(__ll2double_rn(hi[0][c]), sx - 5 * ZR) +
-                           ldexp(__ll2double_rn(lo[0][c]), sx - 8 * ZR));
-          cv.y += a.sgn * (ldexp(__ll2double_rn(hi[1][c]), sx - 5 * ZR) +
-                           ldexp(__ll2double_rn(lo[1][c]), sx - 8 * ZR));
-        }
-        *cp = cv;
+        if (xs[c] == ZX_SKIP) continue;
+        const int sc = ea + xs[c] - 52;
+        cv[c].x += scaled_i64(V[0][c], sc);
+        cv[c].y += scaled_i64(V[1][c], sc);
+        C[i + (int64_t)(ct * ZN + cg * 8 + c) * a.ldc] = cv[c];
       }
     }
   }
@@ -272,99 +318,146 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
   }
 }
 
-// FP64 diagonal step of the Cholesky: L11 of the 64-wide block at k0 and the
-// panel below it, x L11^H = a for every row (two 32-column halves)
-constexpr size_t ZP_SMEM = (2 * TK * TM + 64 * 65) * sizeof(double2) + 64 * sizeof(double);
-#define LSM(i, j) Ls[(i) * 65 + (j)]
+int rows_pad(int rows, int nt) { return (rows + nt - 1) / nt * nt; }
 
-__global__ void __launch_bounds__(LA_THREADS) k_zpanel(double2* G, int64_t estride, int n, int k0,
-                                                       int kb, int* bad) {
-  extern __shared__ double2 zp_dyn[];
-  double2* sm = zp_dyn;
-  double2* Ls = zp_dyn + 2 * TK * TM;
-  const int e = blockIdx.x;
-  double2* A = G + (int64_t)e * estride;
-  double2* D = A + k0 + (int64_t)k0 * n;
-  if (cta_zpotrf(D, n, kb, sm) && threadIdx.x == 0) atomicMin(bad, e);
-  double* rd = (double*)(Ls + 64 * 65);  // reciprocals of the diagonal
-  for (int x = threadIdx.x; x < kb * kb; x += LA_THREADS) {
-    const int i = x % kb, j = x / kb;
-    LSM(i, j) = i >= j ? D[i + (int64_t)j * n] : make_double2(0.0, 0.0);
-    if (i == j) rd[i] = 1.0 / D[i + (int64_t)i * n].x;
+// ---------------------------------------------------------------------------
+// the augmented partial factorization
+// ---------------------------------------------------------------------------
+// FP64 step of one panel of the augmented matrix: the Cholesky factor L11
+// (lower, in place) of the kb x kb diagonal block at (k0, k0) and
+// W = L11^-H (upper, 64 x 64 column-major, zero outside kb x kb), from an
+// unblocked right-looking Cholesky and the forward substitution L11 X = I in
+// shared memory, two barriers per column.
+constexpr int ZDG_THREADS = 256;
+constexpr size_t ZDG_SMEM = 2 * 64 * 65 * sizeof(double2) + 64 * sizeof(double);
+
+__global__ void __launch_bounds__(ZDG_THREADS) k_zdiag(double2* M, int64_t estride, int ld, int k0,
+                                                       int kb, double2* W, int64_t wstride,
+                                                       int* bad) {
+  extern __shared__ double2 zdg[];
+  double2* Ls = zdg;                     // L: row i, column j at i * 65 + j
+  double2* Xs = zdg + 64 * 65;           // X = L^-1
+  double* dk = (double*)(Xs + 64 * 65);  // pivots, stored when they become final
+  const int e = blockIdx.x, tid = threadIdx.x;
+  double2* D = M + (int64_t)e * estride + k0 + (int64_t)k0 * ld;
+  for (int x = tid; x < 64 * 64; x += ZDG_THREADS) {
+    const int i = x % 64, j = x / 64;
+    Ls[i * 65 + j] = (i < kb && j < kb && i >= j) ? D[i + (int64_t)j * ld] : make_double2(0.0, 0.0);
+    Xs[i * 65 + j] = make_double2((i == j && i < kb) ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
-  const int h1 = kb < 32 ? kb : 32;
-  for (int r = k0 + kb + threadIdx.x; r < n; r += LA_THREADS) {
-    double2 x[32];
-    for (int j = 0; j < h1; ++j) {
-      double2 t = A[r + (int64_t)(k0 + j) * n];
-      for (int q = 0; q < j; ++q) t = zsub(t, zmul(x[q], zconj(LSM(j, q))));
-      x[j] = zscale(rd[j], t);
+  if (tid == 0) dk[0] = Ls[0].x;
+  __syncthreads();
+  bool ok = true;
+  for (int k = 0; k < kb; ++k) {
+    const double dd = dk[k];
+    if (!(dd > 0.0)) ok = false;
+    const double sq = sqrt(dd), rs = 1.0 / sq;
+    // column k of L; row k of X
+    if (tid < kb - k) {
+      const int i = k + tid;
+      Ls[i * 65 + k] = i == k ? make_double2(sq, 0.0) : zscale(rs, Ls[i * 65 + k]);
+    } else if (tid >= 64 && tid - 64 <= k) {
+      const int j = tid - 64;
+      Xs[k * 65 + j] = zscale(rs, Xs[k * 65 + j]);
     }
-    for (int j = 0; j < h1; ++j) A[r + (int64_t)(k0 + j) * n] = x[j];
-    if (kb > 32) {
-      double2 y[32];
-      for (int j = 32; j < kb; ++j) {
-        double2 t = A[r + (int64_t)(k0 + j) * n];
-        for (int q = 0; q < 32; ++q) t = zsub(t, zmul(x[q], zconj(LSM(j, q))));
-        for (int q = 32; q < j; ++q) t = zsub(t, zmul(y[q - 32], zconj(LSM(j, q))));
-        y[j - 32] = zscale(rd[j], t);
+    __syncthreads();
+    // L(i, j) -= L(i, k) conj(L(j, k)) for k < j <= i;  X(i, j) -= L(i, k) X(k, j) for j <= k < i
+    const int nr = kb - k - 1;
+    for (int x = tid; x < nr * kb; x += ZDG_THREADS) {
+      const int i = k + 1 + x / kb, j = x % kb;
+      if (j > k) {
+        if (j <= i) {
+          const double2 v = zsub(Ls[i * 65 + j], zmul(Ls[i * 65 + k], zconj(Ls[j * 65 + k])));
+          Ls[i * 65 + j] = v;
+          if (i == k + 1 && j == k + 1) dk[k + 1] = v.x;
+        }
+      } else {
+        Xs[i * 65 + j] = zsub(Xs[i * 65 + j], zmul(Ls[i * 65 + k], Xs[k * 65 + j]));
       }
-      for (int j = 32; j < kb; ++j) A[r + (int64_t)(k0 + j) * n] = y[j - 32];
+    }
+    __syncthreads();
+  }
+  if (!ok && tid == 0) atomicMin(bad, e);
+  double2* w = W + (int64_t)e * wstride;
+  for (int x = tid; x < 64 * 64; x += ZDG_THREADS) {
+    const int i = x % 64, j = x / 64;
+    if (i < kb && j < kb && i >= j) D[i + (int64_t)j * ld] = Ls[i * 65 + j];
+    w[x] = (j >= i) ? zconj(Xs[j * 65 + i]) : make_double2(0.0, 0.0);  // W(i, j) = conj(X(j, i))
+  }
+}
+
+// the n x n trailing block at (o, o), lower triangle: T := -T
+__global__ void k_zneg(double2* M, int64_t estride, int ld, int o, int n) {
+  double2* m = M + (int64_t)blockIdx.y * estride + o + (int64_t)o * ld;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < (int64_t)n * n;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(x % n), c = (int)(x / n);
+    if (r >= c) {
+      const double2 v = m[r + (int64_t)c * ld];
+      m[r + (int64_t)c * ld] = make_double2(-v.x, -v.y);
     }
   }
 }
 
-// FP64 diagonal step of the forward solve: X[k0:k0+kb, :] = L11^-1 X[k0:k0+kb, :]
-__global__ void __launch_bounds__(LA_THREADS) k_zfsolve(const double2* G, int64_t gstride,
-                                                        double2* S, int64_t sstride, int n,
-                                                        int m, int k0, int kb) {
-  extern __shared__ double2 zp_dyn[];
-  double2* Ls = zp_dyn + 2 * TK * TM;
-  const int e = blockIdx.x;
-  const double2* A = G + (int64_t)e * gstride;
-  double2* X = S + (int64_t)e * sstride;
-  double* rd = (double*)(Ls + 64 * 65);
-  for (int x = threadIdx.x; x < kb * kb; x += LA_THREADS) {
-    const int i = x % kb, j = x / kb;
-    LSM(i, j) = i >= j ? A[(k0 + i) + (int64_t)(k0 + j) * n] : make_double2(0.0, 0.0);
-    if (i == j) rd[i] = 1.0 / A[(k0 + i) + (int64_t)(k0 + i) * n].x;
-  }
-  __syncthreads();
-  const int h1 = kb < 32 ? kb : 32;
-  for (int c = threadIdx.x; c < m; c += LA_THREADS) {
-    double2* xc = X + k0 + (int64_t)c * n;
-    double2 x[32];
-    for (int i = 0; i < h1; ++i) {
-      double2 t = xc[i];
-      for (int q = 0; q < i; ++q) t = zsub(t, zmul(LSM(i, q), x[q]));
-      x[i] = zscale(rd[i], t);
-    }
-    for (int i = 0; i < h1; ++i) xc[i] = x[i];
-    if (kb > 32) {
-      double2 y[32];
-      for (int i = 32; i < kb; ++i) {
-        double2 t = xc[i];
-        for (int q = 0; q < 32; ++q) t = zsub(t, zmul(LSM(i, q), x[q]));
-        for (int q = 32; q < i; ++q) t = zsub(t, zmul(LSM(i, q), y[q - 32]));
-        y[i - 32] = zscale(rd[i], t);
-      }
-      for (int i = 32; i < kb; ++i) xc[i] = y[i - 32];
-    }
-  }
+// position of trial unknown c (interface order [E | Q | l]) in the augmented
+// order [Q | E | l]
+__device__ __forceinline__ int aug_pos(int c, int ni, int nq) {
+  return c < ni ? nq + c : (c < ni + nq ? c - ni : c);
 }
 
-// Z (lower) -> full Hermitian
-__global__ void k_zmirror(double2* Z, int64_t estride, int n1) {
-  double2* z = Z + (int64_t)blockIdx.y * estride;
+// Z (n1 x n1, full, interface order) from the lower trailing block at (o, o)
+__global__ void k_zkeep(const double2* M, int64_t estride, int ld, int o, int n1, int nq,
+                        double2* Z) {
+  const int e = blockIdx.y, ni = n1 - 1 - nq;
+  const double2* m = M + (int64_t)e * estride + o + (int64_t)o * ld;
+  double2* z = Z + (int64_t)e * n1 * n1;
   for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < (int64_t)n1 * n1;
        x += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(x % n1), j = (int)(x / n1);
-    if (i < j) z[x] = zconj(z[j + (int64_t)i * n1]);
+    const int ar = aug_pos((int)(x % n1), ni, nq), ac = aug_pos((int)(x / n1), ni, nq);
+    z[x] = ar >= ac ? m[ar + (int64_t)ac * ld] : zconj(m[ac + (int64_t)ar * ld]);
   }
 }
 
-int rows_pad(int rows, int nt) { return (rows + nt - 1) / nt * nt; }
+// Y (nq x ni1, column-major) = L_EQ^H, L_EQ the panel below the L2 block
+// (rows o + nq .. o + nq + ni1, columns o .. o + nq)
+__global__ void k_zcopyT(const double2* M, int64_t estride, int ld, int o, int nq, int ni1,
+                         double2* Y) {
+  const int e = blockIdx.y;
+  const double2* m = M + (int64_t)e * estride;
+  double2* y = Y + (int64_t)e * nq * ni1;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < (int64_t)nq * ni1;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    const int q = (int)(x % nq), j = (int)(x / nq);
+    y[x] = zconj(m[(o + nq + j) + (int64_t)(o + q) * ld]);
+  }
+}
+
+// outputs: the compressed Schur complement and load (row-major over the
+// extraction list, celem_systemI with ISYM_FLAG = 2) from the lower trailing
+// block at (o, o) in the order [E | l]; ASchur and BSchur from Y
+__global__ void k_dpg_aug_out(const double2* M, int64_t estride, int ld, int o, int ni,
+                              const double2* Y, int nq, const int* nextract,
+                              const int64_t* lcon_off, const int64_t* elem_nnz,
+                              const int64_t* schur_off, const int64_t* bub_off, double2* zastif,
+                              double2* zbload, double2* aschur, double2* bschur) {
+  const int e = blockIdx.x;
+  const double2* m = M + (int64_t)e * estride + o + (int64_t)o * ld;
+  const double2* y = Y + (int64_t)e * nq * (ni + 1);
+  const int64_t lo = lcon_off[e];
+  const int nc = (int)(lcon_off[e + 1] - lo);
+  const int* nx = nextract + lo;
+  double2* za = zastif + elem_nnz[e];
+  for (int64_t x = threadIdx.x; x < (int64_t)nc * nc; x += blockDim.x) {
+    const int r = nx[x / nc], c = nx[x % nc];
+    za[x] = r >= c ? m[r + (int64_t)c * ld] : zconj(m[c + (int64_t)r * ld]);
+  }
+  for (int l1 = threadIdx.x; l1 < nc; l1 += blockDim.x)
+    zbload[lo + l1] = zconj(m[ni + (int64_t)nx[l1] * ld]);
+  double2* as = aschur + schur_off[e];
+  for (int64_t x = threadIdx.x; x < (int64_t)nq * ni; x += blockDim.x) as[x] = y[x];
+  for (int i = threadIdx.x; i < nq; i += blockDim.x) bschur[bub_off[e] + i] = y[i + (int64_t)ni * nq];
+}
 
 }  // namespace
 
@@ -372,22 +465,32 @@ size_t dpg_tc_ex_slots(int rows) { return (size_t)rows_pad(rows, ZM); }
 size_t dpg_tc_a_bytes(int rows) { return (size_t)rows_pad(rows, ZM) / ZM * ZD * ZA_BLK; }
 size_t dpg_tc_b_bytes(int rows) { return (size_t)rows_pad(rows, ZN) / ZN * ZB_TILE; }
 
-// the dense DPG algebra of nel elements on tensor cores: G (nt x nt) ->
-// L (lower), S (nt x n1) -> X = L^-1 S, Z = X^H X (n1 x n1, full)
-int launch_dpg_solve_tc(int nel, int nt, int n1, double* G, double* S, double* Z,
-                        const DpgTcBufs& tb, int* bad, int* err, cudaStream_t st) {
+int dpg_aug_wslots(int nt, int nq) { return 1 + (nq + 63) / 64; }
+
+// the augmented Hermitian matrix [[G, S], [S^H, 0]] (na = nt + n1, trial
+// order [Q | E | l]) factored column panel by column panel:
+//   1: the nt test columns; the trailing block becomes -Z, then Z (negated);
+//   2: the nq L2-field columns of Z; the trailing block becomes the Schur
+//      complement and the panel below holds Y^H, Y = L_QQ^-1 Z_Q[E|l]; then
+//      ASchur | BSchur = L_QQ^-H Y by blocked backward substitution;
+//   3: Z in the interface order to zkeep.
+// Per panel: FP64 L11 and W = L11^-H (k_zdiag), then on tensor cores the
+// panel solve P := P W and the trailing update T -= P P^H.
+int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& w, double* zkeep,
+                      int* bad, int* err, cudaStream_t st) {
   if (nel <= 0) return 0;
   if (raise_smem_limit((const void*)k_zupd, ZU_SMEM) != cudaSuccess ||
-      raise_smem_limit((const void*)k_zpanel, ZP_SMEM) != cudaSuccess ||
-      raise_smem_limit((const void*)k_zfsolve, ZP_SMEM) != cudaSuccess)
+      raise_smem_limit((const void*)k_zdiag, ZDG_SMEM) != cudaSuccess)
     return -1;
-  double2* g = (double2*)G;
-  double2* s = (double2*)S;
-  double2* z = (double2*)Z;
-  const int64_t gst = (int64_t)nt * nt, sst = (int64_t)nt * n1, zst = (int64_t)n1 * n1;
-  const int rmax = nt > n1 ? nt : n1;
-  const int exst = rows_pad(rmax, ZM);  // exponent slots per element (>= every padded row count)
-  const int64_t ast = (int64_t)dpg_tc_a_bytes(rmax), bst = (int64_t)dpg_tc_b_bytes(rmax);
+  const int na = nt + n1, ni1 = n1 - nq;
+  double2* M = (double2*)w.M;
+  double2* W = (double2*)w.W;
+  double2* Y = (double2*)w.Y;
+  const int64_t mst = (int64_t)na * na, wst = (int64_t)dpg_aug_wslots(nt, nq) * 4096;
+  const int64_t yst = (int64_t)nq * ni1;
+  const DpgTcBufs& tb = w.tb;
+  const int exst = rows_pad(na, ZM);
+  const int64_t ast = (int64_t)dpg_tc_a_bytes(na), bst = (int64_t)dpg_tc_b_bytes(na);
   auto slice = [&](const double2* src, int64_t estr, int64_t srow, int64_t sk, int rows, int kc,
                    bool isA, int f0, int f1) {
     ZSlice a;
@@ -402,48 +505,66 @@ int launch_dpg_solve_tc(int nel, int nt, int n1, double* G, double* S, double* Z
     a.ex_estride = exst;
     k_zslice<<<dim3((a.rows_pad + 127) / 128, nel), 128, 0, st>>>(a);
   };
-  auto update = [&](double2* C, int64_t cst, int ldc, int m, int n, bool lower, double sgn) {
+  auto update = [&](double2* C, int64_t cst, int ldc, int m, int n, bool lower, double sgn,
+                    bool beta0) {
     ZUpd u;
     u.a = tb.a; u.a_estride = ast; u.b = tb.b; u.b_estride = bst;
     u.ea = tb.ea; u.ea_estride = exst; u.eb = tb.eb; u.eb_estride = exst;
     u.C = C; u.c_estride = cst; u.ldc = ldc; u.m = m; u.n = n;
-    u.lower = lower ? 1 : 0; u.sgn = sgn;
+    u.lower = lower ? 1 : 0; u.sgn = sgn; u.beta0 = beta0 ? 1 : 0;
     u.nrt = (m + ZM - 1) / ZM;
     u.err = err;
     const int nct = (n + ZN - 1) / ZN;
     k_zupd<<<dim3(u.nrt * nct, nel), ZU_THREADS, ZU_SMEM, st>>>(u);
   };
-  // 1. G = L L^H: diagonal blocks in FP64, trailing updates on tensor cores
-  for (int k0 = 0; k0 < nt; k0 += 64) {
-    const int kb = nt - k0 < 64 ? nt - k0 : 64, rem = nt - k0 - kb;
-    k_zpanel<<<nel, LA_THREADS, ZP_SMEM, st>>>(g, gst, nt, k0, kb, bad);
-    if (rem > 0) {
-      const double2* p = g + (k0 + kb) + (int64_t)k0 * nt;
-      slice(p, gst, 1, nt, rem, kb, true, 0, 0);
-      slice(p, gst, 1, nt, rem, kb, false, 0, 1);
-      update(g + (k0 + kb) + (int64_t)(k0 + kb) * nt, gst, nt, rem, rem, true, -1.0);
+  auto panel = [&](int k0, int kb, int slot) {
+    double2* ws = W + (int64_t)slot * 4096;
+    k_zdiag<<<nel, ZDG_THREADS, ZDG_SMEM, st>>>(M, mst, na, k0, kb, ws, wst, bad);
+    const int rem = na - k0 - kb;  // > 0: the load row is never a pivot
+    double2* P = M + (k0 + kb) + (int64_t)k0 * na;
+    slice(P, mst, 1, na, rem, kb, true, 0, 0);
+    slice(ws, wst, 64, 1, kb, kb, false, 2, 3);  // B row j = column j of W
+    update(P, mst, na, rem, kb, false, 1.0, true);
+    slice(P, mst, 1, na, rem, kb, true, 0, 0);
+    slice(P, mst, 1, na, rem, kb, false, 0, 1);
+    update(M + (k0 + kb) + (int64_t)(k0 + kb) * na, mst, na, rem, rem, true, -1.0, false);
+  };
+  if (part == 1) {
+    for (int k0 = 0; k0 < nt; k0 += 64) panel(k0, nt - k0 < 64 ? nt - k0 : 64, 0);
+    k_zneg<<<dim3(64, nel), 256, 0, st>>>(M, mst, na, nt, n1);
+  } else if (part == 2) {
+    for (int k0 = nt; k0 < nt + nq; k0 += 64)
+      panel(k0, nt + nq - k0 < 64 ? nt + nq - k0 : 64, 1 + (k0 - nt) / 64);
+    k_zcopyT<<<dim3(64, nel), 256, 0, st>>>(M, mst, na, nt, nq, ni1, Y);
+    for (int kq = (nq + 63) / 64 - 1; kq >= 0; --kq) {
+      const int q0 = 64 * kq, qb = nq - q0 < 64 ? nq - q0 : 64;
+      const double2* ws = W + (int64_t)(1 + kq) * 4096;
+      // Y_k := W_k Y_k
+      slice(ws, wst, 1, 64, qb, qb, true, 0, 0);
+      slice(Y + q0, yst, nq, 1, ni1, qb, false, 2, 3);
+      update(Y + q0, yst, nq, qb, ni1, false, 1.0, true);
+      if (q0 > 0) {  // Y_i -= L_ki^H Y_k for the blocks i above
+        slice(M + (nt + q0) + (int64_t)nt * na, mst, na, 1, q0, qb, true, 0, 0);
+        slice(Y + q0, yst, nq, 1, ni1, qb, false, 0, 4);
+        update(Y, yst, nq, q0, ni1, false, -1.0, false);
+      }
     }
+  } else if (part == 3) {
+    k_zkeep<<<dim3(64, nel), 256, 0, st>>>(M, mst, na, nt, n1, nq, (double2*)zkeep);
   }
-  // 2. X = L^-1 S: diagonal solves in FP64, block updates on tensor cores
-  for (int k0 = 0; k0 < nt; k0 += 64) {
-    const int kb = nt - k0 < 64 ? nt - k0 : 64, rem = nt - k0 - kb;
-    k_zfsolve<<<nel, LA_THREADS, ZP_SMEM, st>>>(g, gst, s, sst, nt, n1, k0, kb);
-    if (rem > 0) {
-      slice(g + (k0 + kb) + (int64_t)k0 * nt, gst, 1, nt, rem, kb, true, 0, 0);
-      slice(s + k0, sst, nt, 1, n1, kb, false, 2, 3);
-      update(s + (k0 + kb), sst, nt, rem, n1, false, -1.0);
-    }
-  }
-  // 3. Z = X^H X over 64-row chunks of X
-  if (cudaMemsetAsync(z, 0, (size_t)nel * zst * sizeof(double2), st) != cudaSuccess) return -1;
-  for (int k0 = 0; k0 < nt; k0 += 64) {
-    const int kb = nt - k0 < 64 ? nt - k0 : 64;
-    slice(s + k0, sst, nt, 1, n1, kb, true, 0, 0);
-    slice(s + k0, sst, nt, 1, n1, kb, false, 0, 4);
-    update(z, zst, n1, n1, n1, true, 1.0);
-  }
-  k_zmirror<<<dim3(64, nel), 256, 0, st>>>(z, zst, n1);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+void launch_dpg_aug_out(int nel, int nt, int n1, int nq, const DpgWork& w, const int* nextract,
+                        const int64_t* lcon_off, const int64_t* elem_nnz,
+                        const int64_t* schur_off, const int64_t* bub_off, double* zastif,
+                        double* zbload, double* aschur, double* bschur, cudaStream_t st) {
+  if (nel <= 0) return;
+  const int na = nt + n1, ni = n1 - 1 - nq;
+  k_dpg_aug_out<<<nel, 256, 0, st>>>((const double2*)w.M, (int64_t)na * na, na, nt + nq, ni,
+                                     (const double2*)w.Y, nq, nextract, lcon_off, elem_nnz,
+                                     schur_off, bub_off, (double2*)zastif, (double2*)zbload,
+                                     (double2*)aschur, (double2*)bschur);
 }
 
 }  // namespace hp3dg
