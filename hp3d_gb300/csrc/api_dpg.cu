@@ -280,6 +280,31 @@ int hp3dg_dpg_submit(hp3dg_dpg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
     w.tb.b = dalloc<uint8_t>(c, ne * dpg_tc_b_bytes((int)na), &err);
     w.tb.ea = dalloc<int>(c, ne * dpg_tc_ex_slots((int)na), &err);
     w.tb.eb = dalloc<int>(c, ne * dpg_tc_ex_slots((int)na), &err);
+    if (ozaki_plan(d.nv, d.nEE, 7, 7, &w.gplan)) err = HP3DG_ERR_ARG;
+    for (int which = 0; which < 2 && !err; ++which) {
+      w.gmdig[which] = (uint16_t*)dalloc<uint8_t>(c, ozaki_m_bytes(w.gplan), &err);
+      w.gmscale[which] = dalloc<double>(c, w.gplan.ncols, &err);
+      w.gddig[which] = (uint16_t*)dalloc<uint8_t>(c, ozaki_d_bytes(w.gplan, (int)ne), &err);
+      w.gdscale[which] = dalloc<double>(c, (ne + 127) / 128 * 128, &err);
+      w.gD[which] = dalloc<double>(c, ne * 6 * d.nv, &err);
+    }
+    const int kPR = 3 * d.nv, kT = 9 * 6 * d.nfp;
+    if (ozaki_plan_dense(kPR, d.nEE * d.nQ, 7, 7, &w.bplan[0]) ||
+        ozaki_plan_dense(kPR, d.nEE * d.nQ, 7, 7, &w.bplan[1]) ||
+        ozaki_plan_dense(kT, d.nEE * d.nEi, 7, 7, &w.bplan[2]))
+      err = HP3DG_ERR_ARG;
+    size_t mdense = 0, dbytes = 0;
+    for (int which = 0; which < 3 && !err; ++which) {
+      w.bmdig[which] = (uint16_t*)dalloc<uint8_t>(c, ozaki_m_bytes(w.bplan[which]), &err);
+      w.bmscale[which] = dalloc<double>(c, w.bplan[which].ncols, &err);
+      mdense = std::max(mdense, (size_t)w.bplan[which].kreal * w.bplan[which].nreal);
+      dbytes = std::max(dbytes, ozaki_d_bytes(w.bplan[which], which < 2 ? 3 * (int)ne : (int)ne));
+    }
+    w.bddig = (uint16_t*)dalloc<uint8_t>(c, dbytes, &err);
+    w.bdscale = dalloc<double>(c, (3 * ne + 127) / 128 * 128, &err);
+    w.bDP = dalloc<double>(c, 3 * ne * kPR, &err);
+    w.bDR = dalloc<double>(c, 3 * ne * kPR, &err);
+    w.bMd = dalloc<double>(c, mdense, &err);
   } else {
     w.G = dalloc<double>(c, ne * 2 * nt * nt, &err);
     w.S = dalloc<double>(c, ne * 2 * nt * n1, &err);
@@ -343,6 +368,7 @@ int hp3dg_dpg_run(hp3dg_dpg_ctx* c) {
   if (c->nel == 0) { c->ran = true; return HP3DG_OK; }
   if (!c->tables) {
     launch_dpg_tables(c->d, c->d_xiV, c->d_wV, c->d_xiF, c->d_xiI, c->t, c->w.MFC, st);
+    if (c->w.tc && launch_dpg_gram_tables(c->d, c->t, c->w, st)) return HP3DG_ERR_CUDA;
     c->tables = true;
   }
   CK(cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st));

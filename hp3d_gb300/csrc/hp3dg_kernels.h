@@ -127,6 +127,7 @@ struct OzakiPlan {
   int levels;     // number of exact FP32 level accumulators
   int kdim;       // 6*nint rounded up to the K tile
   int ncols;      // n(n+1)/2 rounded up to the N tile
+  int kreal = 0, nreal = 0;  // dense plans: K and columns before rounding
 };
 int ozaki_plan(int nint, int n, int radix, int digits, OzakiPlan* plan);
 // build the M digit table of a bin (once): B operand, column scales
@@ -143,6 +144,17 @@ int ozaki_pairs(const OzakiPlan& plan);
 int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
                       double* d_PK, int* d_flag, cudaStream_t st);
+
+// the same contraction for a dense bin-constant M (K x ncols, row-major FP64):
+// OUT[r, c] = sum_q D[r, q] M[q, c] for rows r of D (K per row)
+int ozaki_plan_dense(int K, int ncols, int radix, int digits, OzakiPlan* plan);
+int launch_ozaki_build_m_dense(const OzakiPlan& plan, const double* d_M, uint16_t* d_mdig,
+                               double* d_mscale, cudaStream_t st);
+int launch_ozaki_slice_d_dense(const OzakiPlan& plan, int nrows, const double* d_D,
+                               uint16_t* d_ddig, double* d_dscale, cudaStream_t st);
+int launch_ozaki_gemm_dense(const OzakiPlan& plan, int nrows, const uint16_t* d_ddig,
+                            const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                            double* d_out, int* d_flag, cudaStream_t st);
 
 // constrained approximation (hanging nodes) -- k_constrain.cu
 struct ConstrainArgs {
@@ -199,7 +211,27 @@ struct DpgWork {
   // tensor-core path: augmented matrix (nt + nr + 1)^2 per element, the
   // inverse diagonal blocks of the panels (64 x 64 each), ASchur workspace
   double *M = nullptr, *W = nullptr, *Y = nullptr;
+  // M_FF (0) and M_CC (1) as split-BF16 contractions (k_ozaki.cu): the test
+  // function tables as bin-constant digit operands, the per-point metrics as
+  // per-element rows; MFF / MCC then hold packed upper triangles
+  OzakiPlan gplan{};
+  uint16_t* gmdig[2] = {nullptr, nullptr};
+  double* gmscale[2] = {nullptr, nullptr};
+  uint16_t* gddig[2] = {nullptr, nullptr};
+  double* gdscale[2] = {nullptr, nullptr};
+  double* gD[2] = {nullptr, nullptr};
+  // P (0), R (1), T (2) the same way, with dense bin-constant tables:
+  // P/R rows (element, component c) over (point, i), T rows per element over
+  // (face point, a, b); the dense tables are staged in bMd once per batch
+  OzakiPlan bplan[3]{};
+  uint16_t* bmdig[3] = {nullptr, nullptr, nullptr};
+  double* bmscale[3] = {nullptr, nullptr, nullptr};
+  uint16_t* bddig = nullptr;
+  double* bdscale = nullptr;
+  double *bDP = nullptr, *bDR = nullptr, *bMd = nullptr;
 };
+// the digit tables of the test functions (once per batch, tensor-core path)
+int launch_dpg_gram_tables(const DpgDims& d, const DpgTables& t, const DpgWork& w, cudaStream_t st);
 void launch_dpg_tables(const DpgDims& d, const double* xiV, const double* wV, const double* xiF,
                        const double* xiI, const DpgTables& t, double* mfc, cudaStream_t st);
 // the dense DPG algebra on tensor cores -- k_dpg_tc.cu

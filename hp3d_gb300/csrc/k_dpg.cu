@@ -263,6 +263,55 @@ __global__ void k_dpg_geom(DpgDims d, DpgPhys ph, const double* xiV, const doubl
   }
 }
 
+// the metrics D1 and D2 of every volume point as rows [e][l][6] (the
+// per-element operand of the split-BF16 contraction)
+__global__ void k_dpg_dpack(DpgDims d, const double* gV, double* D1, double* D2) {
+  const int e = blockIdx.x;
+  for (int x = threadIdx.x; x < 6 * d.nv; x += blockDim.x) {
+    const double* g = gV + ((size_t)e * d.nv + x / 6) * DPG_GV;
+    D1[(size_t)e * 6 * d.nv + x] = g[x % 6];
+    D2[(size_t)e * 6 * d.nv + x] = g[6 + x % 6];
+  }
+}
+
+// dense bin-constant tables of the couplings (row-major K x ncols):
+//   which 0 (P): [(l, i)][(k1, k2)] = phi_k1,i(l) q_k2(l)
+//   which 1 (R): [(l, i)][(k1, k2)] = (curl phi_k1)_i(l) q_k2(l)
+//   which 2 (T): [(l, a, b)][(k1, m)] = phi_k1,a(l) psi_m,b(l), l over face points
+__global__ void k_dpg_bdense(DpgDims d, DpgTables t, int which, double* Md) {
+  const int nE = d.nEE;
+  const int64_t ncols = which < 2 ? (int64_t)nE * d.nQ : (int64_t)nE * d.nEi;
+  const int64_t K = which < 2 ? 3 * (int64_t)d.nv : 9 * 6 * (int64_t)d.nfp;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < K * ncols;
+       x += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t q = x / ncols, c = x % ncols;
+    const int k1 = (int)(c % nE), k2 = (int)(c / nE);
+    double v;
+    if (which < 2) {
+      const int l = (int)(q / 3), i = (int)(q % 3);
+      const double* T = which ? t.vc : t.vs;
+      v = T[(size_t)l * 3 * nE + (size_t)i * nE + k1] * t.vq[(size_t)l * d.nQ + k2];
+    } else {
+      const int l = (int)(q / 9), a = (int)(q % 9) / 3, b = (int)(q % 3);
+      v = t.fs[(size_t)l * 3 * nE + (size_t)a * nE + k1] *
+          t.ft[(size_t)l * 3 * d.nEi + (size_t)b * d.nEi + k2];
+    }
+    Md[x] = v;
+  }
+}
+
+// D rows of P and R: row (e, c) = A(l)_{i,c} (A = w J^-1) and B(l)_{c,i}
+// (B = w J / detJ) over (l, i)
+__global__ void k_dpg_dpackPR(DpgDims d, const double* gV, double* DP, double* DR) {
+  const int e = blockIdx.x, K = 3 * d.nv;
+  for (int x = threadIdx.x; x < 3 * K; x += blockDim.x) {
+    const int c = x / K, q = x % K, l = q / 3, i = q % 3;
+    const double* g = gV + ((size_t)e * d.nv + l) * DPG_GV;
+    DP[((size_t)3 * e + c) * K + q] = g[12 + 3 * i + c];
+    DR[((size_t)3 * e + c) * K + q] = g[21 + 3 * c + i];
+  }
+}
+
 // M_FF (which 0, metric D1, values) and M_CC (which 1, metric D2, curls):
 // C[k1][k2] = sum_l phi_k1(l)^T D_l phi_k2(l), upper 64x64 tiles, mirrored.
 constexpr int GR_PTS = 8;
@@ -334,10 +383,10 @@ __global__ void __launch_bounds__(256) k_dpg_gram(DpgDims d, DpgTables t, const 
 constexpr int BQ_CH = 8, BT_CH = 12;
 __global__ void __launch_bounds__(128) k_dpg_bmat(DpgDims d, DpgTables t, const double* gV,
                                                   const double* gF, double* P, double* R,
-                                                  double* Tm, double* load) {
+                                                  double* Tm, double* load, int zbase) {
   const int e = blockIdx.x, k1 = blockIdx.y * blockDim.x + threadIdx.x;
   const int nzq = (d.nQ + BQ_CH - 1) / BQ_CH, nzt = (d.nEi + BT_CH - 1) / BT_CH;
-  const int z = blockIdx.z;
+  const int z = zbase + blockIdx.z;
   if (k1 >= d.nEE) return;
   const int n3q = 3 * d.nQ;
   if (z < nzq) {
@@ -422,8 +471,9 @@ __global__ void k_dpg_assemble(DpgDims d, DpgPhys ph, const double* eps, const d
   const double2 za = make_double2(-ph.omega * ei, ph.omega * er);  // i w eps
   const double2 zc1 = make_double2(0.0, ph.omega * ph.mu);
   const double za2 = za.x * za.x + za.y * za.y, zc2 = zc1.y * zc1.y;
-  const double* mff = MFF + (size_t)e * nE * nE;
-  const double* mcc = MCC + (size_t)e * nE * nE;
+  const size_t mst = AUG ? (size_t)nE * (nE + 1) / 2 : (size_t)nE * nE;
+  const double* mff = MFF + (size_t)e * mst;
+  const double* mcc = MCC + (size_t)e * mst;
   const int n1 = d.nr + 1, NA = nt + n1;
   const size_t ldg = AUG ? (size_t)NA : (size_t)nt;
   double2* g = AUG ? G + (size_t)e * NA * NA : G + (size_t)e * nt * nt;
@@ -435,7 +485,10 @@ __global__ void k_dpg_assemble(DpgDims d, DpgPhys ph, const double* eps, const d
     double2 v;
     if (a == b) {
       const double s = (a == 0 ? za2 : zc2) + ph.alpha;
-      v = make_double2(s * mff[k1 + (size_t)k2 * nE] + mcc[k1 + (size_t)k2 * nE], 0.0);
+      // AUG: M_FF and M_CC as packed upper triangles (k_ozaki.cu layout)
+      const size_t ix = AUG ? (k1 < k2 ? (size_t)k2 * (k2 + 1) / 2 + k1 : (size_t)k1 * (k1 + 1) / 2 + k2)
+                            : k1 + (size_t)k2 * nE;
+      v = make_double2(s * mff[ix] + mcc[ix], 0.0);
     } else {
       const double f12 = MFC[k1 + (size_t)k2 * nE], f21 = MFC[k2 + (size_t)k1 * nE];
       if (a == 0)  // -za M_FC(k1,k2) + conj(zc1) M_FC(k2,k1)
@@ -473,7 +526,9 @@ __global__ void k_dpg_assemble(DpgDims d, DpgPhys ph, const double* eps, const d
     } else if (c < nr) {
       const int k2 = (c - ni) / 6, comp = (c - ni) % 6;
       const int cc = comp % 3;
-      const double pv = pe[k1 + (size_t)(3 * k2 + cc) * nE], rv = re[k1 + (size_t)(3 * k2 + cc) * nE];
+      // AUG: P and R from the split-BF16 contraction, rows (element, cc)
+      const size_t pix = AUG ? k1 + (size_t)(cc * d.nQ + k2) * nE : k1 + (size_t)(3 * k2 + cc) * nE;
+      const double pv = pe[pix], rv = re[pix];
       if (a == 0) v = comp < 3 ? make_double2(-za.x * pv, -za.y * pv) : make_double2(rv, 0.0);
       else v = comp < 3 ? make_double2(rv, 0.0) : make_double2(zc1.x * pv, zc1.y * pv);
     } else if (a == 0) {
@@ -595,6 +650,20 @@ void launch_dpg_tables(const DpgDims& d, const double* xiV, const double* wV, co
   k_dpg_mfc<<<dim3((d.nEE + 127) / 128, d.nEE), 128, 0, st>>>(d, wV, t, mfc);
 }
 
+int launch_dpg_gram_tables(const DpgDims& d, const DpgTables& t, const DpgWork& w,
+                           cudaStream_t st) {
+  for (int which = 0; which < 2; ++which)
+    if (launch_ozaki_build_m(w.gplan, d.nv, d.nEE, d.nEE, 0, which ? t.vc : t.vs, w.gmdig[which],
+                             w.gmscale[which], nullptr, st))
+      return -1;
+  for (int which = 0; which < 3; ++which) {
+    k_dpg_bdense<<<1024, 256, 0, st>>>(d, t, which, w.bMd);
+    if (launch_ozaki_build_m_dense(w.bplan[which], w.bMd, w.bmdig[which], w.bmscale[which], st))
+      return -1;
+  }
+  return 0;
+}
+
 void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
                       const DpgTables& t, const DpgWork& w, const double* xvert, const double* eps,
                       const int* imp_mask, const uint32_t* perm, const int* nextract,
@@ -605,11 +674,35 @@ void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
   if (stage == 0) {
     k_dpg_geom<<<nel, 128, 0, st>>>(d, ph, w.xiV, w.wV, w.xiF, w.wF, w.xiI, w.wI, xvert, eps,
                                     w.gV, w.gF, w.gI, flags);
-    const int nt = (d.nEE + 63) / 64;
-    k_dpg_gram<<<dim3(nel, nt * (nt + 1) / 2, 2), 256, 0, st>>>(d, t, w.gV, w.MFF, w.MCC);
+    if (w.tc) {
+      k_dpg_dpack<<<nel, 256, 0, st>>>(d, w.gV, w.gD[0], w.gD[1]);
+      for (int which = 0; which < 2; ++which) {
+        launch_ozaki_slice_d(w.gplan, nel, d.nv, w.gD[which], w.gddig[which], w.gdscale[which], st);
+        launch_ozaki_gemm(w.gplan, nel, d.nEE, w.gddig[which], w.gdscale[which], w.gmdig[which],
+                          w.gmscale[which], which ? w.MCC : w.MFF, flags + 2, st);
+      }
+    } else {
+      const int nt = (d.nEE + 63) / 64;
+      k_dpg_gram<<<dim3(nel, nt * (nt + 1) / 2, 2), 256, 0, st>>>(d, t, w.gV, w.MFF, w.MCC);
+    }
     const int nzq = (d.nQ + BQ_CH - 1) / BQ_CH, nzt = (d.nEi + BT_CH - 1) / BT_CH;
-    k_dpg_bmat<<<dim3(nel, (d.nEE + 127) / 128, nzq + nzt + 1), 128, 0, st>>>(
-        d, t, w.gV, w.gF, w.P, w.R, w.T, w.load);
+    if (w.tc) {
+      k_dpg_dpackPR<<<nel, 256, 0, st>>>(d, w.gV, w.bDP, w.bDR);
+      for (int which = 0; which < 3; ++which) {
+        const int rows = which < 2 ? 3 * nel : nel;
+        const double* D = which == 0 ? w.bDP : (which == 1 ? w.bDR : w.gF);
+        double* out = which == 0 ? w.P : (which == 1 ? w.R : w.T);
+        launch_ozaki_slice_d_dense(w.bplan[which], rows, D, w.bddig, w.bdscale, st);
+        launch_ozaki_gemm_dense(w.bplan[which], rows, w.bddig, w.bdscale, w.bmdig[which],
+                                w.bmscale[which], out, flags + 2, st);
+      }
+      // the load only
+      k_dpg_bmat<<<dim3(nel, (d.nEE + 127) / 128, 1), 128, 0, st>>>(d, t, w.gV, w.gF, w.P, w.R,
+                                                                    w.T, w.load, nzq + nzt);
+    } else {
+      k_dpg_bmat<<<dim3(nel, (d.nEE + 127) / 128, nzq + nzt + 1), 128, 0, st>>>(
+          d, t, w.gV, w.gF, w.P, w.R, w.T, w.load, 0);
+    }
     if (w.tc)
       k_dpg_assemble<true><<<dim3(nel, 32), 256, 0, st>>>(d, ph, eps, w.MFF, w.MCC, w.MFC, w.P,
                                                           w.R, w.T, w.load, perm,

@@ -444,6 +444,33 @@ __global__ void k_build_m(int nint, int n, int ni, int nb, int ncols, int nk, in
   write_digits8(vals, rs, radix, digits, mdig, nk, cb, kb, r, kg);
 }
 
+// dense M (K x ncols, row-major): column scales and digit tiles
+__global__ void k_m_scale_dense(int K, int ncols, int ncols_pad, const double* __restrict__ Md,
+                                double* __restrict__ mscale) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncols_pad) return;
+  if (c >= ncols) { mscale[c] = 1.0; return; }
+  double mx = 0.0;
+  for (int q = 0; q < K; ++q) mx = fmax(mx, fabs(Md[(size_t)q * ncols + c]));
+  mscale[c] = pow2_ceil_scale(mx);
+}
+
+__global__ void k_build_m_dense(int K, int ncols, int nk, int radix, int digits,
+                                const double* __restrict__ Md, const double* __restrict__ mscale,
+                                uint8_t* __restrict__ mdig) {
+  const int kb = blockIdx.x, cb = blockIdx.y;
+  const int r = threadIdx.x >> 1, kg = threadIdx.x & 1;
+  const int c = cb * 128 + r;
+  double vals[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) {
+    const int q = kb * 16 + kg * 8 + t;
+    vals[t] = (c < ncols && q < K) ? Md[(size_t)q * ncols + c] : 0.0;
+  }
+  const double rs = (c < ncols) ? 1.0 / mscale[c] : 0.0;
+  write_digits8(vals, rs, radix, digits, mdig, nk, cb, kb, r, kg);
+}
+
 // D digit tiles: grid (k-blocks, element blocks), 256 threads
 __global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
                           const double* __restrict__ D, const double* __restrict__ dscale,
@@ -480,6 +507,18 @@ int ozaki_plan(int nint, int n, int radix, int digits, OzakiPlan* plan) {
   return 0;
 }
 
+int ozaki_plan_dense(int K, int ncols, int radix, int digits, OzakiPlan* plan) {
+  if (radix < 4 || radix > 8 || digits < 2 || digits > MAXDIG || K <= 0 || ncols <= 0) return -1;
+  plan->radix = radix;
+  plan->digits = digits;
+  plan->levels = digits;
+  plan->kdim = round_up(K, BK);
+  plan->ncols = round_up(ncols, BM);
+  plan->kreal = K;
+  plan->nreal = ncols;
+  return 0;
+}
+
 size_t ozaki_m_bytes(const OzakiPlan& p) { return (size_t)p.digits * p.ncols * p.kdim * 2; }
 size_t ozaki_d_bytes(const OzakiPlan& p, int nel) {
   return (size_t)p.digits * round_up(nel, BN) * p.kdim * 2;
@@ -503,6 +542,26 @@ int launch_ozaki_slice_d(const OzakiPlan& p, int nel, int nint, const double* d_
   k_d_scale<<<nel_pad, 256, 0, st>>>(6 * nint, nel, d_D, d_dscale);
   dim3 g(p.kdim / BK, nel_pad / BN);
   k_slice_d<<<g, 256, 0, st>>>(6 * nint, p.kdim / BK, nel, p.radix, p.digits, d_D, d_dscale,
+                               (uint8_t*)d_ddig);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_ozaki_build_m_dense(const OzakiPlan& p, const double* d_M, uint16_t* d_mdig,
+                               double* d_mscale, cudaStream_t st) {
+  k_m_scale_dense<<<p.ncols / 128, 128, 0, st>>>(p.kreal, p.nreal, p.ncols, d_M, d_mscale);
+  dim3 g(p.kdim / BK, p.ncols / BM);
+  k_build_m_dense<<<g, 256, 0, st>>>(p.kreal, p.nreal, p.kdim / BK, p.radix, p.digits, d_M,
+                                     d_mscale, (uint8_t*)d_mdig);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_ozaki_slice_d_dense(const OzakiPlan& p, int nrows, const double* d_D, uint16_t* d_ddig,
+                               double* d_dscale, cudaStream_t st) {
+  int nel_pad = round_up(nrows, BN);
+  if (nel_pad == 0) return 0;
+  k_d_scale<<<nel_pad, 256, 0, st>>>(p.kreal, nrows, d_D, d_dscale);
+  dim3 g(p.kdim / BK, nel_pad / BN);
+  k_slice_d<<<g, 256, 0, st>>>(p.kreal, p.kdim / BK, nrows, p.radix, p.digits, d_D, d_dscale,
                                (uint8_t*)d_ddig);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -555,9 +614,26 @@ int ozaki_pairs(const OzakiPlan& p) {
   return G.npairs;
 }
 
+static int ozaki_gemm_cols(const OzakiPlan& p, int nel, int ncols_real, const uint16_t* d_ddig,
+                           const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                           double* d_PK, int* d_flag, cudaStream_t st);
+
 int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
                       double* d_PK, int* d_flag, cudaStream_t st) {
+  return ozaki_gemm_cols(p, nel, n * (n + 1) / 2, d_ddig, d_dscale, d_mdig, d_mscale, d_PK, d_flag,
+                         st);
+}
+
+int launch_ozaki_gemm_dense(const OzakiPlan& p, int nrows, const uint16_t* d_ddig,
+                            const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                            double* d_out, int* d_flag, cudaStream_t st) {
+  return ozaki_gemm_cols(p, nrows, p.nreal, d_ddig, d_dscale, d_mdig, d_mscale, d_out, d_flag, st);
+}
+
+static int ozaki_gemm_cols(const OzakiPlan& p, int nel, int ncols_real, const uint16_t* d_ddig,
+                           const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                           double* d_PK, int* d_flag, cudaStream_t st) {
   if (nel <= 0) return 0;
   static int num_sms = 0;
   if (!num_sms) {
@@ -573,7 +649,7 @@ int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig
   G.ncb = p.ncols / BM;
   G.neb = nel_pad / BN;
   G.nel = nel;
-  G.ncols = n * (n + 1) / 2;
+  G.ncols = ncols_real;
   size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024;
   static bool attr = false;
   if (!attr) {
