@@ -29,6 +29,7 @@ struct hp3dg_dpg_ctx {
   DpgPhys ph{};
   std::vector<int64_t> lcon_off, elem_nnz, schur_off, bub_off;
   int32_t last_bad = -1;
+  int64_t launches = 0;    // kernels launched by the last run
   std::vector<void*> dev;  // every device allocation of the batch
   double *d_xiV = nullptr, *d_wV = nullptr, *d_xiF = nullptr, *d_wF = nullptr, *d_xiI = nullptr,
          *d_wI = nullptr;
@@ -373,11 +374,16 @@ int hp3dg_dpg_run(hp3dg_dpg_ctx* c) {
   }
   CK(cudaMemsetAsync(c->d_flags, 0x7f, 4 * sizeof(int), st));
   cudaEventRecord(c->ev[0], st);
+  c->launches = 0;
+  bool fail = false;
   auto stage = [&](int s) {
-    launch_dpg_stage(s, c->nel, c->d, c->ph, c->t, c->w, c->d_xvert, c->d_eps, c->d_imp,
-                     c->d_perm, c->d_nextract, c->d_lcon_off, c->d_elem_nnz, c->d_schur_off,
-                     c->d_bub_off, c->d_zastif, c->d_zbload, c->d_aschur, c->d_bschur,
-                     c->w.tc ? c->d_zkeep : nullptr, c->d_flags, st);
+    const int k = launch_dpg_stage(s, c->nel, c->d, c->ph, c->t, c->w, c->d_xvert, c->d_eps,
+                                   c->d_imp, c->d_perm, c->d_nextract, c->d_lcon_off,
+                                   c->d_elem_nnz, c->d_schur_off, c->d_bub_off, c->d_zastif,
+                                   c->d_zbload, c->d_aschur, c->d_bschur,
+                                   c->w.tc ? c->d_zkeep : nullptr, c->d_flags, st);
+    if (k < 0) fail = true;
+    else c->launches += k;
   };
   stage(0);
   cudaEventRecord(c->ev[1], st);
@@ -392,7 +398,9 @@ int hp3dg_dpg_run(hp3dg_dpg_ctx* c) {
   cudaEventRecord(c->ev[3], st);
   launch_index_maps(c->nel, 26, c->nnodes, c->d_nodes, c->d_ndofm, c->d_lcon_off, c->d_first,
                     c->d_cnt, c->d_scan, c->d_blk, c->d_total, c->d_nfirst, c->d_lcon, st);
+  c->launches += 7;
   cudaEventRecord(c->ev[4], st);
+  if (fail) return HP3DG_ERR_CUDA;
   CK(cudaPeekAtLastError());
   c->ran = true;
   c->downloaded = false;
@@ -520,6 +528,13 @@ int hp3dg_dpg_phase_times(const hp3dg_dpg_ctx* c, float* ms, int32_t n) {
 }
 
 int32_t hp3dg_dpg_last_bad_element(const hp3dg_dpg_ctx* c) { return c ? c->last_bad : -1; }
+
+int hp3dg_dpg_pass_stats(const hp3dg_dpg_ctx* c, int64_t* kernels) {
+  if (!c || !kernels) return HP3DG_ERR_ARG;
+  if (!c->ran) return HP3DG_ERR_STATE;
+  *kernels = c->launches;
+  return HP3DG_OK;
+}
 
 void hp3dg_dpg_end(hp3dg_dpg_ctx* c) {
   if (!c) return;

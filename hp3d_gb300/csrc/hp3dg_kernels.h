@@ -240,19 +240,21 @@ size_t dpg_tc_a_bytes(int rows);
 size_t dpg_tc_b_bytes(int rows);
 // the augmented partial factorization: part 1 eliminates the test unknowns
 // (trailing block -> Z), 2 the L2 fields (-> Schur complement, ASchur), 3
-// writes Z in the interface order [E | Q | l] (full) to zkeep
+// writes Z in the interface order [E | Q | l] (full) to zkeep.  Returns the
+// number of kernels launched, or -1.
 int dpg_aug_wslots(int nt, int nq);
 int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& w, double* zkeep,
                       int* bad, int* err, cudaStream_t st);
-void launch_dpg_aug_out(int nel, int nt, int n1, int nq, const DpgWork& w, const int* nextract,
+int launch_dpg_aug_out(int nel, int nt, int n1, int nq, const DpgWork& w, const int* nextract,
                         const int64_t* lcon_off, const int64_t* elem_nnz,
                         const int64_t* schur_off, const int64_t* bub_off, double* zastif,
                         double* zbload, double* aschur, double* bschur, cudaStream_t st);
 
 // stage 0: geometry, real contractions, assembly of G and [B|l];
 // 1: Cholesky of G, forward solve, Z = X^H X, impedance penalty;
-// 2: condensation of the L2 fields and compression
-void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
+// 2: condensation of the L2 fields and compression.  Returns the number of
+// kernels launched, or -1.
+int launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
                       const DpgTables& t, const DpgWork& w, const double* xvert, const double* eps,
                       const int* imp_mask, const uint32_t* perm, const int* nextract,
                       const int64_t* lcon_off, const int64_t* elem_nnz, const int64_t* schur_off,

@@ -664,83 +664,102 @@ int launch_dpg_gram_tables(const DpgDims& d, const DpgTables& t, const DpgWork& 
   return 0;
 }
 
-void launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
-                      const DpgTables& t, const DpgWork& w, const double* xvert, const double* eps,
-                      const int* imp_mask, const uint32_t* perm, const int* nextract,
-                      const int64_t* lcon_off, const int64_t* elem_nnz, const int64_t* schur_off,
-                      const int64_t* bub_off, double* zastif, double* zbload, double* aschur,
-                      double* bschur, double* zkeep, int* flags, cudaStream_t st) {
-  if (nel <= 0) return;
+int launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
+                     const DpgTables& t, const DpgWork& w, const double* xvert, const double* eps,
+                     const int* imp_mask, const uint32_t* perm, const int* nextract,
+                     const int64_t* lcon_off, const int64_t* elem_nnz, const int64_t* schur_off,
+                     const int64_t* bub_off, double* zastif, double* zbload, double* aschur,
+                     double* bschur, double* zkeep, int* flags, cudaStream_t st) {
+  if (nel <= 0) return 0;
+  int nk = 0;
+  bool fail = false;
+  auto sub = [&](int rc, int kernels) {  // a sub-launcher: 0 or its count, -1 on error
+    if (rc < 0) fail = true;
+    else nk += kernels > 0 ? kernels : rc;
+  };
   if (stage == 0) {
     k_dpg_geom<<<nel, 128, 0, st>>>(d, ph, w.xiV, w.wV, w.xiF, w.wF, w.xiI, w.wI, xvert, eps,
                                     w.gV, w.gF, w.gI, flags);
+    ++nk;
     if (w.tc) {
       k_dpg_dpack<<<nel, 256, 0, st>>>(d, w.gV, w.gD[0], w.gD[1]);
+      ++nk;
       for (int which = 0; which < 2; ++which) {
-        launch_ozaki_slice_d(w.gplan, nel, d.nv, w.gD[which], w.gddig[which], w.gdscale[which], st);
-        launch_ozaki_gemm(w.gplan, nel, d.nEE, w.gddig[which], w.gdscale[which], w.gmdig[which],
-                          w.gmscale[which], which ? w.MCC : w.MFF, flags + 2, st);
+        sub(launch_ozaki_slice_d(w.gplan, nel, d.nv, w.gD[which], w.gddig[which],
+                                 w.gdscale[which], st), 2);
+        sub(launch_ozaki_gemm(w.gplan, nel, d.nEE, w.gddig[which], w.gdscale[which],
+                              w.gmdig[which], w.gmscale[which], which ? w.MCC : w.MFF, flags + 2,
+                              st), 1);
       }
     } else {
       const int nt = (d.nEE + 63) / 64;
       k_dpg_gram<<<dim3(nel, nt * (nt + 1) / 2, 2), 256, 0, st>>>(d, t, w.gV, w.MFF, w.MCC);
+      ++nk;
     }
     const int nzq = (d.nQ + BQ_CH - 1) / BQ_CH, nzt = (d.nEi + BT_CH - 1) / BT_CH;
     if (w.tc) {
       k_dpg_dpackPR<<<nel, 256, 0, st>>>(d, w.gV, w.bDP, w.bDR);
+      ++nk;
       for (int which = 0; which < 3; ++which) {
         const int rows = which < 2 ? 3 * nel : nel;
         const double* D = which == 0 ? w.bDP : (which == 1 ? w.bDR : w.gF);
         double* out = which == 0 ? w.P : (which == 1 ? w.R : w.T);
-        launch_ozaki_slice_d_dense(w.bplan[which], rows, D, w.bddig, w.bdscale, st);
-        launch_ozaki_gemm_dense(w.bplan[which], rows, w.bddig, w.bdscale, w.bmdig[which],
-                                w.bmscale[which], out, flags + 2, st);
+        sub(launch_ozaki_slice_d_dense(w.bplan[which], rows, D, w.bddig, w.bdscale, st), 2);
+        sub(launch_ozaki_gemm_dense(w.bplan[which], rows, w.bddig, w.bdscale, w.bmdig[which],
+                                    w.bmscale[which], out, flags + 2, st), 1);
       }
       // the load only
       k_dpg_bmat<<<dim3(nel, (d.nEE + 127) / 128, 1), 128, 0, st>>>(d, t, w.gV, w.gF, w.P, w.R,
                                                                     w.T, w.load, nzq + nzt);
-    } else {
-      k_dpg_bmat<<<dim3(nel, (d.nEE + 127) / 128, nzq + nzt + 1), 128, 0, st>>>(
-          d, t, w.gV, w.gF, w.P, w.R, w.T, w.load, 0);
-    }
-    if (w.tc)
       k_dpg_assemble<true><<<dim3(nel, 32), 256, 0, st>>>(d, ph, eps, w.MFF, w.MCC, w.MFC, w.P,
                                                           w.R, w.T, w.load, perm,
                                                           (double2*)w.M, nullptr);
-    else
+    } else {
+      k_dpg_bmat<<<dim3(nel, (d.nEE + 127) / 128, nzq + nzt + 1), 128, 0, st>>>(
+          d, t, w.gV, w.gF, w.P, w.R, w.T, w.load, 0);
       k_dpg_assemble<false><<<dim3(nel, 32), 256, 0, st>>>(d, ph, eps, w.MFF, w.MCC, w.MFC, w.P,
                                                            w.R, w.T, w.load, perm,
                                                            (double2*)w.G, (double2*)w.S);
+    }
+    nk += 2;
   } else if (stage == 1) {
     const int n1 = d.nr + 1;
     const dim3 gimp(nel, (d.nEi * d.nEi + 255) / 256);
     if (w.tc) {
       // test block of the augmented matrix -> -Z in the trailing block -> Z
       const int nt = 2 * d.nEE, na = nt + n1, nq = 6 * d.nQ;
-      launch_dpg_aug_tc(1, nel, nt, n1, nq, w, zkeep, flags + 1, flags + 2, st);
-      if (ph.ibcflag == 2)
+      sub(launch_dpg_aug_tc(1, nel, nt, n1, nq, w, zkeep, flags + 1, flags + 2, st), 0);
+      if (ph.ibcflag == 2) {
         k_dpg_imp<<<gimp, 256, 0, st>>>(d, imp_mask, t, w.gI, perm, (double2*)w.M,
                                         (int64_t)na * na, nt + nq, na);
-      if (zkeep) launch_dpg_aug_tc(3, nel, nt, n1, nq, w, zkeep, flags + 1, flags + 2, st);
+        ++nk;
+      }
+      if (zkeep) sub(launch_dpg_aug_tc(3, nel, nt, n1, nq, w, zkeep, flags + 1, flags + 2, st), 0);
     } else {
       k_dpg_dpg<<<nel, LA_THREADS, 0, st>>>(d, (double2*)w.G, (double2*)w.S, (double2*)w.Z,
                                             flags + 1);
-      if (ph.ibcflag == 2)
+      ++nk;
+      if (ph.ibcflag == 2) {
         k_dpg_imp<<<gimp, 256, 0, st>>>(d, imp_mask, t, w.gI, perm, (double2*)w.Z,
                                         (int64_t)n1 * n1, 0, n1);
+        ++nk;
+      }
     }
   } else if (w.tc) {
     // L2 block of Z -> Schur complement, ASchur/BSchur, compression
     const int nt = 2 * d.nEE, n1 = d.nr + 1, nq = 6 * d.nQ;
-    launch_dpg_aug_tc(2, nel, nt, n1, nq, w, nullptr, flags + 1, flags + 2, st);
-    launch_dpg_aug_out(nel, nt, n1, nq, w, nextract, lcon_off, elem_nnz, schur_off, bub_off,
-                       zastif, zbload, aschur, bschur, st);
+    sub(launch_dpg_aug_tc(2, nel, nt, n1, nq, w, nullptr, flags + 1, flags + 2, st), 0);
+    sub(launch_dpg_aug_out(nel, nt, n1, nq, w, nextract, lcon_off, elem_nnz, schur_off, bub_off,
+                           zastif, zbload, aschur, bschur, st), 0);
   } else {
     k_dpg_condense<<<nel, LA_THREADS, 0, st>>>(d, (double2*)w.Z, nextract, lcon_off, elem_nnz,
                                                schur_off, bub_off, (double2*)zastif,
                                                (double2*)zbload, (double2*)aschur,
                                                (double2*)bschur, flags + 1);
+    ++nk;
   }
+  if (fail || cudaPeekAtLastError() != cudaSuccess) return -1;
+  return nk;
 }
 
 }  // namespace hp3dg

@@ -116,6 +116,94 @@ __global__ void k_zslice(ZSlice a) {
   }
 }
 
+// digits of 8 fixed-point integers (most significant first), as BF16 bits
+__device__ __forceinline__ void digits8(long long* X, uint32_t (*h)[8]) {
+  const long long half = 1LL << (ZR - 1);
+  for (int dg = ZD - 1; dg >= 0; --dg)
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      long long d;
+      if (dg > 0) {
+        const long long q = (X[t] + half) >> ZR;
+        d = X[t] - (q << ZR);
+        X[t] = q;
+      } else {
+        d = X[t];
+      }
+      h[dg][t] = __float_as_uint((float)(int)d) >> 16;
+    }
+}
+__device__ __forceinline__ uint4 pack8(const uint32_t* h, uint32_t sign) {
+  uint4 w;
+  w.x = (h[0] | (h[1] << 16)) ^ sign;
+  w.y = (h[2] | (h[3] << 16)) ^ sign;
+  w.z = (h[4] | (h[5] << 16)) ^ sign;
+  w.w = (h[6] | (h[7] << 16)) ^ sign;
+  return w;
+}
+
+// one source row -> the A operand (form [re|im]) and the B operand (forms
+// [re|im] and [-im|re]) with one exponent and one digit expansion: the
+// digits of [-im|re] are those of [re|im] negated and swapped in halves
+// (a negated balanced expansion is again one, digits still <= 2^6)
+struct ZSliceAB {
+  const double2* src;
+  int64_t src_estride, srow, sk;
+  int rows, kc;
+  uint8_t *a, *b;
+  int64_t a_estride, b_estride;
+  int *ea, *eb;
+  int ex_estride;
+};
+__global__ void k_zslice_ab(ZSliceAB a) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = blockIdx.y;
+  const int pa = (a.rows + ZM - 1) / ZM * ZM, pb = (a.rows + ZN - 1) / ZN * ZN;
+  if (row >= pa) return;
+  const bool valid = row < a.rows, inb = row < pb;
+  const double2* s = a.src + (int64_t)e * a.src_estride + (int64_t)row * a.srow;
+  unsigned long long mx = 0;
+  if (valid)
+    for (int k = 0; k < a.kc; ++k) {
+      const double2 z = s[(int64_t)k * a.sk];
+      mx = max(mx, max(mag_bits(z.x), mag_bits(z.y)));
+    }
+  const int ex = row_exponent(mx);
+  a.ea[(int64_t)e * a.ex_estride + row] = valid ? ex : 0;
+  if (inb) a.eb[(int64_t)e * a.ex_estride + row] = valid ? ex : 0;
+  uint8_t* abase = a.a + (int64_t)e * a.a_estride + (size_t)(row / ZM) * ZD * ZA_BLK;
+  uint8_t* bbase = a.b + (int64_t)e * a.b_estride + (size_t)(row / ZN) * ZB_TILE;
+  const int ra = row % ZM, rb = row % ZN;
+  const size_t bdig = (size_t)(2 * ZN / 8) * 256;  // B digit stride (64 rows)
+  for (int g = 0; g < ZGROUPS / 2; ++g) {  // K positions 8g.. (re) and 64 + 8g.. (im)
+    long long Xr[8], Xi[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int k = 8 * g + t;
+      const double2 z = (valid && k < a.kc) ? s[(int64_t)k * a.sk] : make_double2(0.0, 0.0);
+      Xr[t] = fixed_of(z.x, ex, ZFB);
+      Xi[t] = fixed_of(z.y, ex, ZFB);
+    }
+    uint32_t hr[ZD][8], hi[ZD][8];
+    digits8(Xr, hr);
+    digits8(Xi, hi);
+    for (int dg = 0; dg < ZD; ++dg) {
+      const uint4 wr = pack8(hr[dg], 0u), wi = pack8(hi[dg], 0u);
+      const uint4 wmi = pack8(hi[dg], 0x80008000u);  // -im (BF16 sign bits)
+      uint8_t* ad = abase + (size_t)dg * ZA_BLK;
+      *(uint4*)(ad + tile_off(ra, g, ZM)) = wr;
+      *(uint4*)(ad + tile_off(ra, g + ZGROUPS / 2, ZM)) = wi;
+      if (inb) {
+        uint8_t* bd = bbase + (size_t)dg * bdig;
+        *(uint4*)(bd + tile_off(rb, g, ZBROWS)) = wr;                   // form [re|im]
+        *(uint4*)(bd + tile_off(rb, g + ZGROUPS / 2, ZBROWS)) = wi;
+        *(uint4*)(bd + tile_off(ZN + rb, g, ZBROWS)) = wmi;             // form [-im|re]
+        *(uint4*)(bd + tile_off(ZN + rb, g + ZGROUPS / 2, ZBROWS)) = wr;
+      }
+    }
+  }
+}
+
 struct ZUpd {
   const uint8_t* a;
   int64_t a_estride;
@@ -326,24 +414,38 @@ int rows_pad(int rows, int nt) { return (rows + nt - 1) / nt * nt; }
 // FP64 step of one panel of the augmented matrix: the Cholesky factor L11
 // (lower, in place) of the kb x kb diagonal block at (k0, k0) and
 // W = L11^-H (upper, 64 x 64 column-major, zero outside kb x kb), from an
-// unblocked right-looking Cholesky and the forward substitution L11 X = I in
-// shared memory, two barriers per column.
+// unblocked right-looking Cholesky and the forward substitution L11 X = I,
+// both as packed lower triangles in shared memory (67 KB: three CTAs per SM),
+// two barriers per column; row i of the update belongs to one warp, its
+// columns to the lanes.  GB300 issues FP64 at about 1.6 per clock per SM, so
+// the complex updates are 4 fused multiply-adds each.
 constexpr int ZDG_THREADS = 256;
-constexpr size_t ZDG_SMEM = 2 * 64 * 65 * sizeof(double2) + 64 * sizeof(double);
+constexpr int ZDG_TRI = 64 * 65 / 2;
+constexpr size_t ZDG_SMEM = 2 * ZDG_TRI * sizeof(double2) + 64 * sizeof(double);
+
+__device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
+// c - a b and c - a conj(b)
+__device__ __forceinline__ double2 zfms(double2 c, double2 a, double2 b) {
+  return make_double2(fma(a.y, b.y, fma(-a.x, b.x, c.x)), fma(-a.y, b.x, fma(-a.x, b.y, c.y)));
+}
+__device__ __forceinline__ double2 zfms_c(double2 c, double2 a, double2 b) {
+  return make_double2(fma(-a.y, b.y, fma(-a.x, b.x, c.x)), fma(-a.y, b.x, fma(a.x, b.y, c.y)));
+}
 
 __global__ void __launch_bounds__(ZDG_THREADS) k_zdiag(double2* M, int64_t estride, int ld, int k0,
                                                        int kb, double2* W, int64_t wstride,
                                                        int* bad) {
   extern __shared__ double2 zdg[];
-  double2* Ls = zdg;                     // L: row i, column j at i * 65 + j
-  double2* Xs = zdg + 64 * 65;           // X = L^-1
-  double* dk = (double*)(Xs + 64 * 65);  // pivots, stored when they become final
-  const int e = blockIdx.x, tid = threadIdx.x;
+  double2* Ls = zdg;                     // L (packed lower)
+  double2* Xs = zdg + ZDG_TRI;           // X = L^-1 (packed lower)
+  double* dk = (double*)(Xs + ZDG_TRI);  // pivots, stored when they become final
+  const int e = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   double2* D = M + (int64_t)e * estride + k0 + (int64_t)k0 * ld;
   for (int x = tid; x < 64 * 64; x += ZDG_THREADS) {
     const int i = x % 64, j = x / 64;
-    Ls[i * 65 + j] = (i < kb && j < kb && i >= j) ? D[i + (int64_t)j * ld] : make_double2(0.0, 0.0);
-    Xs[i * 65 + j] = make_double2((i == j && i < kb) ? 1.0 : 0.0, 0.0);
+    if (i < j) continue;
+    Ls[tri(i, j)] = (i < kb) ? D[i + (int64_t)j * ld] : make_double2(0.0, 0.0);
+    Xs[tri(i, j)] = make_double2((i == j && i < kb) ? 1.0 : 0.0, 0.0);
   }
   __syncthreads();
   if (tid == 0) dk[0] = Ls[0].x;
@@ -356,24 +458,24 @@ __global__ void __launch_bounds__(ZDG_THREADS) k_zdiag(double2* M, int64_t estri
     // column k of L; row k of X
     if (tid < kb - k) {
       const int i = k + tid;
-      Ls[i * 65 + k] = i == k ? make_double2(sq, 0.0) : zscale(rs, Ls[i * 65 + k]);
+      Ls[tri(i, k)] = i == k ? make_double2(sq, 0.0) : zscale(rs, Ls[tri(i, k)]);
     } else if (tid >= 64 && tid - 64 <= k) {
       const int j = tid - 64;
-      Xs[k * 65 + j] = zscale(rs, Xs[k * 65 + j]);
+      Xs[tri(k, j)] = zscale(rs, Xs[tri(k, j)]);
     }
     __syncthreads();
-    // L(i, j) -= L(i, k) conj(L(j, k)) for k < j <= i;  X(i, j) -= L(i, k) X(k, j) for j <= k < i
-    const int nr = kb - k - 1;
-    for (int x = tid; x < nr * kb; x += ZDG_THREADS) {
-      const int i = k + 1 + x / kb, j = x % kb;
-      if (j > k) {
-        if (j <= i) {
-          const double2 v = zsub(Ls[i * 65 + j], zmul(Ls[i * 65 + k], zconj(Ls[j * 65 + k])));
-          Ls[i * 65 + j] = v;
+    // row i > k: X(i, j) -= L(i, k) X(k, j) for j <= k;
+    //            L(i, j) -= L(i, k) conj(L(j, k)) for k < j <= i
+    for (int i = k + 1 + warp; i < kb; i += ZDG_THREADS / 32) {
+      const double2 lik = Ls[tri(i, k)];
+      for (int j = lane; j <= i; j += 32) {
+        if (j <= k) {
+          Xs[tri(i, j)] = zfms(Xs[tri(i, j)], lik, Xs[tri(k, j)]);
+        } else {
+          const double2 v = zfms_c(Ls[tri(i, j)], lik, Ls[tri(j, k)]);
+          Ls[tri(i, j)] = v;
           if (i == k + 1 && j == k + 1) dk[k + 1] = v.x;
         }
-      } else {
-        Xs[i * 65 + j] = zsub(Xs[i * 65 + j], zmul(Ls[i * 65 + k], Xs[k * 65 + j]));
       }
     }
     __syncthreads();
@@ -382,8 +484,8 @@ __global__ void __launch_bounds__(ZDG_THREADS) k_zdiag(double2* M, int64_t estri
   double2* w = W + (int64_t)e * wstride;
   for (int x = tid; x < 64 * 64; x += ZDG_THREADS) {
     const int i = x % 64, j = x / 64;
-    if (i < kb && j < kb && i >= j) D[i + (int64_t)j * ld] = Ls[i * 65 + j];
-    w[x] = (j >= i) ? zconj(Xs[j * 65 + i]) : make_double2(0.0, 0.0);  // W(i, j) = conj(X(j, i))
+    if (i < kb && j < kb && i >= j) D[i + (int64_t)j * ld] = Ls[tri(i, j)];
+    w[x] = (j >= i) ? zconj(Xs[tri(j, i)]) : make_double2(0.0, 0.0);  // W(i, j) = conj(X(j, i))
   }
 }
 
@@ -483,6 +585,7 @@ int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& 
       raise_smem_limit((const void*)k_zdiag, ZDG_SMEM) != cudaSuccess)
     return -1;
   const int na = nt + n1, ni1 = n1 - nq;
+  int nk = 0;  // kernel launches
   double2* M = (double2*)w.M;
   double2* W = (double2*)w.W;
   double2* Y = (double2*)w.Y;
@@ -504,6 +607,7 @@ int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& 
     a.ex = isA ? tb.ea : tb.eb;
     a.ex_estride = exst;
     k_zslice<<<dim3((a.rows_pad + 127) / 128, nel), 128, 0, st>>>(a);
+    ++nk;
   };
   auto update = [&](double2* C, int64_t cst, int ldc, int m, int n, bool lower, double sgn,
                     bool beta0) {
@@ -516,26 +620,34 @@ int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& 
     u.err = err;
     const int nct = (n + ZN - 1) / ZN;
     k_zupd<<<dim3(u.nrt * nct, nel), ZU_THREADS, ZU_SMEM, st>>>(u);
+    ++nk;
   };
   auto panel = [&](int k0, int kb, int slot) {
     double2* ws = W + (int64_t)slot * 4096;
     k_zdiag<<<nel, ZDG_THREADS, ZDG_SMEM, st>>>(M, mst, na, k0, kb, ws, wst, bad);
+    ++nk;
     const int rem = na - k0 - kb;  // > 0: the load row is never a pivot
     double2* P = M + (k0 + kb) + (int64_t)k0 * na;
     slice(P, mst, 1, na, rem, kb, true, 0, 0);
     slice(ws, wst, 64, 1, kb, kb, false, 2, 3);  // B row j = column j of W
     update(P, mst, na, rem, kb, false, 1.0, true);
-    slice(P, mst, 1, na, rem, kb, true, 0, 0);
-    slice(P, mst, 1, na, rem, kb, false, 0, 1);
+    ZSliceAB ab;
+    ab.src = P; ab.src_estride = mst; ab.srow = 1; ab.sk = na; ab.rows = rem; ab.kc = kb;
+    ab.a = tb.a; ab.b = tb.b; ab.a_estride = ast; ab.b_estride = bst;
+    ab.ea = tb.ea; ab.eb = tb.eb; ab.ex_estride = exst;
+    k_zslice_ab<<<dim3((rem + ZM - 1) / ZM, nel), ZM, 0, st>>>(ab);
+    ++nk;
     update(M + (k0 + kb) + (int64_t)(k0 + kb) * na, mst, na, rem, rem, true, -1.0, false);
   };
   if (part == 1) {
     for (int k0 = 0; k0 < nt; k0 += 64) panel(k0, nt - k0 < 64 ? nt - k0 : 64, 0);
     k_zneg<<<dim3(64, nel), 256, 0, st>>>(M, mst, na, nt, n1);
+    ++nk;
   } else if (part == 2) {
     for (int k0 = nt; k0 < nt + nq; k0 += 64)
       panel(k0, nt + nq - k0 < 64 ? nt + nq - k0 : 64, 1 + (k0 - nt) / 64);
     k_zcopyT<<<dim3(64, nel), 256, 0, st>>>(M, mst, na, nt, nq, ni1, Y);
+    ++nk;
     for (int kq = (nq + 63) / 64 - 1; kq >= 0; --kq) {
       const int q0 = 64 * kq, qb = nq - q0 < 64 ? nq - q0 : 64;
       const double2* ws = W + (int64_t)(1 + kq) * 4096;
@@ -551,20 +663,22 @@ int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& 
     }
   } else if (part == 3) {
     k_zkeep<<<dim3(64, nel), 256, 0, st>>>(M, mst, na, nt, n1, nq, (double2*)zkeep);
+    ++nk;
   }
-  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+  return cudaPeekAtLastError() == cudaSuccess ? nk : -1;
 }
 
-void launch_dpg_aug_out(int nel, int nt, int n1, int nq, const DpgWork& w, const int* nextract,
+int launch_dpg_aug_out(int nel, int nt, int n1, int nq, const DpgWork& w, const int* nextract,
                         const int64_t* lcon_off, const int64_t* elem_nnz,
                         const int64_t* schur_off, const int64_t* bub_off, double* zastif,
                         double* zbload, double* aschur, double* bschur, cudaStream_t st) {
-  if (nel <= 0) return;
+  if (nel <= 0) return 0;
   const int na = nt + n1, ni = n1 - 1 - nq;
   k_dpg_aug_out<<<nel, 256, 0, st>>>((const double2*)w.M, (int64_t)na * na, na, nt + nq, ni,
                                      (const double2*)w.Y, nq, nextract, lcon_off, elem_nnz,
                                      schur_off, bub_off, (double2*)zastif, (double2*)zbload,
                                      (double2*)aschur, (double2*)bschur);
+  return 1;
 }
 
 }  // namespace hp3dg

@@ -60,7 +60,7 @@ EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit",
            "hp3dg_dpg_begin", "hp3dg_dpg_submit", "hp3dg_dpg_run", "hp3dg_dpg_sync",
            "hp3dg_dpg_download", "hp3dg_dpg_sizes", "hp3dg_dpg_get_elem",
            "hp3dg_dpg_get_condensed", "hp3dg_dpg_get_schur", "hp3dg_dpg_index_map",
-           "hp3dg_dpg_phase_times", "hp3dg_dpg_last_bad_element", "hp3dg_dpg_end", "hp3dg_batch_end", "hp3dg_strerror"]
+           "hp3dg_dpg_phase_times", "hp3dg_dpg_pass_stats", "hp3dg_dpg_last_bad_element", "hp3dg_dpg_end", "hp3dg_batch_end", "hp3dg_strerror"]
 
 
 def lib():
@@ -109,6 +109,7 @@ def lib():
         L.hp3dg_dpg_get_schur.argtypes = [_vp, ctypes.c_int32, _f64p, _f64p, _i32p, _i32p]
         L.hp3dg_dpg_index_map.argtypes = [_vp, _i32p, _i64p, _i64p, _i32p, _i64p]
         L.hp3dg_dpg_phase_times.argtypes = [_vp, _f32p, ctypes.c_int32]
+        L.hp3dg_dpg_pass_stats.argtypes = [_vp, _i64p]
         L.hp3dg_dpg_last_bad_element.argtypes = [_vp]
         L.hp3dg_dpg_last_bad_element.restype = ctypes.c_int32
         L.hp3dg_dpg_end.argtypes = [_vp]
@@ -454,6 +455,12 @@ class DPGPass:
         t = (ctypes.c_float * 5)()
         self._check(self.L.hp3dg_dpg_phase_times(self.ctx, t, 5), "times")
         return list(t)
+
+    def pass_stats(self):
+        """Kernels launched on the device by the last run()."""
+        k = ctypes.c_int64()
+        self._check(self.L.hp3dg_dpg_pass_stats(self.ctx, ctypes.byref(k)), "stats")
+        return k.value
 
     def close(self):
         if self.ctx:

@@ -378,6 +378,9 @@ int hp3dg_dpg_index_map(const hp3dg_dpg_ctx *ctx, int32_t *nfirst, int64_t *elem
 /* [0] geometry + contractions + assembly, [1] Cholesky + solve + X^H X,
  * [2] condensation + compression, [3] index maps, [4] whole pass (ms). */
 int hp3dg_dpg_phase_times(const hp3dg_dpg_ctx *ctx, float *ms, int32_t n);
+/* Kernels launched on the device by the last hp3dg_dpg_run (the dense
+ * algebra of the tensor-core path is a sequence of per-panel launches). */
+int hp3dg_dpg_pass_stats(const hp3dg_dpg_ctx *ctx, int64_t *kernels);
 int32_t hp3dg_dpg_last_bad_element(const hp3dg_dpg_ctx *ctx);
 void hp3dg_dpg_end(hp3dg_dpg_ctx *ctx);
 
