@@ -30,6 +30,7 @@ struct hp3dg_dpg_ctx {
   std::vector<int64_t> lcon_off, elem_nnz, schur_off, bub_off;
   int32_t last_bad = -1;
   int64_t launches = 0;    // kernels launched by the last run
+  std::vector<hp3dg_elem_desc> desc_prev;  // descriptors of the current batch
   std::vector<void*> dev;  // every device allocation of the batch
   double *d_xiV = nullptr, *d_wV = nullptr, *d_xiF = nullptr, *d_wF = nullptr, *d_xiI = nullptr,
          *d_wI = nullptr;
@@ -141,7 +142,21 @@ int hp3dg_dpg_submit(hp3dg_dpg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   if (!c || nel < 0 || (nel > 0 && (!desc || !xvert || !eps)) || nnodes < 0) return HP3DG_ERR_ARG;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  // the same mesh again (new vertices or permittivities): keep the device
+  // buffers, the digit tables and the pinned results; upload the two inputs
+  if (c->submitted && nel > 0 && nel == c->nel && nnodes == c->nnodes &&
+      c->desc_prev.size() == (size_t)nel &&
+      memcmp(c->desc_prev.data(), desc, sizeof(hp3dg_elem_desc) * (size_t)nel) == 0) {
+    CK(cudaMemcpyAsync(c->d_xvert, xvert, sizeof(double) * 24 * (size_t)nel,
+                       cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->d_eps, eps, sizeof(double) * 2 * (size_t)nel, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->ran = c->downloaded = false;
+    return HP3DG_OK;
+  }
   free_batch(c);
+  c->desc_prev.clear();
   c->nel = nel;
   c->nnodes = nnodes;
   if (nel == 0) { c->submitted = true; return HP3DG_OK; }
@@ -357,6 +372,7 @@ int hp3dg_dpg_submit(hp3dg_dpg_ctx* c, int32_t nel, const hp3dg_elem_desc* desc,
   if (err) { free_batch(c); return err; }
   w.xiV = c->d_xiV; w.wV = c->d_wV; w.xiF = c->d_xiF; w.wF = c->d_wF;
   w.xiI = c->d_xiI; w.wI = c->d_wI;
+  c->desc_prev.assign(desc, desc + nel);
   c->submitted = true;
   return HP3DG_OK;
 }

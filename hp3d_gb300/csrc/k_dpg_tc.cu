@@ -45,8 +45,11 @@ constexpr int ZB_TILE = 2 * ZD * ZB_BLK;  // both B forms of one column tile
 constexpr int ZFB = 48;                // fraction bits of the split (|v| < 2^e -> |X| <= 2^48)
 constexpr int ZBROWS = 2 * ZD * ZN;    // rows of one B K-step: [digit q][form][32 rows]
 constexpr int ZU_THREADS = 320;        // loader, MMA, 8 epilogue warps (2 per TMEM lane quarter)
+constexpr int ZEPI = ZU_THREADS / 32 - 2;  // epilogue warps
+constexpr int ZCG = ZN / 8 / (ZEPI / 4);   // 8-column groups per epilogue warp
+constexpr int ZNABUF = 2;              // A digit buffers
 constexpr uint32_t ZU_TMEM = 512;      // 7 levels x 2 parts x 32 columns = 448
-constexpr size_t ZU_SMEM = 2 * ZA_BLK + ZB_TILE + 1024;
+constexpr size_t ZU_SMEM = ZNABUF * ZA_BLK + ZB_TILE + 1024;  // 177 KB: one CTA per SM
 
 __host__ __device__ constexpr uint32_t zidesc(int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
@@ -251,7 +254,7 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
   extern __shared__ __align__(1024) uint8_t zsm_raw[];
   uint8_t* sm = (uint8_t*)(((uintptr_t)zsm_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* regA0 = sm;
-  uint8_t* regB = sm + 2 * ZA_BLK;
+  uint8_t* regB = sm + ZNABUF * ZA_BLK;
   __shared__ __align__(8) uint64_t ldB_bar, ldA_bar[2], afree_bar[2], accf_bar;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_;
@@ -283,9 +286,9 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
       bulk_load(smem_u32(regB), bsrc, ZB_TILE, smem_u32(&ldB_bar));
       const uint8_t* asrc = a.a + (int64_t)e * a.a_estride + (size_t)rt * ZD * ZA_BLK;
       for (int p = 0; p < ZD; ++p) {
-        const int buf = p & 1;
-        if (p >= 2) {
-          if (!mbar_wait(smem_u32(&afree_bar[buf]), ((p - 2) >> 1) & 1, &abort_)) {
+        const int buf = p % ZNABUF;
+        if (p >= ZNABUF) {
+          if (!mbar_wait(smem_u32(&afree_bar[buf]), ((p - ZNABUF) / ZNABUF) & 1, &abort_)) {
             abort_ = 1;
             atomicExch(a.err, 41);
             break;
@@ -302,8 +305,8 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
       if (!ok) { abort_ = 1; atomicExch(a.err, 42); }
       const uint64_t dB0 = sdesc_kmajor(smem_u32(regB));
       for (int p = 0; p < ZD && ok; ++p) {
-        const int buf = p & 1;
-        if (!mbar_wait(smem_u32(&ldA_bar[buf]), (p >> 1) & 1, &abort_)) {
+        const int buf = p % ZNABUF;
+        if (!mbar_wait(smem_u32(&ldA_bar[buf]), (p / ZNABUF) & 1, &abort_)) {
           abort_ = 1;
           atomicExch(a.err, 43);
           ok = false;
@@ -311,12 +314,13 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
         }
         tc_fence_after();
         const uint64_t dA = sdesc_kmajor(smem_u32(regA0 + buf * ZA_BLK));
-        // all pairs (p, q), q = 0..6-p, and both parts: B rows [0, 64 (7 - p))
-        // into the TMEM levels p..6 (64 columns each), at most 256 per MMA
+        // all pairs (p, q), q = 0..6-p, and both parts: B rows [0, 2 ZN (7 - p))
+        // into the TMEM levels p..6 (2 ZN columns each), at most 256 per MMA
+        constexpr int QMAX = 256 / (2 * ZN);
         for (int kb = 0; kb < ZK / 16; ++kb) {
           const uint64_t a_kb = dA + (uint64_t)((kb * ZM * 32) >> 4);
           for (int q0 = 0; q0 + p < ZD;) {
-            const int nq = (ZD - p - q0) < 4 ? (ZD - p - q0) : 4;
+            const int nq = (ZD - p - q0) < QMAX ? (ZD - p - q0) : QMAX;
             const uint32_t dt = tbase + (uint32_t)((p + q0) * 2 * ZN);
             const uint64_t db = dB0 + (uint64_t)(((size_t)kb * ZBROWS * 32 + (size_t)q0 * 2 * ZN * 32) >> 4);
             umma_bf16(dt, a_kb, db, zidesc(nq * 2 * ZN), (p > 0 || kb > 0) ? 1u : 0u);
@@ -328,8 +332,8 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
       umma_commit(smem_u32(&accf_bar));
     }
   } else {
-    // epilogue: warps 2..9; TMEM lane quarter warp % 4 = rows of the tile,
-    // (warp - 2) / 4 = which 16 of the 32 columns
+    // epilogue: warps 2..; TMEM lane quarter warp % 4 = rows of the tile,
+    // (warp - 2) / 4 = which ZCG 8-column groups
     const int quarter = warp & 3, half = (warp - 2) >> 2;
     const int i = rt * ZM + quarter * 32 + lane;
     const bool rowok = i < a.m;
@@ -349,19 +353,19 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
         xn[c] = ok ? ebp[j] : ZX_SKIP;
       }
     };
-    const int cg0 = 2 * half;
+    const int cg0 = ZCG * half;
     fetch(cg0);
     const bool okw = mbar_wait(smem_u32(&accf_bar), 0, &abort_);
     if (!okw) { abort_ = 1; atomicExch(a.err, 44); }
     tc_fence_after();
     const uint32_t tl = tbase + ((uint32_t)(quarter * 32) << 16);
     double2* C = a.C + (int64_t)e * a.c_estride;
-    for (int cg = cg0; cg < cg0 + 2; ++cg) {
+    for (int cg = cg0; cg < cg0 + ZCG; ++cg) {
       double2 cv[8];
       int xs[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) { cv[c] = cn[c]; xs[c] = xn[c]; }
-      if (cg + 1 < cg0 + 2) fetch(cg + 1);
+      if (cg + 1 < cg0 + ZCG) fetch(cg + 1);
       // exact recombination in integers.  Digits are at most 2^6 (48-bit
       // split), so each level sum s_L (at most 7 pairs x 128 terms) is an
       // integer below 2^21.8 and (s_L + 1.5 2^23) has it in its low mantissa

@@ -339,9 +339,11 @@ typedef struct hp3dg_dpg_opts {
   int32_t device;
   int32_t timing;    /* record phase times */
   int32_t keep_elem; /* keep the uncondensed DPG element matrices (hp3dg_dpg_get_elem) */
-  int32_t precision; /* HP3DG_FP64: the dense algebra in FP64; HP3DG_MIXED: the Cholesky
-                        trailing updates, the solve's block updates and X^H X on tensor
-                        cores from split-BF16 digits (FP64 diagonal blocks) */
+  int32_t precision; /* HP3DG_FP64: contractions and dense algebra in FP64.  HP3DG_MIXED:
+                        the contractions (M_FF, M_CC, P, R, T) and every O(n^3) product of
+                        the dense algebra and the L2-field condensation on tensor cores from
+                        split-BF16 digits, as one partial Cholesky of the augmented matrix
+                        [[G, [B|l]], [[B|l]^H, 0]] with FP64 64 x 64 diagonal blocks */
   int32_t reserved[4];
 } hp3dg_dpg_opts;
 

@@ -166,3 +166,27 @@ def test_tensor_core_polynomial_solution():
     ee, eh = D.field_errors(m, prm, eps, cond, schur, u, lcon, lcon_off, [ni] * m["nelem"])
     assert ee < 1e-10 and eh < 1e-10, (ee, eh)
     ep.close()
+
+
+@pytest.mark.parametrize("precision", [H.FP64, H.MIXED])
+def test_resubmit_same_mesh_matches_fresh_context(precision):
+    """A resubmit with the same descriptors only uploads the new vertices and
+    permittivities; its outputs equal those of a new context."""
+    m, prm, eps, bc, imp, flags = _setup(2, 2, ((0, 1),))
+    eps2 = eps * (1.5 - 0.2j)
+    ep = H.DPGPass(omega=prm.omega, ibcflag=prm.ibcflag, isol=prm.isol, precision=precision)
+    ep.submit(m, eps, flags)
+    ep.run(); ep.download()
+    ep.submit(m, eps2, flags)
+    ep.run(); ep.download()
+    fresh = H.DPGPass(omega=prm.omega, ibcflag=prm.ibcflag, isol=prm.isol, precision=precision)
+    fresh.submit(m, eps2, flags)
+    fresh.run(); fresh.download()
+    for e in range(m["nelem"]):
+        zb, zs = ep.condensed(e)
+        zb0, zs0 = fresh.condensed(e)
+        assert np.array_equal(zs, zs0) and np.array_equal(zb, zb0), e
+        a, b = ep.schur(e)
+        a0, b0 = fresh.schur(e)
+        assert np.array_equal(a, a0) and np.array_equal(b, b0), e
+    ep.close(); fresh.close()
