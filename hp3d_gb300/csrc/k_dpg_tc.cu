@@ -229,22 +229,6 @@ struct ZUpd {
 
 constexpr int ZX_SKIP = -0x40000000;  // column exponent slot of a skipped output
 
-// V 2^sc rounded to nearest (ties to even), assembled from the bits of V
-// without an FP64 instruction (GB300 issues FP64 and its conversions at
-// about 2 per clock per SM); scales outside the normal range take ldexp
-__device__ __forceinline__ double scaled_i64(long long V, int sc) {
-  if (V == 0) return 0.0;
-  const unsigned long long sb = (unsigned long long)V & 0x8000000000000000ull;
-  unsigned long long u = V < 0 ? (unsigned long long)(-V) : (unsigned long long)V;
-  const int lz = __clzll((long long)u);
-  const int eb = 63 - lz + sc + 1023;  // biased exponent of the leading bit
-  if (eb < 1 || eb > 2045) return ldexp((double)V, sc);
-  u <<= lz;
-  unsigned long long m = u >> 11;  // 53 bits, leading bit at 52
-  const unsigned long long r = u & 0x7ffull;
-  m += (r > 0x400ull || (r == 0x400ull && (m & 1ull))) ? 1ull : 0ull;
-  return __longlong_as_double((long long)(sb | (((unsigned long long)(eb - 1) << 52) + m)));
-}
 
 // one 128 x 32 tile of one element per CTA
 __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
