@@ -412,6 +412,8 @@ struct hp3dg_ctx {
   cudaStream_t branch[NBRANCH] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[NBRANCH] = {};
   std::vector<hp3dg_elem_desc> last_desc;  // descriptors of the current batch
+  double* d_xnod = nullptr;  // isoparametric geometry dof (hp3dg_batch_set_geometry)
+  bool iso = false;
   // constrained approximation: the compression writes a work layout (every
   // element; constrained elements with all their interface dof), which
   // k_constrain turns into the final outputs.  Without constraints the work
@@ -462,8 +464,10 @@ void free_batch(hp3dg_ctx* c) {
                  c->d_schur_off, c->d_bub_off, c->d_zd_off, c->d_zastif, c->d_zbload,
                  c->d_aschur, c->d_bschur, c->d_lcon, c->d_nfirst, c->d_first, c->d_cnt,
                  c->d_scan, c->d_blk, c->d_total, c->d_dof_off, c->d_dofs, c->d_xglob,
-                 c->d_err2, c->d_nrm2, c->d_djdk, c->d_djdx};
+                 c->d_err2, c->d_nrm2, c->d_djdk, c->d_djdx, c->d_xnod};
   for (void* p : dev) cudaFree(p);
+  c->d_xnod = nullptr;
+  c->iso = false;
   cudaFreeHost(c->h_dofs);
   c->h_dofs = nullptr;
   c->d_dof_off = nullptr; c->d_dofs = c->d_xglob = nullptr;
@@ -583,6 +587,12 @@ int hp3dg_batch_submit_constrained(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_d
       CK(cudaStreamSynchronize(st));
     }
     if (zdofd) CK(cudaMemcpyAsync(c->d_zdofd, zdofd, c->zd_off[nel] * 8, cudaMemcpyHostToDevice, st));
+    if (c->iso) {  // back to the vertex geometry; the captured pass read the geometry dof
+      c->iso = false;
+      if (c->graph) cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+      c->graph_kernels = -1;
+    }
     c->ran = c->downloaded = c->have_dofs = false;
     return HP3DG_OK;
   }
@@ -1018,7 +1028,8 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
   if (stage == 0) {
     launch_orient(B.etype, ne, el, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n, perm, st);
     launch_geom(ne, B.nvert, el, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert, c->d_kappa,
-                c->opts.isol, D, F, c->d_flags, st);
+                c->opts.isol, D, F, c->d_flags, st, c->iso ? c->d_xnod : nullptr, c->d_dof_off,
+                perm);
     launch_load_hexa(ne, B.nint, B.n, B.d_shap, F, b0, st);
     if (mixed) launch_ozaki_slice_d(B.plan, ne, B.nint, D, ddig, dscale, st);
     return HP3DG_OK;
@@ -1377,6 +1388,31 @@ int hp3dg_index_map(const hp3dg_ctx* c, int32_t* nfirst_dof, int64_t* elem_nnz,
   return HP3DG_OK;
 }
 
+int hp3dg_batch_set_geometry(hp3dg_ctx* c, const double* xnod) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  CK(cudaStreamSynchronize(st));
+  const int64_t ndof = c->nel > 0 ? c->dof_off[c->nel] : 0;
+  if (xnod && ndof > 0) {
+    if (!c->d_xnod && cudaMalloc(&c->d_xnod, (size_t)ndof * 3 * sizeof(double)) != cudaSuccess) {
+      c->d_xnod = nullptr;
+      return HP3DG_ERR_ALLOC;
+    }
+    CK(cudaMemcpyAsync(c->d_xnod, xnod, (size_t)ndof * 3 * sizeof(double), cudaMemcpyHostToDevice,
+                       st));
+    CK(cudaStreamSynchronize(st));
+  }
+  // the geometry kernel is part of the captured pass: capture again
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->graph = nullptr;
+  c->graph_kernels = -1;
+  c->iso = xnod != nullptr && ndof > 0;
+  c->ran = c->downloaded = c->have_dofs = false;
+  return HP3DG_OK;
+}
+
 int hp3dg_backsub(hp3dg_ctx* c, const double* x_global) {
   if (!c || !x_global) return HP3DG_ERR_ARG;
   if (!c->ran) return HP3DG_ERR_STATE;
@@ -1417,6 +1453,7 @@ int hp3dg_get_dofs(const hp3dg_ctx* c, int32_t iel, double* dof, int32_t* n) {
 }
 
 int hp3dg_element_error(hp3dg_ctx* c, int32_t isol, double* err2, double* nrm2) {
+  if (c && c->iso) return HP3DG_ERR_UNSUPPORTED;  // vertex geometry only
   if (!c || !err2 || !nrm2) return HP3DG_ERR_ARG;
   if (!c->have_dofs) return HP3DG_ERR_STATE;
   cudaSetDevice(c->device);
@@ -1451,6 +1488,7 @@ int hp3dg_element_error(hp3dg_ctx* c, int32_t isol, double* err2, double* nrm2) 
 }
 
 int hp3dg_adjoint(hp3dg_ctx* c, const double* dofs, double* djdkappa, double* djdx) {
+  if (c && c->iso) return HP3DG_ERR_UNSUPPORTED;  // vertex geometry only
   if (!c || !djdkappa || !djdx) return HP3DG_ERR_ARG;
   if (!c->ran) return HP3DG_ERR_STATE;
   if (c->constrained) return HP3DG_ERR_UNSUPPORTED;
@@ -1531,6 +1569,7 @@ int hp3dg_pass_stats(const hp3dg_ctx* c, int64_t* kernels, double* contraction_f
 }
 
 int hp3dg_dirichlet_dofs(hp3dg_ctx* c, int32_t isol, double* zdofd, int64_t* n) {
+  if (c && c->iso) return HP3DG_ERR_UNSUPPORTED;  // vertex geometry only
   if (!c) return HP3DG_ERR_ARG;
   if (!c->submitted) return HP3DG_ERR_STATE;
   const int nel = c->nel;

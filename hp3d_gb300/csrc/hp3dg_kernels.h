@@ -25,10 +25,14 @@ void launch_tables(int etype, const int* nord_loc, const int* face_nori, int nin
 void launch_orient(int etype, int nel, const int* d_elist, const int* d_norder, const int* d_nori_e,
                    const int* d_nori_f, const int* full, int nfull, uint32_t* d_perm,
                    cudaStream_t st);
+// geometry per point; d_xnod != NULL: isoparametric, from every element's
+// nrdofH geometry dof (3 per dof, element order, at 3 * d_dof_off[e]) through
+// its dof map d_perm (j * n + a); else trilinear/linear from d_xvert
 void launch_geom(int nel, int nvert, const int* d_elist, int nint, int n, const double* d_wq,
                  const double* d_shap, const double* d_grad, const double* d_xvert,
                  const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
-                 cudaStream_t st);
+                 cudaStream_t st, const double* d_xnod = nullptr,
+                 const int64_t* d_dof_off = nullptr, const uint32_t* d_perm = nullptr);
 void launch_load_hexa(int nel, int nint, int n, const double* d_shap, const double* d_F,
                       double* d_b0, cudaStream_t st);
 void launch_contract_fp64(int nel, int nint, int n, int ni, int nb, const double* d_grad,

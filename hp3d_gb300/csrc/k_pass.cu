@@ -183,6 +183,40 @@ __device__ inline double getf_dev(int isol, double x1, double x2, double x3) {
   }
 }
 
+// per point: det J (rule of Sarrus), cofactor inverse, D = w kappa detJ
+// J^-1 J^-T (upper 00 11 22 01 02 12) and F = getf(x) w detJ (geom.F90:57-113)
+__device__ __forceinline__ void geom_point(int e, int j, int l, int nint, const double (&dx)[3][3],
+                                           const double (&X)[3], const double* __restrict__ wq,
+                                           const double* __restrict__ kappa, int isol,
+                                           double* __restrict__ D, double* __restrict__ F,
+                                           int* __restrict__ bad) {
+  double r = dx[0][0] * dx[1][1] * dx[2][2] + dx[1][0] * dx[2][1] * dx[0][2] +
+             dx[2][0] * dx[0][1] * dx[1][2] - dx[2][0] * dx[1][1] * dx[0][2] -
+             dx[0][0] * dx[2][1] * dx[1][2] - dx[1][0] * dx[0][1] * dx[2][2];
+  if (!(r > 0.0)) atomicMin(bad, e);
+  double ir = 1.0 / r;
+  double a[3][3];  // a[i][k] = d xi_i / d x_k
+  a[0][0] = (dx[1][1] * dx[2][2] - dx[2][1] * dx[1][2]) * ir;
+  a[1][0] = (-dx[1][0] * dx[2][2] + dx[2][0] * dx[1][2]) * ir;
+  a[2][0] = (dx[1][0] * dx[2][1] - dx[2][0] * dx[1][1]) * ir;
+  a[0][1] = (dx[2][1] * dx[0][2] - dx[0][1] * dx[2][2]) * ir;
+  a[1][1] = (dx[0][0] * dx[2][2] - dx[2][0] * dx[0][2]) * ir;
+  a[2][1] = (-dx[0][0] * dx[2][1] + dx[2][0] * dx[0][1]) * ir;
+  a[0][2] = (dx[0][1] * dx[1][2] - dx[1][1] * dx[0][2]) * ir;
+  a[1][2] = (-dx[0][0] * dx[1][2] + dx[1][0] * dx[0][2]) * ir;
+  a[2][2] = (dx[0][0] * dx[1][1] - dx[1][0] * dx[0][1]) * ir;
+  double weight = r * wq[l];
+  double kw = kappa[e] * weight;
+  double* Dp = D + ((size_t)j * nint + l) * 6;
+  Dp[0] = kw * (a[0][0] * a[0][0] + a[0][1] * a[0][1] + a[0][2] * a[0][2]);
+  Dp[1] = kw * (a[1][0] * a[1][0] + a[1][1] * a[1][1] + a[1][2] * a[1][2]);
+  Dp[2] = kw * (a[2][0] * a[2][0] + a[2][1] * a[2][1] + a[2][2] * a[2][2]);
+  Dp[3] = kw * (a[0][0] * a[1][0] + a[0][1] * a[1][1] + a[0][2] * a[1][2]);
+  Dp[4] = kw * (a[0][0] * a[2][0] + a[0][1] * a[2][1] + a[0][2] * a[2][2]);
+  Dp[5] = kw * (a[1][0] * a[2][0] + a[1][1] * a[2][1] + a[1][2] * a[2][2]);
+  F[(size_t)j * nint + l] = getf_dev(isol, X[0], X[1], X[2]) * weight;
+}
+
 template <int NV>
 __global__ void k_geom(int nel, const int* __restrict__ elist, int nint, int n,
                             const double* __restrict__ wq, const double* __restrict__ tab_shap,
@@ -213,40 +247,66 @@ __global__ void k_geom(int nel, const int* __restrict__ elist, int nint, int n,
       dx[i][2] += xi_ * g2;
     }
   }
-  // geom.F90: determinant (rule of Sarrus) and cofactor inverse
-  double r = dx[0][0] * dx[1][1] * dx[2][2] + dx[1][0] * dx[2][1] * dx[0][2] +
-             dx[2][0] * dx[0][1] * dx[1][2] - dx[2][0] * dx[1][1] * dx[0][2] -
-             dx[0][0] * dx[2][1] * dx[1][2] - dx[1][0] * dx[0][1] * dx[2][2];
-  if (!(r > 0.0)) atomicMin(bad, e);
-  double ir = 1.0 / r;
-  double a[3][3];  // a[i][k] = d xi_i / d x_k
-  a[0][0] = (dx[1][1] * dx[2][2] - dx[2][1] * dx[1][2]) * ir;
-  a[1][0] = (-dx[1][0] * dx[2][2] + dx[2][0] * dx[1][2]) * ir;
-  a[2][0] = (dx[1][0] * dx[2][1] - dx[2][0] * dx[1][1]) * ir;
-  a[0][1] = (dx[2][1] * dx[0][2] - dx[0][1] * dx[2][2]) * ir;
-  a[1][1] = (dx[0][0] * dx[2][2] - dx[2][0] * dx[0][2]) * ir;
-  a[2][1] = (-dx[0][0] * dx[2][1] + dx[2][0] * dx[0][1]) * ir;
-  a[0][2] = (dx[0][1] * dx[1][2] - dx[1][1] * dx[0][2]) * ir;
-  a[1][2] = (-dx[0][0] * dx[1][2] + dx[1][0] * dx[0][2]) * ir;
-  a[2][2] = (dx[0][0] * dx[1][1] - dx[1][0] * dx[0][1]) * ir;
-  double weight = r * wq[l];
-  double kw = kappa[e] * weight;
-  double* Dp = D + ((size_t)j * nint + l) * 6;
-  Dp[0] = kw * (a[0][0] * a[0][0] + a[0][1] * a[0][1] + a[0][2] * a[0][2]);
-  Dp[1] = kw * (a[1][0] * a[1][0] + a[1][1] * a[1][1] + a[1][2] * a[1][2]);
-  Dp[2] = kw * (a[2][0] * a[2][0] + a[2][1] * a[2][1] + a[2][2] * a[2][2]);
-  Dp[3] = kw * (a[0][0] * a[1][0] + a[0][1] * a[1][1] + a[0][2] * a[1][2]);
-  Dp[4] = kw * (a[0][0] * a[2][0] + a[0][1] * a[2][1] + a[0][2] * a[2][2]);
-  Dp[5] = kw * (a[1][0] * a[2][0] + a[1][1] * a[2][1] + a[1][2] * a[2][2]);
-  F[(size_t)j * nint + l] = getf_dev(isol, X[0], X[1], X[2]) * weight;
+  geom_point(e, j, l, nint, dx, X, wq, kappa, isol, D, F, bad);
+}
+
+// isoparametric geometry (geom3D.F90:30-112 with the element's nrdofH
+// geometry dof Xnod): the dof are mapped to the bin's canonical functions
+// through the element's signed dof map, then x and dx/dxi are sums over all
+// n functions of the bin tables
+__global__ void k_geom_iso(int nel, const int* __restrict__ elist, int nint, int n,
+                           const double* __restrict__ wq, const double* __restrict__ tab_shap,
+                           const double* __restrict__ tab_grad, const double* __restrict__ xnod,
+                           const int64_t* __restrict__ dof_off, const uint32_t* __restrict__ perm,
+                           const double* __restrict__ kappa, int isol, double* __restrict__ D,
+                           double* __restrict__ F, int* __restrict__ bad) {
+  extern __shared__ double xc[];  // 3 x n in the bin's dof order
+  const int j = blockIdx.y;
+  const int e = elist[j];
+  const int64_t o = dof_off[e];
+  const int ne = (int)(dof_off[e + 1] - o);
+  for (int t = threadIdx.x; t < 3 * n; t += blockDim.x) xc[t] = 0.0;
+  __syncthreads();
+  for (int a = threadIdx.x; a < ne && a < n; a += blockDim.x) {
+    const uint32_t pm = perm[(size_t)j * n + a];
+    const int k = (int)(pm & 0x7fffffffu);
+    const double sg = (pm >> 31) ? -1.0 : 1.0;
+    for (int i = 0; i < 3; ++i) xc[3 * k + i] = sg * xnod[3 * (o + a) + i];
+  }
+  __syncthreads();
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nint) return;
+  double dx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  double X[3] = {0, 0, 0};
+  const double* gs = tab_shap + (size_t)l * n;
+  const double* gg = tab_grad + (size_t)l * 3 * n;
+  for (int k = 0; k < n; ++k) {
+    const double s = gs[k], g0 = gg[k], g1 = gg[n + k], g2 = gg[2 * n + k];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const double xk = xc[3 * k + i];
+      X[i] = fma(xk, s, X[i]);
+      dx[i][0] = fma(xk, g0, dx[i][0]);
+      dx[i][1] = fma(xk, g1, dx[i][1]);
+      dx[i][2] = fma(xk, g2, dx[i][2]);
+    }
+  }
+  geom_point(e, j, l, nint, dx, X, wq, kappa, isol, D, F, bad);
 }
 
 void launch_geom(int nel, int nvert, const int* d_elist, int nint, int n, const double* d_wq,
                  const double* d_shap, const double* d_grad, const double* d_xvert,
                  const double* d_kappa, int isol, double* d_D, double* d_F, int* d_bad,
-                 cudaStream_t st) {
+                 cudaStream_t st, const double* d_xnod, const int64_t* d_dof_off,
+                 const uint32_t* d_perm) {
   if (nel <= 0) return;
   dim3 g((nint + 127) / 128, nel);
+  if (d_xnod) {
+    k_geom_iso<<<g, 128, (size_t)3 * n * sizeof(double), st>>>(
+        nel, d_elist, nint, n, d_wq, d_shap, d_grad, d_xnod, d_dof_off, d_perm, d_kappa, isol, d_D,
+        d_F, d_bad);
+    return;
+  }
   if (nvert == 4)
     k_geom<4><<<g, 128, 0, st>>>(nel, d_elist, nint, n, d_wq, d_shap, d_grad, d_xvert, d_kappa,
                                  isol, d_D, d_F, d_bad);

@@ -52,7 +52,8 @@ _f64p = ctypes.POINTER(ctypes.c_double)
 _f32p = ctypes.POINTER(ctypes.c_float)
 
 EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit",
-           "hp3dg_batch_submit_constrained", "hp3dg_dirichlet_dofs", "hp3dg_batch_run",
+           "hp3dg_batch_submit_constrained", "hp3dg_dirichlet_dofs", "hp3dg_batch_set_geometry",
+           "hp3dg_batch_run",
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
            "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_output_sizes", "hp3dg_device_outputs",
@@ -77,6 +78,7 @@ def lib():
                                                      _f64p, ctypes.c_int32,
                                                      ctypes.POINTER(Constraints)]
         L.hp3dg_dirichlet_dofs.argtypes = [_vp, ctypes.c_int32, _f64p, _i64p]
+        L.hp3dg_batch_set_geometry.argtypes = [_vp, _f64p]
         L.hp3dg_batch_run.argtypes = [_vp]
         L.hp3dg_batch_sync.argtypes = [_vp]
         L.hp3dg_batch_download.argtypes = [_vp]
@@ -225,6 +227,17 @@ class ElementPass:
 
     def run(self):
         self._check(self.L.hp3dg_batch_run(self.ctx), "run")
+
+    def set_geometry(self, xnod):
+        """Isoparametric geometry: a list of per-element (nrdofH, 3) arrays of
+        geometry dof in element dof order (None: back to the vertices)."""
+        if xnod is None:
+            self._check(self.L.hp3dg_batch_set_geometry(self.ctx, None), "set_geometry")
+            return
+        self._xnod = np.ascontiguousarray(np.concatenate([np.asarray(x, np.float64).reshape(-1, 3)
+                                                          for x in xnod]).ravel())
+        self._check(self.L.hp3dg_batch_set_geometry(self.ctx, _p(self._xnod, _f64p)),
+                    "set_geometry")
 
     def dirichlet_dofs(self, isol):
         """Per element Dirichlet values of the interface dof (update_Ddof on

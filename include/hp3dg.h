@@ -135,6 +135,19 @@ int hp3dg_batch_submit(hp3dg_ctx *ctx, int32_t n_elem, const hp3dg_elem_desc *de
                        const double *xvert, const double *kappa, const double *zdofd,
                        int32_t n_nodes_global);
 
+/* Isoparametric (curved) geometry: the element's nrdofH geometry dof, as
+ * nodcor returns them (constrs/nodcor.F90:19-196) and geom3D consumes them
+ * (element/util/geom3D.F90:30-112): per element 3 values (x, y, z) per dof
+ * in element dof order (vertices, edges, faces, interior; the element's
+ * orientation), elements concatenated in ELEM_ORDER -- 3 * nrdofH(e) values
+ * for element e.  The vertex dof are the vertex coordinates; a trilinear
+ * element has zero higher-order dof.  Call after hp3dg_batch_submit; the
+ * next runs use this geometry until the next submit (which returns to the
+ * vertex coordinates).  NULL returns to the vertex coordinates now.  With
+ * this geometry hp3dg_element_error, hp3dg_adjoint and hp3dg_dirichlet_dofs
+ * return HP3DG_ERR_UNSUPPORTED. */
+int hp3dg_batch_set_geometry(hp3dg_ctx *ctx, const double *xnod);
+
 /* Constrained approximation (hanging nodes): for each constrained element,
  * what logic (constrs/logic.F90) returns for it, as celem_systemI consumes it
  * (celem_systemI.F90:541-760):
