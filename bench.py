@@ -184,6 +184,22 @@ def config_dict(args, world, mesh):
 DPG_METRIC = "DPG Maxwell elements/s (complex FP64, trial p=3, test p=4, condensed)"
 
 
+def measured_traffic(workload, kernel):
+    """DRAM bytes of `kernel` on `workload` from the committed one-pass ncu
+    summary (profiles/dram_traffic_dominant_kernels.md), or None."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                        "dram_traffic_dominant_kernels.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                t = line.split()
+                if len(t) == 5 and t[0] == "traffic" and t[1] == workload and t[2] == kernel:
+                    return int(t[4]), t[3]
+    except OSError:
+        pass
+    return None
+
+
 def dpg_flops(ntest, ntrial, ni, nb):
     """Dense algebra of the DPG element per element (real FLOPs): Cholesky of
     the Gram matrix (ZPPTRF), the triangular solve of [B|l] (ZTPTRS), X^H X
@@ -316,11 +332,14 @@ def run_dpg(args, rank, world):
         tens = fl_el * 28 / 2.0 * 2.0
         ach = ne * tens / t_la / 1e12 if t_la > 0 else None
         roof = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
-                "frac": ach / bf16 if ach else None, "traffic": None,
+                "frac": ach / bf16 if ach else None,
                 "kernel": "k_zupd + k_zdiag + digit slices (augmented partial Cholesky)",
+                "traffic": (measured_traffic(cfg["workload"], "k_zupd") or (None,))[0],
                 "note": f"BF16 digit-pair MMA work of the dense DPG algebra (28 pairs of the "
                         f"complex FLOP count) over the stage's time; peak {peak_kind}; the "
-                        f"complex-FP64-equivalent rate is {ne * fl_el / t_la / 1e12:.3f} TFLOP/s"}
+                        f"complex-FP64-equivalent rate is {ne * fl_el / t_la / 1e12:.3f} TFLOP/s; "
+                        f"traffic: DRAM bytes of the 31 k_zupd launches of one pass (one-pass "
+                        f"ncu capture at this size)"}
     cb = cpu(args.cpu_seconds) if (rank == 0 and not args.no_cpu_baseline) else None
     line = {"metric": DPG_METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -504,7 +523,10 @@ def main():
                 "note": "FP64 CUDA-core contraction measured against the bf16 peak"}
     if roof["achieved"] is not None:
         roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["traffic"] = None
+    tr = measured_traffic(cfg["workload"], roof["kernel"]) if args.workload == "hexa" else None
+    roof["traffic"] = tr[0] if tr else None
+    if tr:
+        roof["note"] += "; traffic: one-pass ncu capture of one launch at this size (bytes)"
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
