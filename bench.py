@@ -523,7 +523,8 @@ def main():
                 "note": "FP64 CUDA-core contraction measured against the bf16 peak"}
     if roof["achieved"] is not None:
         roof["frac"] = roof["achieved"] / roof["peak"]
-    tr = measured_traffic(cfg["workload"], roof["kernel"]) if args.workload == "hexa" else None
+    tr = (measured_traffic(config_dict(args, world, mesh)["workload"], roof["kernel"])
+          if args.workload == "hexa" else None)
     roof["traffic"] = tr[0] if tr else None
     if tr:
         roof["note"] += "; traffic: one-pass ncu capture of one launch at this size (bytes)"

@@ -73,8 +73,8 @@ struct CondTcOut {
 
 // Per element, one warp: gather K_bb (lower triangle, packed) and b_b through
 // the dof map; right-looking Cholesky K_bb = L L^T and the inverse Li = L^-1
-// in place (columns from the last to the first, the original column kept in
-// a scratch vector); BSchur = Li^T (Li b_b); the digits of Li and Li^T.
+// in place (right-looking forward substitution, one column of L kept in a
+// scratch vector); BSchur = Li^T (Li b_b); the digits of Li and Li^T.
 // Warp-synchronous: no block barrier.
 constexpr int CH_WARPS = 4;
 __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
@@ -112,7 +112,10 @@ __global__ void __launch_bounds__(CH_WARPS * 32) k_cond_chol(
   }
   __syncwarp();
   bool fail = false;
-  // Cholesky: lane owns columns jj = k+1+lane (+32)
+  // Cholesky, right-looking.  The trailing update of step k runs over the
+  // packed triangle of the m = nb - k - 1 remaining rows as one flat index,
+  // so every lane of each FP64 instruction has work (GB300 issues FP64 at
+  // about 2 per clock per SM: idle lanes cost the same as busy ones).
   for (int k = 0; k < nb; ++k) {
     double d = A[tri(k, k)];
     if (!(d > 0.0)) { fail = true; d = 1.0; }
@@ -122,25 +125,34 @@ __global__ void __launch_bounds__(CH_WARPS * 32) k_cond_chol(
     if (lane == 0) A[tri(k, k)] = d;
     for (int i = k + 1 + lane; i < nb; i += 32) A[tri(i, k)] *= rk;
     __syncwarp();
-    for (int jj = k + 1 + lane; jj < nb; jj += 32) {
-      const double ljk = A[tri(jj, k)];
-      for (int i = jj; i < nb; ++i) A[tri(i, jj)] -= A[tri(i, k)] * ljk;
+    const int m = nb - k - 1;
+    for (int x = lane; x < m * (m + 1) / 2; x += 32) {
+      int ip = (int)((sqrtf(8.0f * x + 1.0f) - 1.0f) * 0.5f);
+      while (tri(ip + 1, 0) <= x) ++ip;
+      while (tri(ip, 0) > x) --ip;
+      const int i = k + 1 + ip, jj = k + 1 + (x - tri(ip, 0));
+      A[tri(i, jj)] = fma(-A[tri(i, k)], A[tri(jj, k)], A[tri(i, jj)]);
     }
     __syncwarp();
   }
   if (fail && lane == 0) atomicMin(bad_spd, e);
-  // inverse in place, column c from the last: Li[c][c] = 1 / L[c][c],
-  // Li[i][c] = -(sum_{k=c+1..i} Li[i][k] L[k][c]) Li[c][c]
-  for (int c = nb - 1; c >= 0; --c) {
-    for (int k = c + lane; k < nb; k += 32) col[k] = A[tri(k, c)];
+  // inverse in place, right-looking forward substitution L Li = I: at step k
+  // row k of Li is final once scaled by 1 / L(k,k); the rows i > k then take
+  // -L(i,k) Li(k, 0..k) (column k of L kept in col[] first), again one flat
+  // index over the (nb - k - 1) x (k + 1) block
+  for (int k = 0; k < nb; ++k) {
+    for (int i = k + 1 + lane; i < nb; i += 32) col[i] = A[tri(i, k)];
+    const double dk = 1.0 / A[tri(k, k)];
     __syncwarp();
-    const double dc = 1.0 / col[c];
-    for (int i = c + 1 + lane; i < nb; i += 32) {
-      double s = 0.0;
-      for (int k = c + 1; k <= i; ++k) s += A[tri(i, k)] * col[k];
-      A[tri(i, c)] = -s * dc;
+    if (lane == 0) A[tri(k, k)] = dk;
+    for (int jj = lane; jj < k; jj += 32) A[tri(k, jj)] *= dk;
+    __syncwarp();
+    const int w = k + 1, m = nb - k - 1;
+    for (int x = lane; x < m * w; x += 32) {
+      const int ip = x / w, jj = x - ip * w, i = k + 1 + ip;
+      const double lik = col[i];
+      A[tri(i, jj)] = jj == k ? -lik * A[tri(k, k)] : fma(-lik, A[tri(k, jj)], A[tri(i, jj)]);
     }
-    if (lane == 0) A[tri(c, c)] = dc;
     __syncwarp();
   }
   // y = Li b_b, BSchur = Li^T y
