@@ -399,17 +399,19 @@ int rows_pad(int rows, int nt) { return (rows + nt - 1) / nt * nt; }
 // ---------------------------------------------------------------------------
 // the augmented partial factorization
 // ---------------------------------------------------------------------------
-// FP64 step of one panel of the augmented matrix: the Cholesky factor L11
-// (lower, in place) of the kb x kb diagonal block at (k0, k0) and
-// W = L11^-H (upper, 64 x 64 column-major, zero outside kb x kb), from an
-// unblocked right-looking Cholesky and the forward substitution L11 X = I,
-// both as packed lower triangles in shared memory (67 KB: three CTAs per SM),
-// two barriers per column; row i of the update belongs to one warp, its
-// columns to the lanes.  GB300 issues FP64 at about 1.6 per clock per SM, so
-// the complex updates are 4 fused multiply-adds each.
-constexpr int ZDG_THREADS = 256;
+// FP64 step of one panel of the augmented matrix, one warp per element:
+// the Cholesky factor L11 of the kb x kb diagonal block at (k0, k0) and
+// W = L11^-H (upper, 64 x 64 column-major, zero outside kb x kb).  Right-
+// looking Cholesky, then the inverse in place by right-looking forward
+// substitution (column k of L kept in a scratch vector), in one packed lower
+// triangle per warp (34 KB: six warps per SM), warp-synchronous.  Each step's
+// update runs over a flat index, so every lane of an FP64 instruction has
+// work (GB300 issues FP64 at about 1.6 per clock per SM); complex updates are
+// 4 fused multiply-adds.  Only W is written: nothing reads the diagonal block
+// of the augmented matrix after its panel step.
+constexpr int ZDG_WARPS = 2;
 constexpr int ZDG_TRI = 64 * 65 / 2;
-constexpr size_t ZDG_SMEM = 2 * ZDG_TRI * sizeof(double2) + 64 * sizeof(double);
+constexpr size_t ZDG_SMEM = ZDG_WARPS * (ZDG_TRI + 64) * sizeof(double2);
 
 __device__ __forceinline__ int tri(int i, int j) { return i * (i + 1) / 2 + j; }
 // c - a b and c - a conj(b)
@@ -420,61 +422,59 @@ __device__ __forceinline__ double2 zfms_c(double2 c, double2 a, double2 b) {
   return make_double2(fma(-a.y, b.y, fma(-a.x, b.x, c.x)), fma(-a.y, b.x, fma(a.x, b.y, c.y)));
 }
 
-__global__ void __launch_bounds__(ZDG_THREADS) k_zdiag(double2* M, int64_t estride, int ld, int k0,
-                                                       int kb, double2* W, int64_t wstride,
-                                                       int* bad) {
+__global__ void __launch_bounds__(ZDG_WARPS * 32) k_zdiag(const double2* M, int64_t estride, int ld,
+                                                          int k0, int kb, double2* W,
+                                                          int64_t wstride, int* bad, int nel) {
   extern __shared__ double2 zdg[];
-  double2* Ls = zdg;                     // L (packed lower)
-  double2* Xs = zdg + ZDG_TRI;           // X = L^-1 (packed lower)
-  double* dk = (double*)(Xs + ZDG_TRI);  // pivots, stored when they become final
-  const int e = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  double2* D = M + (int64_t)e * estride + k0 + (int64_t)k0 * ld;
-  for (int x = tid; x < 64 * 64; x += ZDG_THREADS) {
-    const int i = x % 64, j = x / 64;
-    if (i < j) continue;
-    Ls[tri(i, j)] = (i < kb) ? D[i + (int64_t)j * ld] : make_double2(0.0, 0.0);
-    Xs[tri(i, j)] = make_double2((i == j && i < kb) ? 1.0 : 0.0, 0.0);
-  }
-  __syncthreads();
-  if (tid == 0) dk[0] = Ls[0].x;
-  __syncthreads();
+  const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int e = blockIdx.x * ZDG_WARPS + wp;
+  if (e >= nel) return;
+  double2* A = zdg + (size_t)wp * (ZDG_TRI + 64);  // L, then X = L^-1 (packed lower)
+  double2* col = A + ZDG_TRI;
+  const double2* D = M + (int64_t)e * estride + k0 + (int64_t)k0 * ld;
+  for (int j = 0; j < kb; ++j)
+    for (int i = j + lane; i < kb; i += 32) A[tri(i, j)] = D[i + (int64_t)j * ld];
+  __syncwarp();
   bool ok = true;
   for (int k = 0; k < kb; ++k) {
-    const double dd = dk[k];
-    if (!(dd > 0.0)) ok = false;
+    double dd = A[tri(k, k)].x;
+    if (!(dd > 0.0)) { ok = false; dd = 1.0; }
     const double sq = sqrt(dd), rs = 1.0 / sq;
-    // column k of L; row k of X
-    if (tid < kb - k) {
-      const int i = k + tid;
-      Ls[tri(i, k)] = i == k ? make_double2(sq, 0.0) : zscale(rs, Ls[tri(i, k)]);
-    } else if (tid >= 64 && tid - 64 <= k) {
-      const int j = tid - 64;
-      Xs[tri(k, j)] = zscale(rs, Xs[tri(k, j)]);
+    __syncwarp();
+    if (lane == 0) A[tri(k, k)] = make_double2(sq, 0.0);
+    for (int i = k + 1 + lane; i < kb; i += 32) A[tri(i, k)] = zscale(rs, A[tri(i, k)]);
+    __syncwarp();
+    const int m = kb - k - 1;
+    for (int x = lane; x < m * (m + 1) / 2; x += 32) {
+      int ip = (int)((sqrtf(8.0f * x + 1.0f) - 1.0f) * 0.5f);
+      while (tri(ip + 1, 0) <= x) ++ip;
+      while (tri(ip, 0) > x) --ip;
+      const int i = k + 1 + ip, jj = k + 1 + (x - tri(ip, 0));
+      A[tri(i, jj)] = zfms_c(A[tri(i, jj)], A[tri(i, k)], A[tri(jj, k)]);
     }
-    __syncthreads();
-    // row i > k: X(i, j) -= L(i, k) X(k, j) for j <= k;
-    //            L(i, j) -= L(i, k) conj(L(j, k)) for k < j <= i
-    for (int i = k + 1 + warp; i < kb; i += ZDG_THREADS / 32) {
-      const double2 lik = Ls[tri(i, k)];
-      for (int j = lane; j <= i; j += 32) {
-        if (j <= k) {
-          Xs[tri(i, j)] = zfms(Xs[tri(i, j)], lik, Xs[tri(k, j)]);
-        } else {
-          const double2 v = zfms_c(Ls[tri(i, j)], lik, Ls[tri(j, k)]);
-          Ls[tri(i, j)] = v;
-          if (i == k + 1 && j == k + 1) dk[k + 1] = v.x;
-        }
-      }
-    }
-    __syncthreads();
+    __syncwarp();
   }
-  if (!ok && tid == 0) atomicMin(bad, e);
+  if (!ok && lane == 0) atomicMin(bad, e);
+  for (int k = 0; k < kb; ++k) {
+    for (int i = k + 1 + lane; i < kb; i += 32) col[i] = A[tri(i, k)];
+    const double dk = 1.0 / A[tri(k, k)].x;
+    __syncwarp();
+    if (lane == 0) A[tri(k, k)] = make_double2(dk, 0.0);
+    for (int jj = lane; jj < k; jj += 32) A[tri(k, jj)] = zscale(dk, A[tri(k, jj)]);
+    __syncwarp();
+    const int w = k + 1, m = kb - k - 1;
+    for (int x = lane; x < m * w; x += 32) {
+      const int ip = x / w, jj = x - ip * w, i = k + 1 + ip;
+      const double2 lik = col[i];
+      A[tri(i, jj)] = jj == k ? make_double2(-lik.x * dk, -lik.y * dk)
+                              : zfms(A[tri(i, jj)], lik, A[tri(k, jj)]);
+    }
+    __syncwarp();
+  }
   double2* w = W + (int64_t)e * wstride;
-  for (int x = tid; x < 64 * 64; x += ZDG_THREADS) {
-    const int i = x % 64, j = x / 64;
-    if (i < kb && j < kb && i >= j) D[i + (int64_t)j * ld] = Ls[tri(i, j)];
-    w[x] = (j >= i) ? zconj(Xs[tri(j, i)]) : make_double2(0.0, 0.0);  // W(i, j) = conj(X(j, i))
-  }
+  for (int j = 0; j < 64; ++j)
+    for (int i = lane; i < 64; i += 32)  // W(i, j) = conj(X(j, i))
+      w[i + 64 * j] = (j >= i && j < kb) ? zconj(A[tri(j, i)]) : make_double2(0.0, 0.0);
 }
 
 // the n x n trailing block at (o, o), lower triangle: T := -T
@@ -612,7 +612,8 @@ int launch_dpg_aug_tc(int part, int nel, int nt, int n1, int nq, const DpgWork& 
   };
   auto panel = [&](int k0, int kb, int slot) {
     double2* ws = W + (int64_t)slot * 4096;
-    k_zdiag<<<nel, ZDG_THREADS, ZDG_SMEM, st>>>(M, mst, na, k0, kb, ws, wst, bad);
+    k_zdiag<<<(nel + ZDG_WARPS - 1) / ZDG_WARPS, ZDG_WARPS * 32, ZDG_SMEM, st>>>(
+        M, mst, na, k0, kb, ws, wst, bad, nel);
     ++nk;
     const int rem = na - k0 - kb;  // > 0: the load row is never a pivot
     double2* P = M + (k0 + kb) + (int64_t)k0 * na;
