@@ -239,13 +239,13 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
   uint8_t* sm = (uint8_t*)(((uintptr_t)zsm_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* regA0 = sm;
   uint8_t* regB = sm + ZNABUF * ZA_BLK;
-  __shared__ __align__(8) uint64_t ldB_bar, ldA_bar[2], afree_bar[2], accf_bar;
+  __shared__ __align__(8) uint64_t ldB_bar, ldA_bar[ZNABUF], afree_bar[ZNABUF], accf_bar;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
     mbar_init(smem_u32(&ldB_bar), 1);
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < ZNABUF; ++i) {
       mbar_init(smem_u32(&ldA_bar[i]), 1);
       mbar_init(smem_u32(&afree_bar[i]), 1);
     }
