@@ -185,10 +185,9 @@ DPG_METRIC = "DPG Maxwell elements/s (complex FP64, trial p=3, test p=4, condens
 
 
 def measured_traffic(workload, kernel):
-    """DRAM bytes of `kernel` on `workload` from the committed one-pass ncu
-    summary (profiles/dram_traffic_dominant_kernels.md), or None."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
-                        "dram_traffic_dominant_kernels.md")
+    """DRAM bytes of `kernel` on `workload` from the committed figures of a
+    one-pass ncu capture (profiles/dram_traffic.txt), or None."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "dram_traffic.txt")
     try:
         with open(path) as f:
             for line in f:
