@@ -35,3 +35,19 @@ def test_strerror_without_gpu():
     L = H.lib()
     assert L.hp3dg_strerror(-1).decode().startswith("negative Jacobian")
     assert L.hp3dg_strerror(0).decode() == "ok"
+
+
+def test_null_context_calls_return_arg_errors_without_gpu():
+    """Entry points reject a NULL context before touching the device."""
+    L = H.lib()
+    ERR_ARG = -7
+    k = ctypes.c_int64()
+    assert L.hp3dg_batch_set_geometry(None, None) == ERR_ARG
+    assert L.hp3dg_dpg_pass_stats(None, ctypes.byref(k)) == ERR_ARG
+    assert L.hp3dg_pass_stats(None, ctypes.byref(k), None) == ERR_ARG
+    assert L.hp3dg_dpg_last_bad_element(None) == -1
+
+
+def test_dpg_opts_layout_matches_header():
+    # 5 doubles, 8 int32 (ibcflag .. precision), 4 reserved
+    assert ctypes.sizeof(H.DpgOpts) == 5 * 8 + 8 * 4 + 4 * 4
