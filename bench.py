@@ -184,6 +184,26 @@ def config_dict(args, world, mesh):
 DPG_METRIC = "DPG Maxwell elements/s (complex FP64, trial p=3, test p=4, condensed)"
 
 
+def job_max(x, world):
+    """The job's figure for a per-rank time: the maximum over the ranks
+    (all_reduce MAX on the process group's device: CUDA under NCCL, the host
+    under gloo).  One rank: x itself."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world, units_per_rank, ms_job):
+    """Whole-job throughput of weak scaling: every rank processes
+    units_per_rank (its own replica), the job takes ms_job."""
+    return world * units_per_rank / (ms_job / 1000.0)
+
+
 def measured_traffic(workload, kernel):
     """DRAM bytes of `kernel` on `workload` from the committed figures of a
     one-pass ncu capture (profiles/dram_traffic.txt), or None."""
@@ -298,12 +318,8 @@ def run_dpg(args, rank, world):
     clocks = clk.stop()
     launches = ep.pass_stats()
     ph = np.array(ph)
-    ms = float(np.median(ph[:, 4]))
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * ne / (ms / 1000.0)
+    ms = job_max(float(np.median(ph[:, 4])), world)
+    value = job_value(world, ne, ms)
     # end to end: submit (descriptors, vertices, permittivities), run, download
     ep.download()
     ntrial, ni, nb = ep.sizes()
@@ -344,7 +360,8 @@ def run_dpg(args, rank, world):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic", "config": cfg,
-            "e2e": {"value": world * ne / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
+            "e2e": {"value": job_value(world, ne, 1000 * e2e_s), "unit": "elements/s",
+                    "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * e2e_s,
                     "note": "submit (descriptors, vertices, permittivities), run, download of "
                             "the condensed systems, Schur blocks and LCON"},
@@ -425,11 +442,7 @@ def main():
             phases.append(ep.phase_times())
         e1.record(stream)
         torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        if world > 1:
-            t = torch.tensor([ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = job_max(e0.elapsed_time(e1), world)
         return ep, ms, phases
 
     clk = ClockSampler(local)
@@ -438,7 +451,7 @@ def main():
     clocks = clk.stop()
     ms_step = ms / args.steps
     nel = mesh["nelem"]
-    value = world * nel / (ms_step / 1000.0)
+    value = job_value(world, nel, ms_step)
 
     # end to end through the C ABI with host buffers (submit + run + download).
     # Each step resubmits the mesh with this step's geometry and coefficient:
@@ -465,11 +478,7 @@ def main():
         epe.run()
         epe.download()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.e2e_steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = job_max((time.perf_counter() - t0) / args.e2e_steps, world)
     epe.close()
     # one cold step: a new context (descriptor processing, allocations, bin
     # tables, operand digits, graph capture, pinned buffers) for reference
@@ -481,7 +490,8 @@ def main():
     torch.cuda.synchronize()
     cold_ms = 1000 * (time.perf_counter() - t0)
     epc.close()
-    e2e = {"value": world * nel / e2e_s, "unit": "elements/s", "h2d_bytes_per_step": h2d,
+    e2e = {"value": job_value(world, nel, 1000 * e2e_s), "unit": "elements/s",
+           "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * e2e_s,
            "cold_step_ms": cold_ms,
            # the chunked pass applies to a batch of one bin (the uniform mesh)
