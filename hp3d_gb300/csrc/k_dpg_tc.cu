@@ -44,7 +44,7 @@ constexpr int ZB_BLK = ZN * ZK * 2;    // one B digit block
 constexpr int ZB_TILE = 2 * ZD * ZB_BLK;  // both B forms of one column tile
 constexpr int ZFB = 48;                // fraction bits of the split (|v| < 2^e -> |X| <= 2^48)
 constexpr int ZBROWS = 2 * ZD * ZN;    // rows of one B K-step: [digit q][form][32 rows]
-constexpr int ZU_THREADS = 320;        // loader, MMA, 8 epilogue warps (2 per TMEM lane quarter)
+constexpr int ZU_THREADS = 576;        // loader, MMA, 16 epilogue warps (4 per TMEM lane quarter)
 constexpr int ZEPI = ZU_THREADS / 32 - 2;  // epilogue warps
 constexpr int ZCG = ZN / 8 / (ZEPI / 4);   // 8-column groups per epilogue warp
 constexpr int ZNABUF = 2;              // A digit buffers
@@ -239,7 +239,8 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
   uint8_t* sm = (uint8_t*)(((uintptr_t)zsm_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* regA0 = sm;
   uint8_t* regB = sm + ZNABUF * ZA_BLK;
-  __shared__ __align__(8) uint64_t ldB_bar, ldA_bar[ZNABUF], afree_bar[ZNABUF], accf_bar;
+  // levfin[p]: the MMAs of A digit p are complete, so the levels 0..p are final
+  __shared__ __align__(8) uint64_t ldB_bar, ldA_bar[ZNABUF], afree_bar[ZNABUF], levfin[ZD];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
       mbar_init(smem_u32(&ldA_bar[i]), 1);
       mbar_init(smem_u32(&afree_bar[i]), 1);
     }
-    mbar_init(smem_u32(&accf_bar), 1);
+    for (int l = 0; l < ZD; ++l) mbar_init(smem_u32(&levfin[l]), 1);
     abort_ = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -312,67 +313,73 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
           }
         }
         umma_commit(smem_u32(&afree_bar[buf]));
+        umma_commit(smem_u32(&levfin[p]));
       }
-      umma_commit(smem_u32(&accf_bar));
     }
   } else {
     // epilogue: warps 2..; TMEM lane quarter warp % 4 = rows of the tile,
-    // (warp - 2) / 4 = which ZCG 8-column groups
+    // (warp - 2) / 4 = which ZCG 8-column groups.  Level p takes only the
+    // digit pairs (p', p - p') with p' <= p, so it is final once the MMAs of
+    // A digit p are (levfin[p]): each level is read and folded into the
+    // running integer while the MMAs of the later digits proceed.
     const int quarter = warp & 3, half = (warp - 2) >> 2;
     const int i = rt * ZM + quarter * 32 + lane;
     const bool rowok = i < a.m;
     const int ea = rowok ? a.ea[(int64_t)e * a.ea_estride + i] : 0;
     const double2* crow = a.C + (int64_t)e * a.c_estride + i;
     const int* ebp = a.eb + (int64_t)e * a.eb_estride;
-    // C and the column exponents of the next 8-column group are loaded one
-    // group ahead (independent loads in flight while the levels are combined)
-    double2 cn[8];
-    int xn[8];
-    auto fetch = [&](int cg) {
+    const uint32_t tl = tbase + ((uint32_t)(quarter * 32) << 16);
+    double2* C = a.C + (int64_t)e * a.c_estride;
+    for (int cg = ZCG * half; cg < ZCG * (half + 1); ++cg) {
+      // C and the column exponents, loaded while the MMAs run
+      double2 cv[8];
+      int xs[8];
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
         const int j = ct * ZN + cg * 8 + c;
         const bool ok = rowok && j < a.n && !(a.lower && j > i);
-        cn[c] = (ok && !a.beta0) ? crow[(int64_t)j * a.ldc] : make_double2(0.0, 0.0);
-        xn[c] = ok ? ebp[j] : ZX_SKIP;
+        cv[c] = (ok && !a.beta0) ? crow[(int64_t)j * a.ldc] : make_double2(0.0, 0.0);
+        xs[c] = ok ? ebp[j] : ZX_SKIP;
       }
-    };
-    const int cg0 = ZCG * half;
-    fetch(cg0);
-    const bool okw = mbar_wait(smem_u32(&accf_bar), 0, &abort_);
-    if (!okw) { abort_ = 1; atomicExch(a.err, 44); }
-    tc_fence_after();
-    const uint32_t tl = tbase + ((uint32_t)(quarter * 32) << 16);
-    double2* C = a.C + (int64_t)e * a.c_estride;
-    for (int cg = cg0; cg < cg0 + ZCG; ++cg) {
-      double2 cv[8];
-      int xs[8];
-#pragma unroll
-      for (int c = 0; c < 8; ++c) { cv[c] = cn[c]; xs[c] = xn[c]; }
-      if (cg + 1 < cg0 + ZCG) fetch(cg + 1);
       // exact recombination in integers.  Digits are at most 2^6 (48-bit
       // split), so each level sum s_L (at most 7 pairs x 128 terms) is an
       // integer below 2^21.8 and (s_L + 1.5 2^23) has it in its low mantissa
-      // bits.  hi = sum_{L<=3} s_L 2^7(3-L) (< 2^42.8), lo = sum_{L>=4}
-      // s_L 2^7(6-L); V = hi 2^19 + lo / 4 (< 2^61.8) carries the product in
-      // units of 2^(sx - 52), below the 2^(sx - 48) of the split itself
+      // bits.  V = sum_{L<=3} s_L 2^(7(3-L)+19) + sum_{L>=4} s_L 2^(7(6-L)-2)
+      // (< 2^61.1; the last level rounded down to a unit) carries the
+      // product in units of 2^(sx - 52), below the 2^(sx - 48) of the split
       long long V[2][8];
 #pragma unroll
-      for (int part = 0; part < 2; ++part) {
-        uint32_t r[ZD][8];
+      for (int part = 0; part < 2; ++part)
 #pragma unroll
-        for (int L = 0; L < ZD; ++L) tmem_ld8_nowait(tl + (uint32_t)((L * 2 + part) * ZN + cg * 8), r[L]);
+        for (int c = 0; c < 8; ++c) V[part][c] = 0;
+      bool okw = true;
+#pragma unroll
+      for (int L = 0; L < ZD; ++L) {
+        if (!mbar_wait(smem_u32(&levfin[L]), 0, &abort_)) {
+          abort_ = 1;
+          atomicExch(a.err, 44);
+          okw = false;
+          break;
+        }
+        tc_fence_after();
+        uint32_t r0[8], r1[8];
+        tmem_ld8_nowait(tl + (uint32_t)((L * 2 + 0) * ZN + cg * 8), r0);
+        tmem_ld8_nowait(tl + (uint32_t)((L * 2 + 1) * ZN + cg * 8), r1);
         tmem_wait();
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
-          int sl[ZD];
-#pragma unroll
-          for (int L = 0; L < ZD; ++L)
-            sl[L] = __float_as_int(__uint_as_float(r[L][c]) + 12582912.0f) - 0x4B400000;
-          const long long hi = ((long long)(sl[0] * 128 + sl[1]) << 14) + ((long long)sl[2] << 7) + sl[3];
-          const long long lo = ((long long)(sl[4] * 128 + sl[5]) << 7) + sl[6];
-          const long long v = (hi << 19) + (lo >> 2);
-          V[part][c] = a.sgn < 0.0 ? -v : v;
+          const long long s0 = __float_as_int(__uint_as_float(r0[c]) + 12582912.0f) - 0x4B400000;
+          const long long s1 = __float_as_int(__uint_as_float(r1[c]) + 12582912.0f) - 0x4B400000;
+          if (L <= 3) {
+            V[0][c] += s0 << (ZR * (3 - L) + 19);
+            V[1][c] += s1 << (ZR * (3 - L) + 19);
+          } else if (L < 6) {
+            V[0][c] += s0 << (ZR * (6 - L) - 2);
+            V[1][c] += s1 << (ZR * (6 - L) - 2);
+          } else {
+            V[0][c] += s0 >> 2;
+            V[1][c] += s1 >> 2;
+          }
         }
       }
       if (!okw || !rowok) continue;
@@ -380,8 +387,10 @@ __global__ void __launch_bounds__(ZU_THREADS) k_zupd(ZUpd a) {
       for (int c = 0; c < 8; ++c) {
         if (xs[c] == ZX_SKIP) continue;
         const int sc = ea + xs[c] - 52;
-        cv[c].x += scaled_i64(V[0][c], sc);
-        cv[c].y += scaled_i64(V[1][c], sc);
+        const long long v0 = a.sgn < 0.0 ? -V[0][c] : V[0][c];
+        const long long v1 = a.sgn < 0.0 ? -V[1][c] : V[1][c];
+        cv[c].x += scaled_i64(v0, sc);
+        cv[c].y += scaled_i64(v1, sc);
         C[i + (int64_t)(ct * ZN + cg * 8 + c) * a.ldc] = cv[c];
       }
     }
