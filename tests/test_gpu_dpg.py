@@ -190,3 +190,20 @@ def test_resubmit_same_mesh_matches_fresh_context(precision):
         a0, b0 = fresh.schur(e)
         assert np.array_equal(a, a0) and np.array_equal(b, b0), e
     ep.close(); fresh.close()
+
+
+def test_tensor_core_p4_element_matrices():
+    """p = 4 (test order 5: augmented size 1849, Gram table of 146k packed
+    columns) on the mixed path: two elements with different orientation
+    codes against the oracle (one oracle element takes seconds)."""
+    m, prm, eps, bc, imp, flags = _setup(2, 4, ((0, 1),))
+    ep = H.DPGPass(omega=prm.omega, ibcflag=prm.ibcflag, isol=prm.isol, keep_elem=True,
+                   precision=H.MIXED)
+    ep.submit(m, eps, flags)
+    ep.run(); ep.download()
+    for e in (0, 5):
+        A, b, rc = O.dpg_elem(m["norder"][e], m["nori_edge"][e], m["nori_face"][e],
+                              m["xvert"][e], eps[e], int(imp[e]), prm)
+        Ag, bg = ep.elem(e)
+        assert _rel(Ag, A) < 1e-10 and _rel(bg, b) < 1e-10, (e, _rel(Ag, A), _rel(bg, b))
+    ep.close()
