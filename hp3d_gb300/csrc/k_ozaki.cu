@@ -92,6 +92,11 @@ __host__ __device__ constexpr uint32_t idesc_bf16_m128_n128() {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
          ((uint32_t)(BM >> 4) << 24);
 }
+// the same with N = 256: two consecutive B digit tiles into two slots
+__host__ __device__ constexpr uint32_t idesc_bf16_m128_n256() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(2 * BN >> 3) << 17) |
+         ((uint32_t)(BM >> 4) << 24);
+}
 
 // exponent k of an exact power of two 2^k (the digit scales)
 __device__ __forceinline__ int pow2_exponent(double x) {
@@ -222,6 +227,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16_m128_n128();
+      const uint32_t idesc2 = idesc_bf16_m128_n256();
       int stage = 0;
       uint32_t phase = 0, accph = 0;
       for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
@@ -250,14 +256,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
             if (abort_) break;
             tc_fence_after();
-            for (int p = pd.pair0; p < pd.pair0 + pd.npair; ++p) {
-              const uint32_t aoff = (uint32_t)(P.pi[p] - 1) * TILE_BYTES;
-              const uint32_t boff = (uint32_t)(MAXDIG + P.pj[p] - 1) * TILE_BYTES;
-              const uint32_t dt = tbase + (uint32_t)P.pslot[p] * BN;
-              for (int g = 0; g < ng; ++g) {
-                uint32_t acc = (kb0 + g > 0 || !P.pfirst[p]) ? 1u : 0u;
-                umma_bf16(dt, sdesc_kmajor(sbase[g] + aoff), sdesc_kmajor(sbase[g] + boff), idesc,
-                          acc);
+            // the pass's pairs by A digit i: its B digits j = jlo..jhi are
+            // consecutive 128-row tiles of the stage and their levels i + j
+            // consecutive 128-column accumulator slots, so two of them make
+            // one N = 256 MMA (A read once from shared memory for both).
+            // Digit i = 1 is the first to write every slot of a pass.
+            for (int i = 1; i <= pd.nA; ++i) {
+              const int jlo = pd.first_level - i > 1 ? pd.first_level - i : 1;
+              const int jtop = pd.first_level + pd.nlev - 1 - i;
+              const int jhi = jtop < P.digits ? jtop : P.digits;
+              const uint32_t aoff = (uint32_t)(i - 1) * TILE_BYTES;
+              for (int j = jlo; j <= jhi; j += 2) {
+                const bool two = j + 1 <= jhi;
+                const uint32_t boff = (uint32_t)(MAXDIG + j - 1) * TILE_BYTES;
+                const uint32_t dt = tbase + (uint32_t)(i + j - pd.first_level) * BN;
+                for (int g = 0; g < ng; ++g) {
+                  const uint32_t acc = (kb0 + g > 0 || i > 1) ? 1u : 0u;
+                  umma_bf16(dt, sdesc_kmajor(sbase[g] + aoff), sdesc_kmajor(sbase[g] + boff),
+                            two ? idesc2 : idesc, acc);
+                }
               }
             }
             for (int g = 0; g < ng; ++g) {
