@@ -33,7 +33,6 @@
 namespace hp3dg {
 
 namespace {
-constexpr int F2_THREADS = 256;
 constexpr int CT_NC = 64;          // TMEM columns per level slot
 constexpr int CT_MAXDIG = 7;
 constexpr int CT_MAXCHUNK = 8;

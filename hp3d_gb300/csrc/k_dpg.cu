@@ -103,31 +103,23 @@ __device__ double inv3(const double J[3][3], double Ji[3][3]) {
 // mfd_solutions cases 1 and 2 (component icomp of E), H = curl E/(-i w mu),
 // J = curl H - i w eps E (common/mfd_solutions.F90, exact.F90, getf.F90)
 __device__ void dpg_source(const DpgPhys& ph, double epr, double epi, const double* X, double2* J) {
-  double p[2] = {0, 0}, gp[3][2], g2[3][3][2];
-  for (int i = 0; i < 3; ++i) {
-    gp[i][0] = gp[i][1] = 0.0;
+  double p[2] = {0, 0}, g2[3][3][2];  // the scalar p and its second derivatives
+  for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) g2[i][j][0] = g2[i][j][1] = 0.0;
-  }
   const double x = X[0], y = X[1], z = X[2];
   if (ph.isol == 1) {
     const double w = ph.omega, sx = sin(w * x), sy = sin(w * y), sz = sin(w * z);
     const double cx = cos(w * x), cy = cos(w * y), cz = cos(w * z);
     double v = sx * sy * sz;  // times (1 + i)
     p[0] = p[1] = v;
-    double g[3] = {w * cx * sy * sz, w * sx * cy * sz, w * sx * sy * cz};
     double h[3][3] = {{-w * w * v, w * w * cx * cy * sz, w * w * cx * sy * cz},
                       {w * w * cx * cy * sz, -w * w * v, w * w * sx * cy * cz},
                       {w * w * cx * sy * cz, w * w * sx * cy * cz, -w * w * v}};
-    for (int i = 0; i < 3; ++i) {
-      gp[i][0] = gp[i][1] = g[i];
+    for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) g2[i][j][0] = g2[i][j][1] = h[i][j];
-    }
   } else if (ph.isol == 2) {
     const double cn = 100.0;
     p[0] = -cn * x * y * z * (x - 1.0) * (y - 1.0) * (z - 1.0);
-    gp[0][0] = -cn * y * z * (2.0 * x - 1.0) * (y - 1.0) * (z - 1.0);
-    gp[1][0] = -cn * x * z * (2.0 * y - 1.0) * (x - 1.0) * (z - 1.0);
-    gp[2][0] = -cn * x * y * (2.0 * z - 1.0) * (x - 1.0) * (y - 1.0);
     g2[0][0][0] = cn * y * z * (y - 1.0) * (z - 1.0) * (-2.0);
     g2[1][1][0] = cn * x * z * (x - 1.0) * (z - 1.0) * (-2.0);
     g2[2][2][0] = cn * x * y * (x - 1.0) * (y - 1.0) * (-2.0);
