@@ -56,3 +56,14 @@ def test_single_rank_needs_no_process_group():
     import bench
     assert bench.job_max(12.5, 1) == 12.5
     assert bench.job_value(1, 1000, 500.0) == pytest.approx(2000.0)
+
+
+def test_roofline_traffic_figures_are_read_from_the_profiles():
+    """The bench's roofline traffic comes from the committed one-pass ncu
+    figures: both dominant kernels are present, unknown pairs give None."""
+    import bench
+    t, unit = bench.measured_traffic("galerkin_poisson_hexa_24^3_p5_integration1", "k_ozaki_gemm")
+    assert unit == "per_launch" and t > 1e10
+    t, unit = bench.measured_traffic("ultraweak_dpg_maxwell_hexa_10^3_p3_impedance", "k_zupd")
+    assert unit == "per_pass" and t > 1e11
+    assert bench.measured_traffic("galerkin_poisson_hexa_8^3_p5_integration1", "k_ozaki_gemm") is None
