@@ -22,7 +22,10 @@
 //            of the B = D digit tiles (128 elements x 16 q); the digits are
 //            stored in HBM already in the UMMA canonical K-major layout
 //            (8-row x 16-byte core matrices), 4-stage ring
-//   warp 1   TMEM allocation (512 columns) and the single MMA-issuing thread
+//   warp 1   TMEM allocation (512 columns) and the single MMA-issuing thread;
+//            the pairs (i, j), (i, j+1) of an A digit read consecutive B digit
+//            tiles into consecutive level slots, so they run as one
+//            128 x 256 x 16 MMA (the A tile read once for both)
 //   warps 2-5 epilogue: tcgen05.ld of up to 4 level accumulators, exact
 //            integer recombination, FP64 scaling, coalesced stores of PK
 // Levels are processed in passes of <= 4 accumulators (4 x 128 TMEM
