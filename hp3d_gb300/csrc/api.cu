@@ -312,9 +312,18 @@ int bin_quadrature(int t, const int* full, int integration, std::vector<double>&
   return hexa_quadrature(full, integration, xi, w);
 }
 
+// testing (hp3dg_opts.fault_inject = 2): the submit running on this thread
+// makes every device allocation fail
+thread_local bool tl_alloc_fault = false;
+struct AllocFaultScope {
+  explicit AllocFaultScope(bool on) { tl_alloc_fault = on; }
+  ~AllocFaultScope() { tl_alloc_fault = false; }
+};
+
 template <class T>
 T* dalloc(size_t count, int* err) {
   if (count == 0) count = 1;
+  if (tl_alloc_fault) { *err = HP3DG_ERR_ALLOC; return nullptr; }
   void* p = nullptr;
   if (cudaMalloc(&p, count * sizeof(T)) != cudaSuccess) { *err = HP3DG_ERR_ALLOC; return nullptr; }
   return (T*)p;
@@ -596,6 +605,7 @@ int hp3dg_batch_submit_constrained(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_d
     c->ran = c->downloaded = c->have_dofs = false;
     return HP3DG_OK;
   }
+  AllocFaultScope fault_scope(c->opts.fault_inject == 2);
   free_batch(c);
   c->last_desc.clear();
   c->nel = nel;
@@ -1037,7 +1047,7 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
   if (stage == 1) {
     if (mixed) {
       if (launch_ozaki_gemm(B.plan, ne, B.n, ddig, dscale, B.d_mdig, B.d_mscale, PK, c->d_flags + 2,
-                            st))
+                            st, c->opts.fault_inject == 1 ? 1 : 0))
         return HP3DG_ERR_CUDA;
     } else {
       launch_contract_fp64(ne, B.nint, B.n, B.ni, B.nb, B.d_grad, D, PK, st);
@@ -1242,9 +1252,12 @@ int hp3dg_batch_sync(hp3dg_ctx* c) {
   }
   const int NONE = 0x7f7f7f7f;
   c->last_bad = -1;
+  // a bad Jacobian is an input error found before the products; a timeout of
+  // a tensor-core kernel leaves the later stages reading unfinished data, so
+  // it is reported before what those stages flagged
   if (fl[0] != NONE) { c->last_bad = fl[0]; return HP3DG_ERR_NEG_JACOBIAN; }
-  if (fl[1] != NONE) { c->last_bad = fl[1]; return HP3DG_ERR_NOT_SPD; }
   if (fl[2] != NONE) return HP3DG_ERR_TIMEOUT;  // a bounded wait of the tensor-core kernel gave up
+  if (fl[1] != NONE) { c->last_bad = fl[1]; return HP3DG_ERR_NOT_SPD; }
   return HP3DG_OK;
 }
 

@@ -435,9 +435,10 @@ int hp3dg_dpg_sync(hp3dg_dpg_ctx* c) {
   cudaEventElapsedTime(&c->times[4], c->ev[0], c->ev[4]);
   const int NONE = 0x7f7f7f7f;
   c->last_bad = -1;
+  // a timeout leaves the later stages reading unfinished data: reported first
   if (fl[0] != NONE) { c->last_bad = fl[0]; return HP3DG_ERR_NEG_JACOBIAN; }
-  if (fl[1] != NONE) { c->last_bad = fl[1]; return HP3DG_ERR_NOT_SPD; }
   if (fl[2] != NONE) return HP3DG_ERR_TIMEOUT;  // a bounded wait of a tensor-core kernel gave up
+  if (fl[1] != NONE) { c->last_bad = fl[1]; return HP3DG_ERR_NOT_SPD; }
   return HP3DG_OK;
 }
 

@@ -144,10 +144,14 @@ int launch_ozaki_slice_d(const OzakiPlan& plan, int nel, int nint, const double*
                          uint16_t* d_ddig, double* d_dscale, cudaStream_t st);
 size_t ozaki_d_bytes(const OzakiPlan& plan, int nel);
 int ozaki_pairs(const OzakiPlan& plan);
-// the tensor-core contraction: PK = dscale*mscale*sum_s 2^-radix*s acc_s
+// k-blocks (16 q each) per exact accumulation run of the contraction
+int ozaki_kchunk(const OzakiPlan& plan);
+// the tensor-core contraction: PK = dscale*mscale*sum_s 2^-radix*s acc_s.
+// fault = 1 (testing only): the loader withholds one stage, so the bounded
+// waits run out and the kernel reports through d_flag instead of finishing.
 int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                      double* d_PK, int* d_flag, cudaStream_t st);
+                      double* d_PK, int* d_flag, cudaStream_t st, int fault = 0);
 
 // the same contraction for a dense bin-constant M (K x ncols, row-major FP64):
 // OUT[r, c] = sum_q D[r, q] M[q, c] for rows r of D (K per row)

@@ -43,6 +43,21 @@ __device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity, volatile 
   }
   return false;
 }
+// the same with a caller-chosen iteration limit
+__device__ __forceinline__ bool mbar_wait_n(uint32_t a, uint32_t parity, volatile int* abort_,
+                                            long limit) {
+  for (long it = 0; it < limit; ++it) {
+    if (mbar_try(a, parity)) return true;
+    if ((it & 255) == 255 && *abort_) return false;
+  }
+  return false;
+}
+// wait without the abort test (draining a role's own asynchronous work)
+__device__ __forceinline__ bool mbar_drain(uint32_t a, uint32_t parity, long limit) {
+  for (long it = 0; it < limit; ++it)
+    if (mbar_try(a, parity)) return true;
+  return false;
+}
 __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes,
                                           uint32_t mbar) {
   asm volatile(

@@ -159,13 +159,23 @@ __global__ void __launch_bounds__(NT) k_condense_dense(int n, int ni, int nb,
 extern "C" int hp3dg_condense_noalloc(int32_t n_elem, int32_t n, int32_t nb, const double* K,
                                       const double* b, double* aii, double* bi, double* aschur,
                                       double* bschur, int32_t* bad_element, void* stream) {
+  if (bad_element) *bad_element = -1;
   if (n_elem < 0 || nb < 1 || n <= nb || !K || !b || !aii || !bi || !aschur || !bschur)
     return HP3DG_ERR_ARG;
   const int ni = n - nb;
   if ((long long)n_elem * ((long long)ni * (ni + 1) / 2) > kScratchDoubles - 1) return HP3DG_ERR_ARG;
-  const size_t smem = ((size_t)nb * nb + (size_t)nb * (ni + 1) + ni) * sizeof(double);
-  if (smem > 227 * 1024) return HP3DG_ERR_UNSUPPORTED;
   if (n_elem == 0) return HP3DG_OK;
+  // one element's bubble block, [K_bi | b_b] and condensed load sit in shared
+  // memory next to the kernel's static shared word: hexahedra up to p = 5
+  // (nb = 64, ni = 152: 112 KB) fit, p = 6 (nb = 125, ni = 218: 345 KB) does not
+  const size_t smem = ((size_t)nb * nb + (size_t)nb * (ni + 1) + ni) * sizeof(double);
+  int dev = 0, optin = 0;
+  cudaFuncAttributes fa;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      cudaFuncGetAttributes(&fa, (const void*)k_condense_dense) != cudaSuccess)
+    return HP3DG_ERR_CUDA;
+  if (smem + fa.sharedSizeBytes > (size_t)optin) return HP3DG_ERR_UNSUPPORTED;
   double* scratch = nullptr;
   int rc = scratch_for_device(&scratch);
   if (rc != HP3DG_OK) return rc;

@@ -6,30 +6,46 @@
 //   PK[e, c] = sum_q D[e, q] M[q, c],   q = (point l, component pair ij),
 //   c = packed (a <= b) entry,  M[(l,ij), (a,b)] = G_i[l,a] G_j[l,b] (+ sym).
 //
-// Both operands are FP64.  They are split into balanced integer digits of
-// `radix` bits (scaled per element row / per column by powers of two):
-//   D = s_e * sum_i d_i 2^(-radix*i),   M = t_c * sum_j m_j 2^(-radix*j),
-// every digit an integer |d| <= 2^radix, exact in BF16.  The digit products
-// d_i * m_j are exact and, grouped by level s = i + j, their sums over q stay
-// below 2^24 and are therefore exact in the FP32 TMEM accumulators.  The
-// levels s = 2 .. digits+1 are recombined exactly as 64-bit integers and
-// scaled to FP64 in the epilogue (the FP64 residual correction of the
-// split): the result carries ~radix*digits bits.
+// Both operands are FP64.  They are split into balanced integer digits of R
+// = `radix` bits, scaled per element row / per column by powers of two:
+//   D = s_e * sum_i d_i 2^(-R i),   M = t_c * sum_j m_j 2^(-R j),
+// with |d_1|, |m_1| <= 2^R and every later digit <= 2^(R-1), all exact in
+// BF16.  A digit product d_i m_j is exact in FP32; the products of one level
+// s = i + j (s = 2 .. digits+1) are summed into one FP32 TMEM accumulator.
 //
-// Kernel structure (one CTA per SM, persistent over 128 x 128 output tiles):
-//   warp 0   producer: per k-block one contiguous bulk copy (cp.async.bulk)
-//            of the A = M digit tiles (128 packed columns x 16 q each) and one
-//            of the B = D digit tiles (128 elements x 16 q); the digits are
-//            stored in HBM already in the UMMA canonical K-major layout
-//            (8-row x 16-byte core matrices), 4-stage ring
-//   warp 1   TMEM allocation (512 columns) and the single MMA-issuing thread;
-//            the pairs (i, j), (i, j+1) of an A digit read consecutive B digit
-//            tiles into consecutive level slots, so they run as one
-//            128 x 256 x 16 MMA (the A tile read once for both)
-//   warps 2-5 epilogue: tcgen05.ld of up to 4 level accumulators, exact
-//            integer recombination, FP64 scaling, coalesced stores of PK
-// Levels are processed in passes of <= 4 accumulators (4 x 128 TMEM
-// columns); pass > 1 adds into the FP64 tile written by pass 1.
+// Exactness, a priori: the accumulators are restarted every `kchunk`
+// k-blocks (16 q each), with kchunk * 16 * max_s sum_{i+j=s} b_i b_j <= 2^24
+// (b_1 = 2^R, b_i = 2^(R-1)): every partial sum of every level, in any order
+// of accumulation, is an integer of magnitude below 2^24 and therefore exact
+// in FP32.  At R = 7 and 7 digits the largest level bound per q is
+// 2 * 2^13 + 5 * 2^12 = 36864, so kchunk = 28 (448 q; K = 2058 at p = 5 with
+// INTEGRATION = 1 is five runs).  After each run the epilogue adds the levels
+// exactly into one 64-bit integer per output, V += sum_s L_s 2^(R(S-s) - t)
+// (S = the last level, t >= 0 chosen so that |V| < 2^62 over all runs; only
+// the last level loses its t low bits), and at the end forms the FP64 result
+// V 2^(ke + kc - R S + t) with one rounding (the FP64 recombination of the
+// split): the result carries about R * digits bits.
+//
+// Kernel structure (one CTA per SM, persistent over 128 x 64 output tiles):
+//   warp 0    producer: per k-block one contiguous bulk copy (cp.async.bulk)
+//             of the A = M digit tiles (128 packed columns x 16 q each) and
+//             one of the B = D digit tiles (64 elements x 16 q each); digits
+//             are stored in HBM already in the UMMA canonical K-major layout
+//             (8-row x 16-byte core matrices), ring of 5 stages
+//   warp 1    TMEM allocation (512 columns) and the single MMA-issuing thread:
+//             every level has its own 64-column slot, all levels of a tile in
+//             one pass (7 x 64 = 448 columns); the B digits j of one A digit i
+//             are consecutive tiles in shared memory and their levels i + j
+//             consecutive slots, so up to four pairs run as one
+//             128 x 256 x 16 MMA (A read once for all of them)
+//   warps 2-17 epilogue: after each accumulation run tcgen05.ld of the level
+//             accumulators (warp w reads TMEM lane quarter w % 4, elements
+//             16 (w - 2) / 4 ..), exact integer accumulation; after the last
+//             run FP64 assembly from the bits and coalesced stores of PK
+// Every mbarrier wait is bounded; a role that gives up sets the error flag and
+// the abort word, the MMA thread and the producer wait (bounded) for their own
+// tensor-core and copy work in flight, and TMEM is freed before the CTA exits.
+#include "../../include/hp3dg.h"
 #include "hp3dg_internal.cuh"
 #include "hp3dg_kernels.h"
 #include "hp3dg_tc.cuh"
@@ -42,46 +58,39 @@ namespace hp3dg {
 
 namespace {
 constexpr int BM = 128;       // packed columns per tile (MMA M, TMEM lanes)
-constexpr int BN = 128;       // elements per tile (MMA N, TMEM columns per level)
+constexpr int BN = 64;        // elements per tile (TMEM columns per level slot)
 constexpr int BK = 16;        // q per k-block (one MMA K step), 32-byte rows
 constexpr int MAXDIG = 7;
-constexpr int MAXPASS = 4;
-constexpr int MAXPAIR = 40;
-constexpr int NSTAGE = 4;
-#ifndef KGROUP
-#define KGROUP 2  // k-blocks per accumulator run (NSTAGE / KGROUP groups in flight)
-#endif
-constexpr int TILE_BYTES = BM * BK * 2;  // 4096, A and B tiles have the same size
-constexpr int STAGE_BYTES = 2 * MAXDIG * TILE_BYTES;  // room for all digits
-constexpr int NTHREADS = 192;
+constexpr int MAXSTAGE = 8;
+constexpr int KGROUP = 2;     // k-blocks per accumulator run between slot switches
+constexpr int A_TILE = BM * BK * 2;          // 4096 bytes: one M digit tile
+constexpr int B_TILE = BN * BK * 2;          // 2048 bytes: one D digit tile
+constexpr int B_OFF = MAXDIG * A_TILE;       // B digits after the A digits in a stage
+constexpr int STAGE_BYTES = MAXDIG * (A_TILE + B_TILE);  // 43008
+constexpr int NEPI = 16;                     // epilogue warps
+constexpr int EPI_ELEMS = BN / (NEPI / 4);   // 16 elements per epilogue warp
+constexpr int NTHREADS = 64 + 32 * NEPI;     // 576
 constexpr uint32_t TMEM_COLS = 512;
 
-
-struct PassDesc {
-  int first_level;  // level of accumulator slot 0
-  int nlev;         // accumulator slots used (<= 4)
-  int nA, nB;       // digits of A (M) and B (D) needed: 1..nA, 1..nB
-  int pair0, npair; // range in the pair table
-};
 struct GemmParams {
-  int npass;
-  PassDesc pass[MAXPASS];
-  int npairs;
-  int8_t pi[MAXPAIR], pj[MAXPAIR], pslot[MAXPAIR], pfirst[MAXPAIR];
-  int radix;
-  int s1;           // two-pass recombination shift (see epi_chunk)
-  int scale_shift;  // radix*last level of pass 0 (+ s1) : final power-of-two shift
-  int digits;
-  int nk;        // k-blocks
-  int ncb, neb;  // column / element blocks
+  int radix, digits, nlev;  // levels 2 .. digits+1 in slots 0 .. nlev-1
+  int nk;                   // k-blocks
+  int kchunk;               // k-blocks per exact accumulation run
+  int ncb, neb;             // column / element blocks
   int nel, ncols;
+  int nstage;
+  int grp;                  // column blocks per raster group
+  int shift0;               // slot s: V += L << (shift0 - radix s), or >> when negative
+  int scale_shift;          // PK = V * 2^(ke + kc - scale_shift)
+  long wait_limit;          // bounded mbarrier waits (iterations)
+  int fault;                // testing: 1 = the producer withholds one stage
 };
 }  // namespace
 
-// tile t -> (column block, element block): groups of 8 column blocks sweep
-// all element blocks, so the digit tiles of a group stay resident in L2.
+// tile t -> (column block, element block): groups of `grp` column blocks sweep
+// all element blocks, so the M digit strips of a group stay resident in L2.
 __device__ __forceinline__ void tile_coords(int t, const GemmParams& P, int& cb, int& eb) {
-  const int grp = 8;
+  const int grp = P.grp;
   int g = t / (grp * P.neb);
   int r = t - g * grp * P.neb;
   int gw = P.ncb - g * grp;
@@ -90,74 +99,15 @@ __device__ __forceinline__ void tile_coords(int t, const GemmParams& P, int& cb,
   eb = r / gw;
 }
 
-// instruction descriptor: kind::f16, A = B = BF16, D = F32, K-major, M=128, N=128
-__host__ __device__ constexpr uint32_t idesc_bf16_m128_n128() {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-         ((uint32_t)(BM >> 4) << 24);
-}
-// the same with N = 256: two consecutive B digit tiles into two slots
-__host__ __device__ constexpr uint32_t idesc_bf16_m128_n256() {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(2 * BN >> 3) << 17) |
+// instruction descriptor: kind::f16, A = B = BF16, D = F32, both K-major, M = 128
+__host__ __device__ constexpr uint32_t idesc_bf16_m128(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
          ((uint32_t)(BM >> 4) << 24);
 }
 
 // exponent k of an exact power of two 2^k (the digit scales)
 __device__ __forceinline__ int pow2_exponent(double x) {
   return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1023;
-}
-// x * 2^k for normal results (k within the normal range), exact
-__device__ __forceinline__ double times_pow2(double x, int k) {
-  if (k >= -1022 && k <= 1023) return x * __longlong_as_double((long long)(k + 1023) << 52);
-  return ldexp(x, k);
-}
-
-// Epilogue of one 16-element chunk of one pass.  The level accumulators are
-// exact integers (< 2^24) in FP32; they are recombined exactly as 64-bit
-// integers.  With two passes, pass 0 stores its integer V1 in the output
-// slot and the last pass forms W = V1 * 2^S1 + V2 * 2^(S1 - radix*nlev2)
-// (|W| < 2^63) before the single conversion to FP64 and the power-of-two
-// scaling by the element and column scales.
-template <int NLEV>
-__device__ __forceinline__ void epi_chunk(const GemmParams& P, int ps, uint32_t tlane, int ch,
-                                          int e0, int c, bool cok, int kc,
-                                          const double* __restrict__ dscale,
-                                          double* __restrict__ PK, int lane) {
-  uint32_t v[NLEV][16];
-#pragma unroll
-  for (int k = 0; k < NLEV; ++k) tmem_ld16(tlane + (uint32_t)(k * BN + ch * 16), v[k]);
-  const int el = e0 + (lane & 15);
-  const int ke_lane = (el < P.nel) ? pow2_exponent(dscale[el]) : 0;
-  long long* out = (long long*)PK;
-  const bool two = P.npass == 2;
-  const bool last = ps == P.npass - 1;
-  long long prev[16];
-  if (two && last) {
-#pragma unroll
-    for (int q = 0; q < 16; ++q) {
-      const int e = e0 + q;
-      prev[q] = (cok && e < P.nel) ? out[(size_t)e * P.ncols + c] : 0;
-    }
-  }
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    long long s = 0;
-#pragma unroll
-    for (int k = 0; k < NLEV; ++k)
-      s = s * (1LL << P.radix) + (long long)__float2int_rn(__uint_as_float(v[k][q]));
-    const int e = e0 + q;
-    const int ke = __shfl_sync(0xffffffffu, ke_lane, q);
-    if (!(cok && e < P.nel)) continue;
-    const size_t idx = (size_t)e * P.ncols + c;
-    if (two && !last) {
-      out[idx] = s;  // exact partial sum V1
-    } else if (two) {
-      const int sh = P.radix * P.pass[1].nlev - P.s1;
-      long long w = prev[q] * (1LL << P.s1) + (sh >= 0 ? (s >> sh) : s * (1LL << (-sh)));
-      PK[idx] = times_pow2((double)w, ke + kc - P.scale_shift);
-    } else {
-      PK[idx] = times_pow2((double)s, ke + kc - P.scale_shift);
-    }
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -169,21 +119,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                  const double* __restrict__ mscale, double* __restrict__ PK,
                  int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smraw[];
-  // align the ring to 1024 bytes (swizzle repeat)
   uint8_t* ring = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  __shared__ __align__(8) uint64_t full_bar[NSTAGE], empty_bar[NSTAGE], acc_full, acc_empty;
+  __shared__ __align__(8) uint64_t full_bar[MAXSTAGE], empty_bar[MAXSTAGE];
+  __shared__ __align__(8) uint64_t acc_full, acc_empty, drain_bar;
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = P.ncb * P.neb;
+  const int nchunk = (P.nk + P.kchunk - 1) / P.kchunk;
+  const long lim = P.wait_limit;
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < NSTAGE; ++s) {
+    for (int s = 0; s < P.nstage; ++s) {
       mbar_init(smem_u32(&full_bar[s]), 1);
       mbar_init(smem_u32(&empty_bar[s]), 1);
     }
     mbar_init(smem_u32(&acc_full), 1);
-    mbar_init(smem_u32(&acc_empty), 128);
+    mbar_init(smem_u32(&acc_empty), NEPI);
+    mbar_init(smem_u32(&drain_bar), 1);
     abort_ = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -199,104 +152,123 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const uint32_t tbase = tmem_base;
 
   if (warp == 0) {
-    // ---------------- TMA producer ----------------
+    // ---------------- producer ----------------
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
+      uint32_t issued = 0, last_par = 0;  // per stage: a copy issued / its phase parity
+      const uint32_t bytes = (uint32_t)P.digits * (A_TILE + B_TILE);
+      bool withheld = false;
       for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
         int cb, eb;
         tile_coords(t, P, cb, eb);
-        for (int ps = 0; ps < P.npass && !abort_; ++ps) {
-          const PassDesc& pd = P.pass[ps];
-          for (int kb = 0; kb < P.nk; ++kb) {
-            if (!mbar_wait(smem_u32(&empty_bar[stage]), phase ^ 1, &abort_)) {
-              abort_ = 1; atomicExch(err, 1); break;
-            }
-            uint32_t fb = smem_u32(&full_bar[stage]);
-            mbar_expect_tx(fb, (uint32_t)(pd.nA + pd.nB) * TILE_BYTES);
+        for (int kb = 0; kb < P.nk; ++kb) {
+          if (!mbar_wait_n(smem_u32(&empty_bar[stage]), phase ^ 1, &abort_, lim)) {
+            abort_ = 1; atomicExch(err, 1); break;
+          }
+          if (P.fault == 1 && !withheld && kb == 1) {
+            // testing: this stage is never filled, so the MMA thread's bounded
+            // wait on it runs out
+            withheld = true;
+            issued &= ~(1u << stage);
+          } else {
+            const uint32_t fb = smem_u32(&full_bar[stage]);
+            mbar_expect_tx(fb, bytes);
             uint8_t* st = ring + (size_t)stage * STAGE_BYTES;
-            // digits 0..nA-1 of (column block, k-block) are contiguous, likewise for B
+            // digits 0..D-1 of (column block, k-block) are contiguous, likewise for B
             const size_t ablk = ((size_t)cb * P.nk + kb) * P.digits;
             const size_t bblk = ((size_t)eb * P.nk + kb) * P.digits;
-            bulk_load(smem_u32(st), Atiles + ablk * TILE_BYTES, (uint32_t)pd.nA * TILE_BYTES, fb);
-            bulk_load(smem_u32(st + MAXDIG * TILE_BYTES), Btiles + bblk * TILE_BYTES,
-                      (uint32_t)pd.nB * TILE_BYTES, fb);
-            if (++stage == NSTAGE) { stage = 0; phase ^= 1; }
+            bulk_load(smem_u32(st), Atiles + ablk * A_TILE, (uint32_t)P.digits * A_TILE, fb);
+            bulk_load(smem_u32(st + B_OFF), Btiles + bblk * B_TILE, (uint32_t)P.digits * B_TILE, fb);
+            issued |= 1u << stage;
+            last_par = (last_par & ~(1u << stage)) | (phase << stage);
           }
+          if (++stage == P.nstage) { stage = 0; phase ^= 1; }
         }
       }
+      // the copies this thread started have landed before the CTA exits
+      for (int s = 0; s < P.nstage; ++s)
+        if (issued >> s & 1u) mbar_drain(smem_u32(&full_bar[s]), (last_par >> s) & 1u, lim);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_m128_n128();
-      const uint32_t idesc2 = idesc_bf16_m128_n256();
       int stage = 0;
       uint32_t phase = 0, accph = 0;
+      bool any = false;
       for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
-        for (int ps = 0; ps < P.npass && !abort_; ++ps) {
-          const PassDesc& pd = P.pass[ps];
+        for (int ch = 0; ch < nchunk && !abort_; ++ch) {
+          const int kc0 = ch * P.kchunk;
+          const int kc1 = (kc0 + P.kchunk) < P.nk ? (kc0 + P.kchunk) : P.nk;
           // the epilogue must have drained the accumulators
-          if (!mbar_wait(smem_u32(&acc_empty), accph ^ 1, &abort_)) {
+          if (!mbar_wait_n(smem_u32(&acc_empty), accph ^ 1, &abort_, lim)) {
             abort_ = 1; atomicExch(err, 2); break;
           }
           accph ^= 1;
           tc_fence_after();
-          // k-blocks are consumed in groups of KGROUP stages so that each level
-          // accumulator receives a run of (pairs of the level) x KGROUP MMAs:
-          // switching the accumulator between MMAs stalls the tensor pipe.
-          for (int kb0 = 0; kb0 < P.nk && !abort_; kb0 += KGROUP) {
-            const int ng = (P.nk - kb0) < KGROUP ? (P.nk - kb0) : KGROUP;
+          for (int kb0 = kc0; kb0 < kc1 && !abort_; kb0 += KGROUP) {
+            const int ng = (kc1 - kb0) < KGROUP ? (kc1 - kb0) : KGROUP;
             uint32_t sbase[KGROUP];
-            for (int g = 0; g < ng; ++g) {
+#pragma unroll
+            for (int g = 0; g < KGROUP; ++g) {
+              sbase[g] = 0;
+              if (g >= ng || abort_) continue;
               int sg = stage + g;
               uint32_t pg = phase;
-              if (sg >= NSTAGE) { sg -= NSTAGE; pg ^= 1; }
-              if (!mbar_wait(smem_u32(&full_bar[sg]), pg, &abort_)) {
-                abort_ = 1; atomicExch(err, 3); break;
+              if (sg >= P.nstage) { sg -= P.nstage; pg ^= 1; }
+              if (!mbar_wait_n(smem_u32(&full_bar[sg]), pg, &abort_, lim)) {
+                abort_ = 1; atomicExch(err, 3); continue;
               }
               sbase[g] = smem_u32(ring + (size_t)sg * STAGE_BYTES);
             }
             if (abort_) break;
             tc_fence_after();
-            // the pass's pairs by A digit i: its B digits j = jlo..jhi are
-            // consecutive 128-row tiles of the stage and their levels i + j
-            // consecutive 128-column accumulator slots, so two of them make
-            // one N = 256 MMA (A read once from shared memory for both).
-            // Digit i = 1 is the first to write every slot of a pass.
-            for (int i = 1; i <= pd.nA; ++i) {
-              const int jlo = pd.first_level - i > 1 ? pd.first_level - i : 1;
-              const int jtop = pd.first_level + pd.nlev - 1 - i;
-              const int jhi = jtop < P.digits ? jtop : P.digits;
-              const uint32_t aoff = (uint32_t)(i - 1) * TILE_BYTES;
-              for (int j = jlo; j <= jhi; j += 2) {
-                const bool two = j + 1 <= jhi;
-                const uint32_t boff = (uint32_t)(MAXDIG + j - 1) * TILE_BYTES;
-                const uint32_t dt = tbase + (uint32_t)(i + j - pd.first_level) * BN;
-                for (int g = 0; g < ng; ++g) {
-                  const uint32_t acc = (kb0 + g > 0 || i > 1) ? 1u : 0u;
+            // A digit i pairs with B digits j = 1 .. min(D, S - i) (levels
+            // i + j <= S = D + 1); their slots i + j - 2 are consecutive, so
+            // up to four B tiles make one MMA of N = 64 * count.  Digit i = 1
+            // covers every slot and starts each accumulation run.
+            for (int i = 1; i <= P.digits; ++i) {
+              const int jhi = (P.digits + 1 - i) < P.digits ? (P.digits + 1 - i) : P.digits;
+              const uint32_t aoff = (uint32_t)(i - 1) * A_TILE;
+              for (int j0 = 1; j0 <= jhi; j0 += 4) {
+                const int nd = (jhi - j0 + 1) < 4 ? (jhi - j0 + 1) : 4;
+                const uint32_t idesc = idesc_bf16_m128(BN * nd);
+                const uint32_t boff = (uint32_t)(B_OFF + (j0 - 1) * B_TILE);
+                const uint32_t dt = tbase + (uint32_t)(i + j0 - 2) * BN;
+#pragma unroll
+                for (int g = 0; g < KGROUP; ++g) {
+                  if (g >= ng) continue;
+                  const uint32_t acc = (kb0 + g > kc0 || i > 1) ? 1u : 0u;
                   umma_bf16(dt, sdesc_kmajor(sbase[g] + aoff), sdesc_kmajor(sbase[g] + boff),
-                            two ? idesc2 : idesc, acc);
+                            idesc, acc);
                 }
               }
             }
+            any = true;
             for (int g = 0; g < ng; ++g) {
               int sg = stage + g;
-              if (sg >= NSTAGE) sg -= NSTAGE;
+              if (sg >= P.nstage) sg -= P.nstage;
               umma_commit(smem_u32(&empty_bar[sg]));  // frees the stage when done
             }
             stage += ng;
-            if (stage >= NSTAGE) { stage -= NSTAGE; phase ^= 1; }
+            if (stage >= P.nstage) { stage -= P.nstage; phase ^= 1; }
           }
-          umma_commit(smem_u32(&acc_full));  // accumulators complete
+          if (abort_) break;
+          umma_commit(smem_u32(&acc_full));  // this run's level sums are complete
         }
+      }
+      // every MMA this thread issued has completed before TMEM is freed
+      if (any) {
+        umma_commit(smem_u32(&drain_bar));
+        mbar_drain(smem_u32(&drain_bar), 0, lim);
       }
     }
   } else {
-    // ---------------- epilogue (warps 2..5, one TMEM lane quarter each) ----------------
-    const int quarter = warp & 3;
-    const int row = quarter * 32 + lane;  // TMEM lane = packed column within the tile
-    const uint32_t tlane = tbase + ((uint32_t)(quarter * 32) << 16);
+    // ---------------- epilogue (warps 2..17) ----------------
+    const int quarter = warp & 3;              // TMEM lanes this warp may read
+    const int eg = (warp - 2) >> 2;            // its 16 elements of the tile
+    const int row = quarter * 32 + lane;       // TMEM lane = packed column in the tile
+    const uint32_t tlane = tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(eg * EPI_ELEMS);
     uint32_t accph = 0;
     for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
       int cb, eb;
@@ -304,27 +276,47 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int c = cb * BM + row;
       const bool cok = c < P.ncols;
       const int kc = cok ? pow2_exponent(mscale[c]) : 0;
-      for (int ps = 0; ps < P.npass; ++ps) {
-        const PassDesc& pd = P.pass[ps];
-        if (!mbar_wait(smem_u32(&acc_full), accph, &abort_)) {
-          abort_ = 1; atomicExch(err, 4); break;
+      const int e0 = eb * BN + eg * EPI_ELEMS;
+      const int el = e0 + (lane & 15);
+      const int ke_lane = (el < P.nel) ? pow2_exponent(dscale[el]) : 0;
+      long long V[EPI_ELEMS];
+#pragma unroll
+      for (int q = 0; q < EPI_ELEMS; ++q) V[q] = 0;
+      bool ok = true;
+      for (int ch = 0; ch < nchunk; ++ch) {
+        if (!mbar_wait_n(smem_u32(&acc_full), accph, &abort_, lim)) {
+          abort_ = 1; atomicExch(err, 4); ok = false; break;
         }
         accph ^= 1;
         tc_fence_after();
-        for (int ch = 0; ch < BN / 16; ++ch) {
-          const int e0 = eb * BN + ch * 16;
-          switch (pd.nlev) {
-            case 1: epi_chunk<1>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
-            case 2: epi_chunk<2>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
-            case 3: epi_chunk<3>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
-            default: epi_chunk<4>(P, ps, tlane, ch, e0, c, cok, kc, dscale, PK, lane); break;
+        for (int s = 0; s < P.nlev; ++s) {
+          uint32_t v[EPI_ELEMS];
+          tmem_ld16(tlane + (uint32_t)(s * BN), v);
+          const int sh = P.shift0 - P.radix * s;
+          if (sh >= 0) {
+#pragma unroll
+            for (int q = 0; q < EPI_ELEMS; ++q)
+              V[q] += (long long)__float2int_rn(__uint_as_float(v[q])) << sh;
+          } else {
+#pragma unroll
+            for (int q = 0; q < EPI_ELEMS; ++q)
+              V[q] += (long long)__float2int_rn(__uint_as_float(v[q])) >> (-sh);
           }
         }
         tc_fence_before();
-        mbar_arrive(smem_u32(&acc_empty));
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_u32(&acc_empty));
+      }
+      if (!ok) break;
+#pragma unroll
+      for (int q = 0; q < EPI_ELEMS; ++q) {
+        const int ke = __shfl_sync(0xffffffffu, ke_lane, q);
+        const int e = e0 + q;
+        if (cok && e < P.nel) PK[(size_t)e * P.ncols + c] = scaled_i64(V[q], ke + kc - P.scale_shift);
       }
     }
   }
+  tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
@@ -336,12 +328,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 // ---------------------------------------------------------------------------
 // digit builders
 // ---------------------------------------------------------------------------
-// Digit tiles in HBM: tile (block, k-block, digit) = 128 rows x 16 q in the
-// UMMA canonical K-major layout; byte offset of (row r, q-in-block k):
+// Digit tiles in HBM: tile (block, k-block, digit) = rows x 16 q in the UMMA
+// canonical K-major layout (M: 128 packed columns per block, 4 KB tiles; D:
+// 64 elements per block, 2 KB tiles); byte offset of (row r, q-in-block k):
 //   (r/8)*256 + (k/8)*128 + (r%8)*16 + (k%8)*2
-// Tiles of one (block, k-block) are consecutive over the digits.
-__host__ __device__ __forceinline__ size_t tile_base(int blk, int kb, int dig, int nk, int ndig) {
-  return (((size_t)blk * nk + kb) * ndig + dig) * (size_t)TILE_BYTES;
+// Tiles of one (block, k-block) are consecutive over the digits, so the 64-row
+// D tiles of consecutive digits form one canonical operand of 64 * count rows.
+__host__ __device__ __forceinline__ size_t tile_base(int blk, int kb, int dig, int nk, int ndig,
+                                                     int tile_bytes) {
+  return (((size_t)blk * nk + kb) * ndig + dig) * (size_t)tile_bytes;
 }
 
 __device__ __forceinline__ double pow2_ceil_scale(double mx) {
@@ -421,7 +416,7 @@ __global__ void k_d_scale(int K, int nel, const double* __restrict__ D, double* 
 // digits of 8 consecutive values -> one 16-byte core-matrix row per digit
 __device__ __forceinline__ void write_digits8(const double* vals, double rs, int radix, int digits,
                                               uint8_t* __restrict__ base, int nk, int blk, int kb,
-                                              int r, int kg) {
+                                              int r, int kg, int tile_bytes) {
   double up = ldexp(1.0, radix);
   double rr[8];
 #pragma unroll
@@ -440,7 +435,7 @@ __device__ __forceinline__ void write_digits8(const double* vals, double rs, int
     w.y = bf16pair(d[2], d[3]);
     w.z = bf16pair(d[4], d[5]);
     w.w = bf16pair(d[6], d[7]);
-    *(uint4*)(base + tile_base(blk, kb, s, nk, digits) + off) = w;
+    *(uint4*)(base + tile_base(blk, kb, s, nk, digits, tile_bytes) + off) = w;
   }
 }
 
@@ -461,7 +456,7 @@ __global__ void k_build_m(int nint, int n, int ni, int nb, int ncols, int nk, in
     vals[t] = (c < ncols && q < K) ? m_entry(grad, n, q / 6, q % 6, a, b) : 0.0;
   }
   double rs = (c < ncols) ? 1.0 / mscale[c] : 0.0;
-  write_digits8(vals, rs, radix, digits, mdig, nk, cb, kb, r, kg);
+  write_digits8(vals, rs, radix, digits, mdig, nk, cb, kb, r, kg, A_TILE);
 }
 
 // dense M (K x ncols, row-major): column scales and digit tiles
@@ -488,16 +483,16 @@ __global__ void k_build_m_dense(int K, int ncols, int nk, int radix, int digits,
     vals[t] = (c < ncols && q < K) ? Md[(size_t)q * ncols + c] : 0.0;
   }
   const double rs = (c < ncols) ? 1.0 / mscale[c] : 0.0;
-  write_digits8(vals, rs, radix, digits, mdig, nk, cb, kb, r, kg);
+  write_digits8(vals, rs, radix, digits, mdig, nk, cb, kb, r, kg, A_TILE);
 }
 
-// D digit tiles: grid (k-blocks, element blocks), 256 threads
+// D digit tiles: grid (k-blocks, 64-element blocks), 128 threads = 64 rows x 2 q-groups
 __global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
                           const double* __restrict__ D, const double* __restrict__ dscale,
                           uint8_t* __restrict__ ddig) {
   const int kb = blockIdx.x, eb = blockIdx.y;
   const int r = threadIdx.x >> 1, kg = threadIdx.x & 1;
-  const int e = eb * 128 + r;
+  const int e = eb * BN + r;
   double vals[8];
 #pragma unroll
   for (int t = 0; t < 8; ++t) {
@@ -505,7 +500,7 @@ __global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
     vals[t] = (e < nel && q < K) ? D[(size_t)e * K + q] : 0.0;
   }
   double rs = (e < nel) ? 1.0 / dscale[e] : 0.0;
-  write_digits8(vals, rs, radix, digits, ddig, nk, eb, kb, r, kg);
+  write_digits8(vals, rs, radix, digits, ddig, nk, eb, kb, r, kg, B_TILE);
 }
 
 // ---------------------------------------------------------------------------
@@ -561,8 +556,8 @@ int launch_ozaki_slice_d(const OzakiPlan& p, int nel, int nint, const double* d_
   if (nel_pad == 0) return 0;
   k_d_scale<<<nel_pad, 256, 0, st>>>(6 * nint, nel, d_D, d_dscale);
   dim3 g(p.kdim / BK, nel_pad / BN);
-  k_slice_d<<<g, 256, 0, st>>>(6 * nint, p.kdim / BK, nel, p.radix, p.digits, d_D, d_dscale,
-                               (uint8_t*)d_ddig);
+  k_slice_d<<<g, 2 * BN, 0, st>>>(6 * nint, p.kdim / BK, nel, p.radix, p.digits, d_D, d_dscale,
+                                  (uint8_t*)d_ddig);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -581,108 +576,158 @@ int launch_ozaki_slice_d_dense(const OzakiPlan& p, int nrows, const double* d_D,
   if (nel_pad == 0) return 0;
   k_d_scale<<<nel_pad, 256, 0, st>>>(p.kreal, nrows, d_D, d_dscale);
   dim3 g(p.kdim / BK, nel_pad / BN);
-  k_slice_d<<<g, 256, 0, st>>>(p.kreal, p.kdim / BK, nrows, p.radix, p.digits, d_D, d_dscale,
-                               (uint8_t*)d_ddig);
+  k_slice_d<<<g, 2 * BN, 0, st>>>(p.kreal, p.kdim / BK, nrows, p.radix, p.digits, d_D, d_dscale,
+                                  (uint8_t*)d_ddig);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-// pass / pair table: levels 2..digits+1 in passes of <= 4 accumulators
+// Exactness and recombination parameters of a plan (see the file header).
 static void build_params(const OzakiPlan& p, GemmParams* G) {
   memset(G, 0, sizeof(*G));
-  G->radix = p.radix;
-  int lev_lo = 2, lev_hi = p.digits + 1;
-  int np = 0, npair = 0;
-  for (int L0 = lev_lo; L0 <= lev_hi; L0 += 4) {
-    PassDesc& pd = G->pass[np++];
-    pd.first_level = L0;
-    pd.nlev = (lev_hi - L0 + 1) < 4 ? (lev_hi - L0 + 1) : 4;
-    pd.pair0 = npair;
-    pd.nA = pd.nB = 0;
-    for (int s = L0; s < L0 + pd.nlev; ++s) {
-      bool first = true;
-      for (int i = 1; i <= p.digits; ++i) {
-        int j = s - i;
-        if (j < 1 || j > p.digits) continue;
-        G->pi[npair] = (int8_t)i;
-        G->pj[npair] = (int8_t)j;
-        G->pslot[npair] = (int8_t)(s - L0);
-        G->pfirst[npair] = first ? 1 : 0;
-        first = false;
-        pd.nA = pd.nA > i ? pd.nA : i;
-        pd.nB = pd.nB > j ? pd.nB : j;
-        ++npair;
-      }
+  const int R = p.radix, D = p.digits, S = D + 1;
+  G->radix = R;
+  G->digits = D;
+  G->nlev = D;
+  // largest level bound per q: sum over i + j = s of b_i b_j
+  double worst = 0.0;
+  for (int s = 2; s <= S; ++s) {
+    double b = 0.0;
+    for (int i = 1; i <= D; ++i) {
+      const int j = s - i;
+      if (j < 1 || j > D) continue;
+      b += ldexp(1.0, i == 1 ? R : R - 1) * ldexp(1.0, j == 1 ? R : R - 1);
     }
-    pd.npair = npair - pd.pair0;
+    worst = b > worst ? b : worst;
   }
-  G->npass = np;
-  G->npairs = npair;
-  const PassDesc& p0 = G->pass[0];
-  int last0 = p0.first_level + p0.nlev - 1;
-  if (np == 2) {
-    G->s1 = 62 - (24 + p.radix * (p0.nlev - 1));
-    G->scale_shift = p.radix * last0 + G->s1;
-  } else {
-    G->s1 = 0;
-    G->scale_shift = p.radix * last0;
-  }
+  int kchunk = (int)floor(ldexp(1.0, 24) / (BK * worst));
+  kchunk = kchunk / KGROUP * KGROUP;
+  G->kchunk = kchunk < KGROUP ? KGROUP : kchunk;
+  // (a kchunk of KGROUP always satisfies the bound for R <= 8: 2 * 16 * 147456 < 2^24)
+  const int nk = p.kdim / BK;
+  const int nchunk = (nk + G->kchunk - 1) / G->kchunk;
+  // V = sum over runs and levels of L_s 2^(R(S-s) - t) stays below 2^62
+  const double vmax = log2((double)nchunk) + 24.0 + R * (D - 1) - log2(1.0 - ldexp(1.0, -R));
+  int t = (int)ceil(vmax - 62.0);
+  if (t < 0) t = 0;
+  G->shift0 = R * (S - 2) - t;
+  G->scale_shift = R * S - t;
 }
 
 int ozaki_pairs(const OzakiPlan& p) {
+  int n = 0;
+  for (int i = 1; i <= p.digits; ++i)
+    for (int j = 1; j <= p.digits; ++j) n += (i + j <= p.digits + 1) ? 1 : 0;
+  return n;
+}
+
+int ozaki_kchunk(const OzakiPlan& p) {
   GemmParams G;
   build_params(p, &G);
-  return G.npairs;
+  return G.kchunk;
 }
 
 static int ozaki_gemm_cols(const OzakiPlan& p, int nel, int ncols_real, const uint16_t* d_ddig,
                            const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                           double* d_PK, int* d_flag, cudaStream_t st);
+                           double* d_PK, int* d_flag, cudaStream_t st, int fault);
 
 int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                      double* d_PK, int* d_flag, cudaStream_t st) {
+                      double* d_PK, int* d_flag, cudaStream_t st, int fault) {
   return ozaki_gemm_cols(p, nel, n * (n + 1) / 2, d_ddig, d_dscale, d_mdig, d_mscale, d_PK, d_flag,
-                         st);
+                         st, fault);
 }
 
 int launch_ozaki_gemm_dense(const OzakiPlan& p, int nrows, const uint16_t* d_ddig,
                             const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
                             double* d_out, int* d_flag, cudaStream_t st) {
-  return ozaki_gemm_cols(p, nrows, p.nreal, d_ddig, d_dscale, d_mdig, d_mscale, d_out, d_flag, st);
+  return ozaki_gemm_cols(p, nrows, p.nreal, d_ddig, d_dscale, d_mdig, d_mscale, d_out, d_flag, st,
+                         0);
 }
 
 static int ozaki_gemm_cols(const OzakiPlan& p, int nel, int ncols_real, const uint16_t* d_ddig,
                            const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                           double* d_PK, int* d_flag, cudaStream_t st) {
+                           double* d_PK, int* d_flag, cudaStream_t st, int fault) {
   if (nel <= 0) return 0;
-  static int num_sms = 0;
-  if (!num_sms) {
-    int dev;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
-  }
+  int dev = 0, num_sms = 0, optin = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+    return -1;
   GemmParams G;
   build_params(p, &G);
-  int nel_pad = round_up(nel, BN);
+  const int nel_pad = round_up(nel, BN);
   G.nk = p.kdim / BK;
-  G.digits = p.digits;
   G.ncb = p.ncols / BM;
   G.neb = nel_pad / BN;
   G.nel = nel;
   G.ncols = ncols_real;
-  size_t smem = (size_t)NSTAGE * STAGE_BYTES + 1024;
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(k_ozaki_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess)
-      return -1;
-    attr = true;
-  }
-  int ntiles = G.ncb * G.neb;
-  int grid = ntiles < num_sms ? ntiles : num_sms;
+  // raster groups whose M digit strips take about 48 MB of L2
+  const double strip = (double)G.nk * p.digits * A_TILE;
+  int grp = (int)(48.0 * 1024 * 1024 / strip);
+  G.grp = grp < 1 ? 1 : (grp > G.ncb ? G.ncb : grp);
+  // as many ring stages as fit next to the static shared memory (barriers)
+  int nst = (optin - 1024 - 1024) / STAGE_BYTES;
+  G.nstage = nst > MAXSTAGE ? MAXSTAGE : nst;
+  if (G.nstage < KGROUP + 1) return -1;
+  G.fault = fault;
+  // bounded waits: about a second or more at the normal limit; a fault test
+  // runs out quickly
+  G.wait_limit = fault ? (1L << 14) : TC_WAIT_LIMIT;
+  const size_t smem = (size_t)G.nstage * STAGE_BYTES + 1024;
+  if (raise_smem_limit((const void*)k_ozaki_gemm, smem) != cudaSuccess) return -1;
+  const int ntiles = G.ncb * G.neb;
+  const int grid = ntiles < num_sms ? ntiles : num_sms;
   k_ozaki_gemm<<<grid, NTHREADS, smem, st>>>((const uint8_t*)d_mdig, (const uint8_t*)d_ddig, G,
                                               d_dscale, d_mscale, d_PK, d_flag);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 }  // namespace hp3dg
+
+// ---------------------------------------------------------------------------
+// C ABI: the contraction on caller-supplied operands
+// ---------------------------------------------------------------------------
+extern "C" int hp3dg_mixed_contract(int32_t nrows, int32_t K, int32_t ncols, const double* D,
+                                    const double* M, double* out, int32_t radix, int32_t digits,
+                                    void* stream) {
+  using namespace hp3dg;
+  if (nrows < 0 || K <= 0 || ncols <= 0 || (nrows > 0 && (!D || !M || !out)))
+    return HP3DG_ERR_ARG;
+  if (nrows == 0) return HP3DG_OK;
+  OzakiPlan p;
+  if (ozaki_plan_dense(K, ncols, radix > 0 ? radix : 7, digits > 0 ? digits : 7, &p))
+    return HP3DG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  uint8_t *mdig = nullptr, *ddig = nullptr;
+  double *mscale = nullptr, *dscale = nullptr;
+  int* flag = nullptr;
+  int rc = HP3DG_OK;
+  if (cudaMalloc(&mdig, ozaki_m_bytes(p)) != cudaSuccess ||
+      cudaMalloc(&ddig, ozaki_d_bytes(p, nrows)) != cudaSuccess ||
+      cudaMalloc(&mscale, (size_t)p.ncols * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&dscale, (size_t)(nrows + 128) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&flag, sizeof(int)) != cudaSuccess) {
+    rc = HP3DG_ERR_ALLOC;
+  } else if (cudaMemsetAsync(flag, 0x7f, sizeof(int), st) != cudaSuccess ||
+             launch_ozaki_build_m_dense(p, M, (uint16_t*)mdig, mscale, st) ||
+             launch_ozaki_slice_d_dense(p, nrows, D, (uint16_t*)ddig, dscale, st) ||
+             launch_ozaki_gemm_dense(p, nrows, (const uint16_t*)ddig, dscale,
+                                     (const uint16_t*)mdig, mscale, out, flag, st)) {
+    rc = HP3DG_ERR_CUDA;
+  } else {
+    int h = 0;
+    if (cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = HP3DG_ERR_CUDA;
+    else if (h != 0x7f7f7f7f)
+      rc = HP3DG_ERR_TIMEOUT;
+  }
+  if (rc != HP3DG_OK) cudaStreamSynchronize(st);
+  cudaFree(mdig);
+  cudaFree(ddig);
+  cudaFree(mscale);
+  cudaFree(dscale);
+  cudaFree(flag);
+  return rc;
+}
+

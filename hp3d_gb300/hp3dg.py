@@ -37,7 +37,7 @@ class Opts(ctypes.Structure):
                 ("ozaki_radix", ctypes.c_int32), ("ozaki_digits", ctypes.c_int32),
                 ("stc_method", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
                 ("schur_fp64", ctypes.c_int32), ("download_chunks", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("fault_inject", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 DESC_DTYPE = np.dtype([("etype", np.int32), ("mdle", np.int32), ("norder", np.int32, 19),
@@ -56,7 +56,7 @@ EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit",
            "hp3dg_batch_run",
            "hp3dg_batch_sync", "hp3dg_batch_download", "hp3dg_get_elem", "hp3dg_get_condensed",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
-           "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_output_sizes", "hp3dg_device_outputs",
+           "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_mixed_contract", "hp3dg_output_sizes", "hp3dg_device_outputs",
            "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_pass_stats", "hp3dg_last_bad_element",
            "hp3dg_dpg_begin", "hp3dg_dpg_submit", "hp3dg_dpg_run", "hp3dg_dpg_sync",
            "hp3dg_dpg_download", "hp3dg_dpg_sizes", "hp3dg_dpg_get_elem",
@@ -99,6 +99,8 @@ def lib():
         L.hp3dg_last_bad_element.restype = ctypes.c_int32
         L.hp3dg_batch_end.argtypes = [_vp]
         L.hp3dg_batch_end.restype = None
+        L.hp3dg_mixed_contract.argtypes = [ctypes.c_int32] * 3 + [_vp] * 3 + \
+            [ctypes.c_int32] * 2 + [_vp]
         L.hp3dg_strerror.argtypes = [ctypes.c_int]
         L.hp3dg_strerror.restype = ctypes.c_char_p
         L.hp3dg_dpg_begin.argtypes = [ctypes.POINTER(DpgOpts), ctypes.POINTER(_vp)]
@@ -178,7 +180,7 @@ class ElementPass:
 
     def __init__(self, precision=FP64, integration=0, isol=10, keep_elem=False, timing=False,
                  device=0, ozaki_radix=0, ozaki_digits=0, graph=True, schur_tc=True,
-                 download_chunks=0):
+                 download_chunks=0, fault_inject=0):
         self.L = lib()
         o = Opts()
         o.precision = precision
@@ -192,6 +194,7 @@ class ElementPass:
         o.launch_mode = 0 if graph else 1
         o.schur_fp64 = 0 if schur_tc else 1
         o.download_chunks = download_chunks
+        o.fault_inject = fault_inject
         self.ctx = _vp()
         self._check(self.L.hp3dg_batch_begin(ctypes.byref(o), ctypes.byref(self.ctx)), "begin")
         self.nel = 0

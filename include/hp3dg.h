@@ -87,7 +87,14 @@ typedef struct hp3dg_opts {
                           hp3dg_batch_download copies each chunk's outputs
                           as soon as it is done, overlapping the copies with
                           the rest of the pass (same results) */
-  int32_t reserved[4];
+  int32_t fault_inject;  /* testing only, 0 otherwise.  1: the mixed
+                          contraction's loader withholds one stage, so the
+                          kernel's bounded waits run out (with a short limit)
+                          and hp3dg_batch_sync returns HP3DG_ERR_TIMEOUT; the
+                          context stays usable.  2: every device allocation
+                          of a submit that allocates fails, which returns
+                          HP3DG_ERR_ALLOC; the context can be ended. */
+  int32_t reserved[3];
 } hp3dg_opts;
 
 /* Element descriptor: what find_order (datstrs/find_order.F90:5),
@@ -297,17 +304,39 @@ int hp3dg_pass_stats(const hp3dg_ctx *ctx, int64_t *kernels, double *contraction
  *   aschur n_elem x (nb x ni) column-major inv(Abb) Abi
  *   bschur n_elem x nb inv(Abb) Bb
  * Scratch: the packed Schur triangles, n_elem * ni*(ni+1)/2 doubles, live in
- * a fixed device array of HP3DG_NOALLOC_SCRATCH_DOUBLES - 1 usable doubles;
- * larger batches are rejected with HP3DG_ERR_ARG (split them).  Calls share
- * that array: calls whose kernels overlap on the GPU race and must be
- * ordered by the caller.  The first call on a device looks up the array's
- * device address; make it before any stream capture begins.  The call waits
- * for its kernel on `stream` (NULL = legacy default stream) and returns
- * HP3DG_ERR_NOT_SPD with *bad_element set when a bubble block is not
- * positive definite. */
+ * a fixed device array of HP3DG_NOALLOC_SCRATCH_DOUBLES - 1 usable doubles
+ * (90 elements of a p = 5 hexahedron, ni = 152); larger batches are rejected
+ * with HP3DG_ERR_ARG (split them).  One element's bubble block, [K_bi | b_b]
+ * and condensed load, (nb^2 + nb(ni+1) + ni) doubles, must fit in the
+ * device's opt-in shared memory per block: hexahedra up to p = 5 do, p = 6
+ * (345 KB) returns HP3DG_ERR_UNSUPPORTED.  Calls share the scratch array:
+ * calls whose kernels overlap on the GPU race and must be ordered by the
+ * caller.  The first call on a device looks up the array's device address;
+ * make it before any stream capture begins.  The call waits for its kernel
+ * on `stream` (NULL = legacy default stream).  *bad_element is set to -1, or
+ * on HP3DG_ERR_NOT_SPD to the first element whose bubble block is not
+ * positive definite.  n_elem = 0 returns HP3DG_OK. */
 int hp3dg_condense_noalloc(int32_t n_elem, int32_t n, int32_t nb, const double *K,
                            const double *b, double *aii, double *bi, double *aschur,
                            double *bschur, int32_t *bad_element, void *stream);
+
+/* The contraction kernel of HP3DG_MIXED on caller-supplied FP64 operands:
+ * out[r, c] = sum_q D[r, q] M[q, c] for D nrows x K, M K x ncols and out
+ * nrows x ncols, all row-major device pointers.  Both operands are split
+ * into balanced BF16 digits of `radix` bits (0 = 7), `digits` per operand
+ * (0 = 7), with power-of-two row / column scales; the digit products of
+ * each level are summed on tcgen05 tensor cores in FP32 accumulators that
+ * are restarted before any partial sum can exceed 2^24, so every level sum
+ * is exact, and the levels are recombined exactly as 64-bit integers before
+ * one rounding to FP64.  Allocates its digit buffers, runs on `stream`
+ * (NULL = legacy default stream) and waits for it.  No counterpart in the
+ * reference: the element pass applies this kernel with K = 6 nint and M the
+ * bin's shape-function products (elem_opt.F90:86-137); this entry point
+ * takes operands of any content, so the exactness bound can be checked on
+ * worst-case data. */
+int hp3dg_mixed_contract(int32_t nrows, int32_t K, int32_t ncols, const double *D,
+                         const double *M, double *out, int32_t radix, int32_t digits,
+                         void *stream);
 
 /* Dirichlet data of the submitted batch by projection-based interpolation
  * (update_Ddof, hpinterp/update_Ddof.F90 with dhpvert, dhpedgeH, dhpfaceH)
