@@ -54,6 +54,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <vector>
+
 namespace hp3dg {
 
 namespace {
@@ -71,6 +73,7 @@ constexpr int NEPI = 16;                     // epilogue warps
 constexpr int EPI_ELEMS = BN / (NEPI / 4);   // 16 elements per epilogue warp
 constexpr int NTHREADS = 64 + 32 * NEPI;     // 576
 constexpr uint32_t TMEM_COLS = 512;
+constexpr int MAXMMA = 16;
 
 struct GemmParams {
   int radix, digits, nlev;  // levels 2 .. digits+1 in slots 0 .. nlev-1
@@ -84,6 +87,8 @@ struct GemmParams {
   int scale_shift;          // PK = V * 2^(ke + kc - scale_shift)
   long wait_limit;          // bounded mbarrier waits (iterations)
   int fault;                // testing: 1 = the producer withholds one stage
+  int nmma;                 // MMAs per k-block, in issue order:
+  uint32_t mma[MAXMMA];     // A digit i | first B digit j0 << 4 | B digit count << 8
 };
 }  // namespace
 
@@ -225,23 +230,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             tc_fence_after();
             // A digit i pairs with B digits j = 1 .. min(D, S - i) (levels
             // i + j <= S = D + 1); their slots i + j - 2 are consecutive, so
-            // up to four B tiles make one MMA of N = 64 * count.  Digit i = 1
-            // covers every slot and starts each accumulation run.
-            for (int i = 1; i <= P.digits; ++i) {
-              const int jhi = (P.digits + 1 - i) < P.digits ? (P.digits + 1 - i) : P.digits;
-              const uint32_t aoff = (uint32_t)(i - 1) * A_TILE;
-              for (int j0 = 1; j0 <= jhi; j0 += 4) {
-                const int nd = (jhi - j0 + 1) < 4 ? (jhi - j0 + 1) : 4;
-                const uint32_t idesc = idesc_bf16_m128(BN * nd);
-                const uint32_t boff = (uint32_t)(B_OFF + (j0 - 1) * B_TILE);
-                const uint32_t dt = tbase + (uint32_t)(i + j0 - 2) * BN;
+            // up to four B tiles make one MMA of N = 64 * count.  The MMAs
+            // come in the host's order (no MMA follows one whose accumulator
+            // range overlaps its own without being equal); the two of digit
+            // i = 1 come first, cover every slot and start each run.
 #pragma unroll
-                for (int g = 0; g < KGROUP; ++g) {
-                  if (g >= ng) continue;
-                  const uint32_t acc = (kb0 + g > kc0 || i > 1) ? 1u : 0u;
-                  umma_bf16(dt, sdesc_kmajor(sbase[g] + aoff), sdesc_kmajor(sbase[g] + boff),
-                            idesc, acc);
-                }
+            for (int ci = 0; ci < MAXMMA; ++ci) {
+              if (ci >= P.nmma) break;
+              const uint32_t m = P.mma[ci];
+              const int i = (int)(m & 15u), j0 = (int)((m >> 4) & 15u), nd = (int)(m >> 8);
+              const uint32_t aoff = (uint32_t)(i - 1) * A_TILE;
+              const uint32_t idesc = idesc_bf16_m128(BN * nd);
+              const uint32_t boff = (uint32_t)(B_OFF + (j0 - 1) * B_TILE);
+              const uint32_t dt = tbase + (uint32_t)(i + j0 - 2) * BN;
+#pragma unroll
+              for (int g = 0; g < KGROUP; ++g) {
+                if (g >= ng) continue;
+                const uint32_t acc = (kb0 + g > kc0 || i > 1) ? 1u : 0u;
+                umma_bf16(dt, sdesc_kmajor(sbase[g] + aoff), sdesc_kmajor(sbase[g] + boff),
+                          idesc, acc);
               }
             }
             any = true;
@@ -581,6 +588,70 @@ int launch_ozaki_slice_d_dense(const OzakiPlan& p, int nrows, const double* d_D,
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
+// MMA order of a k-block.  Slots of A digit i: [i-1, D-1], split at slot
+// h = min(D, 4) into a low MMA [i-1, h-1] and a high MMA [max(i-1, h), D-1]
+// (at most four B tiles each).  An MMA that accumulates into a range that
+// overlaps the previous MMA's without being equal waits for it to finish, so
+// the order is searched (depth first, a few thousand nodes at 7 digits) for
+// the fewest such neighbours, the last MMA counted against the first of the
+// next k-block.  The i = 1 MMAs come first: they restart every slot.
+namespace {
+struct MmaChunk { int i, lo, hi; };
+struct OrderSearch {
+  std::vector<MmaChunk> c;
+  std::vector<int> best, cur;
+  std::vector<char> used;
+  int best_cost = 1 << 30;
+  long nodes = 0;
+  static int hazard(const MmaChunk& a, const MmaChunk& b) {
+    const bool same = a.lo == b.lo && a.hi == b.hi;
+    const bool disjoint = a.hi < b.lo || b.hi < a.lo;
+    return (same || disjoint) ? 0 : 1;
+  }
+  void dfs(int cost) {
+    if (cost >= best_cost || ++nodes > 200000) return;
+    if (cur.size() == c.size()) {
+      const int total = cost + hazard(c[cur.back()], c[cur.front()]);
+      if (total < best_cost) { best_cost = total; best = cur; }
+      return;
+    }
+    for (size_t k = 0; k < c.size(); ++k) {
+      if (used[k]) continue;
+      used[k] = 1;
+      const int add = cur.empty() ? 0 : hazard(c[cur.back()], c[k]);
+      cur.push_back((int)k);
+      dfs(cost + add);
+      cur.pop_back();
+      used[k] = 0;
+    }
+  }
+};
+}  // namespace
+
+static void build_mma_order(int D, GemmParams* G) {
+  const int h = D < 4 ? D : 4;
+  OrderSearch S;
+  std::vector<MmaChunk> first;
+  for (int i = 1; i <= D; ++i) {
+    if (i - 1 < h) (i == 1 ? first : S.c).push_back({i, i - 1, h - 1});
+    if (D > h) (i == 1 ? first : S.c).push_back({i, i - 1 > h ? i - 1 : h, D - 1});
+  }
+  // the i = 1 MMAs are disjoint; they open the order, the rest is searched
+  S.c.insert(S.c.begin(), first.begin(), first.end());
+  S.used.assign(S.c.size(), 0);
+  for (size_t k = 0; k < first.size(); ++k) {
+    S.used[k] = 1;
+    S.cur.push_back((int)k);
+  }
+  S.dfs(0);
+  G->nmma = (int)S.best.size();
+  for (int k = 0; k < G->nmma; ++k) {
+    const MmaChunk& m = S.c[S.best[k]];
+    const int j0 = m.lo - m.i + 2, nd = m.hi - m.lo + 1;
+    G->mma[k] = (uint32_t)m.i | ((uint32_t)j0 << 4) | ((uint32_t)nd << 8);
+  }
+}
+
 // Exactness and recombination parameters of a plan (see the file header).
 static void build_params(const OzakiPlan& p, GemmParams* G) {
   memset(G, 0, sizeof(*G));
@@ -611,6 +682,7 @@ static void build_params(const OzakiPlan& p, GemmParams* G) {
   if (t < 0) t = 0;
   G->shift0 = R * (S - 2) - t;
   G->scale_shift = R * S - t;
+  build_mma_order(D, G);
 }
 
 int ozaki_pairs(const OzakiPlan& p) {
