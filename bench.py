@@ -30,7 +30,11 @@ import sys
 import threading
 import time
 
-import numpy as np
+# the CPU legs run the oracle on OpenMP threads, each calling a single-threaded
+# BLAS; set before numpy / scipy load their BLAS
+os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+
+import numpy as np  # noqa: E402
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
@@ -38,15 +42,23 @@ sys.path.insert(0, ROOT)
 METRIC = "condensed elements/s at p=5: mixed-precision vs plain FP64 GPU at 1e-10 rel err"
 
 
+def mixed_cells(args):
+    """Grid of the hp batching workload: 25^3 cells by default."""
+    return 25 if args.n == 24 else args.n
+
+
 def make_mesh(args, seed=12345):
     """hexa: the metric's uniform mesh.  mixed: the hp-adaptive mesh of
-    hexahedra, prisms and tetrahedra (orders 1..6 drawn per element, minimum
-    rule on shared edges and faces), n^3 cells of which the x > 21/24 and
-    z > 21/24 slabs are split into prisms and tetrahedra."""
+    hexahedra, prisms and tetrahedra of the unit cube (orders 1..6 drawn per
+    element, minimum rule on shared edges and faces, kappa = 10**U(-1, 1)):
+    n^3 cells with the tetrahedra in a 6 x 6 x 7 corner block and prism
+    columns along x, y and z beside it -- at n = 25, 19,129 elements,
+    68.6 / 23.5 / 7.9 % hexa / prism / tet."""
     from hp3d_gb300 import mesh as M
     if args.workload == "mixed":
-        return M.mixed_mesh(args.n, a=21 / 24, b=21 / 24, pmax=6, perturb=0.1,
-                            kappa_logrange=(-2, 2), seed=seed)
+        n = mixed_cells(args)
+        return M.mixed_mesh(n, a=(n - 6) / n, b=(n - 7) / n, cy=(n - 6) / n, pmax=6,
+                            perturb=0.0, kappa_logrange=(-1, 1), seed=seed)
     return M.structured_hexa(args.n, args.p, perturb=0.15, kappa_logrange=(-2, 2), seed=seed)
 
 
@@ -104,16 +116,70 @@ class ClockSampler:
 
 
 def measured_peaks():
+    """(HBM GB/s, BF16 TFLOP/s burst, BF16 TFLOP/s sustained, kind)."""
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         d = json.load(open(p))
-        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
-    return 6800.0, 1900.0, "fallback"
+        return (d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0),
+                d.get("bf16_tflops_sustained", d.get("bf16_tflops", 1700.0)), "measured")
+    return 6800.0, 1900.0, 1700.0, "fallback"
 
 
-def cpu_baseline(mesh, isol, integration, seconds=15.0, nthreads=0):
-    """Time the oracle (OpenMP, all host cores) on a bounded sample."""
+def measured_fp64_tflops(device):
+    """FP64 rate of this GPU: cuBLAS DGEMM 4096^3 through torch, best of 5."""
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=device)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=device)
+    for _ in range(2):
+        a @ b
+    torch.cuda.synchronize()
+    best = float("inf")
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    for _ in range(5):
+        e0.record(); a @ b; e1.record(); torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1000.0)
+    return 2.0 * 4096 ** 3 / best / 1e12
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.startswith("Model name:"):
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def seg_rel(x, y, off):
+    """Largest per-segment relative difference max|x - y| / max|y| over the
+    segments [off[k], off[k+1]) of two concatenated arrays."""
+    off = np.asarray(off, np.int64)
+    keep = np.diff(off) > 0
+    if not keep.any():
+        return 0.0
+    idx = off[:-1][keep]
+    end = int(off[-1])
+    d = np.maximum.reduceat(np.abs(x[:end] - y[:end]), idx)
+    m = np.maximum.reduceat(np.abs(y[:end]), idx)
+    return float((d / np.maximum(m, 1e-300)).max())
+
+
+OUT_KEYS = (("zastif", "elem_nnz"), ("zbload", "lcon_off"), ("aschur", "schur_off"),
+            ("bschur", "bub_off"))
+
+
+def cpu_baseline(mesh, isol, integration, seconds=15.0, nthreads=0, gpu_out=None,
+                 min_sample=0):
+    """Time the oracle (OpenMP over the host cores, BLAS-3 DSYRK and
+    DGETRF / DGETRS / DGEMM from SciPy's bundled OpenBLAS, as the reference
+    calls them) on a bounded sample of the mesh; with gpu_out (the mixed GPU
+    pass's outputs) also the largest per-element relative difference of the
+    GPU's condensed blocks from the oracle's on that sample."""
     from oracle import oracle as O
+    blas = O.use_blas() or "oracle loops (no BLAS library found)"
     cores = nthreads if nthreads > 0 else (os.cpu_count() or 1)
     # size the sample: one probe round of `cores` elements, spread evenly over
     # the mesh (an hp mesh's orders vary with position)
@@ -126,36 +192,156 @@ def cpu_baseline(mesh, isol, integration, seconds=15.0, nthreads=0):
     dt = time.perf_counter() - t0
     per_round = max(dt, 1e-3)
     rounds = max(1, int(seconds / per_round))
-    sample = spread(min(nel, rounds * len(probe)))
+    sample = spread(min(nel, max(rounds * len(probe), min_sample)))
     ns = len(sample)
     t0 = time.perf_counter()
     r = O.element_pass(mesh, isol=isol, integration=integration, stc_method=0, nthreads=cores,
                        elements=sample)
     dt = time.perf_counter() - t0
     assert r["rc"] == 0
-    return {"value": ns / dt, "unit": "elements/s", "cores": cores, "kind": "port",
-            "sample": f"{ns} of {nel} elements (evenly spread over ELEM_ORDER), one pass, "
-                      f"{dt:.1f} s, oracle C restatement (elem_opt DSYRK form + LU condensation "
-                      f"+ compression), OpenMP"}
+    out = {"value": ns / dt, "unit": "elements/s", "cores": cores, "cpu": cpu_model(),
+           "kind": "port",
+           "sample": f"{ns} of {nel} elements (evenly spread over ELEM_ORDER), one pass, "
+                     f"{dt:.1f} s, oracle C restatement (elem_opt with DSYRK, stc_fwd_gen with "
+                     f"DGETRF/DGETRS/DGEMM, compression), OpenMP, {blas}"}
+    if gpu_out is not None:
+        worst = {}
+        for key, okey in OUT_KEYS:
+            w = 0.0
+            for j, e in enumerate(sample):
+                a0, a1 = r[okey][j], r[okey][j + 1]
+                g0 = gpu_out[okey][e]
+                ref = r[key][a0:a1]
+                if ref.size == 0:
+                    continue
+                got = gpu_out[key][g0:g0 + (a1 - a0)]
+                w = max(w, float(np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300)))
+            worst[key] = w
+        out["gpu_vs_oracle_on_sample"] = worst
+    return out
+
+
+def final_solution_check(args, local, n=6):
+    """The condensed interface system (what MUMPS solves) on n^3 hexahedra of
+    the metric's kind (p, INTEGRATION, perturbation, kappa range as the
+    workload), assembled from the mixed GPU pass, the FP64 GPU pass and the
+    FP64 oracle; each solved to the working accuracy by iterative refinement
+    on one sparse LU of the oracle's matrix.  Returns the relative 2-norm
+    differences mixed vs FP64 GPU and FP64 GPU vs oracle (the FP64 floor)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import fem_harness as FH
+    from hp3d_gb300 import hp3dg as H
+    from hp3d_gb300 import mesh as M
+    from oracle import oracle as O
+    O.use_blas()
+    m = M.structured_hexa(n, args.p, perturb=0.15, kappa_logrange=(-2, 2), seed=7)
+    systems = {}
+    for name, prec in (("mixed", H.MIXED), ("fp64", H.FP64)):
+        ep = H.ElementPass(prec, integration=args.integration, isol=args.isol, device=local)
+        ep.submit(m); ep.run(); ep.download()
+        systems[name] = FH.gpu_elements(ep, m)
+        ep.close()
+    systems["oracle"] = FH.oracle_element_outputs(m, args.isol, integration=args.integration,
+                                                  stc_method=0)
+    ndofm = np.stack([el["ndofm"] for el in systems["oracle"]]).astype(np.int32)
+    nrdof, _, lcon, lcon_off, _ = O.index_maps(FH.nnode_of(m), m["nodes"], ndofm, m["nnodes"])
+    mats = {}
+    for name, els in systems.items():
+        rows, cols, vals = [], [], []
+        rhs = np.zeros(nrdof)
+        for e in range(m["nelem"]):
+            lc = lcon[lcon_off[e]:lcon_off[e + 1]] - 1
+            nc = len(lc)
+            if nc == 0:
+                continue
+            rows.append(np.repeat(lc, nc)); cols.append(np.tile(lc, nc))
+            vals.append(els[e]["zastif"].ravel())
+            np.add.at(rhs, lc, els[e]["zbload"])
+        A = sp.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                          shape=(nrdof, nrdof)).tocsc()
+        mats[name] = (A, rhs)
+    lu = spla.splu(mats["oracle"][0])
+    sol = {}
+    for name, (A, rhs) in mats.items():
+        x = lu.solve(rhs)
+        for _ in range(8):
+            dx = lu.solve(rhs - A @ x)
+            x = x + dx
+            if np.linalg.norm(dx) <= 1e-16 * np.linalg.norm(x):
+                break
+        sol[name] = x
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    return {"mesh": f"{n}^3 hexahedra, p={args.p}, INTEGRATION={args.integration}, "
+                    f"U(-0.15h,0.15h), kappa 10**U(-2,2)",
+            "unknowns": int(nrdof),
+            "mixed_vs_fp64_gpu": rel(sol["mixed"], sol["fp64"]),
+            "fp64_gpu_vs_fp64_oracle": rel(sol["fp64"], sol["oracle"]),
+            "note": "interface solution of the condensed system (the MUMPS solve), relative "
+                    "2-norm; the FP64-vs-FP64 figure is the floor set by the global "
+                    "conditioning"}
+
+
+def gpu_accuracy(mesh, args, local, stream):
+    """Mixed vs plain FP64 GPU pass on every element of the workload (untimed
+    contexts keeping the element matrices): the largest per-element relative
+    difference of the element matrices, condensed matrices and loads, ASchur
+    and BSchur.  Returns (figures, the mixed pass's outputs)."""
+    from hp3d_gb300 import hp3dg as H
+    eps = {}
+    for prec in (H.FP64, H.MIXED):
+        ep = H.ElementPass(prec, integration=args.integration, isol=args.isol, keep_elem=True,
+                           device=local)
+        ep.set_stream(stream.cuda_stream)
+        ep.submit(mesh); ep.run(); ep.download()
+        eps[prec] = ep
+    om, of = eps[H.MIXED].outputs(), eps[H.FP64].outputs()
+    res = {"elements": int(mesh["nelem"])}
+    for key, okey in OUT_KEYS:
+        res[key] = seg_rel(om[key], of[key], of[okey])
+    n = (args.p + 1) ** 3
+    w = 0.0
+    for e in range(mesh["nelem"]):
+        km, _ = eps[H.MIXED].elem(e, n)
+        kf, _ = eps[H.FP64].elem(e, n)
+        w = max(w, float(np.abs(km - kf).max() / np.abs(kf).max()))
+    res["element_matrix"] = w
+    for ep in eps.values():
+        ep.close()
+    return res, om
 
 
 def run_reference(args, rank, world):
+    """The reference's element pass on the host cores: the oracle restatement
+    (per-element shape functions at every point, DSYRK, DGETRF / DGETRS /
+    DGEMM from SciPy's OpenBLAS, compression) with OpenMP over all cores, the
+    whole mesh every step (warm-up steps included)."""
     if rank != 0:
         return
+    from oracle import oracle as O
+    blas = O.use_blas() or "oracle loops (no BLAS library found)"
     mesh = make_mesh(args)
-    vals = []
-    cb = None
-    # each step a bounded sample, the whole run about two minutes at most
-    sec = min(args.cpu_seconds, 120.0 / max(1, args.warmup + args.steps))
+    cores = os.cpu_count() or 1
+    nel = mesh["nelem"]
+    times = []
     for i in range(args.warmup + args.steps):
-        c = cpu_baseline(mesh, args.isol, args.integration, seconds=sec)
+        t0 = time.perf_counter()
+        r = O.element_pass(mesh, isol=args.isol, integration=args.integration, stc_method=0,
+                           nthreads=cores)
+        dt = time.perf_counter() - t0
+        assert r["rc"] == 0
         if i >= args.warmup:
-            vals.append(c["value"])
-            cb = c
-    v = statistics.median(vals)
+            times.append(dt)
+    ms = 1000.0 * statistics.median(times)
+    v = nel / (ms / 1000.0)
+    cb = {"value": v, "unit": "elements/s", "cores": cores, "cpu": cpu_model(), "kind": "port",
+          "sample": f"the whole mesh ({nel} elements) every step, oracle C restatement "
+                    f"(elem_opt with DSYRK, stc_fwd_gen with DGETRF/DGETRS/DGEMM, "
+                    f"compression), OpenMP, {blas}"}
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "elements/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * mesh["nelem"] / v, "higher_is_better": True,
+            "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_dict(args, world, mesh),
             "cpu_baseline": cb,
@@ -167,10 +353,11 @@ def run_reference(args, rank, world):
 def config_dict(args, world, mesh):
     if args.workload == "mixed":
         cnt = np.bincount(mesh["etype"], minlength=4)[1:]
-        return {"workload": f"galerkin_poisson_hp_mixed_{args.n}^3_cells_pmax6_integration{args.integration}",
+        return {"workload": f"galerkin_poisson_hp_mixed_{mixed_cells(args)}^3_cells_pmax6_integration{args.integration}",
                 "elements_per_gpu": int(mesh["nelem"]),
                 "hexa_prism_tet": [int(x) for x in cnt], "orders": "1..6 per element, min rule",
-                "perturbation": "U(-0.1h,0.1h) interior vertices", "kappa": "10**U(-2,2)",
+                "layout": "tetrahedra in a 6x6x7 corner block, prism columns along x, y, z",
+                "perturbation": "none (unit-cube geometry)", "kappa": "10**U(-1,1)",
                 "precision": args.precision,
                 "parallelism": f"replicas{world}" if world > 1 else "single",
                 "l2": "working set per step > L2, no flush needed"}
@@ -205,8 +392,8 @@ def job_value(world, units_per_rank, ms_job):
 
 
 def measured_traffic(workload, kernel):
-    """DRAM bytes of `kernel` on `workload` from the committed figures of a
-    one-pass ncu capture (profiles/dram_traffic.txt), or None."""
+    """DRAM bytes of `kernel` on `workload` from the committed figures of an
+    ncu capture (profiles/dram_traffic.txt), or None."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", "dram_traffic.txt")
     try:
         with open(path) as f:
@@ -332,15 +519,17 @@ def run_dpg(args, rank, world):
     e2e_s = (time.perf_counter() - t0) / max(1, args.e2e_steps)
     med = np.median(ph, axis=0)
     t_la = (med[1] + med[2]) / 1000.0
-    hbm, bf16, peak_kind = measured_peaks()
+    hbm, bf16, bf16s, peak_kind = measured_peaks()
     achieved = ne * fl_el / t_la / 1e12 if t_la > 0 else None
     if dprec == H.FP64:
-        roof = {"bound": "fp64", "achieved": achieved, "peak": 1.25, "unit": "TFLOP/s",
-                "frac": achieved / 1.25 if achieved else None, "traffic": None,
+        fp64 = measured_fp64_tflops(f"cuda:{local}")
+        roof = {"bound": "fp64", "achieved": achieved, "peak": fp64, "unit": "TFLOP/s",
+                "frac": achieved / fp64 if achieved else None, "traffic": None,
                 "kernel": "k_dpg_dpg + k_dpg_condense",
                 "note": "dense DPG algebra (Gram Cholesky, forward solve of [B|l], X^H X, L2-field "
-                        "condensation) per element over the two kernels' time; peak = nominal "
-                        "GB300 FP64 (not in the measured peaks)"}
+                        "condensation) per element over the two kernels' time; peak = cuBLAS "
+                        "DGEMM 4096^3 measured in this run (the measured-peaks file has no FP64 "
+                        "figure)"}
     else:
         # tensor work: 28 digit pairs x 2 real products of K = 128 per complex update
         # (4 real MACs per complex MAC); the algorithmic count is the complex FLOPs
@@ -352,9 +541,7 @@ def run_dpg(args, rank, world):
                 "traffic": (measured_traffic(cfg["workload"], "k_zupd") or (None,))[0],
                 "note": f"BF16 digit-pair MMA work of the dense DPG algebra (28 pairs of the "
                         f"complex FLOP count) over the stage's time; peak {peak_kind}; the "
-                        f"complex-FP64-equivalent rate is {ne * fl_el / t_la / 1e12:.3f} TFLOP/s; "
-                        f"traffic: DRAM bytes of the 31 k_zupd launches of one pass (one-pass "
-                        f"ncu capture at this size)"}
+                        f"complex-FP64-equivalent rate is {ne * fl_el / t_la / 1e12:.3f} TFLOP/s"}
     cb = cpu(args.cpu_seconds) if (rank == 0 and not args.no_cpu_baseline) else None
     line = {"metric": DPG_METRIC, "value": value, "unit": "elements/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -395,6 +582,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-compare", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the per-element mixed-vs-FP64 and oracle comparisons and the "
+                         "final-solution check")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--download-chunks", type=int, default=4,
                     help="e2e: pass in this many element chunks, each copied to the host "
@@ -509,9 +699,9 @@ def main():
         ep64.close()
 
     ph = np.median(np.array(phases), axis=0)
-    hbm, bf16, peak_kind = measured_peaks()
+    hbm, bf16, bf16s, peak_kind = measured_peaks()
     # dominant kernel = the contraction (one launch per bin; one bin for the
-    # uniform mesh); its algorithmic FLOPs per run come from the library
+    # uniform mesh); its FLOPs per run come from the library
     kernels, flops = ep.pass_stats()
     t_con = ph[2] / 1000.0
     con_note = ""
@@ -522,25 +712,64 @@ def main():
         con_note = "; time = whole pass (bins run concurrently), a lower bound on the rate"
     if prec == H.MIXED:
         pairs = ep.ozaki_pairs()
-        roof = {"bound": "tensor", "achieved": flops / t_con / 1e12 if t_con > 0 else None,
+        # algorithmic work: the DSYRK count n(n+1) 3 nint per element
+        # (elem_opt.F90:131) times the digit-pair products; the library counts
+        # the executed MMA FLOPs, pairs x 2 (6 nint) n(n+1)/2, twice that (the
+        # shared-operand form D.M expands the symmetric 3x3 D into 6 terms)
+        alg = flops / 2.0
+        roof = {"bound": "tensor", "achieved": alg / t_con / 1e12 if t_con > 0 else None,
                 "peak": bf16, "unit": "TFLOP/s", "kernel": "k_ozaki_gemm",
-                "note": f"{pairs} digit-pair products of the D.M contraction, "
-                        f"2*(6*nint)*n(n+1)/2 each per element; peak {peak_kind}{con_note}"}
+                "algorithmic_flop_per_launch": alg,
+                "executed_mma_tflops": flops / t_con / 1e12 if t_con > 0 else None,
+                "note": f"achieved = (n(n+1) 3 nint per element, the DSYRK count) x {pairs} "
+                        f"digit-pair passes x elements / contraction time; peak = {peak_kind} "
+                        f"BF16 burst: the SM clock stayed at its maximum with no power-cap "
+                        f"reason during the timed region (clocks field){con_note}"}
+        if roof["achieved"]:
+            roof["executed_frac"] = roof["executed_mma_tflops"] / bf16
+            roof["frac_of_sustained_peak"] = roof["achieved"] / bf16s
     else:
-        roof = {"bound": "tensor", "achieved": flops / t_con / 1e12 if t_con > 0 else None,
-                "peak": bf16, "unit": "TFLOP/s", "kernel": "k_contract_fp64",
-                "note": "FP64 CUDA-core contraction measured against the bf16 peak"}
+        roof = {"bound": "fp64", "achieved": flops / t_con / 1e12 if t_con > 0 else None,
+                "peak": measured_fp64_tflops(f"cuda:{local}"), "unit": "TFLOP/s",
+                "kernel": "k_contract_fp64",
+                "note": "FP64 CUDA-core contraction (DSYRK count) against cuBLAS DGEMM measured "
+                        "in this run"}
     if roof["achieved"] is not None:
         roof["frac"] = roof["achieved"] / roof["peak"]
     tr = (measured_traffic(config_dict(args, world, mesh)["workload"], roof["kernel"])
           if args.workload == "hexa" else None)
     roof["traffic"] = tr[0] if tr else None
     if tr:
-        roof["note"] += "; traffic: one-pass ncu capture of one launch at this size (bytes)"
+        roof["note"] += "; traffic: DRAM bytes per launch from an ncu capture of this size"
+    elif prec == H.MIXED and args.workload == "hexa":
+        # captures of smaller meshes of the same kind; traffic per element is not
+        # constant across sizes, so nothing is scaled to this one
+        small = {}
+        for nn in (12, 16):
+            t = measured_traffic(f"galerkin_poisson_hexa_{nn}^3_p{args.p}_integration{args.integration}",
+                                 roof["kernel"])
+            if t:
+                small[f"{nn}^3"] = t[0]
+        if small:
+            roof["traffic_small_cases"] = small
+            roof["note"] += ("; traffic null: DRAM bytes per launch were captured on 12^3 and "
+                             "16^3 (traffic_small_cases) and do not grow in proportion to the "
+                             "elements, so they are not scaled to this size")
+
+    accuracy, mixed_out = None, None
+    if prec == H.MIXED and args.workload == "hexa" and not args.no_accuracy:
+        accuracy, mixed_out = gpu_accuracy(mesh, args, local, stream)
+        accuracy = {"mixed_vs_fp64_gpu_per_element_max_rel": accuracy}
 
     cb = None
     if rank == 0 and not args.no_cpu_baseline:
-        cb = cpu_baseline(mesh, args.isol, args.integration, seconds=args.cpu_seconds)
+        cb = cpu_baseline(mesh, args.isol, args.integration, seconds=args.cpu_seconds,
+                          gpu_out=mixed_out, min_sample=256 if mixed_out is not None else 0)
+        if accuracy is not None:
+            accuracy["mixed_vs_oracle_per_element_max_rel"] = cb.pop("gpu_vs_oracle_on_sample")
+            accuracy["oracle_sample"] = cb["sample"].split(",")[0]
+            accuracy["final_solution"] = final_solution_check(args, local)
+    mixed_out = None
 
     # kernel launches per pass: the kernel nodes of the captured graph
     launches_per_step = kernels
@@ -556,7 +785,8 @@ def main():
                          "contraction": float(ph[2]), "condensation": float(ph[3]),
                          "index_maps": float(ph[4]), "pass": float(ph[5])},
             "fp64_gpu": fp64,
-            "speedup_vs_fp64_gpu": (value / fp64["value"]) if fp64 else None}
+            "speedup_vs_fp64_gpu": (value / fp64["value"]) if fp64 else None,
+            "accuracy": accuracy}
     ep.close()
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -291,6 +291,34 @@ class ElementPass:
                                            ctypes.byref(nb), ctypes.byref(ni)), "schur")
         return (a[: nb.value * ni.value].reshape(ni.value, nb.value).T.copy(), b[: nb.value])
 
+    def outputs(self):
+        """Every element's condensed outputs after download, concatenated in
+        element order: dict of zastif (row-major nrdofc^2 blocks), zbload,
+        aschur (column-major nb x ni blocks), bschur and the offsets of each
+        (elem_nnz, lcon_off, schur_off, bub_off; n_elem + 1 entries)."""
+        nnz, nl, ns, nbub = self.sizes()
+        _, _, _, lo, en = self.index_map()
+        nb = np.zeros(self.nel, np.int64); ni = np.zeros(self.nel, np.int64)
+        b_, i_ = ctypes.c_int32(), ctypes.c_int32()
+        for e in range(self.nel):
+            self._check(self.L.hp3dg_get_schur(self.ctx, e, None, None, ctypes.byref(b_),
+                                               ctypes.byref(i_)), "schur")
+            nb[e], ni[e] = b_.value, i_.value
+        so = np.concatenate([[0], np.cumsum(nb * ni)]).astype(np.int64)
+        bo = np.concatenate([[0], np.cumsum(nb)]).astype(np.int64)
+        za = np.zeros(max(nnz, 1)); zb = np.zeros(max(nl, 1))
+        sa = np.zeros(max(ns, 1)); sb = np.zeros(max(nbub, 1))
+        nc = ctypes.c_int32()
+        for e in range(self.nel):
+            self._check(self.L.hp3dg_get_condensed(self.ctx, e, zb[lo[e]:].ctypes.data_as(_f64p),
+                                                   za[en[e]:].ctypes.data_as(_f64p),
+                                                   ctypes.byref(nc)), "cond")
+            self._check(self.L.hp3dg_get_schur(self.ctx, e, sa[so[e]:].ctypes.data_as(_f64p),
+                                               sb[bo[e]:].ctypes.data_as(_f64p),
+                                               ctypes.byref(b_), ctypes.byref(i_)), "schur")
+        return dict(zastif=za, zbload=zb, aschur=sa, bschur=sb, elem_nnz=en, lcon_off=lo,
+                    schur_off=so, bub_off=bo)
+
     def elem(self, e, n):
         a = np.zeros((n, n), order="F"); b = np.zeros(n)
         self._check(self.L.hp3dg_get_elem(self.ctx, e, a.ctypes.data_as(_f64p), n,

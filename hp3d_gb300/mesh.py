@@ -529,7 +529,8 @@ def _prism_cells(vid, c, axis):
     """The two prisms of the unit cell at c extruded along `axis`, their
     cross-section squares split along the diagonal through the cell's low
     corner (matching the Kuhn split of the neighbouring tetrahedra)."""
-    u, w = [a for a in range(3) if a != axis]
+    # (u, w, axis) right-handed, so every prism has a positive Jacobian
+    u, w = {0: (1, 2), 1: (2, 0), 2: (0, 1)}[axis]
     e = np.eye(3, dtype=int)
     p00, p10, p11, p01 = c, c + e[u], c + e[u] + e[w], c + e[w]
     out = []
@@ -563,13 +564,18 @@ def structured_prism(n, ph, pz, perturb=0.0, kappa_logrange=None, seed=12345, di
 
 
 def mixed_mesh(n, a=0.875, b=0.875, p=None, pmax=6, perturb=0.0, kappa_logrange=(-1, 1),
-               seed=2024, dirichlet=True):
+               seed=2024, dirichlet=True, cy=None):
     """Mixed hexa / prism / tet mesh of [0,1]^3 on an n^3 grid of cells:
 
       x < a, z < b : hexahedra
       x > a, z < b : prisms extruded along z
       x > a, z > b : tetrahedra (Kuhn split of each cell)
       x < a, z > b : prisms extruded along x
+
+    With cy given the tetrahedra fill only the corner block x > a, y > cy,
+    z > b: prisms extruded along z below it, along x beside it in x and
+    along y beside it in y (each column reaching the boundary), hexahedra
+    everywhere else.
 
     Every interface is conforming: hexa faces meet prism quads, prism
     triangles meet tetrahedron faces split along the same diagonals.  With
@@ -583,6 +589,7 @@ def mixed_mesh(n, a=0.875, b=0.875, p=None, pmax=6, perturb=0.0, kappa_logrange=
     nv1 = n + 1
     vid = lambda i, j, k: int(i + nv1 * (j + nv1 * k))  # noqa: E731
     ia, kb = int(round(a * n)), int(round(b * n))
+    jc = 0 if cy is None else int(round(cy * n))
     et, verts, orders = [], [], []
     e3 = np.eye(3, dtype=int)
     perms = [(0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)]
@@ -591,12 +598,17 @@ def mixed_mesh(n, a=0.875, b=0.875, p=None, pmax=6, perturb=0.0, kappa_logrange=
             for i in range(n):
                 c = np.array([i, j, k])
                 centre = (c + 0.5) / n
-                if i < ia and k < kb:
+                # inside the tetrahedron block along x, y, z: all three ->
+                # tetrahedra, two -> prisms extruded along the third axis,
+                # fewer -> hexahedra
+                inside = (i >= ia, j >= jc, k >= kb)
+                cnt = sum(inside)
+                if cnt <= 1:
                     v = [vid(*(c + d)) for d in _VOFF]
                     et.append(HEXA); verts.append(v)
                     orders.append((p, p, p) if p else _hp_order(rng, centre, pmax, 3))
-                elif k < kb or i < ia:
-                    for v in _prism_cells(vid, c, 2 if k < kb else 0):
+                elif cnt == 2:
+                    for v in _prism_cells(vid, c, inside.index(False)):
                         et.append(PRISM); verts.append(v)
                         orders.append((p, p) if p else _hp_order(rng, centre, pmax, 2))
                 else:

@@ -524,6 +524,35 @@ static int quad_dispatch(int etype, const int32_t *norder, const int32_t *noriF,
   return -1;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Optional BLAS-3 / LAPACK kernels (the reference calls DSYRK in elem_opt and  */
+/* DGETRF / DGETRS / DGEMM in stc_fwd_gen).  The caller (the Python harness)   */
+/* passes pointers to an optimised library's routines with the Fortran         */
+/* calling convention (all arguments by reference); without them the oracle   */
+/* runs its own loops in the same order of operations.                        */
+/* ------------------------------------------------------------------------ */
+typedef void (*orc_dsyrk_t)(char *, char *, int *, int *, double *, double *, int *, double *,
+                            double *, int *);
+typedef void (*orc_dgetrf_t)(int *, int *, double *, int *, int *, int *);
+typedef void (*orc_dgetrs_t)(char *, int *, int *, double *, int *, int *, double *, int *, int *);
+typedef void (*orc_dgemm_t)(char *, char *, int *, int *, int *, double *, double *, int *,
+                            double *, int *, double *, double *, int *);
+static struct {
+  orc_dsyrk_t dsyrk;
+  orc_dgetrf_t dgetrf;
+  orc_dgetrs_t dgetrs;
+  orc_dgemm_t dgemm;
+} g_blas;
+
+void orc_set_blas(void *dsyrk, void *dgetrf, void *dgetrs, void *dgemm) {
+  g_blas.dsyrk = (orc_dsyrk_t)dsyrk;
+  g_blas.dgetrf = (orc_dgetrf_t)dgetrf;
+  g_blas.dgetrs = (orc_dgetrs_t)dgetrs;
+  g_blas.dgemm = (orc_dgemm_t)dgemm;
+}
+
+int orc_blas_active(void) { return g_blas.dsyrk && g_blas.dgetrf && g_blas.dgetrs && g_blas.dgemm; }
+
 int orc_elem(int etype, const int32_t *norder, const int32_t *nori_edge,
              const int32_t *nori_face, const double *xnod, double kappa,
              int isol, int integration, int variant, double *zaloc, int ld,
@@ -591,12 +620,19 @@ int orc_elem(int etype, const int32_t *norder, const int32_t *nori_edge,
   }
   if (variant == 0) {
     /* DSYRK('U','N') + lower fill (elem_opt.F90:131-137) */
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i <= j; ++i) {
-        double s = 0.0;
-        for (int k = 0; k < nda; ++k) s += atest[i + (size_t)n * k] * atest[j + (size_t)n * k];
-        zaloc[i + (size_t)ld * j] = s;
-      }
+    if (g_blas.dsyrk) {
+      char up = 'U', no = 'N';
+      int nn = n, kk = nda, lda = n, ldc = ld;
+      double one = 1.0, zero = 0.0;
+      g_blas.dsyrk(&up, &no, &nn, &kk, &one, atest, &lda, &zero, zaloc, &ldc);
+    } else {
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i <= j; ++i) {
+          double s = 0.0;
+          for (int k = 0; k < nda; ++k) s += atest[i + (size_t)n * k] * atest[j + (size_t)n * k];
+          zaloc[i + (size_t)ld * j] = s;
+        }
+    }
     for (int k = 0; k < n; ++k)
       for (int i = k + 1; i < n; ++i) zaloc[i + (size_t)ld * k] = zaloc[k + (size_t)ld * i];
     free(atest);
@@ -629,6 +665,28 @@ int orc_stc_fwd(int ni, int nb, const double *a, int lda, const double *b,
   for (int i = 0; i < ni; ++i) bi[i] = b[i];
   for (int i = 0; i < nb; ++i) bschur[i] = b[ni + i];
   int rc = 0;
+  if (method == 0 && g_blas.dgetrf && nb > 0) {
+    /* stc_fwd_gen with the library: DGETRF, DGETRS on [Abi | Bb], then
+       DGEMM / the load update (stc.F90:462-507) */
+    int *piv = (int *)malloc(sizeof(int) * nb);
+    int nn = nb, info = 0;
+    g_blas.dgetrf(&nn, &nn, abb, &nn, piv, &info);
+    if (info != 0) rc = -1;
+    if (rc == 0) {
+      char no = 'N';
+      int one_i = 1, nrhs = ni;
+      g_blas.dgetrs(&no, &nn, &nrhs, abb, &nn, piv, aschur, &nn, &info);
+      g_blas.dgetrs(&no, &nn, &one_i, abb, &nn, piv, bschur, &nn, &info);
+      double m1 = -1.0, p1 = 1.0;
+      int mi = ni;
+      g_blas.dgemm(&no, &no, &mi, &mi, &nn, &m1, aib, &mi, aschur, &nn, &p1, aii, &mi);
+      g_blas.dgemm(&no, &no, &mi, &one_i, &nn, &m1, aib, &mi, bschur, &nn, &p1, bi, &mi);
+    }
+    free(piv);
+    free(abb);
+    free(aib);
+    return rc;
+  }
   if (method == 0) {
     /* DGETRF: right-looking LU with partial pivoting (first max |.|) */
     int *piv = (int *)malloc(sizeof(int) * (nb > 0 ? nb : 1));

@@ -105,6 +105,12 @@ int orc_elem(int etype, const int32_t *norder, const int32_t *nori_edge,
  * ld nb), BSchur = inv(Abb) Bb (nb).  method 0 = LU (stc_fwd_gen),
  * 1 = Cholesky (stc_fwd_herm, stc.F90:338-416).  Returns 0 or -1 on a zero
  * pivot / non-positive Cholesky pivot. */
+/* Optional optimised BLAS-3 / LAPACK routines (Fortran calling convention):
+ * DSYRK for elem_opt.F90:131 and DGETRF / DGETRS / DGEMM for stc.F90:462-507.
+ * NULL pointers restore the oracle's own loops. */
+void orc_set_blas(void *dsyrk, void *dgetrf, void *dgetrs, void *dgemm);
+int orc_blas_active(void);
+
 int orc_stc_fwd(int ni, int nb, const double *a, int lda, const double *b,
                 int method, double *aii, double *bi, double *aschur,
                 double *bschur);

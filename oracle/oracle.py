@@ -41,6 +41,8 @@ def lib():
         build()
         L = ctypes.CDLL(_LIB)
         L.orc_gauss1d.argtypes = [ctypes.c_int, _f64p, _f64p]
+        L.orc_set_blas.argtypes = [ctypes.c_void_p] * 4
+        L.orc_set_blas.restype = None
         L.orc_set_3D_int_hexa.argtypes = [_i32p, _i32p, ctypes.c_int, _f64p, _f64p]
         L.orc_set_3D_int_tet.argtypes = [_i32p, ctypes.c_int, _f64p, _f64p]
         L.orc_nrdofH_hexa.argtypes = [_i32p]
@@ -128,6 +130,45 @@ def _i32(a):
 
 def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _capsule_pointer(capsule):
+    get_name = ctypes.pythonapi.PyCapsule_GetName
+    get_name.restype = ctypes.c_char_p
+    get_name.argtypes = [ctypes.py_object]
+    get_ptr = ctypes.pythonapi.PyCapsule_GetPointer
+    get_ptr.restype = ctypes.c_void_p
+    get_ptr.argtypes = [ctypes.py_object, ctypes.c_char_p]
+    return get_ptr(capsule, get_name(capsule))
+
+
+def use_blas(on=True):
+    """Route the oracle's DSYRK (elem_opt.F90:131) and DGETRF / DGETRS / DGEMM
+    (stc.F90:462-507) through the optimised BLAS / LAPACK that SciPy bundles
+    (its Cython-level routines, Fortran calling convention), as the reference
+    does through its BLAS.  Returns a one-line description of the library, or
+    None when SciPy is missing (the oracle's own loops stay in use).  Set
+    OPENBLAS_NUM_THREADS=1 before SciPy loads when the oracle runs its own
+    OpenMP threads."""
+    if not on:
+        lib().orc_set_blas(None, None, None, None)
+        return None
+    try:
+        import scipy
+        from scipy.linalg import cython_blas, cython_lapack
+    except ImportError:
+        return None
+    b, la = cython_blas.__pyx_capi__, cython_lapack.__pyx_capi__
+    lib().orc_set_blas(_capsule_pointer(b["dsyrk"]), _capsule_pointer(la["dgetrf"]),
+                       _capsule_pointer(la["dgetrs"]), _capsule_pointer(b["dgemm"]))
+    desc = f"scipy {scipy.__version__} BLAS/LAPACK"
+    try:
+        cfg = scipy.show_config(mode="dicts")
+        bl = cfg.get("Build Dependencies", {}).get("blas", {})
+        desc += f" ({bl.get('name', '?')} {bl.get('version', '')})".rstrip()
+    except Exception:
+        pass
+    return desc
 
 
 def gauss1d(n):

@@ -97,3 +97,36 @@ def test_linear_solution_hp_mixed_mesh():
     ref = FH.oracle_element_outputs(m, 13, zdofd=zd)
     err, nrm, _, _ = FH.solve_and_error(m, ref, 13, zdofd=zd)
     assert err < 1e-12 * nrm
+
+
+def test_poly_pois_corner_mixed_mesh():
+    """The corner layout (tetrahedra in a corner block, prisms extruded along
+    x, y and z beside it, hexahedra elsewhere) is conforming: u = xyz is
+    reproduced (test/poly_pois.F90:101) at p = 3 on a perturbed mesh."""
+    m = M.mixed_mesh(4, a=0.5, b=0.5, cy=0.5, p=3, perturb=0.1, seed=7, kappa_logrange=None)
+    assert set(np.unique(m["etype"])) == {1, 2, 3}
+    zd = FH.dirichlet_data(m, 12)
+    ref = FH.oracle_element_outputs(m, 12, zdofd=zd)
+    err, nrm, _, _ = FH.solve_and_error(m, ref, 12, zdofd=zd)
+    assert err < 1e-12 * nrm
+
+
+def test_linear_solution_hp_corner_mixed_mesh():
+    m = M.mixed_mesh(4, a=0.5, b=0.5, cy=0.5, perturb=0.1, seed=9, kappa_logrange=None)
+    assert len({tuple(o) for o in m["orders"]}) > 10
+    zd = FH.dirichlet_data(m, 13)
+    ref = FH.oracle_element_outputs(m, 13, zdofd=zd)
+    err, nrm, _, _ = FH.solve_and_error(m, ref, 13, zdofd=zd)
+    assert err < 1e-12 * nrm
+
+
+def test_batching_mesh_composition():
+    """The hp batching workload: 25^3 cells, tetrahedra in a 6 x 6 x 7 corner
+    block: 19,129 elements, 68.6 / 23.5 / 7.9 % hexa / prism / tet (the
+    conforming layout's closest split to 70 / 20 / 10 near 20,000 elements:
+    prism columns bound the tetrahedra's share)."""
+    m = M.mixed_mesh(25, a=19 / 25, b=18 / 25, cy=19 / 25, pmax=6, perturb=0.1,
+                     kappa_logrange=(-1, 1), seed=12345)
+    cnt = np.bincount(m["etype"], minlength=4)[1:]
+    assert m["nelem"] == 19129 and list(cnt) == [13129, 4488, 1512]
+    assert np.all(m["kappa"] >= 0.1 - 1e-12) and np.all(m["kappa"] <= 10 + 1e-12)
