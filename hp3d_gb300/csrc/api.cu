@@ -377,6 +377,9 @@ struct hp3dg_ctx {
   std::vector<int64_t> elem_nnz, lcon_off, schur_off, bub_off, zd_off;
   std::vector<int> nextract;
   std::vector<Bin> bins;
+  StageGroup sg;  // grouped launches of the per-element stage kernels (bins or chunks)
+  CondGroup cg;   // grouped launches of the fused condensation (its bins or chunks)
+  std::vector<int> cg_index;  // stage-group unit -> condensation segment, or -1
   bool have_zdofd = false;
   // device inputs
   int *d_norder = nullptr, *d_nori_e = nullptr, *d_nori_f = nullptr, *d_nodes = nullptr,
@@ -454,6 +457,9 @@ void free_bin(Bin& b) {
 void free_batch(hp3dg_ctx* c) {
   for (void* p : c->cbufs) cudaFree(p);
   c->cbufs.clear();
+  c->sg = StageGroup{};
+  c->cg = CondGroup{};
+  c->cg_index.clear();
   if (c->constrained) {
     c->d_wnextract = nullptr;
     c->d_wlcon_off = c->d_welem_nnz = nullptr;
@@ -501,6 +507,119 @@ void free_batch(hp3dg_ctx* c) {
   do {                                         \
     if ((x) != cudaSuccess) return HP3DG_ERR_CUDA; \
   } while (0)
+
+}  // namespace
+
+namespace {
+
+// Segment tables of the grouped stage launches (device arrays freed with the
+// batch): one segment per bin, or for a batch of one bin that runs in element
+// chunks one per chunk.  Every vertex-geometry pass launches its stage-0
+// kernels through these tables, so an element's arithmetic is the same
+// whatever batch it is in.
+int build_stage_group(hp3dg_ctx* c) {
+  c->sg = StageGroup{};
+  if (c->bins.empty()) return HP3DG_OK;
+  const bool mixed = c->opts.precision == HP3DG_MIXED;
+  std::vector<StageSeg> segs;
+  std::vector<int> pel{0}, pgeo{0}, pdsc{0}, psl{0};
+  int max_nint = 0;
+  auto add = [&](Bin& B, int j0, int j1) {
+    StageSeg g{};
+    const int nel = j1 - j0;
+    g.etype = B.etype;
+    g.nvert = B.nvert;
+    g.n = B.n;
+    g.nint = B.nint;
+    g.nel = nel;
+    for (int i = 0; i < 19; ++i) g.full[i] = B.nord_loc[i];
+    g.elist = B.d_elist + j0;
+    g.wq = B.d_wq;
+    g.shap = B.d_shap;
+    g.grad = B.d_grad;
+    g.D = B.d_D + (size_t)j0 * B.nint * 6;
+    g.F = B.d_F + (size_t)j0 * B.nint;
+    g.b0 = B.d_b0 + (size_t)j0 * B.n;
+    g.perm = B.d_perm + (size_t)j0 * B.n;
+    const int neb = (nel + 63) / 64;
+    if (mixed) {
+      g.K = 6 * B.nint;
+      g.nk = B.plan.kdim / 16;
+      g.radix = B.plan.radix;
+      g.digits = B.plan.digits;
+      // D digit tiles of 64 elements; a chunk starts at a multiple of 128
+      g.ddig = (uint16_t*)((uint8_t*)B.d_ddig + (size_t)(j0 / 128) * ozaki_d_bytes(B.plan, 128));
+      g.dscale = B.d_dscale + j0;
+    }
+    segs.push_back(g);
+    pel.push_back(pel.back() + nel);
+    pgeo.push_back(pgeo.back() + nel * ((B.nint + 127) / 128));
+    pdsc.push_back(pdsc.back() + neb * 64);
+    psl.push_back(psl.back() + (mixed ? g.nk * neb : 0));
+    max_nint = std::max(max_nint, B.nint);
+  };
+  if (c->bins.size() == 1 && c->nchunk > 1)
+    for (int k = 0; k < c->nchunk; ++k) add(c->bins[0], c->chunk_lo[k], c->chunk_lo[k + 1]);
+  else
+    for (Bin& B : c->bins) add(B, 0, (int)B.elems.size());
+  int err = 0;
+  StageGroup& G = c->sg;
+  G.segs = dalloc<StageSeg>(segs.size(), &err);
+  G.pre_el = dalloc<int>(pel.size(), &err);
+  G.pre_geom = dalloc<int>(pgeo.size(), &err);
+  G.pre_dsc = dalloc<int>(pdsc.size(), &err);
+  G.pre_slice = dalloc<int>(psl.size(), &err);
+  for (void* p : {(void*)G.segs, (void*)G.pre_el, (void*)G.pre_geom, (void*)G.pre_dsc,
+                  (void*)G.pre_slice})
+    if (p) c->cbufs.push_back(p);
+  if (err) { c->sg = StageGroup{}; return err; }
+  CK(cudaMemcpy(G.segs, segs.data(), segs.size() * sizeof(StageSeg), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G.pre_el, pel.data(), pel.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G.pre_geom, pgeo.data(), pgeo.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G.pre_dsc, pdsc.data(), pdsc.size() * 4, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(G.pre_slice, psl.data(), psl.size() * 4, cudaMemcpyHostToDevice));
+  G.nseg = (int)segs.size();
+  G.h_pre.clear();
+  for (auto* v : {&pel, &pgeo, &pdsc, &psl}) G.h_pre.insert(G.h_pre.end(), v->begin(), v->end());
+  G.max_nint = max_nint;
+  // the fused condensation's segments: the same units, where the bin uses it
+  std::vector<CondSegIn> cin;
+  c->cg_index.assign(G.nseg, -1);
+  auto cadd = [&](int unit, Bin& B, int j0, int j1) {
+    if (!B.cond_tc) return;
+    const size_t nsu = (size_t)B.ni * (B.ni + 1) / 2, npk = (size_t)B.n * (B.n + 1) / 2;
+    CondSegIn q;
+    q.nfull = B.n; q.nif = B.ni; q.nbf = B.nb; q.nel = j1 - j0;
+    q.elist = B.d_elist + j0;
+    q.PK = B.d_PK + (size_t)j0 * npk;
+    q.b0 = B.d_b0 + (size_t)j0 * B.n;
+    q.perm = B.d_perm + (size_t)j0 * B.n;
+    q.W = B.d_S + (size_t)j0 * nsu;
+    q.dmask = B.d_dmask + (size_t)j0 * B.ni;
+    CondTcBufs t = B.ctb;
+    t.kbd += (size_t)j0 * t.bytes_a;
+    t.lid += (size_t)j0 * t.bytes_b;
+    t.ltd += (size_t)j0 * t.bytes_b;
+    t.ekb += (size_t)j0 * t.nr;
+    t.eli += (size_t)j0 * t.nbr;
+    t.elt += (size_t)j0 * t.nbr;
+    t.bi += (size_t)j0 * B.ni;
+    q.t = t;
+    c->cg_index[unit] = (int)cin.size();
+    cin.push_back(q);
+  };
+  if (c->bins.size() == 1 && c->nchunk > 1)
+    for (int k = 0; k < c->nchunk; ++k) cadd(k, c->bins[0], c->chunk_lo[k], c->chunk_lo[k + 1]);
+  else
+    for (size_t b = 0; b < c->bins.size(); ++b)
+      cadd((int)b, c->bins[b], 0, (int)c->bins[b].elems.size());
+  if (!cin.empty()) {
+    const int rc = cond_tc_group_build(cin, &c->cg, &c->cbufs);
+    if (rc == -1) return HP3DG_ERR_ALLOC;
+    if (rc) return HP3DG_ERR_UNSUPPORTED;
+  }
+  return HP3DG_OK;
+}
 
 }  // namespace
 
@@ -997,6 +1116,7 @@ int hp3dg_batch_submit_constrained(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_d
     c->nchunk = k;
     c->chunk_lo[k] = nel;
   }
+  if (int rc = build_stage_group(c)) { free_batch(c); return rc; }
   c->submitted = true;
   return HP3DG_OK;
 }
@@ -1035,6 +1155,21 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
   const size_t dblk = mixed ? ozaki_d_bytes(B.plan, 128) : 0;  // D digits of 128 elements
   uint16_t* ddig = mixed ? (uint16_t*)((uint8_t*)B.d_ddig + (size_t)(j0 / 128) * dblk) : nullptr;
   double* dscale = mixed ? B.d_dscale + j0 : nullptr;
+  if (stage == 0 && !c->iso) {
+    // the segment of this range in the stage group: bin b, or chunk k of a
+    // chunked one-bin batch
+    int k = 0;
+    if (c->bins.size() == 1 && c->nchunk > 1) {
+      while (k < c->nchunk && c->chunk_lo[k] != j0) ++k;
+    } else {
+      k = (int)(&B - c->bins.data());
+    }
+    if (k >= c->sg.nseg) return HP3DG_ERR_STATE;
+    launch_stage0_grouped(c->sg, k, k + 1, c->d_norder, c->d_nori_e, c->d_nori_f, c->d_xvert,
+                          c->d_kappa, c->opts.isol, c->d_flags, st);
+    if (mixed && launch_slice_d_grouped(c->sg, k, k + 1, st)) return HP3DG_ERR_CUDA;
+    return HP3DG_OK;
+  }
   if (stage == 0) {
     launch_orient(B.etype, ne, el, c->d_norder, c->d_nori_e, c->d_nori_f, B.nord_loc, B.n, perm, st);
     launch_geom(ne, B.nvert, el, B.nint, B.n, B.d_wq, B.d_shap, B.d_grad, c->d_xvert, c->d_kappa,
@@ -1056,22 +1191,22 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
   }
   if (B.cond_tc) {
     // Cholesky + explicit inverse in FP64; Y, W = Y^T Y and ASchur on tensor
-    // cores; then S = K_ii - W and the compression
-    CondTcBufs t = B.ctb;
-    t.kbd += (size_t)j0 * t.bytes_a;
-    t.lid += (size_t)j0 * t.bytes_b;
-    t.ltd += (size_t)j0 * t.bytes_b;
-    t.ekb += (size_t)j0 * t.nr;
-    t.eli += (size_t)j0 * t.nbr;
-    t.elt += (size_t)j0 * t.nbr;
-    t.bi += (size_t)j0 * B.ni;
-    if (launch_cond_tc(ne, B.n, B.ni, B.nb, el, c->d_ni_e, c->d_nb_e, PK, b0, perm,
-                       c->d_schur_off, c->d_bub_off, S, c->d_aschur, c->d_bschur, t,
-                       c->d_flags + 1, c->d_flags + 2, st))
+    // cores; then S = K_ii - W and the compression, through the condensation
+    // group's segment of this bin or chunk
+    int k = 0;
+    if (c->bins.size() == 1 && c->nchunk > 1) {
+      while (k < c->nchunk && c->chunk_lo[k] != j0) ++k;
+    } else {
+      k = (int)(&B - c->bins.data());
+    }
+    const int cgk = k < (int)c->cg_index.size() ? c->cg_index[k] : -1;
+    if (cgk < 0) return HP3DG_ERR_STATE;
+    if (launch_cond_tc_group(c->cg, cgk, cgk + 1, c->d_ni_e, c->d_nb_e, c->d_schur_off,
+                             c->d_bub_off, c->d_aschur, c->d_bschur, c->d_flags + 1,
+                             c->d_flags + 2, st))
       return HP3DG_ERR_CUDA;
-    launch_compress(ne, B.n, B.ni, B.nb, el, c->d_ni_e, PK, perm, S, t.bi, c->d_wnextract,
-                    c->d_wlcon_off, c->d_welem_nnz, c->d_zd_off, zd, dm, c->d_zwork, c->d_bwork,
-                    st);
+    launch_compress_group(c->cg, cgk, cgk + 1, c->d_ni_e, c->d_wnextract, c->d_wlcon_off,
+                          c->d_welem_nnz, c->d_zd_off, zd, c->d_zwork, c->d_bwork, st);
     return HP3DG_OK;
   }
   TcFactorOut tco = B.tco;
@@ -1145,19 +1280,57 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
       owner[b] = k;
       load[k] += work[b];
     }
-    if (cudaEventRecord(c->fork_ev, st) != cudaSuccess) return HP3DG_ERR_CUDA;
-    for (int k = 0; k < hp3dg_ctx::NBRANCH; ++k)
-      if (cudaStreamWaitEvent(c->branch[k], c->fork_ev, 0) != cudaSuccess) return HP3DG_ERR_CUDA;
+    auto fork = [&]() -> bool {
+      if (cudaEventRecord(c->fork_ev, st) != cudaSuccess) return false;
+      for (int k = 0; k < hp3dg_ctx::NBRANCH; ++k)
+        if (cudaStreamWaitEvent(c->branch[k], c->fork_ev, 0) != cudaSuccess) return false;
+      return true;
+    };
+    auto join = [&]() -> bool {
+      for (int k = 0; k < hp3dg_ctx::NBRANCH; ++k) {
+        if (cudaEventRecord(c->join_ev[k], c->branch[k]) != cudaSuccess) return false;
+        if (cudaStreamWaitEvent(st, c->join_ev[k], 0) != cudaSuccess) return false;
+      }
+      return true;
+    };
+    const bool mixed = c->opts.precision == HP3DG_MIXED;
+    // Stage 0 (orientation maps, geometry, loads, digit slicing) of every
+    // bin in one launch per kernel over the segment tables (vertex geometry);
+    // in mixed precision the contractions of all bins as one persistent
+    // launch over their joint tile space; the rest per bin on the branches.
+    const bool grouped0 = c->sg.nseg == (int)c->bins.size() && !c->iso;
+    if (grouped0) {
+      launch_stage0_grouped(c->sg, 0, c->sg.nseg, c->d_norder, c->d_nori_e, c->d_nori_f,
+                            c->d_xvert, c->d_kappa, c->opts.isol, c->d_flags, st);
+      if (mixed && launch_slice_d_grouped(c->sg, 0, c->sg.nseg, st)) return HP3DG_ERR_CUDA;
+    } else {
+      if (!fork()) return HP3DG_ERR_CUDA;
+      for (int b : order) {
+        Bin& B = c->bins[b];
+        int rc = enqueue_range(c, B, 0, (int)B.elems.size(), 0, c->branch[owner[b]]);
+        if (rc) return rc;
+      }
+      if (!join()) return HP3DG_ERR_CUDA;
+    }
+    if (mixed) {
+      std::vector<OzakiGemmItem> items;
+      for (int b : order) {
+        Bin& B = c->bins[b];
+        items.push_back({&B.plan, (int)B.elems.size(), B.n * (B.n + 1) / 2, B.d_ddig, B.d_dscale,
+                         B.d_mdig, B.d_mscale, B.d_PK});
+      }
+      if (launch_ozaki_gemm_group(items.data(), (int)items.size(), c->d_flags + 2, st,
+                                  c->opts.fault_inject == 1 ? 1 : 0))
+        return HP3DG_ERR_CUDA;
+    }
+    if (!fork()) return HP3DG_ERR_CUDA;
     for (int b : order)
-      for (int stage = 0; stage < 3; ++stage) {
+      for (int stage = mixed ? 2 : 1; stage < 3; ++stage) {
         Bin& B = c->bins[b];
         int rc = enqueue_range(c, B, 0, (int)B.elems.size(), stage, c->branch[owner[b]]);
         if (rc) return rc;
       }
-    for (int k = 0; k < hp3dg_ctx::NBRANCH; ++k) {
-      if (cudaEventRecord(c->join_ev[k], c->branch[k]) != cudaSuccess) return HP3DG_ERR_CUDA;
-      if (cudaStreamWaitEvent(st, c->join_ev[k], 0) != cudaSuccess) return HP3DG_ERR_CUDA;
-    }
+    if (!join()) return HP3DG_ERR_CUDA;
     // the per-stage timers are not meaningful across branches
     mark(c, 2, st, capturing);
     mark(c, 3, st, capturing);

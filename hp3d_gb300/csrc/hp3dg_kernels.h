@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace hp3dg {
 
 // Raises the dynamic shared-memory limit of a kernel (on the current device)
@@ -35,6 +37,36 @@ void launch_geom(int nel, int nvert, const int* d_elist, int nint, int n, const 
                  const int64_t* d_dof_off = nullptr, const uint32_t* d_perm = nullptr);
 void launch_load_hexa(int nel, int nint, int n, const double* d_shap, const double* d_F,
                       double* d_b0, cudaStream_t st);
+
+// Grouped launches of the per-element stage kernels over several bins: one
+// segment per bin (device arrays built at submit), block offsets per kernel.
+// The per-element arithmetic is the one of the per-bin kernels.
+struct StageSeg {
+  int etype, nvert, n, nint, nel;
+  int full[19];              // bin orders (tet: full[0] = the orientation class)
+  const int* elist;
+  const double *wq, *shap, *grad;
+  double *D, *F, *b0;
+  uint32_t* perm;
+  // mixed precision: the digits of D
+  int K, nk, radix, digits;
+  uint16_t* ddig;
+  double* dscale;
+};
+struct StageGroup {
+  StageSeg* segs = nullptr;  // device
+  int nseg = 0;
+  int *pre_el = nullptr, *pre_geom = nullptr, *pre_dsc = nullptr, *pre_slice = nullptr;  // device
+  std::vector<int> h_pre;    // host copies: [el | geom | dsc | slice] x (nseg + 1)
+  int max_nint = 0;
+};
+// orientation maps, vertex geometry and loads of the group's segments k0..k1-1
+// (one launch per kernel)
+void launch_stage0_grouped(const StageGroup& g, int k0, int k1, const int* d_norder,
+                           const int* d_nori_e, const int* d_nori_f, const double* d_xvert,
+                           const double* d_kappa, int isol, int* d_bad, cudaStream_t st);
+// row scales and digit tiles of D of the segments k0..k1-1 (mixed)
+int launch_slice_d_grouped(const StageGroup& g, int k0, int k1, cudaStream_t st);
 void launch_contract_fp64(int nel, int nint, int n, int ni, int nb, const double* d_grad,
                           const double* d_D, double* d_PK, cudaStream_t st);
 size_t condense_smem(int ni, int nb);
@@ -76,6 +108,50 @@ struct CondTcBufs {
   int nr = 0, nbr = 0, nkb = 0, digits = 0, radix = 0;
   size_t bytes_a = 0, bytes_b = 0;                          // per element
 };
+// Grouped launches of the fused condensation (k_cond_chol, k_cond_kbi,
+// k_cond_tc, k_compress) over several bins or element chunks: one segment
+// each, tables built once per batch; an element's arithmetic is the same in
+// any batch.
+struct CondSegIn {
+  int nfull, nif, nbf, nel;
+  const int* elist;
+  const double *PK, *b0;
+  const uint32_t* perm;
+  double* W;             // Schur scratch, nif(nif+1)/2 per element
+  CondTcBufs t;          // digit buffers offset to the segment's first element
+  const uint8_t* dmask;  // Dirichlet mask, nif per element
+};
+struct CompressSeg {
+  int nfull, nif, nbf;
+  const int* elist;
+  const double* PK;
+  const uint32_t* perm;
+  const double* W;
+  const double* bi;
+  const uint8_t* dmask;
+};
+struct CondGroup {
+  void* segs = nullptr;           // device segment table of the fused kernels
+  CompressSeg* csegs = nullptr;   // device
+  int nseg = 0;
+  int *pre_chol = nullptr, *pre_kbi = nullptr, *pre_el = nullptr;  // device block offsets
+  std::vector<int> h_pre;         // host copies: [chol | kbi | el] x (nseg + 1)
+  size_t smem_chol = 0, smem_tc = 0;
+};
+// builds the device tables (allocations appended to *allocs, freed by the caller)
+int cond_tc_group_build(const std::vector<CondSegIn>& in, CondGroup* g,
+                        std::vector<void*>* allocs);
+// Cholesky + inverse, K_bi digits, the fused tensor-core kernel, for the
+// segments k0..k1-1
+int launch_cond_tc_group(const CondGroup& g, int k0, int k1, const int* d_ni_e, const int* d_nb_e,
+                         const int64_t* d_schur_off, const int64_t* d_bub_off, double* d_aschur,
+                         double* d_bschur, int* d_bad_spd, int* d_flag, cudaStream_t st);
+// S = K_ii - W, compression and lift for the segments k0..k1-1
+void launch_compress_group(const CondGroup& g, int k0, int k1, const int* d_ni_e,
+                           const int* d_nextract, const int64_t* d_lcon_off,
+                           const int64_t* d_elem_nnz, const int64_t* d_zd_off,
+                           const double* d_zdofd, double* d_zastif, double* d_zbload,
+                           cudaStream_t st);
 bool cond_tc_supported(int nif, int nbf, int digits);
 void cond_tc_make_out(int nif, int nbf, int radix, int digits, CondTcBufs& b);
 int launch_cond_tc(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
@@ -152,6 +228,21 @@ int ozaki_kchunk(const OzakiPlan& plan);
 int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
                       double* d_PK, int* d_flag, cudaStream_t st, int fault = 0);
+// The contraction of several bins (same radix and digits) in one persistent
+// launch over their joint tile space (split into launches of at most 128
+// bins): out[r, c] = sum_q D[r, q] M[q, c] per bin.
+struct OzakiGemmItem {
+  const OzakiPlan* plan;
+  int nrows;        // elements (rows of D)
+  int ncols_real;   // columns of the output (n(n+1)/2, or a dense plan's nreal)
+  const uint16_t* ddig;
+  const double* dscale;
+  const uint16_t* mdig;
+  const double* mscale;
+  double* out;
+};
+int launch_ozaki_gemm_group(const OzakiGemmItem* items, int nitems, int* d_flag,
+                            cudaStream_t st, int fault = 0);
 
 // the same contraction for a dense bin-constant M (K x ncols, row-major FP64):
 // OUT[r, c] = sum_q D[r, q] M[q, c] for rows r of D (K per row)

@@ -54,6 +54,7 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 namespace hp3dg {
@@ -75,30 +76,55 @@ constexpr int NTHREADS = 64 + 32 * NEPI;     // 576
 constexpr uint32_t TMEM_COLS = 512;
 constexpr int MAXMMA = 16;
 
+// One bin of a grouped launch: its operands, outputs and tile space.
+struct GemmBin {
+  const uint8_t* A;          // M digit tiles
+  const uint8_t* B;          // D digit tiles
+  const double* dscale;
+  const double* mscale;
+  double* PK;
+  int nk;                    // k-blocks
+  int nchunk;                // exact accumulation runs per tile
+  int ncb, neb;              // column / element blocks
+  int nel, ncols;
+  int grp;                   // column blocks per raster group
+  int tile0;                 // first tile of the bin in the launch's tile space
+  int shift0;                // slot s: V += L << (shift0 - radix s), or >> when negative
+  int scale_shift;           // PK = V * 2^(ke + kc - scale_shift)
+};
+constexpr int MAXBINS = 128;
 struct GemmParams {
   int radix, digits, nlev;  // levels 2 .. digits+1 in slots 0 .. nlev-1
-  int nk;                   // k-blocks
   int kchunk;               // k-blocks per exact accumulation run
-  int ncb, neb;             // column / element blocks
-  int nel, ncols;
   int nstage;
-  int grp;                  // column blocks per raster group
-  int shift0;               // slot s: V += L << (shift0 - radix s), or >> when negative
-  int scale_shift;          // PK = V * 2^(ke + kc - scale_shift)
   long wait_limit;          // bounded mbarrier waits (iterations)
   int fault;                // testing: 1 = the producer withholds one stage
   int nmma;                 // MMAs per k-block, in issue order:
   uint32_t mma[MAXMMA];     // A digit i | first B digit j0 << 4 | B digit count << 8
+  int nbins, ntiles;
+  GemmBin bin[MAXBINS];
 };
 }  // namespace
 
-// tile t -> (column block, element block): groups of `grp` column blocks sweep
-// all element blocks, so the M digit strips of a group stay resident in L2.
-__device__ __forceinline__ void tile_coords(int t, const GemmParams& P, int& cb, int& eb) {
-  const int grp = P.grp;
-  int g = t / (grp * P.neb);
-  int r = t - g * grp * P.neb;
-  int gw = P.ncb - g * grp;
+// the bin of tile t (bins in tile order)
+__device__ __forceinline__ int find_bin(const GemmParams& P, int t) {
+  int lo = 0, hi = P.nbins - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (P.bin[mid].tile0 <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// local tile t of bin B -> (column block, element block): groups of `grp`
+// column blocks sweep all element blocks, so the M digit strips of a group
+// stay resident in L2.
+__device__ __forceinline__ void tile_coords(int t, const GemmBin& B, int& cb, int& eb) {
+  const int grp = B.grp;
+  int g = t / (grp * B.neb);
+  int r = t - g * grp * B.neb;
+  int gw = B.ncb - g * grp;
   if (gw > grp) gw = grp;
   cb = g * grp + r % gw;
   eb = r / gw;
@@ -119,10 +145,7 @@ __device__ __forceinline__ int pow2_exponent(double x) {
 // the GEMM
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_ozaki_gemm(const uint8_t* __restrict__ Atiles, const uint8_t* __restrict__ Btiles,
-                 const GemmParams P, const double* __restrict__ dscale,
-                 const double* __restrict__ mscale, double* __restrict__ PK,
-                 int* __restrict__ err) {
+    k_ozaki_gemm(const __grid_constant__ GemmParams P, int* __restrict__ err) {
   extern __shared__ __align__(1024) uint8_t smraw[];
   uint8_t* ring = (uint8_t*)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   __shared__ __align__(8) uint64_t full_bar[MAXSTAGE], empty_bar[MAXSTAGE];
@@ -130,8 +153,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = P.ncb * P.neb;
-  const int nchunk = (P.nk + P.kchunk - 1) / P.kchunk;
+  const int ntiles = P.ntiles;
   const long lim = P.wait_limit;
 
   if (threadIdx.x == 0) {
@@ -165,9 +187,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const uint32_t bytes = (uint32_t)P.digits * (A_TILE + B_TILE);
       bool withheld = false;
       for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
+        const GemmBin& B = P.bin[find_bin(P, t)];
         int cb, eb;
-        tile_coords(t, P, cb, eb);
-        for (int kb = 0; kb < P.nk; ++kb) {
+        tile_coords(t - B.tile0, B, cb, eb);
+        for (int kb = 0; kb < B.nk; ++kb) {
           if (!mbar_wait_n(smem_u32(&empty_bar[stage]), phase ^ 1, &abort_, lim)) {
             abort_ = 1; atomicExch(err, 1); break;
           }
@@ -181,10 +204,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             mbar_expect_tx(fb, bytes);
             uint8_t* st = ring + (size_t)stage * STAGE_BYTES;
             // digits 0..D-1 of (column block, k-block) are contiguous, likewise for B
-            const size_t ablk = ((size_t)cb * P.nk + kb) * P.digits;
-            const size_t bblk = ((size_t)eb * P.nk + kb) * P.digits;
-            bulk_load(smem_u32(st), Atiles + ablk * A_TILE, (uint32_t)P.digits * A_TILE, fb);
-            bulk_load(smem_u32(st + B_OFF), Btiles + bblk * B_TILE, (uint32_t)P.digits * B_TILE, fb);
+            const size_t ablk = ((size_t)cb * B.nk + kb) * P.digits;
+            const size_t bblk = ((size_t)eb * B.nk + kb) * P.digits;
+            bulk_load(smem_u32(st), B.A + ablk * A_TILE, (uint32_t)P.digits * A_TILE, fb);
+            bulk_load(smem_u32(st + B_OFF), B.B + bblk * B_TILE, (uint32_t)P.digits * B_TILE, fb);
             issued |= 1u << stage;
             last_par = (last_par & ~(1u << stage)) | (phase << stage);
           }
@@ -202,9 +225,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       uint32_t phase = 0, accph = 0;
       bool any = false;
       for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
+        const GemmBin& B = P.bin[find_bin(P, t)];
+        const int nk = B.nk, nchunk = B.nchunk;
         for (int ch = 0; ch < nchunk && !abort_; ++ch) {
           const int kc0 = ch * P.kchunk;
-          const int kc1 = (kc0 + P.kchunk) < P.nk ? (kc0 + P.kchunk) : P.nk;
+          const int kc1 = (kc0 + P.kchunk) < nk ? (kc0 + P.kchunk) : nk;
           // the epilogue must have drained the accumulators
           if (!mbar_wait_n(smem_u32(&acc_empty), accph ^ 1, &abort_, lim)) {
             abort_ = 1; atomicExch(err, 2); break;
@@ -278,19 +303,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const uint32_t tlane = tbase + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(eg * EPI_ELEMS);
     uint32_t accph = 0;
     for (int t = blockIdx.x; t < ntiles && !abort_; t += gridDim.x) {
+      const GemmBin& B = P.bin[find_bin(P, t)];
       int cb, eb;
-      tile_coords(t, P, cb, eb);
+      tile_coords(t - B.tile0, B, cb, eb);
       const int c = cb * BM + row;
-      const bool cok = c < P.ncols;
-      const int kc = cok ? pow2_exponent(mscale[c]) : 0;
+      const bool cok = c < B.ncols;
       const int e0 = eb * BN + eg * EPI_ELEMS;
       const int el = e0 + (lane & 15);
-      const int ke_lane = (el < P.nel) ? pow2_exponent(dscale[el]) : 0;
+      // exponents of the element scale (of element lane & 15) and of this
+      // lane's column scale, less the recombination shift
+      const int ke_lane = (el < B.nel) ? pow2_exponent(B.dscale[el]) : 0;
+      const int kcs = (cok ? pow2_exponent(B.mscale[c]) : 0) - B.scale_shift;
       long long V[EPI_ELEMS];
 #pragma unroll
       for (int q = 0; q < EPI_ELEMS; ++q) V[q] = 0;
       bool ok = true;
-      for (int ch = 0; ch < nchunk; ++ch) {
+      for (int ch = 0; ch < B.nchunk; ++ch) {
         if (!mbar_wait_n(smem_u32(&acc_full), accph, &abort_, lim)) {
           abort_ = 1; atomicExch(err, 4); ok = false; break;
         }
@@ -299,7 +327,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int s = 0; s < P.nlev; ++s) {
           uint32_t v[EPI_ELEMS];
           tmem_ld16(tlane + (uint32_t)(s * BN), v);
-          const int sh = P.shift0 - P.radix * s;
+          const int sh = B.shift0 - P.radix * s;
           if (sh >= 0) {
 #pragma unroll
             for (int q = 0; q < EPI_ELEMS; ++q)
@@ -315,11 +343,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (lane == 0) mbar_arrive(smem_u32(&acc_empty));
       }
       if (!ok) break;
+      double* PK = B.PK;
+      const int nel = B.nel, ncols = B.ncols;
 #pragma unroll
       for (int q = 0; q < EPI_ELEMS; ++q) {
         const int ke = __shfl_sync(0xffffffffu, ke_lane, q);
         const int e = e0 + q;
-        if (cok && e < P.nel) PK[(size_t)e * P.ncols + c] = scaled_i64(V[q], ke + kc - P.scale_shift);
+        if (cok && e < nel) PK[(size_t)e * ncols + c] = scaled_i64(V[q], ke + kcs);
       }
     }
   }
@@ -405,8 +435,8 @@ __global__ void k_m_scale(int nint, int n, int ni, int nb, int ncols, int ncols_
 }
 
 // row scales of D: 2^ceil(log2 max_q |D[e,q]|); one block per element row
-__global__ void k_d_scale(int K, int nel, const double* __restrict__ D, double* __restrict__ dscale) {
-  int e = blockIdx.x;
+__device__ __forceinline__ void d_scale_row(int e, int K, int nel, const double* __restrict__ D,
+                                            double* __restrict__ dscale) {
   __shared__ double red[256];
   double mx = 0.0;
   if (e < nel)
@@ -418,6 +448,10 @@ __global__ void k_d_scale(int K, int nel, const double* __restrict__ D, double* 
     __syncthreads();
   }
   if (threadIdx.x == 0) dscale[e] = (e < nel) ? pow2_ceil_scale(red[0]) : 1.0;
+}
+
+__global__ void k_d_scale(int K, int nel, const double* __restrict__ D, double* __restrict__ dscale) {
+  d_scale_row(blockIdx.x, K, nel, D, dscale);
 }
 
 // digits of 8 consecutive values -> one 16-byte core-matrix row per digit
@@ -494,10 +528,10 @@ __global__ void k_build_m_dense(int K, int ncols, int nk, int radix, int digits,
 }
 
 // D digit tiles: grid (k-blocks, 64-element blocks), 128 threads = 64 rows x 2 q-groups
-__global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
-                          const double* __restrict__ D, const double* __restrict__ dscale,
-                          uint8_t* __restrict__ ddig) {
-  const int kb = blockIdx.x, eb = blockIdx.y;
+__device__ __forceinline__ void slice_d_tile(int kb, int eb, int K, int nk, int nel, int radix,
+                                             int digits, const double* __restrict__ D,
+                                             const double* __restrict__ dscale,
+                                             uint8_t* __restrict__ ddig) {
   const int r = threadIdx.x >> 1, kg = threadIdx.x & 1;
   const int e = eb * BN + r;
   double vals[8];
@@ -508,6 +542,40 @@ __global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
   }
   double rs = (e < nel) ? 1.0 / dscale[e] : 0.0;
   write_digits8(vals, rs, radix, digits, ddig, nk, eb, kb, r, kg, B_TILE);
+}
+
+__global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
+                          const double* __restrict__ D, const double* __restrict__ dscale,
+                          uint8_t* __restrict__ ddig) {
+  slice_d_tile(blockIdx.x, blockIdx.y, K, nk, nel, radix, digits, D, dscale, ddig);
+}
+
+// the same over the bins of a group: one block per (padded) element row, and
+// one per (k-block, 64-element block) of each bin
+__device__ __forceinline__ int group_seg(const int* __restrict__ pre, int nseg, int b) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+__global__ void k_d_scale_grp(const StageSeg* __restrict__ segs, const int* __restrict__ pre,
+                              int nseg, int off) {
+  const int blk = blockIdx.x + off;
+  const int s = group_seg(pre, nseg, blk);
+  const StageSeg& G = segs[s];
+  d_scale_row(blk - pre[s], G.K, G.nel, G.D, G.dscale);
+}
+__global__ void k_slice_d_grp(const StageSeg* __restrict__ segs, const int* __restrict__ pre,
+                              int nseg, int off) {
+  const int blk = blockIdx.x + off;
+  const int s = group_seg(pre, nseg, blk);
+  const StageSeg& G = segs[s];
+  const int loc = blk - pre[s];
+  slice_d_tile(loc % G.nk, loc / G.nk, G.K, G.nk, G.nel, G.radix, G.digits, G.D, G.dscale,
+               (uint8_t*)G.ddig);
 }
 
 // ---------------------------------------------------------------------------
@@ -565,6 +633,16 @@ int launch_ozaki_slice_d(const OzakiPlan& p, int nel, int nint, const double* d_
   dim3 g(p.kdim / BK, nel_pad / BN);
   k_slice_d<<<g, 2 * BN, 0, st>>>(6 * nint, p.kdim / BK, nel, p.radix, p.digits, d_D, d_dscale,
                                   (uint8_t*)d_ddig);
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+int launch_slice_d_grouped(const StageGroup& g, int k0, int k1, cudaStream_t st) {
+  if (k1 <= k0) return 0;
+  const int* h = g.h_pre.data();
+  const int ns = g.nseg + 1;
+  const int d0 = h[2 * ns + k0], d1 = h[2 * ns + k1], s0 = h[3 * ns + k0], s1 = h[3 * ns + k1];
+  if (d1 > d0) k_d_scale_grp<<<d1 - d0, 256, 0, st>>>(g.segs, g.pre_dsc, g.nseg, d0);
+  if (s1 > s0) k_slice_d_grp<<<s1 - s0, 2 * BN, 0, st>>>(g.segs, g.pre_slice, g.nseg, s0);
   return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
@@ -652,7 +730,7 @@ static void build_mma_order(int D, GemmParams* G) {
   }
 }
 
-// Exactness and recombination parameters of a plan (see the file header).
+// Exactness parameters shared by every bin of a plan's digits (file header).
 static void build_params(const OzakiPlan& p, GemmParams* G) {
   memset(G, 0, sizeof(*G));
   const int R = p.radix, D = p.digits, S = D + 1;
@@ -674,15 +752,34 @@ static void build_params(const OzakiPlan& p, GemmParams* G) {
   kchunk = kchunk / KGROUP * KGROUP;
   G->kchunk = kchunk < KGROUP ? KGROUP : kchunk;
   // (a kchunk of KGROUP always satisfies the bound for R <= 8: 2 * 16 * 147456 < 2^24)
-  const int nk = p.kdim / BK;
-  const int nchunk = (nk + G->kchunk - 1) / G->kchunk;
+  build_mma_order(D, G);
+}
+
+// One bin's tile space and recombination shifts.
+static void build_bin(const OzakiGemmItem& it, int kchunk, GemmBin* b) {
+  const OzakiPlan& p = *it.plan;
+  const int R = p.radix, D = p.digits, S = D + 1;
+  b->A = (const uint8_t*)it.mdig;
+  b->B = (const uint8_t*)it.ddig;
+  b->dscale = it.dscale;
+  b->mscale = it.mscale;
+  b->PK = it.out;
+  b->nk = p.kdim / BK;
+  b->nchunk = (b->nk + kchunk - 1) / kchunk;
+  b->ncb = p.ncols / BM;
+  b->neb = round_up(it.nrows, BN) / BN;
+  b->nel = it.nrows;
+  b->ncols = it.ncols_real;
+  // raster groups whose M digit strips take about 48 MB of L2
+  const double strip = (double)b->nk * D * A_TILE;
+  const int grp = (int)(48.0 * 1024 * 1024 / strip);
+  b->grp = grp < 1 ? 1 : (grp > b->ncb ? b->ncb : grp);
   // V = sum over runs and levels of L_s 2^(R(S-s) - t) stays below 2^62
-  const double vmax = log2((double)nchunk) + 24.0 + R * (D - 1) - log2(1.0 - ldexp(1.0, -R));
+  const double vmax = log2((double)b->nchunk) + 24.0 + R * (D - 1) - log2(1.0 - ldexp(1.0, -R));
   int t = (int)ceil(vmax - 62.0);
   if (t < 0) t = 0;
-  G->shift0 = R * (S - 2) - t;
-  G->scale_shift = R * S - t;
-  build_mma_order(D, G);
+  b->shift0 = R * (S - 2) - t;
+  b->scale_shift = R * S - t;
 }
 
 int ozaki_pairs(const OzakiPlan& p) {
@@ -693,65 +790,77 @@ int ozaki_pairs(const OzakiPlan& p) {
 }
 
 int ozaki_kchunk(const OzakiPlan& p) {
-  GemmParams G;
-  build_params(p, &G);
-  return G.kchunk;
+  GemmParams* G = new GemmParams;
+  build_params(p, G);
+  const int k = G->kchunk;
+  delete G;
+  return k;
 }
 
-static int ozaki_gemm_cols(const OzakiPlan& p, int nel, int ncols_real, const uint16_t* d_ddig,
-                           const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                           double* d_PK, int* d_flag, cudaStream_t st, int fault);
-
-int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig,
-                      const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                      double* d_PK, int* d_flag, cudaStream_t st, int fault) {
-  return ozaki_gemm_cols(p, nel, n * (n + 1) / 2, d_ddig, d_dscale, d_mdig, d_mscale, d_PK, d_flag,
-                         st, fault);
-}
-
-int launch_ozaki_gemm_dense(const OzakiPlan& p, int nrows, const uint16_t* d_ddig,
-                            const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                            double* d_out, int* d_flag, cudaStream_t st) {
-  return ozaki_gemm_cols(p, nrows, p.nreal, d_ddig, d_dscale, d_mdig, d_mscale, d_out, d_flag, st,
-                         0);
-}
-
-static int ozaki_gemm_cols(const OzakiPlan& p, int nel, int ncols_real, const uint16_t* d_ddig,
-                           const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                           double* d_PK, int* d_flag, cudaStream_t st, int fault) {
-  if (nel <= 0) return 0;
+int launch_ozaki_gemm_group(const OzakiGemmItem* items, int nitems, int* d_flag,
+                            cudaStream_t st, int fault) {
+  std::vector<int> order;
+  for (int k = 0; k < nitems; ++k)
+    if (items[k].nrows > 0) order.push_back(k);
+  if (order.empty()) return 0;
+  for (int k : order)
+    if (items[k].plan->radix != items[order[0]].plan->radix ||
+        items[k].plan->digits != items[order[0]].plan->digits)
+      return -1;
   int dev = 0, num_sms = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
     return -1;
-  GemmParams G;
-  build_params(p, &G);
-  const int nel_pad = round_up(nel, BN);
-  G.nk = p.kdim / BK;
-  G.ncb = p.ncols / BM;
-  G.neb = nel_pad / BN;
-  G.nel = nel;
-  G.ncols = ncols_real;
-  // raster groups whose M digit strips take about 48 MB of L2
-  const double strip = (double)G.nk * p.digits * A_TILE;
-  int grp = (int)(48.0 * 1024 * 1024 / strip);
-  G.grp = grp < 1 ? 1 : (grp > G.ncb ? G.ncb : grp);
+  // the longest tiles (most k-blocks) first, so the persistent CTAs end together
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return items[a].plan->kdim > items[b].plan->kdim;
+  });
+  std::vector<GemmParams> groups;  // one launch per MAXBINS bins
+  GemmParams* G = new GemmParams;
+  build_params(*items[order[0]].plan, G);
   // as many ring stages as fit next to the static shared memory (barriers)
-  int nst = (optin - 1024 - 1024) / STAGE_BYTES;
-  G.nstage = nst > MAXSTAGE ? MAXSTAGE : nst;
-  if (G.nstage < KGROUP + 1) return -1;
-  G.fault = fault;
+  const int nst = (optin - 1024 - 1024) / STAGE_BYTES;
+  G->nstage = nst > MAXSTAGE ? MAXSTAGE : nst;
+  if (G->nstage < KGROUP + 1) { delete G; return -1; }
+  G->fault = fault;
   // bounded waits: about a second or more at the normal limit; a fault test
   // runs out quickly
-  G.wait_limit = fault ? (1L << 14) : TC_WAIT_LIMIT;
-  const size_t smem = (size_t)G.nstage * STAGE_BYTES + 1024;
-  if (raise_smem_limit((const void*)k_ozaki_gemm, smem) != cudaSuccess) return -1;
-  const int ntiles = G.ncb * G.neb;
-  const int grid = ntiles < num_sms ? ntiles : num_sms;
-  k_ozaki_gemm<<<grid, NTHREADS, smem, st>>>((const uint8_t*)d_mdig, (const uint8_t*)d_ddig, G,
-                                              d_dscale, d_mscale, d_PK, d_flag);
-  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+  G->wait_limit = fault ? (1L << 14) : TC_WAIT_LIMIT;
+  const size_t smem = (size_t)G->nstage * STAGE_BYTES + 1024;
+  if (raise_smem_limit((const void*)k_ozaki_gemm, smem) != cudaSuccess) { delete G; return -1; }
+  int rc = 0;
+  for (size_t k0 = 0; k0 < order.size() && rc == 0; k0 += MAXBINS) {
+    const size_t k1 = std::min(order.size(), k0 + (size_t)MAXBINS);
+    G->nbins = (int)(k1 - k0);
+    int tiles = 0;
+    for (size_t k = k0; k < k1; ++k) {
+      GemmBin& b = G->bin[k - k0];
+      build_bin(items[order[k]], G->kchunk, &b);
+      b.tile0 = tiles;
+      tiles += b.ncb * b.neb;
+    }
+    G->ntiles = tiles;
+    const int grid = tiles < num_sms ? tiles : num_sms;
+    k_ozaki_gemm<<<grid, NTHREADS, smem, st>>>(*G, d_flag);
+    if (cudaPeekAtLastError() != cudaSuccess) rc = -1;
+  }
+  delete G;
+  return rc;
+}
+
+int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig,
+                      const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                      double* d_PK, int* d_flag, cudaStream_t st, int fault) {
+  OzakiGemmItem it{&p, nel, n * (n + 1) / 2, d_ddig, d_dscale, d_mdig, d_mscale, d_PK};
+  return launch_ozaki_gemm_group(&it, 1, d_flag, st, fault);
+}
+
+int launch_ozaki_gemm_dense(const OzakiPlan& p, int nrows, const uint16_t* d_ddig,
+                            const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
+                            double* d_out, int* d_flag, cudaStream_t st) {
+  OzakiGemmItem it{&p, nrows, p.nreal, d_ddig, d_dscale, d_mdig, d_mscale, d_out};
+  return launch_ozaki_gemm_group(&it, 1, d_flag, st, 0);
 }
 
 }  // namespace hp3dg

@@ -217,21 +217,11 @@ __device__ __forceinline__ void geom_point(int e, int j, int l, int nint, const 
   F[(size_t)j * nint + l] = getf_dev(isol, X[0], X[1], X[2]) * weight;
 }
 
+// x and dx/dxi at point l from the NV vertex functions of the bin tables
 template <int NV>
-__global__ void k_geom(int nel, const int* __restrict__ elist, int nint, int n,
-                            const double* __restrict__ wq, const double* __restrict__ tab_shap,
-                            const double* __restrict__ tab_grad, const double* __restrict__ xvert,
-                            const double* __restrict__ kappa, int isol, double* __restrict__ D,
-                            double* __restrict__ F, int* __restrict__ bad) {
-  int j = blockIdx.y;
-  int e = elist[j];
-  __shared__ double xv[24];
-  if (threadIdx.x < 24) xv[threadIdx.x] = xvert[(size_t)e * 24 + threadIdx.x];
-  __syncthreads();
-  int l = blockIdx.x * blockDim.x + threadIdx.x;
-  if (l >= nint) return;
-  double dx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // dx[i][c] = d x_i / d xi_c
-  double X[3] = {0, 0, 0};
+__device__ __forceinline__ void vertex_map(int l, int n, const double* __restrict__ tab_shap,
+                                           const double* __restrict__ tab_grad, const double* xv,
+                                           double (&dx)[3][3], double (&X)[3]) {
   const double* gs = tab_shap + (size_t)l * n;
   const double* gg = tab_grad + (size_t)l * 3 * n;
 #pragma unroll
@@ -247,6 +237,24 @@ __global__ void k_geom(int nel, const int* __restrict__ elist, int nint, int n,
       dx[i][2] += xi_ * g2;
     }
   }
+}
+
+template <int NV>
+__global__ void k_geom(int nel, const int* __restrict__ elist, int nint, int n,
+                            const double* __restrict__ wq, const double* __restrict__ tab_shap,
+                            const double* __restrict__ tab_grad, const double* __restrict__ xvert,
+                            const double* __restrict__ kappa, int isol, double* __restrict__ D,
+                            double* __restrict__ F, int* __restrict__ bad) {
+  int j = blockIdx.y;
+  int e = elist[j];
+  __shared__ double xv[24];
+  if (threadIdx.x < 24) xv[threadIdx.x] = xvert[(size_t)e * 24 + threadIdx.x];
+  __syncthreads();
+  int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= nint) return;
+  double dx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};  // dx[i][c] = d x_i / d xi_c
+  double X[3] = {0, 0, 0};
+  vertex_map<NV>(l, n, tab_shap, tab_grad, xv, dx, X);
   geom_point(e, j, l, nint, dx, X, wq, kappa, isol, D, F, bad);
 }
 
@@ -319,10 +327,9 @@ void launch_geom(int nel, int nvert, const int* d_elist, int nint, int n, const 
 }
 
 // b0[j][k] = sum_l shap[l][k] F[j][l]   (reference enumeration)
-__global__ void k_load_hexa(int nint, int n, const double* __restrict__ tab_shap,
-                            const double* __restrict__ F, double* __restrict__ b0) {
-  int j = blockIdx.x;
-  extern __shared__ double fs[];
+__device__ __forceinline__ void load_elem(int j, int nint, int n, const double* __restrict__ tab_shap,
+                                          const double* __restrict__ F, double* __restrict__ b0,
+                                          double* fs) {
   for (int l = threadIdx.x; l < nint; l += blockDim.x) fs[l] = F[(size_t)j * nint + l];
   __syncthreads();
   for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -332,9 +339,111 @@ __global__ void k_load_hexa(int nint, int n, const double* __restrict__ tab_shap
   }
 }
 
+__global__ void k_load_hexa(int nint, int n, const double* __restrict__ tab_shap,
+                            const double* __restrict__ F, double* __restrict__ b0) {
+  extern __shared__ double fs[];
+  load_elem(blockIdx.x, nint, n, tab_shap, F, b0, fs);
+}
+
 void launch_load_hexa(int nel, int nint, int n, const double* d_shap, const double* d_F,
                       double* d_b0, cudaStream_t st) {
   if (nel > 0) k_load_hexa<<<nel, 256, nint * sizeof(double), st>>>(nint, n, d_shap, d_F, d_b0);
+}
+
+// ---------------------------------------------------------------------------
+// grouped launches: the per-element stage kernels of many bins in one launch
+// ---------------------------------------------------------------------------
+// The segment (bin) of block b: pre holds nseg + 1 block offsets.
+__device__ __forceinline__ int seg_of(const int* __restrict__ pre, int nseg, int b) {
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// orientation maps of every element of every bin: one block per element
+__global__ void k_orient_grp(const StageSeg* __restrict__ segs, const int* __restrict__ pre,
+                             int nseg, int off, const int* __restrict__ norder,
+                             const int* __restrict__ nori_e, const int* __restrict__ nori_f) {
+  const int blk = blockIdx.x + off;
+  const int s = seg_of(pre, nseg, blk);
+  const StageSeg& G = segs[s];
+  const int j = blk - pre[s];
+  const int e = G.elist[j];
+  __shared__ int no[19], oe[12], of[6];
+  if (threadIdx.x < 19) no[threadIdx.x] = norder[19 * e + threadIdx.x];
+  if (threadIdx.x < 12) oe[threadIdx.x] = nori_e[12 * e + threadIdx.x];
+  if (threadIdx.x < 6) of[threadIdx.x] = nori_f[6 * e + threadIdx.x];
+  __syncthreads();
+  const int nfull = G.n;
+  uint32_t* perm = G.perm + (size_t)j * nfull;
+  if (G.etype == ETYPE_TET) {
+    const int n = tet_ndof(no);
+    for (int a = threadIdx.x; a < nfull; a += blockDim.x)
+      perm[a] = a < n ? tet_dof_map(a, no, oe, of, G.full[0]) : 0u;
+  } else if (G.etype == ETYPE_PRISM) {
+    const int n = prism_ndof(no);
+    for (int a = threadIdx.x; a < nfull; a += blockDim.x)
+      perm[a] = a < n ? prism_dof_map(a, no, oe, of, G.full) : 0u;
+  } else {
+    const int n = hexa_ndof(no);
+    for (int a = threadIdx.x; a < nfull; a += blockDim.x)
+      perm[a] = a < n ? hexa_dof_map(a, no, oe, of, G.full) : 0u;
+  }
+}
+
+// geometry (vertex maps): ceil(nint / 128) blocks of 128 points per element
+__global__ void k_geom_grp(const StageSeg* __restrict__ segs, const int* __restrict__ pre, int nseg,
+                           int off, const double* __restrict__ xvert,
+                           const double* __restrict__ kappa, int isol, int* __restrict__ bad) {
+  const int blk = blockIdx.x + off;
+  const int s = seg_of(pre, nseg, blk);
+  const StageSeg& G = segs[s];
+  const int nbx = (G.nint + 127) / 128;
+  const int loc = blk - pre[s];
+  const int j = loc / nbx, bx = loc - j * nbx;
+  const int e = G.elist[j];
+  __shared__ double xv[24];
+  if (threadIdx.x < 24) xv[threadIdx.x] = xvert[(size_t)e * 24 + threadIdx.x];
+  __syncthreads();
+  const int l = bx * blockDim.x + threadIdx.x;
+  if (l >= G.nint) return;
+  double dx[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  double X[3] = {0, 0, 0};
+  if (G.nvert == 4) vertex_map<4>(l, G.n, G.shap, G.grad, xv, dx, X);
+  else if (G.nvert == 6) vertex_map<6>(l, G.n, G.shap, G.grad, xv, dx, X);
+  else vertex_map<8>(l, G.n, G.shap, G.grad, xv, dx, X);
+  geom_point(e, j, l, G.nint, dx, X, G.wq, kappa, isol, G.D, G.F, bad);
+}
+
+// loads: one block per element, the element's F in shared memory
+__global__ void k_load_grp(const StageSeg* __restrict__ segs, const int* __restrict__ pre,
+                           int nseg, int off) {
+  extern __shared__ double fs[];
+  const int blk = blockIdx.x + off;
+  const int s = seg_of(pre, nseg, blk);
+  const StageSeg& G = segs[s];
+  load_elem(blk - pre[s], G.nint, G.n, G.shap, G.F, G.b0, fs);
+}
+
+void launch_stage0_grouped(const StageGroup& g, int k0, int k1, const int* d_norder,
+                           const int* d_nori_e, const int* d_nori_f, const double* d_xvert,
+                           const double* d_kappa, int isol, int* d_bad, cudaStream_t st) {
+  if (k1 <= k0) return;
+  const int* h = g.h_pre.data();  // host copies: [el | geom | dsc | slice] x (nseg + 1)
+  const int ns = g.nseg + 1;
+  const int el0 = h[k0], el1 = h[k1], ge0 = h[ns + k0], ge1 = h[ns + k1];
+  if (el1 > el0) {
+    k_orient_grp<<<el1 - el0, 128, 0, st>>>(g.segs, g.pre_el, g.nseg, el0, d_norder, d_nori_e,
+                                            d_nori_f);
+    k_geom_grp<<<ge1 - ge0, 128, 0, st>>>(g.segs, g.pre_geom, g.nseg, ge0, d_xvert, d_kappa, isol,
+                                          d_bad);
+    k_load_grp<<<el1 - el0, 256, (size_t)g.max_nint * sizeof(double), st>>>(g.segs, g.pre_el,
+                                                                            g.nseg, el0);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -702,14 +811,14 @@ int launch_condense(int nel, int nfull, int nif, int nbf, const int* d_elist, co
 // compression after the tensor-core Schur update: one block per element.
 // S = K_ii - W is formed in place (K_ii gathered through the dof map), then
 // compressed as in the FP64 path.
-__global__ void __launch_bounds__(CND_THREADS) k_compress(
-    int nfull, int nif, int nbf, const int* __restrict__ elist, const int* __restrict__ ni_e,
+__device__ __forceinline__ void compress_elem(
+    int j, int nfull, int nif, int nbf, const int* __restrict__ elist, const int* __restrict__ ni_e,
     const double* __restrict__ PK, const uint32_t* __restrict__ perm, double* __restrict__ Wbuf,
     const double* __restrict__ Bi, const int* __restrict__ nextract,
     const int64_t* __restrict__ lcon_off, const int64_t* __restrict__ elem_nnz,
     const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
     const uint8_t* __restrict__ dmask, double* __restrict__ zastif, double* __restrict__ zbload) {
-  const int j = blockIdx.x, e = elist[j];
+  const int e = elist[j];
   const int ni = ni_e[e];
   const double* PKj = PK + (size_t)j * ((size_t)nfull * (nfull + 1) / 2);
   const uint32_t* pm = perm + (size_t)j * nfull;
@@ -723,6 +832,45 @@ __global__ void __launch_bounds__(CND_THREADS) k_compress(
   __syncthreads();
   compress_out(e, j, ni, nif, S, Bi + (size_t)j * nif, nextract, lcon_off, elem_nnz, zd_off, zdofd,
                dmask, zastif, zbload);
+}
+
+__global__ void __launch_bounds__(CND_THREADS) k_compress(
+    int nfull, int nif, int nbf, const int* __restrict__ elist, const int* __restrict__ ni_e,
+    const double* __restrict__ PK, const uint32_t* __restrict__ perm, double* __restrict__ Wbuf,
+    const double* __restrict__ Bi, const int* __restrict__ nextract,
+    const int64_t* __restrict__ lcon_off, const int64_t* __restrict__ elem_nnz,
+    const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
+    const uint8_t* __restrict__ dmask, double* __restrict__ zastif, double* __restrict__ zbload) {
+  compress_elem(blockIdx.x, nfull, nif, nbf, elist, ni_e, PK, perm, Wbuf, Bi, nextract, lcon_off,
+                elem_nnz, zd_off, zdofd, dmask, zastif, zbload);
+}
+
+// the same over the segments of a condensation group: one block per element
+__global__ void __launch_bounds__(CND_THREADS) k_compress_grp(
+    const CompressSeg* __restrict__ segs, const int* __restrict__ pre, int nseg, int off,
+    const int* __restrict__ ni_e, const int* __restrict__ nextract,
+    const int64_t* __restrict__ lcon_off, const int64_t* __restrict__ elem_nnz,
+    const int64_t* __restrict__ zd_off, const double* __restrict__ zdofd,
+    double* __restrict__ zastif, double* __restrict__ zbload) {
+  const int blk = blockIdx.x + off;
+  const int s = seg_of(pre, nseg, blk);
+  const CompressSeg& G = segs[s];
+  compress_elem(blk - pre[s], G.nfull, G.nif, G.nbf, G.elist, ni_e, G.PK, G.perm, (double*)G.W,
+                G.bi, nextract, lcon_off, elem_nnz, zd_off, zdofd, G.dmask, zastif, zbload);
+}
+
+void launch_compress_group(const CondGroup& g, int k0, int k1, const int* d_ni_e,
+                           const int* d_nextract, const int64_t* d_lcon_off,
+                           const int64_t* d_elem_nnz, const int64_t* d_zd_off,
+                           const double* d_zdofd, double* d_zastif, double* d_zbload,
+                           cudaStream_t st) {
+  if (k1 <= k0) return;
+  const int ns = g.nseg + 1;
+  const int e0 = g.h_pre[2 * ns + k0], e1 = g.h_pre[2 * ns + k1];
+  if (e1 > e0)
+    k_compress_grp<<<e1 - e0, CND_THREADS, 0, st>>>(g.csegs, g.pre_el, g.nseg, e0, d_ni_e,
+                                                    d_nextract, d_lcon_off, d_elem_nnz, d_zd_off,
+                                                    d_zdofd, d_zastif, d_zbload);
 }
 
 void launch_compress(int nel, int nfull, int nif, int nbf, const int* d_elist, const int* d_ni_e,
