@@ -585,8 +585,10 @@ int build_stage_group(hp3dg_ctx* c) {
   // the fused condensation's segments: the same units, where the bin uses it
   std::vector<CondSegIn> cin;
   c->cg_index.assign(G.nseg, -1);
-  auto cadd = [&](int unit, Bin& B, int j0, int j1) {
-    if (!B.cond_tc) return;
+  // (multi-bin batches: bins without bubbles follow, condensed by the
+  // compression kernel alone)
+  auto cadd = [&](int unit, Bin& B, int j0, int j1, bool plain) {
+    if (plain ? B.nb != 0 : !B.cond_tc) return;
     const size_t nsu = (size_t)B.ni * (B.ni + 1) / 2, npk = (size_t)B.n * (B.n + 1) / 2;
     CondSegIn q;
     q.nfull = B.n; q.nif = B.ni; q.nbf = B.nb; q.nel = j1 - j0;
@@ -597,6 +599,12 @@ int build_stage_group(hp3dg_ctx* c) {
     q.W = B.d_S + (size_t)j0 * nsu;
     q.dmask = B.d_dmask + (size_t)j0 * B.ni;
     CondTcBufs t = B.ctb;
+    if (plain) {
+      q.t = CondTcBufs{};
+      c->cg_index[unit] = (int)cin.size();
+      cin.push_back(q);
+      return;
+    }
     t.kbd += (size_t)j0 * t.bytes_a;
     t.lid += (size_t)j0 * t.bytes_b;
     t.ltd += (size_t)j0 * t.bytes_b;
@@ -608,11 +616,16 @@ int build_stage_group(hp3dg_ctx* c) {
     c->cg_index[unit] = (int)cin.size();
     cin.push_back(q);
   };
-  if (c->bins.size() == 1 && c->nchunk > 1)
-    for (int k = 0; k < c->nchunk; ++k) cadd(k, c->bins[0], c->chunk_lo[k], c->chunk_lo[k + 1]);
-  else
+  if (c->bins.size() == 1 && c->nchunk > 1) {
+    for (int k = 0; k < c->nchunk; ++k)
+      cadd(k, c->bins[0], c->chunk_lo[k], c->chunk_lo[k + 1], false);
+  } else {
     for (size_t b = 0; b < c->bins.size(); ++b)
-      cadd((int)b, c->bins[b], 0, (int)c->bins[b].elems.size());
+      cadd((int)b, c->bins[b], 0, (int)c->bins[b].elems.size(), false);
+    if (c->bins.size() > 1)
+      for (size_t b = 0; b < c->bins.size(); ++b)
+        cadd((int)b, c->bins[b], 0, (int)c->bins[b].elems.size(), true);
+  }
   if (!cin.empty()) {
     const int rc = cond_tc_group_build(cin, &c->cg, &c->cbufs);
     if (rc == -1) return HP3DG_ERR_ALLOC;
@@ -1324,13 +1337,31 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
         return HP3DG_ERR_CUDA;
     }
     if (!fork()) return HP3DG_ERR_CUDA;
+    // the condensation of every bin in the condensation group (the
+    // tensor-core path, and bins without bubbles): one launch per kernel, on
+    // the main stream beside the branches that condense the other bins (in
+    // FP64 after them, once every bin's contraction is done)
+    const bool grouped2 = c->cg.nseg > 0;
+    auto cond_group = [&]() -> int {
+      const double* zd = c->have_zdofd ? c->d_zdofd : nullptr;
+      if (launch_cond_tc_group(c->cg, 0, c->cg.ntc, c->d_ni_e, c->d_nb_e, c->d_schur_off,
+                               c->d_bub_off, c->d_aschur, c->d_bschur, c->d_flags + 1,
+                               c->d_flags + 2, st))
+        return HP3DG_ERR_CUDA;
+      launch_compress_group(c->cg, 0, c->cg.nseg, c->d_ni_e, c->d_wnextract, c->d_wlcon_off,
+                            c->d_welem_nnz, c->d_zd_off, zd, c->d_zwork, c->d_bwork, st);
+      return HP3DG_OK;
+    };
+    if (grouped2 && mixed && cond_group()) return HP3DG_ERR_CUDA;
     for (int b : order)
       for (int stage = mixed ? 2 : 1; stage < 3; ++stage) {
         Bin& B = c->bins[b];
+        if (grouped2 && stage == 2 && c->cg_index[b] >= 0) continue;
         int rc = enqueue_range(c, B, 0, (int)B.elems.size(), stage, c->branch[owner[b]]);
         if (rc) return rc;
       }
     if (!join()) return HP3DG_ERR_CUDA;
+    if (grouped2 && !mixed && cond_group()) return HP3DG_ERR_CUDA;
     // the per-stage timers are not meaningful across branches
     mark(c, 2, st, capturing);
     mark(c, 3, st, capturing);

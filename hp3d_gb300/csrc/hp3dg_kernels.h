@@ -111,7 +111,8 @@ struct CondTcBufs {
 // Grouped launches of the fused condensation (k_cond_chol, k_cond_kbi,
 // k_cond_tc, k_compress) over several bins or element chunks: one segment
 // each, tables built once per batch; an element's arithmetic is the same in
-// any batch.
+// any batch.  Segments with nbf = 0 (no bubbles: S = K_ii, the condensed load
+// is b_i) come after the tensor-core ones and only enter the compression.
 struct CondSegIn {
   int nfull, nif, nbf, nel;
   const int* elist;
@@ -129,13 +130,17 @@ struct CompressSeg {
   const double* W;
   const double* bi;
   const uint8_t* dmask;
+  const double* b0;  // nbf = 0: the load, b_i gathered through perm
 };
 struct CondGroup {
   void* segs = nullptr;           // device segment table of the fused kernels
   CompressSeg* csegs = nullptr;   // device
   int nseg = 0;
+  int ntc = 0;                    // segments 0..ntc-1 use the tensor-core kernels
+  size_t smem_plain = 0;          // compression of nbf = 0 segments: b_i in shared memory
   int *pre_chol = nullptr, *pre_kbi = nullptr, *pre_el = nullptr;  // device block offsets
   std::vector<int> h_pre;         // host copies: [chol | kbi | el] x (nseg + 1)
+  std::vector<CondSegIn> h_in;    // the segments as built (one-segment launches)
   size_t smem_chol = 0, smem_tc = 0;
 };
 // builds the device tables (allocations appended to *allocs, freed by the caller)

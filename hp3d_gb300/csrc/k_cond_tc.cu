@@ -1000,23 +1000,36 @@ int cond_tc_group_build(const std::vector<CondSegIn>& in, CondGroup* g,
   std::vector<CondSegDev> segs;
   std::vector<CompressSeg> cs;
   std::vector<int> pch{0}, pkb{0}, pel{0};
+  bool plain_seen = false;
   for (const CondSegIn& q : in) {
-    if (!cond_tc_supported(q.nif, q.nbf, q.t.digits) || q.t.digits != COND_TC_DIGITS ||
-        q.t.radix != COND_TC_RADIX)
-      return -2;
     CondSegDev d;
     memset(&d, 0, sizeof(d));
     d.nfull = q.nfull; d.nif = q.nif; d.nbf = q.nbf; d.nel = q.nel;
     d.elist = q.elist; d.PK = q.PK; d.b0 = q.b0; d.perm = q.perm; d.W = q.W;
+    if (q.nbf == 0) {
+      // compression only: no blocks of the tensor-core kernels
+      plain_seen = true;
+      segs.push_back(d);
+      cs.push_back({q.nfull, q.nif, 0, q.elist, q.PK, q.perm, q.W, nullptr, q.dmask, q.b0});
+      pch.push_back(pch.back());
+      pkb.push_back(pkb.back());
+      pel.push_back(pel.back() + q.nel);
+      g->smem_plain = std::max(g->smem_plain, (size_t)q.nif * sizeof(double));
+      continue;
+    }
+    if (plain_seen || !cond_tc_supported(q.nif, q.nbf, q.t.digits) ||
+        q.t.digits != COND_TC_DIGITS || q.t.radix != COND_TC_RADIX)
+      return -2;
     d.o = cond_tc_out(q.t);
     cond_tc_params(q.nif, q.nbf, q.nel, q.t, &d.P);
     segs.push_back(d);
-    cs.push_back({q.nfull, q.nif, q.nbf, q.elist, q.PK, q.perm, q.W, q.t.bi, q.dmask});
+    cs.push_back({q.nfull, q.nif, q.nbf, q.elist, q.PK, q.perm, q.W, q.t.bi, q.dmask, nullptr});
     pch.push_back(pch.back() + (q.nel + CH_WARPS - 1) / CH_WARPS);
     pkb.push_back(pkb.back() + q.nel * ((q.t.nr + 127) / 128));
     pel.push_back(pel.back() + q.nel);
     g->smem_chol = std::max(g->smem_chol, cond_chol_smem(q.nbf));
     g->smem_tc = std::max(g->smem_tc, q.t.bytes_a + q.t.bytes_b + 1024);
+    ++g->ntc;
   }
   auto dput = [&](const void* src, size_t bytes) -> void* {
     void* p = nullptr;
@@ -1036,13 +1049,23 @@ int cond_tc_group_build(const std::vector<CondSegIn>& in, CondGroup* g,
   }
   g->nseg = (int)segs.size();
   for (auto* v : {&pch, &pkb, &pel}) g->h_pre.insert(g->h_pre.end(), v->begin(), v->end());
+  g->h_in = in;
   return 0;
 }
 
 int launch_cond_tc_group(const CondGroup& g, int k0, int k1, const int* d_ni_e, const int* d_nb_e,
                          const int64_t* d_schur_off, const int64_t* d_bub_off, double* d_aschur,
                          double* d_bschur, int* d_bad_spd, int* d_flag, cudaStream_t st) {
+  k1 = std::min(k1, g.ntc);
   if (k1 <= k0) return 0;
+  if (k1 == k0 + 1) {
+    // one bin or chunk: the kernels with the segment's parameters in the
+    // launch arguments (same device bodies and arithmetic as the grouped ones)
+    const CondSegIn& q = g.h_in[k0];
+    return launch_cond_tc(q.nel, q.nfull, q.nif, q.nbf, q.elist, d_ni_e, d_nb_e, q.PK, q.b0,
+                          q.perm, d_schur_off, d_bub_off, q.W, d_aschur, d_bschur, q.t, d_bad_spd,
+                          d_flag, st);
+  }
   const int ns = g.nseg + 1;
   const int* h = g.h_pre.data();
   const int c0 = h[k0], c1 = h[k1], b0 = h[ns + k0], b1 = h[ns + k1];

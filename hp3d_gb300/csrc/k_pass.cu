@@ -855,8 +855,35 @@ __global__ void __launch_bounds__(CND_THREADS) k_compress_grp(
   const int blk = blockIdx.x + off;
   const int s = seg_of(pre, nseg, blk);
   const CompressSeg& G = segs[s];
-  compress_elem(blk - pre[s], G.nfull, G.nif, G.nbf, G.elist, ni_e, G.PK, G.perm, (double*)G.W,
-                G.bi, nextract, lcon_off, elem_nnz, zd_off, zdofd, G.dmask, zastif, zbload);
+  const int j = blk - pre[s];
+  if (G.nbf > 0) {
+    compress_elem(j, G.nfull, G.nif, G.nbf, G.elist, ni_e, G.PK, G.perm, (double*)G.W, G.bi,
+                  nextract, lcon_off, elem_nnz, zd_off, zdofd, G.dmask, zastif, zbload);
+    return;
+  }
+  // no bubbles: S = K_ii and the condensed load b_i, in k_condense's
+  // arithmetic (v - 0.0 with an empty bubble sum, which is v)
+  extern __shared__ double bsm[];
+  const int e = G.elist[j];
+  const int ni = ni_e[e];
+  const double* PKj = G.PK + (size_t)j * ((size_t)G.nfull * (G.nfull + 1) / 2);
+  const uint32_t* pm = G.perm + (size_t)j * G.nfull;
+  const double* bj = G.b0 + (size_t)j * G.nfull;
+  double* S = (double*)G.W + (size_t)j * ((size_t)G.nif * (G.nif + 1) / 2);
+  const int64_t nup = (int64_t)ni * (ni + 1) / 2;
+  for (int64_t idx = threadIdx.x; idx < nup; idx += CND_THREADS) {
+    int a, b;
+    upper_decode(idx, a, b);
+    S[idx] = pk_get(PKj, pm, a, b, G.nif, 0);
+  }
+  for (int a = threadIdx.x; a < ni; a += CND_THREADS) {
+    const uint32_t ma = pm[a];
+    const double v = bj[ma & 0x7fffffffu];
+    bsm[a] = (ma & 0x80000000u) ? -v : v;
+  }
+  __syncthreads();
+  compress_out(e, j, ni, G.nif, S, bsm, nextract, lcon_off, elem_nnz, zd_off, zdofd, G.dmask,
+               zastif, zbload);
 }
 
 void launch_compress_group(const CondGroup& g, int k0, int k1, const int* d_ni_e,
@@ -868,7 +895,7 @@ void launch_compress_group(const CondGroup& g, int k0, int k1, const int* d_ni_e
   const int ns = g.nseg + 1;
   const int e0 = g.h_pre[2 * ns + k0], e1 = g.h_pre[2 * ns + k1];
   if (e1 > e0)
-    k_compress_grp<<<e1 - e0, CND_THREADS, 0, st>>>(g.csegs, g.pre_el, g.nseg, e0, d_ni_e,
+    k_compress_grp<<<e1 - e0, CND_THREADS, g.smem_plain, st>>>(g.csegs, g.pre_el, g.nseg, e0, d_ni_e,
                                                     d_nextract, d_lcon_off, d_elem_nnz, d_zd_off,
                                                     d_zdofd, d_zastif, d_zbload);
 }

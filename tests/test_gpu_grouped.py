@@ -1,9 +1,11 @@
-"""The contraction of a multi-bin batch runs as one persistent launch over the
-joint tile space of all its (type, order, orientation class) bins.  Each tile
-does the same arithmetic as in a launch of its bin alone, so every element's
-outputs must be bit-identical to those of a batch holding that element only
-(a one-bin launch).  Checked on the hp mixed hexa / prism / tet mesh in mixed
-precision, and the graph's kernel count falls with the grouping."""
+"""A multi-bin batch runs its per-element kernels as grouped launches over
+all its (type, order, orientation class) bins: stage 0 (orientation maps,
+geometry, loads, digit slicing) and the condensation through segment tables,
+the mixed-precision contraction as one persistent launch over the joint tile
+space.  Each element goes through the same arithmetic as in a launch of its
+bin alone, so its outputs must be bit-identical to those of a batch holding
+that element only (a one-bin launch).  Checked on the hp mixed hexa / prism /
+tet mesh in both precisions, on elements with and without bubbles."""
 import numpy as np
 import pytest
 
@@ -21,18 +23,24 @@ def _sub(m, idx):
     return d
 
 
-def test_grouped_contraction_bit_identical_to_one_bin_launches():
+@pytest.mark.parametrize("prec", [H.MIXED, H.FP64])
+def test_grouped_launches_bit_identical_to_one_bin_launches(prec):
     m = M.mixed_mesh(4, a=0.5, b=0.5, cy=0.5, perturb=0.1, seed=21, kappa_logrange=(-1, 1))
-    ep = H.ElementPass(H.MIXED, integration=1, isol=10)
+    ep = H.ElementPass(prec, integration=1, isol=10)
     ep.submit(m)
     ep.run()
     ep.download()
     kernels, _ = ep.pass_stats()
     rng = np.random.default_rng(2)
-    picks = sorted(set(rng.choice(m["nelem"], 12, replace=False)) |
-                   {int(np.where(m["etype"] == t)[0][0]) for t in (1, 2, 3)})
-    for e in picks:
-        one = H.ElementPass(H.MIXED, integration=1, isol=10)
+    nb = np.array([len(ep.schur(e)[1]) for e in range(m["nelem"])])
+    picks = set(rng.choice(m["nelem"], 12, replace=False))
+    picks |= {int(np.where(m["etype"] == t)[0][0]) for t in (1, 2, 3)}
+    # elements without bubbles (condensed by the compression kernel alone)
+    picks |= set(int(e) for e in np.where(nb == 0)[0][:4])
+    picks |= set(int(e) for e in np.where(nb > 0)[0][:4])
+    assert (nb == 0).any() and (nb > 0).any()
+    for e in sorted(picks):
+        one = H.ElementPass(prec, integration=1, isol=10)
         one.submit(_sub(m, [e]))
         one.run()
         one.download()
