@@ -350,7 +350,28 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def tuning_info():
+    """The tuning table the pass reads at submit (loaded with the library)."""
+    from hp3d_gb300 import hp3dg as H
+    path = os.environ.get("HP3DG_TUNE_FILE") or H.DEFAULT_TUNE_FILE
+    if not os.path.exists(path):
+        return None
+    try:
+        with open(path) as f:
+            tab = json.load(f)
+        return {"file": os.path.relpath(path, os.path.dirname(os.path.abspath(__file__))),
+                "bin_entries": len(tab.get("bins", [])), "device": tab.get("device")}
+    except (OSError, ValueError):
+        return None
+
+
 def config_dict(args, world, mesh):
+    cfg = _config_dict(args, world, mesh)
+    cfg["tuning"] = tuning_info()
+    return cfg
+
+
+def _config_dict(args, world, mesh):
     if args.workload == "mixed":
         cnt = np.bincount(mesh["etype"], minlength=4)[1:]
         return {"workload": f"galerkin_poisson_hp_mixed_{mixed_cells(args)}^3_cells_pmax6_integration{args.integration}",

@@ -356,6 +356,9 @@ struct Bin {
   // condensation with every product on tensor cores (mixed, nb <= 64)
   bool cond_tc = false;
   CondTcBufs ctb{};
+  // tuning-table variant (0 = built-in rules)
+  int tune_cond = 0, tune_grp = 0;
+  bool tuned = false;
   // tensor-core Schur update (mixed): Y digits, column exponents, condensed load
   bool tc_schur = false;
   TcFactorOut tco{};
@@ -1082,10 +1085,23 @@ int hp3dg_batch_submit_constrained(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_d
       if (rc) { free_batch(c); return HP3DG_ERR_UNSUPPORTED; }
       B.d_ddig = (uint16_t*)dalloc<uint8_t>(ozaki_d_bytes(B.plan, (int)ne), &err);
       B.d_dscale = dalloc<double>(ne + 128, &err);
+      // the tuning table's variant for this bin (cond, raster group); a
+      // variant the bin cannot use falls back to the built-in rule
+      TuneRec tr;
+      if (c->opts.tune == 0 && tune_lookup(B.etype, B.n, B.nb, B.nint, HP3DG_MIXED, &tr)) {
+        B.tune_cond = tr.cond;
+        B.tune_grp = tr.grp;
+        B.tuned = true;
+      }
+      const bool ok_cond_tc = !c->opts.schur_fp64 && !B.d_Yg &&
+                              cond_tc_supported(B.ni, B.nb, COND_TC_DIGITS);
+      const bool ok_tc_schur = !c->opts.schur_fp64 && !B.d_Yg &&
+                               schur_tc_supported(B.ni, B.nb, B.plan.digits);
+      int cond = B.tune_cond;
+      if ((cond == 1 && !ok_cond_tc) || (cond == 2 && !ok_tc_schur)) cond = 0;
       // the condensation products have K = nb <= 64: radix 8, 6 digits keep
       // every level sum exact (below 2^23) with 21 digit pairs
-      B.cond_tc = !c->opts.schur_fp64 && !B.d_Yg &&
-                  cond_tc_supported(B.ni, B.nb, COND_TC_DIGITS);
+      B.cond_tc = ok_cond_tc && (cond == 0 || cond == 1);
       if (B.cond_tc) {
         CondTcBufs& t = B.ctb;
         cond_tc_make_out(B.ni, B.nb, COND_TC_RADIX, COND_TC_DIGITS, t);
@@ -1097,8 +1113,7 @@ int hp3dg_batch_submit_constrained(hp3dg_ctx* c, int32_t nel, const hp3dg_elem_d
         t.elt = dalloc<int>(ne * (size_t)t.nbr, &err);
         t.bi = dalloc<double>(ne * (size_t)B.ni, &err);
       }
-      B.tc_schur = !B.cond_tc && !c->opts.schur_fp64 && !B.d_Yg &&
-                   schur_tc_supported(B.ni, B.nb, B.plan.digits);
+      B.tc_schur = !B.cond_tc && ok_tc_schur && (cond == 0 || cond == 2);
       if (B.tc_schur) {
         TcFactorOut& t = B.tco;
         t.nr = schur_tc_rows(B.ni);
@@ -1195,7 +1210,7 @@ int enqueue_range(hp3dg_ctx* c, Bin& B, int j0, int j1, int stage, cudaStream_t 
   if (stage == 1) {
     if (mixed) {
       if (launch_ozaki_gemm(B.plan, ne, B.n, ddig, dscale, B.d_mdig, B.d_mscale, PK, c->d_flags + 2,
-                            st, c->opts.fault_inject == 1 ? 1 : 0))
+                            st, c->opts.fault_inject == 1 ? 1 : 0, B.tune_grp))
         return HP3DG_ERR_CUDA;
     } else {
       launch_contract_fp64(ne, B.nint, B.n, B.ni, B.nb, B.d_grad, D, PK, st);
@@ -1330,7 +1345,7 @@ int enqueue_pass(hp3dg_ctx* c, cudaStream_t st, bool capturing) {
       for (int b : order) {
         Bin& B = c->bins[b];
         items.push_back({&B.plan, (int)B.elems.size(), B.n * (B.n + 1) / 2, B.d_ddig, B.d_dscale,
-                         B.d_mdig, B.d_mscale, B.d_PK});
+                         B.d_mdig, B.d_mscale, B.d_PK, B.tune_grp});
       }
       if (launch_ozaki_gemm_group(items.data(), (int)items.size(), c->d_flags + 2, st,
                                   c->opts.fault_inject == 1 ? 1 : 0))
@@ -1764,6 +1779,25 @@ int hp3dg_mixed_config(const hp3dg_ctx* c, int32_t* radix, int32_t* digits, int3
   if (radix) *radix = p.radix;
   if (digits) *digits = p.digits;
   if (pairs) *pairs = ozaki_pairs(p);
+  return HP3DG_OK;
+}
+
+int hp3dg_bin_info(const hp3dg_ctx* c, int32_t* nbins, int32_t b, int32_t* info,
+                   int32_t* bin_of) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  if (nbins) *nbins = (int32_t)c->bins.size();
+  if (info) {
+    if (b < 0 || b >= (int)c->bins.size()) return HP3DG_ERR_ARG;
+    const Bin& B = c->bins[b];
+    info[0] = B.etype; info[1] = B.n; info[2] = B.nb; info[3] = B.nint;
+    info[4] = (int32_t)B.elems.size();
+    info[5] = B.cond_tc ? 1 : (B.tc_schur ? 2 : 3);
+    info[6] = B.tune_grp;
+    info[7] = B.tuned ? 1 : 0;
+  }
+  if (bin_of)
+    for (int e = 0; e < c->nel; ++e) bin_of[e] = c->bin_of[e];
   return HP3DG_OK;
 }
 

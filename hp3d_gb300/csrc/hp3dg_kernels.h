@@ -232,10 +232,12 @@ int ozaki_kchunk(const OzakiPlan& plan);
 // waits run out and the kernel reports through d_flag instead of finishing.
 int launch_ozaki_gemm(const OzakiPlan& plan, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                      double* d_PK, int* d_flag, cudaStream_t st, int fault = 0);
+                      double* d_PK, int* d_flag, cudaStream_t st, int fault = 0,
+                      int grp = 0);
 // The contraction of several bins (same radix and digits) in one persistent
-// launch over their joint tile space (split into launches of at most 128
-// bins): out[r, c] = sum_q D[r, q] M[q, c] per bin.
+// launch over their joint tile space (split into launches of at most
+// OZAKI_MAXBINS bins): out[r, c] = sum_q D[r, q] M[q, c] per bin.
+constexpr int OZAKI_MAXBINS = 352;
 struct OzakiGemmItem {
   const OzakiPlan* plan;
   int nrows;        // elements (rows of D)
@@ -245,6 +247,7 @@ struct OzakiGemmItem {
   const uint16_t* mdig;
   const double* mscale;
   double* out;
+  int grp = 0;      // column blocks per raster group (0 = sized for L2)
 };
 int launch_ozaki_gemm_group(const OzakiGemmItem* items, int nitems, int* d_flag,
                             cudaStream_t st, int fault = 0);
@@ -364,5 +367,15 @@ int launch_dpg_stage(int stage, int nel, const DpgDims& d, const DpgPhys& ph,
                       const int64_t* lcon_off, const int64_t* elem_nnz, const int64_t* schur_off,
                       const int64_t* bub_off, double* zastif, double* zbload, double* aschur,
                       double* bschur, double* zkeep, int* flags, cudaStream_t st);
+
+// tuning table (tune.cu): the entry of a bin, the contraction's ring stages
+struct TuneRec {
+  int etype = 0, n = 0, nb = 0, nint = 0, precision = 0;
+  int cond = 0;  // 0 = built-in rule, 1 = fused tensor-core, 2 = FP64 factor +
+                 // tensor-core Schur update, 3 = FP64
+  int grp = 0;   // contraction raster group (column blocks), 0 = built-in
+};
+bool tune_lookup(int etype, int n, int nb, int nint, int precision, TuneRec* out);
+int tune_nstage();
 
 }  // namespace hp3dg

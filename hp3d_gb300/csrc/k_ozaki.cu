@@ -92,7 +92,7 @@ struct GemmBin {
   int shift0;                // slot s: V += L << (shift0 - radix s), or >> when negative
   int scale_shift;           // PK = V * 2^(ke + kc - scale_shift)
 };
-constexpr int MAXBINS = 128;
+constexpr int MAXBINS = OZAKI_MAXBINS;
 struct GemmParams {
   int radix, digits, nlev;  // levels 2 .. digits+1 in slots 0 .. nlev-1
   int kchunk;               // k-blocks per exact accumulation run
@@ -104,6 +104,7 @@ struct GemmParams {
   int nbins, ntiles;
   GemmBin bin[MAXBINS];
 };
+static_assert(sizeof(GemmParams) <= 32764, "kernel parameter space");
 }  // namespace
 
 // the bin of tile t (bins in tile order)
@@ -770,9 +771,10 @@ static void build_bin(const OzakiGemmItem& it, int kchunk, GemmBin* b) {
   b->neb = round_up(it.nrows, BN) / BN;
   b->nel = it.nrows;
   b->ncols = it.ncols_real;
-  // raster groups whose M digit strips take about 48 MB of L2
+  // raster groups whose M digit strips take about 48 MB of L2 (or the
+  // tuned width)
   const double strip = (double)b->nk * D * A_TILE;
-  const int grp = (int)(48.0 * 1024 * 1024 / strip);
+  const int grp = it.grp > 0 ? it.grp : (int)(48.0 * 1024 * 1024 / strip);
   b->grp = grp < 1 ? 1 : (grp > b->ncb ? b->ncb : grp);
   // V = sum over runs and levels of L_s 2^(R(S-s) - t) stays below 2^62
   const double vmax = log2((double)b->nchunk) + 24.0 + R * (D - 1) - log2(1.0 - ldexp(1.0, -R));
@@ -819,8 +821,11 @@ int launch_ozaki_gemm_group(const OzakiGemmItem* items, int nitems, int* d_flag,
   std::vector<GemmParams> groups;  // one launch per MAXBINS bins
   GemmParams* G = new GemmParams;
   build_params(*items[order[0]].plan, G);
-  // as many ring stages as fit next to the static shared memory (barriers)
-  const int nst = (optin - 1024 - 1024) / STAGE_BYTES;
+  // as many ring stages as fit next to the static shared memory (barriers),
+  // or the tuned depth
+  int nst = (optin - 1024 - 1024) / STAGE_BYTES;
+  const int tuned = tune_nstage();
+  if (tuned > 0 && tuned < nst) nst = tuned < KGROUP + 1 ? KGROUP + 1 : tuned;
   G->nstage = nst > MAXSTAGE ? MAXSTAGE : nst;
   if (G->nstage < KGROUP + 1) { delete G; return -1; }
   G->fault = fault;
@@ -851,8 +856,8 @@ int launch_ozaki_gemm_group(const OzakiGemmItem* items, int nitems, int* d_flag,
 
 int launch_ozaki_gemm(const OzakiPlan& p, int nel, int n, const uint16_t* d_ddig,
                       const double* d_dscale, const uint16_t* d_mdig, const double* d_mscale,
-                      double* d_PK, int* d_flag, cudaStream_t st, int fault) {
-  OzakiGemmItem it{&p, nel, n * (n + 1) / 2, d_ddig, d_dscale, d_mdig, d_mscale, d_PK};
+                      double* d_PK, int* d_flag, cudaStream_t st, int fault, int grp) {
+  OzakiGemmItem it{&p, nel, n * (n + 1) / 2, d_ddig, d_dscale, d_mdig, d_mscale, d_PK, grp};
   return launch_ozaki_gemm_group(&it, 1, d_flag, st, fault);
 }
 

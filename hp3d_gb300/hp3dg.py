@@ -3,7 +3,9 @@
 This is the host-side interface a Python caller (tests, benchmark, the torch
 autograd harness) uses; the Fortran host binds the same entry points through
 ISO_C_BINDING.  Loading fails loudly when libhp3dg.so is
-missing: there is no CPU fallback.
+missing: there is no CPU fallback.  Loading the library also loads the
+package's tuning table (tune/gb300.json, written by hp3d_gb300.autotune) unless
+the environment variable HP3DG_TUNE_FILE names another.
 """
 from __future__ import annotations
 
@@ -37,7 +39,8 @@ class Opts(ctypes.Structure):
                 ("ozaki_radix", ctypes.c_int32), ("ozaki_digits", ctypes.c_int32),
                 ("stc_method", ctypes.c_int32), ("launch_mode", ctypes.c_int32),
                 ("schur_fp64", ctypes.c_int32), ("download_chunks", ctypes.c_int32),
-                ("fault_inject", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("fault_inject", ctypes.c_int32), ("tune", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 2)]
 
 
 DESC_DTYPE = np.dtype([("etype", np.int32), ("mdle", np.int32), ("norder", np.int32, 19),
@@ -58,6 +61,7 @@ EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
            "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_mixed_contract", "hp3dg_output_sizes", "hp3dg_device_outputs",
            "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_pass_stats", "hp3dg_last_bad_element",
+           "hp3dg_tune_load", "hp3dg_tune_lookup", "hp3dg_bin_info",
            "hp3dg_dpg_begin", "hp3dg_dpg_submit", "hp3dg_dpg_run", "hp3dg_dpg_sync",
            "hp3dg_dpg_download", "hp3dg_dpg_sizes", "hp3dg_dpg_get_elem",
            "hp3dg_dpg_get_condensed", "hp3dg_dpg_get_schur", "hp3dg_dpg_index_map",
@@ -95,6 +99,9 @@ def lib():
         L.hp3dg_phase_times.argtypes = [_vp, _f32p, ctypes.c_int32]
         L.hp3dg_mixed_config.argtypes = [_vp, _i32p, _i32p, _i32p]
         L.hp3dg_pass_stats.argtypes = [_vp, _i64p, _f64p]
+        L.hp3dg_tune_load.argtypes = [ctypes.c_char_p, _i32p]
+        L.hp3dg_tune_lookup.argtypes = [ctypes.c_int32] * 5 + [_i32p] * 3
+        L.hp3dg_bin_info.argtypes = [_vp, _i32p, ctypes.c_int32, _i32p, _i32p]
         L.hp3dg_last_bad_element.argtypes = [_vp]
         L.hp3dg_last_bad_element.restype = ctypes.c_int32
         L.hp3dg_batch_end.argtypes = [_vp]
@@ -119,6 +126,10 @@ def lib():
         L.hp3dg_dpg_end.argtypes = [_vp]
         L.hp3dg_dpg_end.restype = None
         _lib = L
+        # the tuning table shipped with the package, unless the environment
+        # names one (the library reads that itself at the first submit)
+        if not os.environ.get("HP3DG_TUNE_FILE") and os.path.exists(DEFAULT_TUNE_FILE):
+            L.hp3dg_tune_load(os.fsencode(DEFAULT_TUNE_FILE), None)
     return _lib
 
 
@@ -180,7 +191,7 @@ class ElementPass:
 
     def __init__(self, precision=FP64, integration=0, isol=10, keep_elem=False, timing=False,
                  device=0, ozaki_radix=0, ozaki_digits=0, graph=True, schur_tc=True,
-                 download_chunks=0, fault_inject=0):
+                 download_chunks=0, fault_inject=0, tune=True):
         self.L = lib()
         o = Opts()
         o.precision = precision
@@ -195,6 +206,7 @@ class ElementPass:
         o.schur_fp64 = 0 if schur_tc else 1
         o.download_chunks = download_chunks
         o.fault_inject = fault_inject
+        o.tune = 0 if tune else 1
         self.ctx = _vp()
         self._check(self.L.hp3dg_batch_begin(ctypes.byref(o), ctypes.byref(self.ctx)), "begin")
         self.nel = 0
@@ -381,6 +393,24 @@ class ElementPass:
         self._check(self.L.hp3dg_pass_stats(self.ctx, ctypes.byref(k), ctypes.byref(f)), "stats")
         return k.value, f.value
 
+    def bin_info(self):
+        """Per bin of the last submit: dicts of etype, n, nb, nint, nel, cond
+        (condensation variant in use: 1 fused tensor-core, 2 FP64 factor +
+        tensor-core Schur update, 3 FP64), grp (contraction raster group
+        requested, 0 = built-in), tuned (the table supplied the variant); and
+        each element's bin."""
+        nb = ctypes.c_int32()
+        self._check(self.L.hp3dg_bin_info(self.ctx, ctypes.byref(nb), 0, None, None), "bin_info")
+        bins = []
+        info = np.zeros(8, np.int32)
+        for b in range(nb.value):
+            self._check(self.L.hp3dg_bin_info(self.ctx, None, b, _p(info, _i32p), None), "bin_info")
+            bins.append(dict(zip(("etype", "n", "nb", "nint", "nel", "cond", "grp", "tuned"),
+                                 (int(x) for x in info))))
+        bin_of = np.zeros(max(self.nel, 1), np.int32)
+        self._check(self.L.hp3dg_bin_info(self.ctx, None, -1, None, _p(bin_of, _i32p)), "bin_info")
+        return bins, bin_of[: self.nel]
+
     def ozaki_pairs(self):
         return self.mixed_config()[2]
 
@@ -394,6 +424,31 @@ class ElementPass:
             self.close()
         except Exception:
             pass
+
+
+# --------------------------------------------------------------------------
+# tuning table (hp3dg_tune_*)
+DEFAULT_TUNE_FILE = os.path.join(HERE, "tune", "gb300.json")
+
+
+def tune_load(path=DEFAULT_TUNE_FILE):
+    """Load a tuning table (JSON written by hp3d_gb300.autotune) for every
+    later submit of this process; None clears it.  Returns the number of bin
+    entries."""
+    n = ctypes.c_int32()
+    rc = lib().hp3dg_tune_load(None if path is None else os.fsencode(path), ctypes.byref(n))
+    if rc != 0:
+        raise HP3DGError(rc, f"tune_load {path}")
+    return n.value
+
+
+def tune_lookup(etype, n, nb, nint, precision=MIXED):
+    """(cond, grp, nstage) of the loaded table for a bin, or None when the
+    table has no entry for it."""
+    c, g, s = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+    rc = lib().hp3dg_tune_lookup(etype, n, nb, nint, precision, ctypes.byref(c), ctypes.byref(g),
+                                 ctypes.byref(s))
+    return (c.value, g.value, s.value) if rc == 0 else None
 
 
 # --------------------------------------------------------------------------

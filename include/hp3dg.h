@@ -94,7 +94,11 @@ typedef struct hp3dg_opts {
                           context stays usable.  2: every device allocation
                           of a submit that allocates fails, which returns
                           HP3DG_ERR_ALLOC; the context can be ended. */
-  int32_t reserved[3];
+  int32_t tune;        /* 0: per-bin kernel variants from the tuning table
+                          (hp3dg_tune_load, or the file named by the
+                          environment variable HP3DG_TUNE_FILE), where it has
+                          an entry for the bin; 1: built-in rules only */
+  int32_t reserved[2];
 } hp3dg_opts;
 
 /* Element descriptor: what find_order (datstrs/find_order.F90:5),
@@ -284,6 +288,32 @@ int hp3dg_mixed_config(const hp3dg_ctx *ctx, int32_t *radix, int32_t *digits, in
  *   2 (6 nint) n(n+1)/2 per element; FP64, n(n+1) 3 nint per element (the
  *   DSYRK count of elem_opt). */
 int hp3dg_pass_stats(const hp3dg_ctx *ctx, int64_t *kernels, double *contraction_flops);
+
+/* Tuning table (JSON, written by hp3d_gb300/autotune.py from timings on the
+ * target GPU): per (element type, n, nb, quadrature points, precision) bin
+ * the condensation variant and the contraction's raster group, and the
+ * contraction's pipeline depth.  Process-wide; read by every later submit of
+ * a context with opts.tune = 0.  path = NULL clears the table.  Returns
+ * HP3DG_ERR_ARG for an unreadable or malformed file (the table is then left
+ * as it was); *nrec = bin entries loaded. */
+int hp3dg_tune_load(const char *path, int32_t *nrec);
+
+/* The table's entry for a bin: cond (0 = built-in rule, 1 = fused
+ * tensor-core condensation, 2 = FP64 factor + tensor-core Schur update,
+ * 3 = FP64), grp (contraction column blocks per raster group, 0 = built-in)
+ * and the table's ring depth nstage (0 = as many as fit).  HP3DG_ERR_ARG
+ * when the table has no entry (cond = grp = 0). */
+int hp3dg_tune_lookup(int32_t etype, int32_t n, int32_t nb, int32_t nint, int32_t precision,
+                      int32_t *cond, int32_t *grp, int32_t *nstage);
+
+/* Bins of the last submit: *nbins, and for bin b (0 <= b < nbins)
+ * info[0..7] = etype, n, nb, nint (quadrature points), elements, the
+ * condensation variant in use (1, 2, 3 as in hp3dg_tune_lookup; FP64
+ * precision: 3), the contraction raster group requested (0 = built-in),
+ * and 1 if the table supplied the bin's variant.  bin_of (nullable, n_elem
+ * entries): each element's bin. */
+int hp3dg_bin_info(const hp3dg_ctx *ctx, int32_t *nbins, int32_t b, int32_t *info,
+                   int32_t *bin_of);
 
 /* Size of the fixed device scratch array used by hp3dg_condense_noalloc:
  * 2^20 doubles (8 MiB), resident on every GPU that loads the library. */

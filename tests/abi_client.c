@@ -45,6 +45,7 @@ static int layout(void) {
   FIELD(hp3dg_opts, schur_fp64);
   FIELD(hp3dg_opts, download_chunks);
   FIELD(hp3dg_opts, fault_inject);
+  FIELD(hp3dg_opts, tune);
   FIELD(hp3dg_opts, reserved);
   SIZE(hp3dg_opts);
   FIELD(hp3dg_elem_desc, etype);
