@@ -1868,6 +1868,225 @@ int hp3dg_dirichlet_dofs(hp3dg_ctx* c, int32_t isol, double* zdofd, int64_t* n) 
   return rc;
 }
 
+}  // extern "C"
+
+namespace {
+
+// hexahedron reference vertices, edge and face vertex lists (element_data.F90)
+const double HBRICK_XI[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+const int HBRICK_E2V[12][2] = {{0, 1}, {1, 2}, {3, 2}, {0, 3}, {4, 5}, {5, 6},
+                               {7, 6}, {4, 7}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+const int HBRICK_F2V[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                              {1, 2, 6, 5}, {3, 2, 6, 7}, {0, 3, 7, 4}};
+const int HBRICK_F2E[6][4] = {{0, 1, 2, 3}, {4, 5, 6, 7}, {0, 9, 4, 8},
+                              {1, 10, 5, 9}, {2, 10, 6, 11}, {3, 11, 7, 8}};
+
+void hexa_node_counts(const int* nord, int* first) {
+  first[0] = 0;
+  for (int i = 0; i < 27; ++i) {
+    int n;
+    if (i < 8) n = 1;
+    else if (i < 20) n = std::max(nord[i - 8] - 1, 0);
+    else if (i < 26) { int a, b; decod2(nord[12 + i - 20], a, b); n = std::max(a - 1, 0) * std::max(b - 1, 0); }
+    else { int x, y, z; decod3(nord[18], x, y, z); n = std::max(x - 1, 0) * std::max(y - 1, 0) * std::max(z - 1, 0); }
+    first[i + 1] = first[i] + n;
+  }
+}
+
+// The projection points of every element (hexahedra): per element its 8
+// vertices, then per edge, face and the interior with dof the points of
+// set_1Dint / set_2Dint (face_order) / set_3Dint at INTEGRATION = integration
+// (xi and the rule's weight: 4 doubles per point), and per element the start
+// of each node's points (28 entries, the last one its end).  nmax: the
+// largest node dof count.
+int gdof_points_build(const hp3dg_ctx* c, std::vector<double>& pts, std::vector<int64_t>& node_pt,
+                      int* nmax) {
+  const int nel = c->nel, I = c->opts.integration;
+  if ((int)c->last_desc.size() != nel) return HP3DG_ERR_STATE;
+  pts.clear();
+  node_pt.assign((size_t)nel * 28, 0);
+  *nmax = 1;
+  double gx[16], gw[16], hx[16], hw[16];
+  for (int e = 0; e < nel; ++e) {
+    const hp3dg_elem_desc& d = c->last_desc[e];
+    if (d.etype != HP3DG_HEXA) return HP3DG_ERR_UNSUPPORTED;
+    int first[28];
+    hexa_node_counts(d.norder, first);
+    int64_t* np = &node_pt[(size_t)e * 28];
+    auto put = [&](const double* xi, double w) {
+      pts.push_back(xi[0]); pts.push_back(xi[1]); pts.push_back(xi[2]); pts.push_back(w);
+    };
+    for (int v = 0; v < 8; ++v) {
+      np[v] = (int64_t)pts.size() / 4;
+      put(HBRICK_XI[v], 1.0);
+    }
+    for (int id = 0; id < 12; ++id) {
+      np[8 + id] = (int64_t)pts.size() / 4;
+      if (first[9 + id] == first[8 + id]) continue;
+      *nmax = std::max(*nmax, first[9 + id] - first[8 + id]);
+      const int nint = std::min(d.norder[id] + I, MAXP) + 1;
+      gauss_rule01(nint, gx, gw);
+      const double *x1 = HBRICK_XI[HBRICK_E2V[id][0]], *x2 = HBRICK_XI[HBRICK_E2V[id][1]];
+      for (int l = 0; l < nint; ++l) {
+        double xi[3];
+        for (int q = 0; q < 3; ++q) xi[q] = x1[q] + gx[l] * (x2[q] - x1[q]);
+        put(xi, gw[l]);
+      }
+    }
+    for (int id = 0; id < 6; ++id) {
+      np[20 + id] = (int64_t)pts.size() / 4;
+      if (first[21 + id] == first[20 + id]) continue;
+      *nmax = std::max(*nmax, first[21 + id] - first[20 + id]);
+      int h, v;
+      decod2(d.norder[12 + id], h, v);
+      const int* fe = HBRICK_F2E[id];
+      const int nx = std::min(std::max(std::max(d.norder[fe[0]], d.norder[fe[2]]), h) + I, MAXP) + 1;
+      const int ny = std::min(std::max(std::max(d.norder[fe[1]], d.norder[fe[3]]), v) + I, MAXP) + 1;
+      gauss_rule01(nx, gx, gw);
+      gauss_rule01(ny, hx, hw);
+      const double *v1 = HBRICK_XI[HBRICK_F2V[id][0]], *v2 = HBRICK_XI[HBRICK_F2V[id][1]],
+                   *v3 = HBRICK_XI[HBRICK_F2V[id][3]];
+      for (int l2 = 0; l2 < ny; ++l2)
+        for (int l1 = 0; l1 < nx; ++l1) {
+          double xi[3];
+          for (int q = 0; q < 3; ++q)
+            xi[q] = v1[q] + gx[l1] * (v2[q] - v1[q]) + hx[l2] * (v3[q] - v1[q]);
+          put(xi, gw[l1] * hw[l2]);
+        }
+    }
+    np[26] = (int64_t)pts.size() / 4;
+    if (first[27] > first[26]) {
+      *nmax = std::max(*nmax, first[27] - first[26]);
+      int loc[19];
+      hexa_order_loc(d.norder, d.nori_face, loc);
+      std::vector<double> xq, wq;
+      hexa_quadrature(loc, I, xq, wq);
+      for (size_t l = 0; l < wq.size(); ++l) put(&xq[3 * l], wq[l]);
+    }
+    np[27] = (int64_t)pts.size() / 4;
+  }
+  return HP3DG_OK;
+}
+
+// eta(xi): trilinear in the element's vertex coordinates in the block
+void eta_trilinear(const double* ev, const double* xi, double* eta) {
+  for (int q = 0; q < 3; ++q) eta[q] = 0.0;
+  for (int v = 0; v < 8; ++v) {
+    double b = 1.0;
+    for (int a = 0; a < 3; ++a) b *= HBRICK_XI[v][a] > 0.5 ? xi[a] : 1.0 - xi[a];
+    for (int q = 0; q < 3; ++q) eta[q] += ev[3 * v + q] * b;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int hp3dg_gdof_points(hp3dg_ctx* c, const double* etav, double* eta, int64_t* npts) {
+  if (!c) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  std::vector<double> pts;
+  std::vector<int64_t> node_pt;
+  int nmax = 0;
+  const int rc = gdof_points_build(c, pts, node_pt, &nmax);
+  if (rc != HP3DG_OK) return rc;
+  const int64_t n = (int64_t)pts.size() / 4;
+  if (npts) *npts = n;
+  if (eta) {
+    if (!etav) return HP3DG_ERR_ARG;
+    for (int e = 0; e < c->nel; ++e)
+      for (int64_t l = node_pt[(size_t)e * 28]; l < node_pt[(size_t)e * 28 + 27]; ++l)
+        eta_trilinear(etav + (size_t)24 * e, &pts[4 * l], eta + 3 * l);
+  }
+  return HP3DG_OK;
+}
+
+int hp3dg_update_gdof(hp3dg_ctx* c, const double* etav, const double* x, const double* dxdeta,
+                      const int32_t* linear, double* xnod, int32_t apply) {
+  if (!c || !etav || !x || !dxdeta) return HP3DG_ERR_ARG;
+  if (!c->submitted) return HP3DG_ERR_STATE;
+  const int nel = c->nel;
+  if (nel == 0) return HP3DG_OK;
+  std::vector<double> pts;
+  std::vector<int64_t> node_pt;
+  int nmax = 0;
+  int rc = gdof_points_build(c, pts, node_pt, &nmax);
+  if (rc != HP3DG_OK) return rc;
+  const int64_t npts = (int64_t)pts.size() / 4;
+  // each node takes the values of the first element containing it
+  std::vector<int> src((size_t)nel * 26, -1);
+  {
+    std::map<int, int> firstv;
+    for (int e = 0; e < nel; ++e)
+      for (int i = 0; i < 26; ++i) {
+        const int nod = c->last_desc[e].nodes[i];
+        auto it = firstv.find(nod);
+        if (it == firstv.end()) firstv[nod] = e * 26 + i;
+        else src[(size_t)e * 26 + i] = it->second;
+      }
+  }
+  cudaSetDevice(c->device);
+  cudaStream_t st = c->stream;
+  const int64_t ndof = c->dof_off[nel];
+  const int64_t wstride = (int64_t)gdof_work_doubles(nmax);
+  int chunk = (int)std::min<int64_t>(nel, std::max<int64_t>(64, (256LL << 20) / (8 * wstride)));
+  double *d_etav = nullptr, *d_pts = nullptr, *d_x = nullptr, *d_j = nullptr, *d_xn = nullptr,
+         *d_work = nullptr;
+  int64_t* d_np = nullptr;
+  int *d_src = nullptr, *d_lin = nullptr, *d_bad = nullptr;
+  int err = 0;
+  d_etav = dalloc<double>((size_t)nel * 24, &err);
+  d_pts = dalloc<double>(pts.size(), &err);
+  d_x = dalloc<double>((size_t)npts * 3, &err);
+  d_j = dalloc<double>((size_t)npts * 9, &err);
+  d_xn = dalloc<double>((size_t)ndof * 3, &err);
+  d_work = dalloc<double>((size_t)chunk * wstride, &err);
+  d_np = dalloc<int64_t>(node_pt.size(), &err);
+  d_src = dalloc<int>(src.size(), &err);
+  d_lin = linear ? dalloc<int>(nel, &err) : nullptr;
+  d_bad = dalloc<int>(1, &err);
+  rc = err;
+  int badv = 0x7f7f7f7f;
+  if (rc == HP3DG_OK &&
+      (cudaMemcpyAsync(d_etav, etav, (size_t)nel * 24 * 8, cudaMemcpyHostToDevice, st) ||
+       cudaMemcpyAsync(d_pts, pts.data(), pts.size() * 8, cudaMemcpyHostToDevice, st) ||
+       cudaMemcpyAsync(d_x, x, (size_t)npts * 3 * 8, cudaMemcpyHostToDevice, st) ||
+       cudaMemcpyAsync(d_j, dxdeta, (size_t)npts * 9 * 8, cudaMemcpyHostToDevice, st) ||
+       cudaMemcpyAsync(d_np, node_pt.data(), node_pt.size() * 8, cudaMemcpyHostToDevice, st) ||
+       cudaMemcpyAsync(d_src, src.data(), src.size() * 4, cudaMemcpyHostToDevice, st) ||
+       (linear && cudaMemcpyAsync(d_lin, linear, (size_t)nel * 4, cudaMemcpyHostToDevice, st)) ||
+       cudaMemcpyAsync(d_bad, &badv, 4, cudaMemcpyHostToDevice, st)))
+    rc = HP3DG_ERR_CUDA;
+  if (rc == HP3DG_OK &&
+      launch_gdof(nel, c->d_norder, c->d_nori_e, c->d_nori_f, d_etav, d_np, d_pts, d_x, d_j,
+                  d_lin, d_src, c->d_dof_off, d_xn, d_work, wstride, chunk, d_bad, st))
+    rc = HP3DG_ERR_CUDA;
+  if (rc == HP3DG_OK &&
+      ((xnod && cudaMemcpyAsync(xnod, d_xn, (size_t)ndof * 3 * 8, cudaMemcpyDeviceToHost, st)) ||
+       cudaMemcpyAsync(&badv, d_bad, 4, cudaMemcpyDeviceToHost, st) ||
+       cudaStreamSynchronize(st)))
+    rc = HP3DG_ERR_CUDA;
+  if (rc == HP3DG_OK && badv != 0x7f7f7f7f) {
+    c->last_bad = badv;
+    rc = HP3DG_ERR_NOT_SPD;
+  }
+  if (rc == HP3DG_OK && apply) {
+    // the projected dof become the pass's isoparametric geometry
+    if (c->d_xnod) cudaFree(c->d_xnod);
+    c->d_xnod = d_xn;
+    d_xn = nullptr;
+    if (c->graph) cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+    c->graph_kernels = -1;
+    c->iso = true;
+    c->ran = c->downloaded = c->have_dofs = false;
+  }
+  cudaFree(d_etav); cudaFree(d_pts); cudaFree(d_x); cudaFree(d_j); cudaFree(d_xn);
+  cudaFree(d_work); cudaFree(d_np); cudaFree(d_src); cudaFree(d_lin); cudaFree(d_bad);
+  return rc;
+}
+
 int32_t hp3dg_last_bad_element(const hp3dg_ctx* c) { return c ? c->last_bad : -1; }
 
 void hp3dg_batch_end(hp3dg_ctx* c) {

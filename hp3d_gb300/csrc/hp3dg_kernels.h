@@ -200,6 +200,15 @@ void launch_adjoint(int nel, int nvert, int nint, int n, int isol, const int* d_
 // Dirichlet data by projection-based interpolation (hexahedra) -- k_post.cu.
 // d_gx / d_gw: the n-point Gauss rules on [0,1] at [16 n + l], n <= 10.
 size_t dirichlet_work_doubles(int nel);
+// geometry dof by projection of block maps (k_post.cu): per-thread scratch
+// for projections of up to nmax dof; the three phases with the first-visit
+// gathers between them, elements in chunks of `chunk` threads' scratch
+size_t gdof_work_doubles(int nmax);
+int launch_gdof(int nel, const int* d_norder, const int* d_nori_e, const int* d_nori_f,
+                const double* d_etav, const int64_t* d_node_pt, const double* d_pts,
+                const double* d_x, const double* d_dxdeta, const int* d_linear,
+                const int* d_src, const int64_t* d_dof_off, double* d_xnod, double* d_work,
+                int64_t wstride, int chunk, int* d_bad, cudaStream_t st);
 void launch_dirichlet(int nel, const int* d_norder, const int* d_nori_e, const int* d_nori_f,
                       const int* d_bc, const double* d_xvert, const int64_t* d_zd_off,
                       const double* d_gx, const double* d_gw, int isol, double* d_work,

@@ -508,9 +508,247 @@ __global__ void k_dirichlet(int nel, const int* __restrict__ norder, const int* 
   }
 }
 
+// ---------------------------------------------------------------------------
+// geometry dof by projection-based interpolation of a geometry-block map
+// (update_gdof.F90:80-200 and 404-435; hpvert / hpedge / hpface / hpmdle),
+// hexahedra.  The host evaluates its block maps x(eta), dx/deta at the
+// points of hp3dg_gdof_points; here, one thread per element, each node's dof
+// solve the eta-space H1 projection of what the lower-order dof leave:
+// tangential derivative on edges, surface gradient on faces, full gradient
+// in the interior.  Phase 0: vertices and edges; 1: faces; 2: the interior.
+// Between phases every node takes the values of the first element (in batch
+// order) that contains it, as the reference projects each node once.
+// ---------------------------------------------------------------------------
+__device__ inline int lu_small3(int n, double* A, double* b) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
+    if (A[p + n * k] == 0.0) return -1;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) { double t = A[k + n * j]; A[k + n * j] = A[p + n * j]; A[p + n * j] = t; }
+      for (int c = 0; c < 3; ++c) { double t = b[c * n + k]; b[c * n + k] = b[c * n + p]; b[c * n + p] = t; }
+    }
+    for (int i = k + 1; i < n; ++i) {
+      const double f = A[i + n * k] / A[k + n * k];
+      A[i + n * k] = f;
+      for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
+      for (int c = 0; c < 3; ++c) b[c * n + i] -= f * b[c * n + k];
+    }
+  }
+  for (int c = 0; c < 3; ++c)
+    for (int k = n - 1; k >= 0; --k) {
+      double t = b[c * n + k];
+      for (int j = k + 1; j < n; ++j) t -= A[k + n * j] * b[c * n + j];
+      b[c * n + k] = t / A[k + n * k];
+    }
+  return 0;
+}
+
+__device__ inline void inv3(const double J[3][3], double Ji[3][3], double& det) {
+  const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  const double r = 1.0 / det;
+  Ji[0][0] = c00 * r; Ji[1][0] = c01 * r; Ji[2][0] = c02 * r;
+  Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+  Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+  Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+}
+
+// dof count of node i (0..7 vertices, 8..19 edges, 20..25 faces, 26 the
+// interior) of a hexahedron, and the element dof of its first function
+__device__ inline int hexa_node_n(const int* nord, int i) {
+  if (i < 8) return 1;
+  if (i < 20) return nord[i - 8] > 1 ? nord[i - 8] - 1 : 0;
+  if (i < 26) {
+    int a, b;
+    decod2(nord[12 + i - 20], a, b);
+    return (a > 1 && b > 1) ? (a - 1) * (b - 1) : 0;
+  }
+  int x, y, z;
+  decod3(nord[18], x, y, z);
+  return (x > 1 && y > 1 && z > 1) ? (x - 1) * (y - 1) * (z - 1) : 0;
+}
+__device__ inline int hexa_node_a0(const int* nord, int i) {
+  int s = 0;
+  for (int k = 0; k < i; ++k) s += hexa_node_n(nord, k);
+  return s;
+}
+
+__global__ void k_gdof(int phase, int e0, int e1, const int* __restrict__ norder,
+                       const int* __restrict__ nori_e, const int* __restrict__ nori_f,
+                       const double* __restrict__ etav, const int64_t* __restrict__ node_pt,
+                       const double* __restrict__ pts, const double* __restrict__ xg,
+                       const double* __restrict__ jg, const int* __restrict__ linear,
+                       const int64_t* __restrict__ dof_off, double* __restrict__ xnod,
+                       double* __restrict__ work, int64_t wstride, int* __restrict__ bad) {
+  const int e = e0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= e1) return;
+  int nord[19], ne[12], nf[6], loc[19];
+  for (int i = 0; i < 19; ++i) nord[i] = norder[19 * (size_t)e + i];
+  for (int i = 0; i < 12; ++i) ne[i] = nori_e[12 * (size_t)e + i];
+  for (int i = 0; i < 6; ++i) nf[i] = nori_f[6 * (size_t)e + i];
+  hexa_order_loc(nord, nf, loc);
+  const double* ev = etav + (size_t)24 * e;
+  const int64_t* np = node_pt + (size_t)28 * e;
+  double* X = xnod + 3 * dof_off[e];
+  double* shap = work + (size_t)(e - e0) * wstride;
+  double* grad = shap + MAXN;
+  double* A = grad + 3 * MAXN;
+  if (phase == 0) {
+    for (int v = 0; v < 8; ++v)
+      for (int c = 0; c < 3; ++c) X[3 * v + c] = xg[3 * np[v] + c];
+    const int ndof = hexa_node_a0(nord, 27);
+    for (int k = 3 * 8; k < 3 * ndof; ++k) X[k] = 0.0;
+  }
+  if (linear && linear[e]) return;
+  const int n0 = phase == 0 ? 8 : (phase == 1 ? 20 : 26);
+  const int n1 = phase == 0 ? 20 : (phase == 1 ? 26 : 27);
+  for (int node = n0; node < n1; ++node) {
+    const int n = hexa_node_n(nord, node);
+    if (n == 0) continue;
+    const int kind = node < 20 ? 0 : (node < 26 ? 1 : 2);
+    const int a0 = hexa_node_a0(nord, node);
+    const int nlow = kind == 0 ? 8 : hexa_node_a0(nord, node < 26 ? 20 : 26);
+    double* b = A + (size_t)n * n;
+    for (int q = 0; q < n * n; ++q) A[q] = 0.0;
+    for (int q = 0; q < 3 * n; ++q) b[q] = 0.0;
+    double t1[3] = {0, 0, 0}, t2[3] = {0, 0, 0};
+    if (kind == 0) {
+      const int id = node - 8;
+      for (int c = 0; c < 3; ++c)
+        t1[c] = DBRICK_XI[DBRICK_E2V[id][1]][c] - DBRICK_XI[DBRICK_E2V[id][0]][c];
+    } else if (kind == 1) {
+      const int id = node - 20;
+      for (int c = 0; c < 3; ++c) {
+        t1[c] = DBRICK_XI[DBRICK_F2V[id][1]][c] - DBRICK_XI[DBRICK_F2V[id][0]][c];
+        t2[c] = DBRICK_XI[DBRICK_F2V[id][3]][c] - DBRICK_XI[DBRICK_F2V[id][0]][c];
+      }
+    }
+    for (int64_t l = np[node]; l < np[node + 1]; ++l) {
+      const double* pq = pts + 4 * l;
+      const double xi[3] = {pq[0], pq[1], pq[2]};
+      hexa_shape0(xi, loc, shap, grad, MAXN);
+      double eta[3], J[3][3], Ji[3][3], det;
+      trilin_dev(ev, xi, eta, J);  // eta(xi) and d eta / d xi (refgeom3D)
+      inv3(J, Ji, det);
+      double w = pq[3], rv[3] = {0, 0, 0};
+      if (kind == 0) {
+        for (int i = 0; i < 3; ++i) rv[i] = J[i][0] * t1[0] + J[i][1] * t1[1] + J[i][2] * t1[2];
+        const double bj = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+        for (int i = 0; i < 3; ++i) rv[i] /= bj;
+        w *= bj;
+      } else if (kind == 1) {
+        double a1[3], a2[3];
+        for (int i = 0; i < 3; ++i) {
+          a1[i] = J[i][0] * t1[0] + J[i][1] * t1[1] + J[i][2] * t1[2];
+          a2[i] = J[i][0] * t2[0] + J[i][1] * t2[1] + J[i][2] * t2[2];
+        }
+        rv[0] = a1[1] * a2[2] - a1[2] * a2[1];
+        rv[1] = a1[2] * a2[0] - a1[0] * a2[2];
+        rv[2] = a1[0] * a2[1] - a1[1] * a2[0];
+        const double bj = sqrt(rv[0] * rv[0] + rv[1] * rv[1] + rv[2] * rv[2]);
+        for (int i = 0; i < 3; ++i) rv[i] /= bj;  // the unit normal (its sign is immaterial)
+        w *= bj;
+      } else {
+        w *= det;
+      }
+      // what the lower-order dof leave of dx/deta
+      double R[3][3];
+      for (int c = 0; c < 3; ++c)
+        for (int i = 0; i < 3; ++i) R[c][i] = jg[9 * l + 3 * c + i];
+      for (int k = 0; k < nlow; ++k) {
+        double gx[3], g[3];
+        grad_oriented(k, nord, ne, nf, loc, grad, gx);
+        for (int i = 0; i < 3; ++i) g[i] = gx[0] * Ji[0][i] + gx[1] * Ji[1][i] + gx[2] * Ji[2][i];
+        for (int c = 0; c < 3; ++c) {
+          const double xk = X[3 * k + c];
+          for (int i = 0; i < 3; ++i) R[c][i] -= xk * g[i];
+        }
+      }
+      for (int j = 0; j < n; ++j) {
+        double gx[3], dv[3];
+        grad_oriented(a0 + j, nord, ne, nf, loc, grad, gx);
+        for (int i = 0; i < 3; ++i) dv[i] = gx[0] * Ji[0][i] + gx[1] * Ji[1][i] + gx[2] * Ji[2][i];
+        if (kind == 0) {
+          const double pr = dv[0] * rv[0] + dv[1] * rv[1] + dv[2] * rv[2];
+          for (int i = 0; i < 3; ++i) dv[i] = pr * rv[i];
+        } else if (kind == 1) {
+          const double pr = dv[0] * rv[0] + dv[1] * rv[1] + dv[2] * rv[2];
+          for (int i = 0; i < 3; ++i) dv[i] -= pr * rv[i];
+        }
+        for (int c = 0; c < 3; ++c)
+          b[c * n + j] += (R[c][0] * dv[0] + R[c][1] * dv[1] + R[c][2] * dv[2]) * w;
+        for (int i = 0; i < n; ++i) {
+          double gi[3], du[3];
+          grad_oriented(a0 + i, nord, ne, nf, loc, grad, gi);
+          for (int m = 0; m < 3; ++m)
+            du[m] = gi[0] * Ji[0][m] + gi[1] * Ji[1][m] + gi[2] * Ji[2][m];
+          A[j + n * i] += (dv[0] * du[0] + dv[1] * du[1] + dv[2] * du[2]) * w;
+        }
+      }
+    }
+    if (lu_small3(n, A, b)) { atomicMin(bad, e); return; }
+    for (int j = 0; j < n; ++j)
+      for (int c = 0; c < 3; ++c) X[3 * (a0 + j) + c] = b[c * n + j];
+  }
+}
+
+// every node of phase `phase` (0: vertices and edges, 1: faces) takes the
+// values of its first element: one thread per (element, node slot)
+__global__ void k_gdof_gather(int phase, int nel, const int* __restrict__ norder,
+                              const int* __restrict__ src, const int64_t* __restrict__ dof_off,
+                              double* __restrict__ xnod) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nel * 26) return;
+  const int e = (int)(t / 26), slot = (int)(t % 26);
+  if (phase == 0 ? slot >= 20 : slot < 20) return;
+  const int sv = src[t];
+  if (sv < 0) return;
+  const int f = sv / 26, fs = sv % 26;
+  int nord[19], nordf[19];
+  for (int i = 0; i < 19; ++i) { nord[i] = norder[19 * (size_t)e + i]; nordf[i] = norder[19 * (size_t)f + i]; }
+  int n = hexa_node_n(nord, slot);
+  const int nfs = hexa_node_n(nordf, fs);
+  n = n < nfs ? n : nfs;
+  const double* s = xnod + 3 * (dof_off[f] + hexa_node_a0(nordf, fs));
+  double* d = xnod + 3 * (dof_off[e] + hexa_node_a0(nord, slot));
+  for (int k = 0; k < 3 * n; ++k) d[k] = s[k];
+}
+
 }  // namespace
 
 size_t dirichlet_work_doubles(int nel) { return (size_t)nel * (4 * MAXN + 64 * 64 + 64); }
+size_t gdof_work_doubles(int nmax) { return (size_t)4 * MAXN + (size_t)nmax * nmax + 3 * (size_t)nmax; }
+
+int launch_gdof(int nel, const int* d_norder, const int* d_nori_e, const int* d_nori_f,
+                const double* d_etav, const int64_t* d_node_pt, const double* d_pts,
+                const double* d_x, const double* d_dxdeta, const int* d_linear,
+                const int* d_src, const int64_t* d_dof_off, double* d_xnod, double* d_work,
+                int64_t wstride, int chunk, int* d_bad, cudaStream_t st) {
+  if (nel <= 0) return 0;
+  for (int phase = 0; phase < 3; ++phase) {
+    for (int e0 = 0; e0 < nel; e0 += chunk) {
+      const int e1 = e0 + chunk < nel ? e0 + chunk : nel;
+      k_gdof<<<(e1 - e0 + 63) / 64, 64, 0, st>>>(phase, e0, e1, d_norder, d_nori_e, d_nori_f,
+                                                 d_etav, d_node_pt, d_pts, d_x, d_dxdeta,
+                                                 d_linear, d_dof_off, d_xnod, d_work, wstride,
+                                                 d_bad);
+    }
+    if (phase < 2) {
+      const int64_t nt = (int64_t)nel * 26;
+      k_gdof_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(phase, nel, d_norder, d_src,
+                                                                 d_dof_off, d_xnod);
+    }
+  }
+  return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
 
 void launch_dirichlet(int nel, const int* d_norder, const int* d_nori_e, const int* d_nori_f,
                       const int* d_bc, const double* d_xvert, const int64_t* d_zd_off,

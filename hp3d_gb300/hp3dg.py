@@ -61,7 +61,8 @@ EXPORTS = ["hp3dg_batch_begin", "hp3dg_set_stream", "hp3dg_batch_submit",
            "hp3dg_get_schur", "hp3dg_index_map", "hp3dg_backsub", "hp3dg_get_dofs",
            "hp3dg_element_error", "hp3dg_adjoint", "hp3dg_condense_noalloc", "hp3dg_mixed_contract", "hp3dg_output_sizes", "hp3dg_device_outputs",
            "hp3dg_phase_times", "hp3dg_mixed_config", "hp3dg_pass_stats", "hp3dg_last_bad_element",
-           "hp3dg_tune_load", "hp3dg_tune_lookup", "hp3dg_bin_info",
+           "hp3dg_tune_load", "hp3dg_tune_lookup", "hp3dg_bin_info", "hp3dg_gdof_points",
+           "hp3dg_update_gdof",
            "hp3dg_dpg_begin", "hp3dg_dpg_submit", "hp3dg_dpg_run", "hp3dg_dpg_sync",
            "hp3dg_dpg_download", "hp3dg_dpg_sizes", "hp3dg_dpg_get_elem",
            "hp3dg_dpg_get_condensed", "hp3dg_dpg_get_schur", "hp3dg_dpg_index_map",
@@ -83,6 +84,8 @@ def lib():
                                                      ctypes.POINTER(Constraints)]
         L.hp3dg_dirichlet_dofs.argtypes = [_vp, ctypes.c_int32, _f64p, _i64p]
         L.hp3dg_batch_set_geometry.argtypes = [_vp, _f64p]
+        L.hp3dg_gdof_points.argtypes = [_vp, _f64p, _f64p, _i64p]
+        L.hp3dg_update_gdof.argtypes = [_vp, _f64p, _f64p, _f64p, _i32p, _f64p, ctypes.c_int32]
         L.hp3dg_batch_run.argtypes = [_vp]
         L.hp3dg_batch_sync.argtypes = [_vp]
         L.hp3dg_batch_download.argtypes = [_vp]
@@ -254,6 +257,36 @@ class ElementPass:
         self._check(self.L.hp3dg_batch_set_geometry(self.ctx, _p(self._xnod, _f64p)),
                     "set_geometry")
 
+    def gdof_points(self, etav):
+        """Block coordinates (npts x 3) at which the caller evaluates its
+        geometry-block maps for update_gdof; etav: n_elem x 8 x 3 element
+        vertices in block coordinates."""
+        etav = np.ascontiguousarray(etav, np.float64)
+        n = ctypes.c_int64()
+        self._check(self.L.hp3dg_gdof_points(self.ctx, _p(etav, _f64p), None, ctypes.byref(n)),
+                    "gdof_points")
+        eta = np.zeros((max(n.value, 1), 3))
+        self._check(self.L.hp3dg_gdof_points(self.ctx, _p(etav, _f64p), _p(eta, _f64p),
+                                             ctypes.byref(n)), "gdof_points")
+        return eta[: n.value]
+
+    def update_gdof(self, etav, x, dxdeta, linear=None, apply=False):
+        """Geometry dof of every element (list of (nrdofH, 3) arrays, element
+        dof order) from the maps' values x (npts x 3) and Jacobians dxdeta
+        (npts x 3 x 3) at gdof_points(etav); apply=True makes them the pass's
+        geometry."""
+        etav = np.ascontiguousarray(etav, np.float64)
+        x = np.ascontiguousarray(x, np.float64)
+        j = np.ascontiguousarray(dxdeta, np.float64)
+        lin = None if linear is None else np.ascontiguousarray(linear, np.int32)
+        sizes = self.nrdof_h()
+        out = np.zeros(max(3 * int(sizes.sum()), 1))
+        self._check(self.L.hp3dg_update_gdof(self.ctx, _p(etav, _f64p), _p(x, _f64p), _p(j, _f64p),
+                                             None if lin is None else _p(lin, _i32p),
+                                             _p(out, _f64p), int(apply)), "update_gdof")
+        off = np.concatenate([[0], np.cumsum(sizes)])
+        return [out[3 * off[e]: 3 * off[e + 1]].reshape(-1, 3).copy() for e in range(self.nel)]
+
     def dirichlet_dofs(self, isol):
         """Per element Dirichlet values of the interface dof (update_Ddof on
         the GPU), split per element (the zdofd layout of submit)."""
@@ -264,6 +297,16 @@ class ElementPass:
                     "dirichlet")
         ni = [int(sum(self._node_ndof(e))) for e in range(self.nel)]
         return np.split(z[: n.value], np.cumsum(ni)[:-1])
+
+    def nrdof_h(self):
+        """Every element's H1 dof count (hexahedra: the 26 nodes and the
+        interior)."""
+        out = np.zeros(self.nel, np.int64)
+        for e in range(self.nel):
+            o = int(self.mesh["norder"][e][18])
+            x, y, z = o // 100, (o // 10) % 10, o % 10
+            out[e] = sum(self._node_ndof(e)) + max(x - 1, 0) * max(y - 1, 0) * max(z - 1, 0)
+        return out
 
     def _node_ndof(self, e):
         no = self.mesh["norder"][e]

@@ -289,6 +289,34 @@ int hp3dg_mixed_config(const hp3dg_ctx *ctx, int32_t *radix, int32_t *digits, in
  *   DSYRK count of elem_opt). */
 int hp3dg_pass_stats(const hp3dg_ctx *ctx, int64_t *kernels, double *contraction_flops);
 
+/* Geometry dof by projection-based interpolation of the geometry-block maps
+ * (update_gdof, hpinterp/update_gdof.F90:6; hpvert, hpedge, hpface,
+ * hpmdle), hexahedra.  The block maps stay with the caller (the reference's
+ * GMP routines hexa(No, eta, x, dxdeta) and their kin); the projections run
+ * on the GPU.  Two calls:
+ *   hp3dg_gdof_points: the points in block coordinates at which the caller
+ *     evaluates its maps: per element (batch order) its 8 vertices, then per
+ *     edge, face and the interior carrying dof the quadrature points of
+ *     set_1Dint / set_2Dint / set_3Dint at the context's INTEGRATION.
+ *     etav: n_elem x 8 x 3, each element's vertices in its block's
+ *     coordinates (refel); eta(xi) is trilinear in them.  *npts = number of
+ *     points; eta (nullable) receives npts x 3 block coordinates.
+ *   hp3dg_update_gdof: x (npts x 3) and dxdeta (npts x 9, row-major
+ *     dx_i/deta_j) of the maps at those points -> the geometry dof of every
+ *     element in the layout of hp3dg_batch_set_geometry (xnod, nullable).
+ *     Vertex dof are x at the vertices; edge, face and interior dof are the
+ *     eta-space H1 projections (tangential derivative, surface gradient, full
+ *     gradient) of x minus the lower-order part.  Each node takes the values
+ *     of the first element (batch order) that contains it, as the reference
+ *     projects each node once.  linear (nullable, n_elem): 1 = a 'Linear'
+ *     block, vertices only.  apply = 1 makes the result the pass's geometry
+ *     (as hp3dg_batch_set_geometry).  A singular projection returns
+ *     HP3DG_ERR_NOT_SPD (hp3dg_last_bad_element names the element).
+ * Other element types return HP3DG_ERR_UNSUPPORTED. */
+int hp3dg_gdof_points(hp3dg_ctx *ctx, const double *etav, double *eta, int64_t *npts);
+int hp3dg_update_gdof(hp3dg_ctx *ctx, const double *etav, const double *x, const double *dxdeta,
+                      const int32_t *linear, double *xnod, int32_t apply);
+
 /* Tuning table (JSON, written by hp3d_gb300/autotune.py from timings on the
  * target GPU): per (element type, n, nb, quadrature points, precision) bin
  * the condensation variant and the contraction's raster group, and the

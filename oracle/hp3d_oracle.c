@@ -1722,6 +1722,252 @@ int orc_dirichlet_hexa(const int32_t *norder, const int32_t *nori_edge, const in
 }
 
 /* ------------------------------------------------------------------------ */
+/* Geometry dof by projection-based interpolation of a geometry-block map     */
+/* (update_gdof.F90:80-200, 404-435; hpvert.F90, hpedge.F90, hpface.F90,      */
+/* hpmdle.F90) for one hexahedron.  The block map x(eta) and its Jacobian     */
+/* come from gmap (the GMP routine hexa(No, eta, x, dxdeta) of the           */
+/* reference); eta(xi) is trilinear in the element's vertex coordinates etav */
+/* in the block (refgeom3D / brefgeom3D).  Projections are in eta: tangential */
+/* derivative along edges, surface gradient on faces, full gradient in the   */
+/* interior, each of what the lower-order dof leave.                          */
+/* ------------------------------------------------------------------------ */
+static void eta_map(const double *etav, const double *grad, double J[3][3], double Ji[3][3],
+                    double *det) {
+  /* detadxi(i, m) = sum_v etav(i, v) d phi_v / d xi_m over the 8 vertex functions */
+  for (int i = 0; i < 3; ++i)
+    for (int m = 0; m < 3; ++m) {
+      double s = 0.0;
+      for (int v = 0; v < 8; ++v) s += etav[3 * v + i] * grad[3 * v + m];
+      J[i][m] = s;
+    }
+  double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  double d = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  *det = d;
+  /* dxideta = inverse of detadxi */
+  Ji[0][0] = c00 / d;
+  Ji[1][0] = c01 / d;
+  Ji[2][0] = c02 / d;
+  Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / d;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / d;
+  Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / d;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / d;
+  Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / d;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / d;
+}
+
+/* gradient in eta of function k: duHdeta(i) = sum_m gradH(m, k) dxideta(m, i) */
+static void grad_eta(const double *grad, int k, double Ji[3][3], double *g) {
+  for (int i = 0; i < 3; ++i)
+    g[i] = grad[3 * k] * Ji[0][i] + grad[3 * k + 1] * Ji[1][i] + grad[3 * k + 2] * Ji[2][i];
+}
+
+/* LU with partial pivoting and three right-hand sides (b: n x 3, column-major
+ * by component: b[c * n + j]) */
+static int lu_solve3(int n, double *A, double *b) {
+  for (int k = 0; k < n; ++k) {
+    int p = k;
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(A[i + n * k]) > fabs(A[p + n * k])) p = i;
+    if (A[p + n * k] == 0.0) return -1;
+    if (p != k) {
+      for (int j = 0; j < n; ++j) { double t = A[k + n * j]; A[k + n * j] = A[p + n * j]; A[p + n * j] = t; }
+      for (int c = 0; c < 3; ++c) { double t = b[c * n + k]; b[c * n + k] = b[c * n + p]; b[c * n + p] = t; }
+    }
+    for (int i = k + 1; i < n; ++i) {
+      double f = A[i + n * k] / A[k + n * k];
+      A[i + n * k] = f;
+      for (int j = k + 1; j < n; ++j) A[i + n * j] -= f * A[k + n * j];
+      for (int c = 0; c < 3; ++c) b[c * n + i] -= f * b[c * n + k];
+    }
+  }
+  for (int c = 0; c < 3; ++c)
+    for (int k = n - 1; k >= 0; --k) {
+      double t = b[c * n + k];
+      for (int j = k + 1; j < n; ++j) t -= A[k + n * j] * b[c * n + j];
+      b[c * n + k] = t / A[k + n * k];
+    }
+  return 0;
+}
+
+/* one projection point: add the point's contribution to A (n x n) and b
+ * (n x 3).  kind 0: edge (rt = unit tangent in eta), 1: face (rn = unit
+ * normal in eta), 2: interior.  Functions nlow.. nlow+n-1 are projected; the
+ * first nlow carry the current xnod. */
+static void gdof_point(int kind, const double *grad, double Ji[3][3], const double *rv,
+                       const double *dxdeta, const double *xnod, int nlow, int n, double weight,
+                       double *A, double *b) {
+  double R[3][3];
+  for (int c = 0; c < 3; ++c)
+    for (int i = 0; i < 3; ++i) R[c][i] = dxdeta[3 * c + i];
+  for (int k = 0; k < nlow; ++k) {
+    double g[3];
+    grad_eta(grad, k, Ji, g);
+    for (int c = 0; c < 3; ++c)
+      for (int i = 0; i < 3; ++i) R[c][i] -= xnod[3 * k + c] * g[i];
+  }
+  for (int j = 0; j < n; ++j) {
+    double dv[3];
+    grad_eta(grad, nlow + j, Ji, dv);
+    if (kind == 0) {
+      double pr = dv[0] * rv[0] + dv[1] * rv[1] + dv[2] * rv[2];
+      for (int i = 0; i < 3; ++i) dv[i] = pr * rv[i];
+    } else if (kind == 1) {
+      double pr = dv[0] * rv[0] + dv[1] * rv[1] + dv[2] * rv[2];
+      for (int i = 0; i < 3; ++i) dv[i] -= pr * rv[i];
+    }
+    for (int c = 0; c < 3; ++c)
+      b[c * n + j] += (R[c][0] * dv[0] + R[c][1] * dv[1] + R[c][2] * dv[2]) * weight;
+    for (int i = 0; i < n; ++i) {
+      double du[3];
+      grad_eta(grad, nlow + i, Ji, du);
+      A[j + n * i] += (dv[0] * du[0] + dv[1] * du[1] + dv[2] * du[2]) * weight;
+    }
+  }
+}
+
+int orc_gdof_hexa(const int32_t *norder, const int32_t *nori_edge, const int32_t *nori_face,
+                  const double *etav, int integration, orc_gmap_fn gmap, void *user, int linear,
+                  double *xnod) {
+  int32_t nd[32];
+  orc_node_ndof(ORC_HEXA, norder, nd);
+  int first[27];
+  first[0] = 0;
+  for (int i = 0; i < 26; ++i) first[i + 1] = first[i] + nd[i];
+  /* the middle node's dof (node_ndof counts vertex..face nodes only) */
+  const int nrdof = orc_nrdofH_hexa(norder);
+  for (int k = 0; k < 3 * nrdof; ++k) xnod[k] = 0.0;
+  double *shap = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+  double *grad = (double *)malloc(sizeof(double) * 3 * ORC_MAXBRICKH);
+  double *A = (double *)malloc(sizeof(double) * ORC_MAXBRICKH * ORC_MAXBRICKH);
+  double *b = (double *)malloc(sizeof(double) * 3 * ORC_MAXBRICKH);
+  int rc = nrdof;
+  double x[3], dxdeta[9];
+  /* vertices (hpvert) */
+  for (int v = 0; v < 8; ++v) {
+    gmap(&etav[3 * v], x, dxdeta, user);
+    for (int c = 0; c < 3; ++c) xnod[3 * v + c] = x[c];
+  }
+  if (linear) goto done;
+  /* edges (hpedge): vertex functions + this edge's */
+  for (int e = 0; e < 12; ++e) {
+    const int n = nd[8 + e];
+    if (n == 0) continue;
+    int32_t no1[19];
+    for (int i = 0; i < 12; ++i) no1[i] = 1;
+    for (int i = 12; i < 18; ++i) no1[i] = 11;
+    no1[18] = 111;
+    no1[e] = norder[e];
+    const int nint = imin(norder[e] + integration, ORC_MAXP) + 1; /* set_1Dint */
+    double xg[16], wg[16];
+    orc_gauss1d(nint, xg, wg);
+    for (int i = 0; i < n * n; ++i) A[i] = 0.0;
+    for (int i = 0; i < 3 * n; ++i) b[i] = 0.0;
+    const double *x1 = BRICK_XI[BRICK_E2V[e][0]], *x2 = BRICK_XI[BRICK_E2V[e][1]];
+    for (int l = 0; l < nint; ++l) {
+      double xi[3], dxidt[3], J[3][3], Ji[3][3], det, eta[3] = {0, 0, 0};
+      for (int c = 0; c < 3; ++c) { dxidt[c] = x2[c] - x1[c]; xi[c] = x1[c] + xg[l] * dxidt[c]; }
+      const int nr = orc_shape3DH_hexa(xi, no1, nori_edge, nori_face, shap, grad);
+      eta_map(etav, grad, J, Ji, &det);
+      for (int v = 0; v < 8; ++v)
+        for (int c = 0; c < 3; ++c) eta[c] += etav[3 * v + c] * shap[v];
+      double detadt[3], bjac;
+      for (int i = 0; i < 3; ++i) detadt[i] = J[i][0] * dxidt[0] + J[i][1] * dxidt[1] + J[i][2] * dxidt[2];
+      bjac = sqrt(detadt[0] * detadt[0] + detadt[1] * detadt[1] + detadt[2] * detadt[2]);
+      const double rt[3] = {detadt[0] / bjac, detadt[1] / bjac, detadt[2] / bjac};
+      gmap(eta, x, dxdeta, user);
+      /* the lower part: the element's vertex dof (the first nr - n functions) */
+      gdof_point(0, grad, Ji, rt, dxdeta, xnod, nr - n, n, wg[l] * bjac, A, b);
+    }
+    if (lu_solve3(n, A, b)) { rc = -1; goto done; }
+    for (int j = 0; j < n; ++j)
+      for (int c = 0; c < 3; ++c) xnod[3 * (first[8 + e] + j) + c] = b[c * n + j];
+  }
+  /* faces (hpface): vertex and all edge functions + this face's */
+  for (int f = 0; f < 6; ++f) {
+    const int n = nd[20 + f];
+    if (n == 0) continue;
+    int32_t no1[19];
+    for (int i = 0; i < 12; ++i) no1[i] = norder[i];
+    for (int i = 12; i < 18; ++i) no1[i] = 11;
+    no1[18] = 111;
+    no1[12 + f] = norder[12 + f];
+    int hv[2];
+    decod(norder[12 + f], 10, 2, hv);
+    const int *fe = BRICK_F2E[f];
+    /* set_2Dint over face_order: per face axis the max of its edges and the face */
+    const int nx = imin(imax(imax(norder[fe[0]], norder[fe[2]]), hv[0]) + integration, ORC_MAXP) + 1;
+    const int ny = imin(imax(imax(norder[fe[1]], norder[fe[3]]), hv[1]) + integration, ORC_MAXP) + 1;
+    double xa[16], wa[16], xb[16], wb[16];
+    orc_gauss1d(nx, xa, wa);
+    orc_gauss1d(ny, xb, wb);
+    for (int i = 0; i < n * n; ++i) A[i] = 0.0;
+    for (int i = 0; i < 3 * n; ++i) b[i] = 0.0;
+    const double *v1 = BRICK_XI[BRICK_F2V[f][0]], *v2 = BRICK_XI[BRICK_F2V[f][1]],
+                 *v3 = BRICK_XI[BRICK_F2V[f][3]];
+    for (int l2 = 0; l2 < ny; ++l2)
+      for (int l1 = 0; l1 < nx; ++l1) {
+        double xi[3], t1[3], t2[3], J[3][3], Ji[3][3], det, eta[3] = {0, 0, 0};
+        for (int c = 0; c < 3; ++c) {
+          t1[c] = v2[c] - v1[c];
+          t2[c] = v3[c] - v1[c];
+          xi[c] = v1[c] + xa[l1] * t1[c] + xb[l2] * t2[c];
+        }
+        const int nr = orc_shape3DH_hexa(xi, no1, nori_edge, nori_face, shap, grad);
+        eta_map(etav, grad, J, Ji, &det);
+        for (int v = 0; v < 8; ++v)
+          for (int c = 0; c < 3; ++c) eta[c] += etav[3 * v + c] * shap[v];
+        double a1[3], a2[3];
+        for (int i = 0; i < 3; ++i) {
+          a1[i] = J[i][0] * t1[0] + J[i][1] * t1[1] + J[i][2] * t1[2];
+          a2[i] = J[i][0] * t2[0] + J[i][1] * t2[1] + J[i][2] * t2[2];
+        }
+        double rn[3] = {a1[1] * a2[2] - a1[2] * a2[1], a1[2] * a2[0] - a1[0] * a2[2],
+                        a1[0] * a2[1] - a1[1] * a2[0]};
+        const double bjac = sqrt(rn[0] * rn[0] + rn[1] * rn[1] + rn[2] * rn[2]);
+        for (int c = 0; c < 3; ++c) rn[c] /= bjac; /* its sign is immaterial */
+        gmap(eta, x, dxdeta, user);
+        gdof_point(1, grad, Ji, rn, dxdeta, xnod, nr - n, n, wa[l1] * wb[l2] * bjac, A, b);
+      }
+    if (lu_solve3(n, A, b)) { rc = -1; goto done; }
+    for (int j = 0; j < n; ++j)
+      for (int c = 0; c < 3; ++c) xnod[3 * (first[20 + f] + j) + c] = b[c * n + j];
+  }
+  /* the middle node (hpmdle): every other function, the element's own rule */
+  {
+    const int n = nrdof - first[26];
+    if (n > 0) {
+      double *xq = (double *)malloc(sizeof(double) * 3 * ORC_MAXBRICKH);
+      double *wq = (double *)malloc(sizeof(double) * ORC_MAXBRICKH);
+      const int nint = orc_set_3D_int_hexa(norder, nori_face, integration, xq, wq);
+      for (int i = 0; i < n * n; ++i) A[i] = 0.0;
+      for (int i = 0; i < 3 * n; ++i) b[i] = 0.0;
+      for (int l = 0; l < nint; ++l) {
+        double J[3][3], Ji[3][3], det, eta[3] = {0, 0, 0};
+        const int nr = orc_shape3DH_hexa(&xq[3 * l], norder, nori_edge, nori_face, shap, grad);
+        eta_map(etav, grad, J, Ji, &det);
+        for (int v = 0; v < 8; ++v)
+          for (int c = 0; c < 3; ++c) eta[c] += etav[3 * v + c] * shap[v];
+        gmap(eta, x, dxdeta, user);
+        gdof_point(2, grad, Ji, NULL, dxdeta, xnod, nr - n, n, wq[l] * det, A, b);
+      }
+      free(xq);
+      free(wq);
+      if (lu_solve3(n, A, b)) { rc = -1; goto done; }
+      for (int j = 0; j < n; ++j)
+        for (int c = 0; c < 3; ++c) xnod[3 * (first[26] + j) + c] = b[c * n + j];
+    }
+  }
+done:
+  free(shap);
+  free(grad);
+  free(A);
+  free(b);
+  return rc;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Helpers shared with hp3d_oracle_dpg.c (hp3d_oracle_int.h)                  */
 /* ------------------------------------------------------------------------ */
 void orc_i_decod(int nick, int mod, int n, int *arr) { decod(nick, mod, n, arr); }

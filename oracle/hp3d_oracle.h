@@ -165,6 +165,22 @@ int orc_constrain(int ni, const double *aii, const double *bi, int ncoef, const 
 int orc_dirichlet_hexa(const int32_t *norder, const int32_t *nori_edge, const int32_t *nori_face,
                        const double *xvert, const int32_t *bcflag, int isol, double *zd);
 
+/* update_gdof for one hexahedron (update_gdof.F90:80-200 and 404-435,
+ * hpvert.F90, hpedge.F90, hpface.F90, hpmdle.F90): its geometry dof xnod
+ * (nrdofH x 3, row-major, element dof order) from the geometry block's map
+ * x(eta), evaluated by gmap at block coordinates eta (x and dxdeta row-major,
+ * dxdeta[3 i + j] = d x_i / d eta_j).  etav: the element's 8 vertices in the
+ * block's coordinates (refel); eta(xi) is trilinear in them.  Vertex dof are
+ * x at the vertices; edge, face and interior dof are the eta-space H1
+ * projections (tangential, surface, full gradient) of x minus the lower-order
+ * part, with the quadrature of set_1Dint / set_2Dint / set_3Dint at
+ * INTEGRATION = integration.  linear != 0: vertices only (a 'Linear' block).
+ * Returns nrdofH, or -1 for a singular projection. */
+typedef void (*orc_gmap_fn)(const double *eta, double *x, double *dxdeta, void *user);
+int orc_gdof_hexa(const int32_t *norder, const int32_t *nori_edge, const int32_t *nori_face,
+                  const double *etav, int integration, orc_gmap_fn gmap, void *user, int linear,
+                  double *xnod);
+
 /* mumps_sc STEP 1 offsets + STEP 2 connectivities
  * (solver/omp_mumps/mumps_sc.F90:102-188, 266-299).
  * nodes: nelem x nnode_max global node ids (element node order),

@@ -77,6 +77,8 @@ def lib():
         L.orc_constrain.argtypes = [ctypes.c_int, _f64p, _f64p, ctypes.c_int, _i32p, _i32p,
                                     _f64p, ctypes.c_int, _f64p, _f64p]
         L.orc_dirichlet_hexa.argtypes = [_i32p, _i32p, _i32p, _f64p, _i32p, ctypes.c_int, _f64p]
+        L.orc_gdof_hexa.argtypes = [_i32p, _i32p, _i32p, _f64p, ctypes.c_int, GMAP_FN,
+                                    ctypes.c_void_p, ctypes.c_int, _f64p]
         L.orc_nrdofE_hexa.argtypes = [_i32p]
         L.orc_shape3DE_hexa.argtypes = [_f64p, _i32p, _i32p, _i32p, _f64p, _f64p]
         L.orc_shape3DQ_hexa.argtypes = [_f64p, _i32p, _f64p]
@@ -526,6 +528,32 @@ def celem_compress_nodes(nd, bcflag, amod, bmod, zdofd=None):
                                         _p(zd, _f64p), _p(nx, _i32p), _p(zb, _f64p),
                                         _p(zs, _f64p), _p(ndofm, _i32p))
     return nx[:nc].copy(), zb[:nc].copy(), zs[: nc * nc].reshape(nc, nc).copy(), ndofm
+
+
+GMAP_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                           ctypes.POINTER(ctypes.c_double), ctypes.c_void_p)
+
+
+def gdof_hexa(norder, nori_edge, nori_face, etav, gmap, integration=1, linear=False):
+    """update_gdof restated for one hexahedron: its geometry dof (nrdofH x 3,
+    element dof order) from the block map gmap(eta) -> (x (3,), dxdeta (3, 3))
+    and the element's vertices etav (8 x 3) in block coordinates."""
+    def cb(eta, x, dx, _user):
+        e = np.array([eta[0], eta[1], eta[2]])
+        xv, J = gmap(e)
+        for i in range(3):
+            x[i] = float(xv[i])
+            for j in range(3):
+                dx[3 * i + j] = float(J[i, j])
+    fn = GMAP_FN(cb)
+    L = lib()
+    n = L.orc_nrdofH_hexa(_p(_i32(norder), _i32p))
+    out = np.zeros(3 * max(n, 1))
+    rc = L.orc_gdof_hexa(_p(_i32(norder), _i32p), _p(_i32(nori_edge), _i32p),
+                         _p(_i32(nori_face), _i32p), _p(_f64(np.asarray(etav)[:8]), _f64p),
+                         integration, fn, None, int(linear), _p(out, _f64p))
+    assert rc == n, rc
+    return out[: 3 * n].reshape(n, 3).copy()
 
 
 def dirichlet_hexa(norder, nori_edge, nori_face, xvert, bcflag, isol):
