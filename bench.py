@@ -684,10 +684,13 @@ def main():
     epe.submit(mesh); epe.run(); epe.download()  # pinned result buffers exist from here on
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    step_ms = []
     for mk in steps_in:
+        ts = time.perf_counter()
         epe.submit(mk)
         epe.run()
         epe.download()
+        step_ms.append(1000 * (time.perf_counter() - ts))
     torch.cuda.synchronize()
     e2e_s = job_max((time.perf_counter() - t0) / args.e2e_steps, world)
     epe.close()
@@ -707,6 +710,7 @@ def main():
            "cold_step_ms": cold_ms,
            # the chunked pass applies to a batch of one bin (the uniform mesh)
            "download_chunks": args.download_chunks if args.workload == "hexa" else 1,
+           "step_ms": [round(x, 3) for x in step_ms],
            "note": "resubmit of the mesh with new kappa each step (upload xvert+kappa, "
                    "run, download all condensed outputs, each element chunk copied as "
                    "soon as it is done); cold_step_ms = new context"}

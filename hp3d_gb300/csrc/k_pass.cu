@@ -892,6 +892,15 @@ void launch_compress_group(const CondGroup& g, int k0, int k1, const int* d_ni_e
                            const double* d_zdofd, double* d_zastif, double* d_zbload,
                            cudaStream_t st) {
   if (k1 <= k0) return;
+  if (k1 == k0 + 1 && g.h_in[k0].nbf > 0) {
+    // one bin or chunk on the tensor-core path: the kernel with the
+    // segment's parameters in the launch arguments (the same device body)
+    const CondSegIn& q = g.h_in[k0];
+    launch_compress(q.nel, q.nfull, q.nif, q.nbf, q.elist, d_ni_e, q.PK, q.perm, q.W, q.t.bi,
+                    d_nextract, d_lcon_off, d_elem_nnz, d_zd_off, d_zdofd, q.dmask, d_zastif,
+                    d_zbload, st);
+    return;
+  }
   const int ns = g.nseg + 1;
   const int e0 = g.h_pre[2 * ns + k0], e1 = g.h_pre[2 * ns + k1];
   if (e1 > e0)
