@@ -606,7 +606,7 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the per-element mixed-vs-FP64 and oracle comparisons and the "
                          "final-solution check")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--download-chunks", type=int, default=4,
                     help="e2e: pass in this many element chunks, each copied to the host "
                          "as soon as it is done (1 = one piece)")
