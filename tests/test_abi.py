@@ -27,7 +27,7 @@ def test_library_builds_and_exports_all_declared_symbols():
 
 
 def test_struct_layouts_match_header():
-    assert ctypes.sizeof(H.Opts) == 16 * 4
+    assert ctypes.sizeof(H.Opts) == 16 * 4  # 13 fields, tune, 2 reserved
     assert H.DESC_DTYPE.itemsize == 4 * (2 + 19 + 12 + 6 + 26 + 26)
 
 
@@ -46,6 +46,10 @@ def test_null_context_calls_return_arg_errors_without_gpu():
     assert L.hp3dg_dpg_pass_stats(None, ctypes.byref(k)) == ERR_ARG
     assert L.hp3dg_pass_stats(None, ctypes.byref(k), None) == ERR_ARG
     assert L.hp3dg_dpg_last_bad_element(None) == -1
+    n = ctypes.c_int32()
+    assert L.hp3dg_bin_info(None, ctypes.byref(n), 0, None, None) == ERR_ARG
+    assert L.hp3dg_gdof_points(None, None, None, ctypes.byref(k)) == ERR_ARG
+    assert L.hp3dg_update_gdof(None, None, None, None, None, None, 0) == ERR_ARG
 
 
 def test_dpg_opts_layout_matches_header():
