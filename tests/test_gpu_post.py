@@ -176,4 +176,4 @@ def test_autograd_harness_directional_derivative():
                                           xvert + s * torch.from_numpy(dxv), m))
     fd = (Jat(t) - Jat(-t)) / (2 * t)
     ad = float((kappa.grad * torch.from_numpy(dk)).sum() + (xvert.grad * torch.from_numpy(dxv)).sum())
-    assert abs(fd - ad) <= 1e-6 * abs(ad) + 1e-12 * abs(float(J)) / t
+    assert abs(fd - ad) <= 1e-6 * abs(ad) + 1e-12 * abs(float(J.detach())) / t
