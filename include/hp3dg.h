@@ -321,7 +321,8 @@ int hp3dg_update_gdof(hp3dg_ctx *ctx, const double *etav, const double *x, const
  * target GPU): per (element type, n, nb, quadrature points, precision) bin
  * the condensation variant and the contraction's raster group, and the
  * contraction's pipeline depth.  Process-wide; read by every later submit of
- * a context with opts.tune = 0.  path = NULL clears the table.  Returns
+ * a context with opts.tune = 0 that builds its bins (a resubmit of the same
+ * descriptors keeps the batch's variants).  path = NULL clears the table.  Returns
  * HP3DG_ERR_ARG for an unreadable or malformed file (the table is then left
  * as it was); *nrec = bin entries loaded. */
 int hp3dg_tune_load(const char *path, int32_t *nrec);
