@@ -541,8 +541,15 @@ __device__ __forceinline__ void slice_d_tile(int kb, int eb, int K, int nk, int 
     int q = kb * 16 + kg * 8 + t;
     vals[t] = (e < nel && q < K) ? D[(size_t)e * K + q] : 0.0;
   }
-  double rs = (e < nel) ? 1.0 / dscale[e] : 0.0;
-  write_digits8(vals, rs, radix, digits, ddig, nk, eb, kb, r, kg, B_TILE);
+  // the row scale is 2^ex: each value becomes the integer round(v 2^(R D - ex))
+  // from its bits, split into balanced digits in integer arithmetic (GB300
+  // issues FP64 and its conversions at about 2 per clock per SM)
+  const int ex = (e < nel) ? (int)((__double_as_longlong(dscale[e]) >> 52) & 0x7ff) - 1023 : 0;
+  long long X[8];
+#pragma unroll
+  for (int t = 0; t < 8; ++t) X[t] = (e < nel) ? fixed_of(vals[t], ex, radix * digits) : 0;
+  const size_t off = (size_t)(r >> 3) * 256 + (size_t)kg * 128 + (size_t)(r & 7) * 16;
+  store_digits8(X, radix, digits, ddig + tile_base(eb, kb, 0, nk, digits, B_TILE) + off, B_TILE);
 }
 
 __global__ void k_slice_d(int K, int nk, int nel, int radix, int digits,
